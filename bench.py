@@ -1,0 +1,390 @@
+"""Benchmark of the random-walk particle-tracking hot path on one GB300.
+
+Workload (BASELINE config 2): 200x100x20 cells of 1 m, lognormal K
+(sigma2 lnK = 1, geometric mean 10 m/d, exponential covariance 10 m / 2 m,
+seeded FFT field), FP64 steady heads by CG to 1e-12, porosity 0.25,
+alphaL 0.5 m, alphaT 0.05 m, Dm 1e-4 m2/d, 1,000,000 unit-mass particles
+released uniformly in the 10 x 100 x 20 m inlet slab, MIN_ADV_DISP 0.1/0.1,
+EULERIAN, stop at weak sinks (constant-head outlet).  Synthetic inputs with
+the config's shapes and distributions.
+
+One step = one 10-day tracking interval: advance every particle to the next
+GPKDE time point, then the GPKDE histogram of the active particles on the
+1 m grid.  W warm-up intervals are run first; the K timed intervals continue
+the same simulation.  L2 (129 MB) is flushed between timed steps by writing a
+256 MiB buffer outside the timed events.
+
+Reported: ``value`` = particle-steps/s of the plain FP64 path with the state
+resident in HBM; ``e2e`` = the same through the C ABI with pinned host
+buffers (particle state host->device, advance, state + histogram
+device->host every step); ``mixed`` = the MIXED-precision path on the same
+workload with its plume-moment errors against the FP64 run; ``roofline`` of
+the step kernel; ``cpu_baseline`` = the C restatement of the reference
+(OpenMP, all host threads) on a bounded sample.
+
+``--impl reference`` times the reference's CPU algorithm (the C restatement:
+the Fortran reference cannot be compiled on these machines) instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (str(ROOT / "modpath-rw_gb300"), str(ROOT)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "particle-steps/s: plain FP64 vs batched mixed-precision at stated moment error"
+UNIT = "particle-steps/s"
+B_STEP_FP64 = 1008.0   # algorithmic bytes per particle-step, FP64 (state r+w 96 B + cell record 912 B)
+B_STEP_MIXED = 544.0   # MIXED (72 B + 472 B)
+INTERVAL_D = 10.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--particles", type=int, default=1_000_000)
+    ap.add_argument("--cpu-sample", type=int, default=400_000)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per particle-step of the step kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "rwpt_advance_kernel_config2.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.strip().startswith("dram_bytes_per_particle_step:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([s.strip() for s in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 7 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 7 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows if len(r) > 7 for k in range(4) if r[4 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def build_workload(n_particles, rank=0, use_torch=True):
+    from mprw import workloads as W
+    g, f, p, opt, info = W.config2(n_particles=n_particles, seed=0, use_torch=use_torch)
+    if rank:
+        # weak scaling: every rank tracks its own particle set on the same field
+        q = W.release_in_box(g, n_particles, 0.0, 10.0, 0.0, 100.0, float(g.botm[-1]), float(g.top[0]),
+                             seed=1000 + 7919 * rank)
+        q.id = q.id + np.uint64(rank * n_particles)
+        p = q
+    return g, f, p, opt, info
+
+
+def moments(out):
+    act = out["status"] == 1
+    m = {}
+    for k in ("gx", "gy", "gz"):
+        v = out[k][act]
+        m[k] = (float(v.mean()), float(v.var()))
+    return m, int(act.sum())
+
+
+def run_gpu_arm(args, rank, world, local):
+    import torch
+    import mprw
+    from mprw.model import MIXED
+
+    torch.cuda.set_device(local)
+    g, f, p, opt, info = build_workload(args.particles, rank)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    origin, bins, nb = (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (g.ncol, g.nrow, g.nlay)
+
+    stream = torch.cuda.Stream()
+
+    def timed_run(precision, steps, warmup):
+        opt.precision = precision
+        tr = mprw.Tracker(g, opt)
+        tr.set_stream(stream.cuda_stream)   # launch on a stream the events below can see
+        tr.load_flow(f)
+        tr.set_particles(p)
+        t = 0.0
+        for _ in range(warmup):
+            tr.advance(t, t + INTERVAL_D)
+            tr.histogram(origin, bins, nb)
+            t += INTERVAL_D
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        kern_ms, hist_ms, wall_ms, steps_done, launches = [], [], [], 0, 0
+        for k in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ev[k][0].record(stream)
+            s = tr.advance(t, t + INTERVAL_D)
+            tm = tr.timings()
+            tr.histogram(origin, bins, nb)
+            th = tr.timings()
+            ev[k][1].record(stream)
+            torch.cuda.synchronize()
+            wall_ms.append((time.perf_counter() - t0) * 1e3)
+            kern_ms.append(tm["step_ms"])
+            hist_ms.append(th["hist_ms"])
+            launches += tm["launches"] + th["launches"]
+            steps_done += s
+            t += INTERVAL_D
+        ms = [a.elapsed_time(b) for a, b in ev]
+        out = tr.get_particles()
+        tr.close()
+        return dict(ms=ms, kern_ms=kern_ms, hist_ms=hist_ms, wall_ms=wall_ms, steps=steps_done,
+                    launches=launches, out=out, t_end=t)
+
+    with ClockSampler(local) as clk:
+        fp64 = timed_run(0, args.steps, args.warmup)
+    res = dict(fp64=fp64, clocks=clk.summary())
+    if not args.no_mixed:
+        res["mixed"] = timed_run(MIXED, args.steps, args.warmup)
+    if not args.no_e2e:
+        res["e2e"] = e2e_run(args, g, f, p, opt, origin, bins, nb, flush)
+    res["geom"] = (g, f, p, opt)
+    return res
+
+
+def e2e_run(args, g, f, p, opt, origin, bins, nb, flush):
+    """Through the C ABI with pinned host buffers; copies inside the timed region."""
+    import ctypes as C
+
+    import torch
+    import mprw
+    opt.precision = 0
+    tr = mprw.Tracker(g, opt)
+    tr.load_flow(f)
+    n = p.n
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    st = dict(cell=pin(p.cell.astype(np.int32)), lx=pin(p.lx), ly=pin(p.ly), lz=pin(p.lz), t=pin(p.t),
+              status=pin(p.status.astype(np.int32)), mass=pin(p.mass), id=pin(p.id.astype(np.uint64)),
+              ctr=pin(np.zeros(n, np.uint64)))
+    counts = pin(np.zeros(g.ncell))
+    L = tr.lib
+    dp, ip, up = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_uint64)
+    P = lambda a, t_: a.ctypes.data_as(t_)
+    o3 = (C.c_double * 3)(*origin)
+    b3 = (C.c_double * 3)(*bins)
+    n3 = (C.c_int32 * 3)(*nb)
+    h2d = n * (4 + 8 * 3 + 8 + 4 + 8 + 8 + 8)
+    d2h = n * (4 + 8 * 3 + 8 + 4 + 8) + 8 * g.ncell
+    t = 0.0
+    tot_ms, steps = 0.0, 0
+    steps_i = C.c_int64()
+    nbin = C.c_int64()
+    eff = C.c_double()
+    for it in range(args.warmup + args.steps):
+        if it >= args.warmup:
+            flush.zero_()
+            torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = L.mprw_set_particles(tr.h, n, P(st["cell"], ip), P(st["lx"], dp), P(st["ly"], dp), P(st["lz"], dp),
+                                  P(st["t"], dp), P(st["status"], ip), P(st["mass"], dp), P(st["id"], up),
+                                  P(st["ctr"], up))
+        rc |= L.mprw_advance(tr.h, t, t + INTERVAL_D, C.byref(steps_i))
+        rc |= L.mprw_get_particles(tr.h, P(st["cell"], ip), P(st["lx"], dp), P(st["ly"], dp), P(st["lz"], dp),
+                                   P(st["t"], dp), P(st["status"], ip), P(st["ctr"], up), None, None, None)
+        rc |= L.mprw_histogram(tr.h, o3, b3, n3, P(counts, dp), C.byref(nbin), C.byref(eff))
+        t1 = time.perf_counter()
+        if rc != 0:
+            raise RuntimeError("e2e C-ABI call failed: " + L.mprw_last_error(tr.h).decode())
+        if it >= args.warmup:
+            tot_ms += (t1 - t0) * 1e3
+            steps += steps_i.value
+        t += INTERVAL_D
+    tr.close()
+    return dict(value=steps / (tot_ms / 1e3), ms_per_step=tot_ms / args.steps, h2d=h2d, d2h=d2h)
+
+
+def cpu_baseline(g, f, p, opt, n_sample, t_begin_steps, steps):
+    """The oracle (C restatement of the reference, OpenMP on all host threads)
+    on the first n_sample particles, from t=0 over warmup+steps intervals."""
+    from oracle import oracle as O
+    from mprw.model import Particles
+    idx = slice(0, n_sample)
+    q = Particles(cell=p.cell[idx].copy(), lx=p.lx[idx].copy(), ly=p.ly[idx].copy(), lz=p.lz[idx].copy(),
+                  t=p.t[idx].copy(), status=p.status[idx].copy(), mass=p.mass[idx].copy(), id=p.id[idx].copy(),
+                  rng_ctr=np.zeros(n_sample, np.uint64))
+    opt.precision = 0
+    th = O.cpu_count()
+    t = 0.0
+    tot, nsteps = 0.0, 0
+    for it in range(t_begin_steps + steps):
+        t0 = time.perf_counter()
+        q, s = O.advance(g, f, opt, q, t, t + INTERVAL_D, rng_kind=O.RNG_XOROSHIRO, nthreads=th)
+        t1 = time.perf_counter()
+        if it >= t_begin_steps:
+            tot += t1 - t0
+            nsteps += s
+        t += INTERVAL_D
+    return dict(value=nsteps / tot, unit=UNIT, cores=th, kind="port",
+                sample=f"first {n_sample} of the {p.n} particles, {steps} x {INTERVAL_D:g}-day intervals "
+                       f"after {t_begin_steps} untimed; xoroshiro128+ thread streams as the reference",
+                seconds=tot)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        return main_reference(args, rank, world)
+    import torch
+    res = run_gpu_arm(args, rank, world, local)
+    fp = res["fp64"]
+    t_kern = sum(fp["ms"])
+    ms_step = t_kern / args.steps
+    value_rank = fp["steps"] / (t_kern / 1e3)
+    # whole-job: all ranks' steps over the slowest rank's time
+    tot_steps, max_t = fp["steps"], t_kern
+    if world > 1:
+        import torch.distributed as dist
+        v = torch.tensor([float(fp["steps"]), t_kern], dtype=torch.float64)
+        allv = [torch.zeros_like(v) for _ in range(world)]
+        dist.all_gather(allv, v)
+        tot_steps = sum(float(a[0]) for a in allv)
+        max_t = max(float(a[1]) for a in allv)
+    value = tot_steps / (max_t / 1e3)
+    if rank != 0:
+        return
+    hbm, peak_kind = peaks()
+    kern_avg_ms = float(np.mean(fp["kern_ms"]))
+    steps_per_launch = fp["steps"] / args.steps
+    achieved = steps_per_launch * B_STEP_FP64 / (kern_avg_ms / 1e3) / 1e9
+    tr_ps = ncu_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": max_t / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "config2: 200x100x20 lognormal-K field (sigma2 lnK 1, 10 m/2 m), FP64 CG heads, "
+                               f"{args.particles} particles from the inlet slab, step = one 10-day interval "
+                               "(advance + GPKDE histogram on the 1 m grid)",
+                   "particles_per_gpu": args.particles, "interval_days": INTERVAL_D,
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"particles x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_source": f"{peak_kind} hbm_gbs",
+                     "traffic": None if tr_ps is None else tr_ps * steps_per_launch,
+                     "kernel": "rwpt_advance_kernel<double>", "kernel_ms": kern_avg_ms,
+                     "bytes_model": "1008 B per particle-step (state 96 B + cell record 912 B)"},
+        "clocks": res["clocks"],
+        "gpu_launches": int(fp["launches"]),
+        "kernel_time_share": {"advance_kernel_ms": float(np.sum(fp["kern_ms"])),
+                              "histogram_ms": float(np.sum(fp["hist_ms"])), "step_event_ms": float(np.sum(fp["ms"])),
+                              "step_wall_ms": float(np.sum(fp["wall_ms"]))},
+    }
+    if "e2e" in res:
+        e = res["e2e"]
+        line["e2e"] = {"value": e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
+                       "d2h_bytes_per_step": e["d2h"], "ms_per_step": e["ms_per_step"]}
+    if "mixed" in res:
+        mx = res["mixed"]
+        tm = sum(mx["ms"])
+        m64, n64 = moments(fp["out"])
+        m32, n32 = moments(mx["out"])
+        err = {k: {"mean_rel": abs(m32[k][0] - m64[k][0]) / max(abs(m64[k][0]), 1e-30),
+                   "var_rel": abs(m32[k][1] - m64[k][1]) / max(abs(m64[k][1]), 1e-30)} for k in m64}
+        line["mixed"] = {"value": mx["steps"] / (tm / 1e3), "unit": UNIT, "speedup_vs_fp64": (mx["steps"] / tm) /
+                         (fp["steps"] / t_kern), "moment_error_vs_fp64": err, "active_fp64": n64,
+                         "active_mixed": n32, "kernel_ms": float(np.mean(mx["kern_ms"]))}
+    if not args.no_cpu:
+        g, f, p, opt = res["geom"]
+        line["cpu_baseline"] = cpu_baseline(g, f, p, opt, args.cpu_sample, args.warmup, min(args.steps, 5))
+    print(json.dumps(line))
+
+
+def main_reference(args, rank, world):
+    if rank != 0:
+        return
+    g, f, p, opt, info = build_workload(args.particles, 0, use_torch=False)
+    cb = cpu_baseline(g, f, p, opt, args.cpu_sample, args.warmup, args.steps)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "ms_per_step": cb["seconds"] * 1e3 / args.steps,
+            "config": {"workload": "config2 (same field and release), bounded particle sample",
+                       "particles": args.cpu_sample, "interval_days": INTERVAL_D},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference is Fortran and no Fortran compiler exists on these machines; the timed CPU "
+                    "implementation is the C restatement of its algorithm (oracle/), OpenMP on all host threads"}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

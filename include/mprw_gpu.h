@@ -1,0 +1,169 @@
+/*
+ * mprw_gpu.h -- C ABI of the GB300 random-walk particle tracking library.
+ *
+ * Drop-in replacement for the tracking part of MODPATH-RW's OpenMP particle
+ * loop and for its GPKDE histogram.  Every entry point takes plain pointers
+ * and sizes, is callable from Fortran through ISO_C_BINDING, and returns an
+ * int status (0 = ok, < 0 = error; mprw_last_error() gives the message).
+ *
+ * Reference interfaces replaced (paths relative to the reference's src/):
+ *   mprw_advance        <- the per-particle TrackPath call inside the
+ *                          `!$omp parallel do` particle loop, MPathRW.F90:1207-1539
+ *                          (trackingEngine%TrackPath at MPathRW.F90:1320-1322,
+ *                          ParticleTrackingEngine.f90:1051-1254, release checks
+ *                          MPathRW.F90:1256-1302, status map 1337-1403)
+ *   mprw_load_flow      <- FillCellBuffer / FillNeighborCellData / corner
+ *                          variables rebuilt on every cell entry
+ *                          (ParticleTrackingEngine.f90:711-825, 2009-2126;
+ *                          ModpathCellData.f90:674-1098, 2522-2684;
+ *                          TrackSubCell.F90:3667-4363)
+ *   mprw_get_particles  <- ConvertToModelXYZ of the last pathline point
+ *                          (ParticleTrackingEngine.f90:1226-1251,
+ *                          ModflowRectangularGrid.f90:524-548)
+ *   mprw_histogram      <- Histogram%ComputeCountsWeighted / ComputeCounts
+ *                          (lib/gpkde/Histogram.F90:213-350), called from
+ *                          GridProjectedKDE.F90:3964-3987 on the active
+ *                          particles gathered at MPathRW.F90:1568-1624
+ *
+ * Conventions (the reference's): cell numbers are 1-based MODFLOW 6 DIS
+ * node numbers, node = (k-1)*nrow*ncol + (i-1)*ncol + j; IA/JA are the
+ * 1-based CSR arrays of the MODFLOW 6 binary grid file; FLOW-JA-FACE is
+ * positive into the cell; faces 1..6 are -x, +x, -y (front), +y (back),
+ * bottom, top; particle statuses are the driver codes 0..9
+ * (0 pending, 1 active, 2 boundary face, 3 weak sink, 4 weak source,
+ * 5 no exit possible, 6 stop zone, 7 inactive cell, 8 unreleased,
+ * 9 undefined).
+ *
+ * Threading: one handle per host thread.  Calls on one handle are
+ * serialised; the handle owns its device memory and its CUDA stream.
+ */
+#ifndef MPRW_GPU_H
+#define MPRW_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPRW_OK 0
+#define MPRW_E_INVAL -1   /* invalid argument or unsupported option          */
+#define MPRW_E_CUDA -2    /* CUDA runtime error                              */
+#define MPRW_E_OOM -3     /* device allocation failed                        */
+#define MPRW_E_STATE -4   /* call out of order (e.g. advance before flow)    */
+#define MPRW_E_ABORTED -5 /* a kernel hit its iteration cap and set an error */
+
+#define MPRW_FP64 0  /* positions, velocities, dispersion all in FP64        */
+#define MPRW_MIXED 1 /* int32 cell + FP32 local coordinates and arithmetic,  */
+                     /* FP64 tracking time                                   */
+
+typedef struct mprw_handle mprw_handle;
+
+/* Structured MODFLOW 6 DIS grid (RectangularGridDisMf6.f90:122-360). */
+typedef struct {
+  int32_t nlay, nrow, ncol;
+  const double *delr; /* ncol                                               */
+  const double *delc; /* nrow                                               */
+  const double *top;  /* nrow*ncol, top of layer 1                          */
+  const double *botm; /* nlay*nrow*ncol                                     */
+} mprw_grid_desc;
+
+/* Tracking options as the reference parses them (ParticleTrackingOptions.f90,
+ * RWOPTS ModpathSimulationData.f90:1770-2021, DSP TransportModelData.f90). */
+typedef struct {
+  int32_t time_step_kind;     /* 1 ADV, 2 DISP, 3 MIN_ADV_DISP, 4 FIXED      */
+  double ts_param[2];         /* timeStepParameters(1:2)                     */
+  int32_t advection_kind;     /* 2 EULERIAN (1 EXPONENTIAL: not supported)   */
+  int32_t dim_mask[3];        /* random-walk dimension mask                  */
+  int32_t dispersion_model;   /* 0 linear isotropic                          */
+  int32_t stop_weak_sinks;
+  int32_t stop_weak_sources;
+  int32_t backward;
+  int32_t stop_zone;          /* 0 = none                                    */
+  int32_t uniform_porosity;   /* isUniformPorosity (ModpathBasicData.f90:208)*/
+  uint64_t rng_seed;          /* Philox key                                  */
+  int32_t precision;          /* MPRW_FP64 or MPRW_MIXED                     */
+} mprw_options;
+
+/* One flow time step (FlowModelData + TransportModelData arrays). */
+typedef struct {
+  const int32_t *ia;          /* ncell+1, 1-based                            */
+  const int32_t *ja;          /* nja, 1-based, diagonal first in each row    */
+  int64_t nja;
+  const double *flowja;       /* nja FLOW-JA-FACE                            */
+  const double *boundary_flows; /* 6*ncell face-assigned boundary flows, or NULL */
+  const double *porosity;     /* ncell                                       */
+  const double *retardation;  /* ncell                                       */
+  const int32_t *iboundts;    /* ncell IBoundTS                              */
+  const int32_t *icboundts;   /* ncell ICBoundTS, or NULL (all 0)            */
+  int32_t default_icbound;    /* 1 when no IMP file (TransportModelData.f90:202) */
+  const double *heads;        /* ncell, or NULL                              */
+  const int32_t *celltype;    /* ncell ICELLTYPE, or NULL (all confined)     */
+  const double *source_flow;  /* ncell, or NULL                              */
+  const double *sink_flow;    /* ncell, or NULL                              */
+  const int32_t *zones;       /* ncell, or NULL                              */
+  const double *alpha_l;      /* ncell, or 1 value when uniform_dispersion   */
+  const double *alpha_t;
+  const double *dm_eff;
+  int32_t uniform_dispersion;
+  int32_t steady_state;
+} mprw_flow_desc;
+
+/* Create a handle on the current CUDA device.
+ * Replaces trackingEngine%Initialize (ParticleTrackingEngine.f90:393-532)
+ * and InitializeRandomWalk (TrackSubCell.F90:542-631). */
+int mprw_create(mprw_handle **h, const mprw_grid_desc *grid, const mprw_options *opt);
+
+/* Upload one flow time step and build the per-cell records on the device.
+ * Replaces the per-cell-entry buffer fills listed in the header comment. */
+int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *flow);
+
+/* Copy n particles (host arrays) to the device.  cell is 1-based; t is the
+ * TrackingTime (the release time for pending particles); mass may be NULL
+ * (unit mass); id may be NULL (id = index); rng_ctr may be NULL (zeros).
+ * Replaces the particle arrays of ParticleGroups (Particle.f90:7-17). */
+int mprw_set_particles(mprw_handle *h, int64_t n, const int32_t *cell, const double *lx,
+                       const double *ly, const double *lz, const double *t,
+                       const int32_t *status, const double *mass, const uint64_t *id,
+                       const uint64_t *rng_ctr);
+
+/* Advance every particle from tracking-interval start t_begin (the driver's
+ * `time`) to t_end (the driver's `maxTime`), including the release checks.
+ * steps_done (may be NULL) receives the particle-steps taken.
+ * Replaces the tracking part of MPathRW.F90:1207-1539. */
+int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_done);
+
+/* Copy particle state back (any pointer may be NULL).  gx/gy/gz are the
+ * model coordinates of ConvertToModelXYZ. */
+int mprw_get_particles(mprw_handle *h, int32_t *cell, double *lx, double *ly, double *lz,
+                       double *t, int32_t *status, uint64_t *rng_ctr, double *gx,
+                       double *gy, double *gz);
+
+/* Weighted histogram of the ACTIVE particles' model coordinates on the grid
+ * origin[3] + bin_size[3] * (n_bins[3]) (Histogram.F90:276-350), column-major
+ * counts (x fastest).  counts (prod n_bins doubles) receives the sum of the
+ * particle masses per bin, identical to the reference's sequential sum;
+ * n_active and eff_mass (Kish effective count (sum w)^2 / sum w^2, computed
+ * over the binned particles) may be NULL.  ordered != 0 forces the
+ * order-preserving sum for arbitrary masses; with unit or equal
+ * power-of-two masses the integer path is exact either way. */
+int mprw_histogram(mprw_handle *h, const double origin[3], const double bin_size[3],
+                   const int32_t n_bins[3], double *counts, int64_t *n_binned,
+                   double *eff_mass);
+
+/* Optional: launch on a caller-provided cudaStream_t (NULL = the handle's). */
+int mprw_set_stream(mprw_handle *h, void *stream);
+
+/* Device time (ms) of the last launch of each kernel family, and the number
+ * of kernel launches issued by the last mprw_advance / mprw_histogram call. */
+int mprw_last_timings(mprw_handle *h, double *step_ms, double *prep_ms, double *hist_ms,
+                      int64_t *launches);
+
+int mprw_destroy(mprw_handle *h);
+
+const char *mprw_last_error(const mprw_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,642 @@
+// api.cu -- the C ABI declared in include/mprw_gpu.h.
+//
+// The handle owns the device copy of the grid, one flow time step (raw
+// arrays + per-cell records), the particle state and a CUDA stream.  All
+// work is issued on that stream; calls that return data synchronise it.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mprw_gpu.h"
+#include "mprw_kernels.cuh"
+
+using namespace mprw;
+
+struct mprw_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  GridDims g{};
+  mprw_options opt{};
+  int ndim = 3, d1 = 0, d2 = 1;
+  int ncell_bits = 1;
+  // grid
+  double *d_delr = nullptr, *d_delc = nullptr, *d_top = nullptr, *d_botm = nullptr;
+  double *d_colL = nullptr, *d_colR = nullptr, *d_rowF = nullptr, *d_rowB = nullptr, *d_sattop = nullptr;
+  std::vector<double> h_top_cell;  // Top(n) after layer propagation
+  // flow time step
+  int32_t *d_ia = nullptr, *d_ja = nullptr;
+  int64_t nja_cap = 0;
+  double *d_flowja = nullptr, *d_bflow = nullptr, *d_por = nullptr, *d_ret = nullptr, *d_heads = nullptr;
+  double *d_src = nullptr, *d_snk = nullptr, *d_aL = nullptr, *d_aT = nullptr, *d_dm = nullptr;
+  int32_t *d_ibts = nullptr, *d_icb = nullptr, *d_ctype = nullptr, *d_zones = nullptr;
+  CellBase base{};
+  uint8_t *d_massb = nullptr;
+  CellRec<double> *d_rec64 = nullptr;
+  CellRec<float> *d_rec32 = nullptr;
+  bool flow_loaded = false;
+  // particles
+  int64_t n = 0, cap = 0;
+  int32_t *d_cell = nullptr, *d_status = nullptr;
+  void *d_x = nullptr, *d_y = nullptr, *d_z = nullptr;
+  double *d_t = nullptr, *d_mass = nullptr, *d_stage = nullptr;
+  uint64_t *d_ctr = nullptr, *d_id = nullptr;
+  uint32_t *d_perm = nullptr;
+  bool unit_mass = true;
+  bool has_id = false;
+  unsigned long long *d_counters = nullptr;  // [0] queue, [1] steps, [2] nbinned
+  unsigned long long *h_counters = nullptr;  // pinned
+  void *scratch = nullptr;
+  size_t scratch_bytes = 0;
+  void *hscratch = nullptr;
+  size_t hscratch_bytes = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+  double step_ms = 0, prep_ms = 0, hist_ms = 0;
+  int64_t launches = 0;
+  int sms = 152;
+  int sort_enabled = 1;
+  std::string err;
+};
+
+namespace {
+
+int fail(mprw_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                            \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return fail(h, e_ == cudaErrorMemoryAllocation ? MPRW_E_OOM : MPRW_E_CUDA,            \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t count) {
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc((void **)p, sizeof(T) * count);
+}
+
+template <typename T>
+cudaError_t upload(mprw_handle *h, T **p, const T *src, size_t count) {
+  cudaError_t e = dalloc(p, count);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(*p, src, sizeof(T) * count, cudaMemcpyHostToDevice, h->stream);
+}
+
+void free_all(mprw_handle *h) {
+  void *ptrs[] = {h->d_delr, h->d_delc, h->d_top, h->d_botm, h->d_colL, h->d_colR, h->d_rowF, h->d_rowB,
+                  h->d_sattop, h->d_ia, h->d_ja, h->d_flowja, h->d_bflow, h->d_por, h->d_ret, h->d_heads,
+                  h->d_src, h->d_snk, h->d_aL, h->d_aT, h->d_dm, h->d_ibts, h->d_icb, h->d_ctype,
+                  h->d_zones, h->base.q, h->base.dz, h->base.conn, h->base.flags, h->d_massb, h->d_rec64,
+                  h->d_rec32, h->d_cell, h->d_status, h->d_x, h->d_y, h->d_z, h->d_t, h->d_mass,
+                  h->d_stage, h->d_ctr, h->d_id, h->d_perm, h->d_counters, h->scratch};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (h->h_counters) cudaFreeHost(h->h_counters);
+  if (h->hscratch) cudaFreeHost(h->hscratch);
+  cudaEvent_t evs[] = {h->ev0, h->ev1, h->ev2, h->ev3};
+  for (auto e : evs)
+    if (e) cudaEventDestroy(e);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+}
+
+__global__ void f64_to_f32_kernel(const double *in, float *out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+__global__ void f32_to_f64_kernel(const float *in, double *out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (double)in[i];
+}
+__global__ void cell_shift_kernel(int32_t *cell, int64_t n, int32_t delta) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    cell[i] += delta;
+}
+__global__ void div_kernel(double *x, int64_t n, double d) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = x[i] / d;
+}
+
+int grid1d(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  return b < 1 ? 1 : (int)b;
+}
+
+Geometry geometry(mprw_handle *h) {
+  Geometry geo;
+  geo.col_left = h->d_colL;
+  geo.col_right = h->d_colR;
+  geo.row_front = h->d_rowF;
+  geo.row_back = h->d_rowB;
+  geo.botm = h->d_botm;
+  geo.sattop = h->d_sattop;
+  geo.g = h->g;
+  return geo;
+}
+
+cudaError_t ensure_host(mprw_handle *h, size_t bytes) {
+  if (h->hscratch_bytes >= bytes) return cudaSuccess;
+  if (h->hscratch) cudaFreeHost(h->hscratch);
+  h->hscratch = nullptr;
+  h->hscratch_bytes = 0;
+  cudaError_t e = cudaMallocHost(&h->hscratch, bytes);
+  if (e == cudaSuccess) h->hscratch_bytes = bytes;
+  return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mprw_create(mprw_handle **out, const mprw_grid_desc *gd, const mprw_options *o) {
+  if (!out || !gd || !o) return MPRW_E_INVAL;
+  *out = nullptr;
+  if (gd->nlay <= 0 || gd->nrow <= 0 || gd->ncol <= 0 || !gd->delr || !gd->delc || !gd->top || !gd->botm)
+    return MPRW_E_INVAL;
+  int64_t ncell = (int64_t)gd->nlay * gd->nrow * gd->ncol;
+  if (ncell >= (int64_t)1 << 31) return MPRW_E_INVAL;
+  mprw_handle *h = new mprw_handle();
+  *out = h;
+  if (o->advection_kind != 2) return fail(h, MPRW_E_INVAL, "advection_kind: only EULERIAN (2) is supported");
+  if (o->dispersion_model != 0) return fail(h, MPRW_E_INVAL, "dispersion_model: only linear isotropic (0)");
+  if (o->time_step_kind < 1 || o->time_step_kind > 4) return fail(h, MPRW_E_INVAL, "time_step_kind");
+  if (o->precision != MPRW_FP64 && o->precision != MPRW_MIXED) return fail(h, MPRW_E_INVAL, "precision");
+  h->opt = *o;
+  int dims[3], nd = 0;
+  for (int d = 0; d < 3; ++d)
+    if (o->dim_mask[d]) dims[nd++] = d;
+  if (nd == 0) return fail(h, MPRW_E_INVAL, "dim_mask selects no dimension");
+  h->ndim = nd;
+  h->d1 = dims[0];
+  h->d2 = nd > 1 ? dims[1] : 0;
+  h->g.nlay = gd->nlay;
+  h->g.nrow = gd->nrow;
+  h->g.ncol = gd->ncol;
+  h->g.ncpl = gd->nrow * gd->ncol;
+  h->g.ncell = (int32_t)ncell;
+  while (((int64_t)1 << h->ncell_bits) < ncell) ++h->ncell_bits;
+  CK(cudaGetDevice(&h->device));
+  CK(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device));
+  CK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
+  h->stream = h->own_stream;
+  CK(cudaEventCreate(&h->ev0));
+  CK(cudaEventCreate(&h->ev1));
+  CK(cudaEventCreate(&h->ev2));
+  CK(cudaEventCreate(&h->ev3));
+  CK(cudaMallocHost(&h->h_counters, 4 * sizeof(unsigned long long)));
+  CK(dalloc(&h->d_counters, 4));
+  // geometry as the binary-grid reader builds it (RectangularGridDisMf6.f90:301-340)
+  const int ncol = gd->ncol, nrow = gd->nrow, ncpl = h->g.ncpl;
+  std::vector<double> colL(ncol), colR(ncol), rowF(nrow), rowB(nrow);
+  double X = 0.0;
+  for (int c = 0; c < ncol; ++c) {
+    double Xn = X + gd->delr[c];
+    double cx = (X + Xn) / 2.0;
+    colL[c] = cx - (gd->delr[c] / 2.0);
+    colR[c] = cx + (gd->delr[c] / 2.0);
+    X = Xn;
+  }
+  double Y = 0.0;
+  for (int r = 0; r < nrow; ++r) Y = Y + gd->delc[r];
+  for (int r = 0; r < nrow; ++r) {
+    double Yn = Y - gd->delc[r];
+    double cy = (Y + Yn) / 2.0;
+    rowF[r] = cy - (gd->delc[r] / 2.0);
+    rowB[r] = cy + (gd->delc[r] / 2.0);
+    Y = Yn;
+  }
+  h->h_top_cell.resize(ncell);
+  for (int64_t c = 0; c < ncell; ++c) h->h_top_cell[c] = (c < ncpl) ? gd->top[c] : gd->botm[c - ncpl];
+  CK(upload(h, &h->d_delr, gd->delr, ncol));
+  CK(upload(h, &h->d_delc, gd->delc, nrow));
+  CK(upload(h, &h->d_top, gd->top, ncpl));
+  CK(upload(h, &h->d_botm, gd->botm, ncell));
+  CK(upload(h, &h->d_colL, colL.data(), ncol));
+  CK(upload(h, &h->d_colR, colR.data(), ncol));
+  CK(upload(h, &h->d_rowF, rowF.data(), nrow));
+  CK(upload(h, &h->d_rowB, rowB.data(), nrow));
+  CK(upload(h, &h->d_sattop, h->h_top_cell.data(), ncell));
+  CK(cudaStreamSynchronize(h->stream));
+  return MPRW_OK;
+}
+
+int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *f) {
+  if (!h) return MPRW_E_INVAL;
+  if (!f || !f->ia || !f->ja || !f->flowja || !f->porosity || !f->retardation || !f->iboundts || !f->alpha_l ||
+      !f->alpha_t || !f->dm_eff)
+    return fail(h, MPRW_E_INVAL, "mprw_load_flow: missing required array");
+  const int64_t nc = h->g.ncell;
+  if (f->nja < nc || f->ia[0] != 1 || f->ia[nc] - 1 != f->nja)
+    return fail(h, MPRW_E_INVAL, "mprw_load_flow: IA/JA inconsistent with the grid");
+  for (int64_t c = 0; c < nc; ++c) {
+    if (f->porosity[c] <= 0.0 || f->retardation[c] <= 0.0)
+      return fail(h, MPRW_E_INVAL, "mprw_load_flow: porosity and retardation must be > 0");
+  }
+  for (int64_t p = 0; p < f->nja; ++p)
+    if (f->ja[p] < 1 || f->ja[p] > nc) return fail(h, MPRW_E_INVAL, "mprw_load_flow: JA entry out of range");
+  const size_t nd = f->uniform_dispersion ? 1 : (size_t)nc;
+  CK(upload(h, &h->d_ia, f->ia, nc + 1));
+  CK(upload(h, &h->d_ja, f->ja, f->nja));
+  CK(upload(h, &h->d_flowja, f->flowja, f->nja));
+  if (f->boundary_flows) CK(upload(h, &h->d_bflow, f->boundary_flows, 6 * nc));
+  CK(upload(h, &h->d_por, f->porosity, nc));
+  CK(upload(h, &h->d_ret, f->retardation, nc));
+  CK(upload(h, &h->d_ibts, f->iboundts, nc));
+  if (f->icboundts) CK(upload(h, &h->d_icb, f->icboundts, nc));
+  if (f->heads) CK(upload(h, &h->d_heads, f->heads, nc));
+  if (f->celltype) CK(upload(h, &h->d_ctype, f->celltype, nc));
+  if (f->source_flow) CK(upload(h, &h->d_src, f->source_flow, nc));
+  if (f->sink_flow) CK(upload(h, &h->d_snk, f->sink_flow, nc));
+  if (f->zones) CK(upload(h, &h->d_zones, f->zones, nc));
+  CK(upload(h, &h->d_aL, f->alpha_l, nd));
+  CK(upload(h, &h->d_aT, f->alpha_t, nd));
+  CK(upload(h, &h->d_dm, f->dm_eff, nd));
+  // SaturatedTop (FlowModelData.f90:258-279) for ConvertToModelXYZ
+  std::vector<double> sat(h->h_top_cell);
+  {
+    std::vector<double> botm(nc);
+    CK(cudaMemcpyAsync(botm.data(), h->d_botm, sizeof(double) * nc, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (f->celltype && f->heads)
+      for (int64_t c = 0; c < nc; ++c)
+        if (f->celltype[c] == 1 && f->iboundts[c] != 0 && f->heads[c] <= h->h_top_cell[c] && f->heads[c] >= botm[c])
+          sat[c] = f->heads[c];
+  }
+  CK(cudaMemcpyAsync(h->d_sattop, sat.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, h->stream));
+  if (!h->base.q) {
+    CK(dalloc(&h->base.q, 6 * nc));
+    CK(dalloc(&h->base.dz, nc));
+    CK(dalloc(&h->base.conn, 6 * nc));
+    CK(dalloc(&h->base.flags, nc));
+    CK(dalloc(&h->d_massb, nc));
+    if (h->opt.precision == MPRW_FP64) CK(dalloc(&h->d_rec64, nc));
+    else CK(dalloc(&h->d_rec32, nc));
+  }
+  PrepInputs in{};
+  in.g = h->g;
+  in.delr = h->d_delr;
+  in.delc = h->d_delc;
+  in.top = h->d_top;
+  in.botm = h->d_botm;
+  in.ia = h->d_ia;
+  in.ja = h->d_ja;
+  in.flowja = h->d_flowja;
+  in.bflow = f->boundary_flows ? h->d_bflow : nullptr;
+  in.porosity = h->d_por;
+  in.retardation = h->d_ret;
+  in.iboundts = h->d_ibts;
+  in.icboundts = f->icboundts ? h->d_icb : nullptr;
+  in.default_icbound = f->default_icbound;
+  in.heads = f->heads ? h->d_heads : nullptr;
+  in.celltype = f->celltype ? h->d_ctype : nullptr;
+  in.source_flow = f->source_flow ? h->d_src : nullptr;
+  in.sink_flow = f->sink_flow ? h->d_snk : nullptr;
+  in.zones = f->zones ? h->d_zones : nullptr;
+  in.alpha_l = h->d_aL;
+  in.alpha_t = h->d_aT;
+  in.dm_eff = h->d_dm;
+  in.uniform_dispersion = f->uniform_dispersion;
+  in.steady_state = f->steady_state;
+  in.time_step_kind = h->opt.time_step_kind;
+  in.ts_param0 = h->opt.ts_param[0];
+  in.ts_param1 = h->opt.ts_param[1];
+  in.backward = h->opt.backward;
+  in.stop_weak_sinks = h->opt.stop_weak_sinks;
+  in.stop_weak_sources = h->opt.stop_weak_sources;
+  in.stop_zone = h->opt.stop_zone;
+  in.uniform_porosity = h->opt.uniform_porosity;
+  CK(cudaEventRecord(h->ev2, h->stream));
+  CK(launch_prep(in, h->base, h->d_massb, h->d_rec64, h->d_rec32, h->stream));
+  CK(cudaEventRecord(h->ev3, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, h->ev2, h->ev3));
+  h->prep_ms = ms;
+  h->flow_loaded = true;
+  return MPRW_OK;
+}
+
+int mprw_set_particles(mprw_handle *h, int64_t n, const int32_t *cell, const double *lx, const double *ly,
+                       const double *lz, const double *t, const int32_t *status, const double *mass,
+                       const uint64_t *id, const uint64_t *rng_ctr) {
+  if (!h) return MPRW_E_INVAL;
+  if (n < 0 || n >= ((int64_t)1 << 32)) return fail(h, MPRW_E_INVAL, "particle count out of range");
+  if (n > 0 && (!cell || !lx || !ly || !lz || !t || !status))
+    return fail(h, MPRW_E_INVAL, "mprw_set_particles: missing required array");
+  for (int64_t p = 0; p < n; ++p)
+    if (cell[p] < 1 || cell[p] > h->g.ncell) return fail(h, MPRW_E_INVAL, "particle cell number out of range");
+  const bool mixed = h->opt.precision == MPRW_MIXED;
+  const size_t rs = mixed ? sizeof(float) : sizeof(double);
+  if (n > h->cap) {
+    size_t c = (size_t)n;
+    CK(dalloc(&h->d_cell, c));
+    CK(dalloc(&h->d_status, c));
+    CK(dalloc((char **)&h->d_x, c * rs));
+    CK(dalloc((char **)&h->d_y, c * rs));
+    CK(dalloc((char **)&h->d_z, c * rs));
+    CK(dalloc(&h->d_t, c));
+    CK(dalloc(&h->d_mass, c));
+    CK(dalloc(&h->d_ctr, c));
+    CK(dalloc(&h->d_id, c));
+    CK(dalloc(&h->d_perm, c));
+    if (mixed) CK(dalloc(&h->d_stage, c));
+    h->cap = n;
+  }
+  h->n = n;
+  if (n == 0) return MPRW_OK;
+  cudaStream_t s = h->stream;
+  CK(cudaMemcpyAsync(h->d_cell, cell, 4 * n, cudaMemcpyHostToDevice, s));
+  cell_shift_kernel<<<grid1d(n), 256, 0, s>>>(h->d_cell, n, -1);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(h->d_status, status, 4 * n, cudaMemcpyHostToDevice, s));
+  const double *src[3] = {lx, ly, lz};
+  void *dst[3] = {h->d_x, h->d_y, h->d_z};
+  for (int a = 0; a < 3; ++a) {
+    if (mixed) {
+      CK(cudaMemcpyAsync(h->d_stage, src[a], 8 * n, cudaMemcpyHostToDevice, s));
+      f64_to_f32_kernel<<<grid1d(n), 256, 0, s>>>(h->d_stage, (float *)dst[a], n);
+      CK(cudaGetLastError());
+      CK(cudaStreamSynchronize(s));  // staging buffer reused
+    } else {
+      CK(cudaMemcpyAsync(dst[a], src[a], 8 * n, cudaMemcpyHostToDevice, s));
+    }
+  }
+  CK(cudaMemcpyAsync(h->d_t, t, 8 * n, cudaMemcpyHostToDevice, s));
+  h->unit_mass = true;
+  if (mass) {
+    for (int64_t p = 0; p < n && h->unit_mass; ++p) h->unit_mass = (mass[p] == 1.0);
+    CK(cudaMemcpyAsync(h->d_mass, mass, 8 * n, cudaMemcpyHostToDevice, s));
+  }
+  h->has_id = id != nullptr;
+  if (id) CK(cudaMemcpyAsync(h->d_id, id, 8 * n, cudaMemcpyHostToDevice, s));
+  if (rng_ctr) CK(cudaMemcpyAsync(h->d_ctr, rng_ctr, 8 * n, cudaMemcpyHostToDevice, s));
+  else CK(cudaMemsetAsync(h->d_ctr, 0, 8 * n, s));
+  CK(cudaStreamSynchronize(s));
+  return MPRW_OK;
+}
+
+int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_done) {
+  if (!h) return MPRW_E_INVAL;
+  if (!h->flow_loaded) return fail(h, MPRW_E_STATE, "mprw_advance before mprw_load_flow");
+  if (!(t_end >= t_begin)) return fail(h, MPRW_E_INVAL, "t_end < t_begin");
+  h->launches = 0;
+  if (h->n == 0) {
+    if (steps_done) *steps_done = 0;
+    return MPRW_OK;
+  }
+  cudaStream_t s = h->stream;
+  if (h->sort_enabled) {
+    CK(sort_cells(h->d_cell, h->d_perm, h->n, h->ncell_bits, &h->scratch, &h->scratch_bytes, s));
+    h->launches += 2;
+  }
+  CK(cudaMemsetAsync(h->d_counters, 0, 4 * sizeof(unsigned long long), s));
+  const bool mixed = h->opt.precision == MPRW_MIXED;
+  const int threads = kStepThreads;
+  CK(cudaEventRecord(h->ev0, s));
+  if (mixed) {
+    AdvanceArgs<float> a{};
+    a.recs = h->d_rec32;
+    a.iboundts = h->d_ibts;
+    a.cellflags = h->base.flags;
+    a.cell = h->d_cell;
+    a.status = h->d_status;
+    a.x = (float *)h->d_x;
+    a.y = (float *)h->d_y;
+    a.z = (float *)h->d_z;
+    a.t = h->d_t;
+    a.ctr = h->d_ctr;
+    a.id = h->has_id ? h->d_id : nullptr;
+    a.perm = h->sort_enabled ? h->d_perm : nullptr;
+    a.queue = h->d_counters;
+    a.steps = h->d_counters + 1;
+    a.n = h->n;
+    a.t_begin = t_begin;
+    a.t_end = t_end;
+    a.ndim = h->ndim;
+    a.d1 = h->d1;
+    a.d2 = h->d2;
+    a.seed = h->opt.rng_seed;
+    int blocks = h->sms * 2;
+    int64_t need = (h->n + threads - 1) / threads;
+    if (need < blocks) blocks = (int)need;
+    CK(launch_advance<float>(a, blocks, threads, s));
+  } else {
+    AdvanceArgs<double> a{};
+    a.recs = h->d_rec64;
+    a.iboundts = h->d_ibts;
+    a.cellflags = h->base.flags;
+    a.cell = h->d_cell;
+    a.status = h->d_status;
+    a.x = (double *)h->d_x;
+    a.y = (double *)h->d_y;
+    a.z = (double *)h->d_z;
+    a.t = h->d_t;
+    a.ctr = h->d_ctr;
+    a.id = h->has_id ? h->d_id : nullptr;
+    a.perm = h->sort_enabled ? h->d_perm : nullptr;
+    a.queue = h->d_counters;
+    a.steps = h->d_counters + 1;
+    a.n = h->n;
+    a.t_begin = t_begin;
+    a.t_end = t_end;
+    a.ndim = h->ndim;
+    a.d1 = h->d1;
+    a.d2 = h->d2;
+    a.seed = h->opt.rng_seed;
+    int blocks = h->sms * 1;
+    int64_t need = (h->n + threads - 1) / threads;
+    if (need < blocks) blocks = (int)need;
+    CK(launch_advance<double>(a, blocks, threads, s));
+  }
+  h->launches += 1;
+  CK(cudaEventRecord(h->ev1, s));
+  CK(cudaMemcpyAsync(h->h_counters, h->d_counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  h->step_ms = ms;
+  if (steps_done) *steps_done = (int64_t)h->h_counters[1];
+  return MPRW_OK;
+}
+
+int mprw_get_particles(mprw_handle *h, int32_t *cell, double *lx, double *ly, double *lz, double *t,
+                       int32_t *status, uint64_t *rng_ctr, double *gx, double *gy, double *gz) {
+  if (!h) return MPRW_E_INVAL;
+  const int64_t n = h->n;
+  if (n == 0) return MPRW_OK;
+  cudaStream_t s = h->stream;
+  const bool mixed = h->opt.precision == MPRW_MIXED;
+  if (cell) {
+    CK(cudaMemcpyAsync(cell, h->d_cell, 4 * n, cudaMemcpyDeviceToHost, s));
+  }
+  double *outs[3] = {lx, ly, lz};
+  void *srcs[3] = {h->d_x, h->d_y, h->d_z};
+  for (int a = 0; a < 3; ++a) {
+    if (!outs[a]) continue;
+    if (mixed) {
+      if (!h->d_stage) CK(dalloc(&h->d_stage, h->cap));
+      f32_to_f64_kernel<<<grid1d(n), 256, 0, s>>>((const float *)srcs[a], h->d_stage, n);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(outs[a], h->d_stage, 8 * n, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+    } else {
+      CK(cudaMemcpyAsync(outs[a], srcs[a], 8 * n, cudaMemcpyDeviceToHost, s));
+    }
+  }
+  if (t) CK(cudaMemcpyAsync(t, h->d_t, 8 * n, cudaMemcpyDeviceToHost, s));
+  if (status) CK(cudaMemcpyAsync(status, h->d_status, 4 * n, cudaMemcpyDeviceToHost, s));
+  if (rng_ctr) CK(cudaMemcpyAsync(rng_ctr, h->d_ctr, 8 * n, cudaMemcpyDeviceToHost, s));
+  if (gx || gy || gz) {
+    size_t arr = ((size_t)n * 8 + 255) / 256 * 256;
+    if (h->scratch_bytes < 3 * arr) {
+      if (h->scratch) cudaFree(h->scratch);
+      h->scratch = nullptr;
+      h->scratch_bytes = 0;
+      CK(cudaMalloc(&h->scratch, 3 * arr));
+      h->scratch_bytes = 3 * arr;
+    }
+    double *g0 = (double *)h->scratch, *g1 = (double *)((char *)h->scratch + arr),
+           *g2 = (double *)((char *)h->scratch + 2 * arr);
+    Geometry geo = geometry(h);
+    if (mixed)
+      CK(launch_global_xyz<float>(geo, n, h->d_cell, (const float *)h->d_x, (const float *)h->d_y,
+                                  (const float *)h->d_z, g0, g1, g2, s));
+    else
+      CK(launch_global_xyz<double>(geo, n, h->d_cell, (const double *)h->d_x, (const double *)h->d_y,
+                                   (const double *)h->d_z, g0, g1, g2, s));
+    if (gx) CK(cudaMemcpyAsync(gx, g0, 8 * n, cudaMemcpyDeviceToHost, s));
+    if (gy) CK(cudaMemcpyAsync(gy, g1, 8 * n, cudaMemcpyDeviceToHost, s));
+    if (gz) CK(cudaMemcpyAsync(gz, g2, 8 * n, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  if (cell)
+    for (int64_t p = 0; p < n; ++p) cell[p] += 1;
+  return MPRW_OK;
+}
+
+int mprw_histogram(mprw_handle *h, const double origin[3], const double bin_size[3], const int32_t n_bins[3],
+                   double *counts, int64_t *n_binned, double *eff_mass) {
+  if (!h) return MPRW_E_INVAL;
+  if (!origin || !bin_size || !n_bins || !counts) return fail(h, MPRW_E_INVAL, "mprw_histogram: null argument");
+  int64_t nbins = 1;
+  HistArgs a{};
+  for (int d = 0; d < 3; ++d) {
+    if (n_bins[d] < 1) return fail(h, MPRW_E_INVAL, "mprw_histogram: n_bins must be >= 1");
+    if (bin_size[d] < 0.0) return fail(h, MPRW_E_INVAL, "mprw_histogram: bin_size must be >= 0");
+    nbins *= n_bins[d];
+    a.origin[d] = origin[d];
+    a.bin[d] = bin_size[d];
+    a.inv_bin[d] = bin_size[d] > 0 ? 1.0 / bin_size[d] : 0.0;
+    a.nb[d] = n_bins[d];
+    a.active_dim[d] = bin_size[d] != 0.0;
+  }
+  if (nbins > ((int64_t)1 << 31)) return fail(h, MPRW_E_INVAL, "mprw_histogram: too many bins");
+  cudaStream_t s = h->stream;
+  const int64_t n = h->n;
+  a.geo = geometry(h);
+  a.n = n;
+  a.cell = h->d_cell;
+  a.status = h->d_status;
+  a.x = h->d_x;
+  a.y = h->d_y;
+  a.z = h->d_z;
+  a.mixed = h->opt.precision == MPRW_MIXED;
+  a.nbinned = h->d_counters + 2;
+  h->launches = 0;
+  // device output buffer
+  size_t cbytes = ((size_t)nbins * 8 + 255) / 256 * 256;
+  CK(cudaEventRecord(h->ev2, s));
+  double total = 0, sw2 = 0, eff = 1.0;
+  int64_t nb_out = 0;
+  if (h->unit_mass) {
+    size_t need = cbytes + (size_t)nbins * 4 + 256;
+    if (h->scratch_bytes < need) {
+      if (h->scratch) cudaFree(h->scratch);
+      h->scratch = nullptr;
+      h->scratch_bytes = 0;
+      CK(cudaMalloc(&h->scratch, need));
+      h->scratch_bytes = need;
+    }
+    double *dcounts = (double *)h->scratch;
+    unsigned int *c32 = (unsigned int *)((char *)h->scratch + cbytes);
+    CK(cudaMemsetAsync(c32, 0, (size_t)nbins * 4, s));
+    CK(cudaMemsetAsync(h->d_counters + 2, 0, sizeof(unsigned long long), s));
+    a.counts32 = c32;
+    CK(launch_hist_unit(a, s));
+    CK(launch_u32_to_f64(c32, dcounts, nbins, s));
+    h->launches += 2;
+    CK(cudaMemcpyAsync(counts, dcounts, 8 * (size_t)nbins, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h->h_counters + 2, h->d_counters + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(h->ev3, s));
+    CK(cudaStreamSynchronize(s));
+    nb_out = (int64_t)h->h_counters[2];
+    // active count: unit weights => totalMass = nActive, Kish nEff = nActive, effMass = 1
+    eff = 1.0;
+  } else {
+    // per-particle bins, then order-preserving sums
+    size_t arr = ((size_t)n * 8 + 255) / 256 * 256;
+    void *tmp = nullptr;
+    CK(cudaMalloc(&tmp, arr + cbytes));
+    int64_t *bin_of = (int64_t *)tmp;
+    double *dcounts = (double *)((char *)tmp + arr);
+    a.bin_of = bin_of;
+    cudaError_t e = launch_hist_bins(a, s);
+    if (e == cudaSuccess)
+      e = ordered_bin_sums(bin_of, h->d_mass, h->d_status, n, nbins, dcounts, &total, &sw2, &h->scratch,
+                           &h->scratch_bytes, s);
+    if (e == cudaSuccess && total != 0.0) {
+      double neff = total * total / sw2;  // Kish (Histogram.F90:338-340)
+      eff = total / neff;
+      div_kernel<<<grid1d(nbins), 256, 0, s>>>(dcounts, nbins, eff);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(counts, dcounts, 8 * (size_t)nbins, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaEventRecord(h->ev3, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(tmp);
+    CK(e);
+    h->launches += 5;
+    nb_out = -1;
+  }
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, h->ev2, h->ev3));
+  h->hist_ms = ms;
+  if (n_binned) *n_binned = nb_out;
+  if (eff_mass) *eff_mass = eff;
+  return MPRW_OK;
+}
+
+int mprw_set_stream(mprw_handle *h, void *stream) {
+  if (!h) return MPRW_E_INVAL;
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return MPRW_OK;
+}
+
+int mprw_last_timings(mprw_handle *h, double *step_ms, double *prep_ms, double *hist_ms, int64_t *launches) {
+  if (!h) return MPRW_E_INVAL;
+  if (step_ms) *step_ms = h->step_ms;
+  if (prep_ms) *prep_ms = h->prep_ms;
+  if (hist_ms) *hist_ms = h->hist_ms;
+  if (launches) *launches = h->launches;
+  return MPRW_OK;
+}
+
+int mprw_destroy(mprw_handle *h) {
+  if (!h) return MPRW_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_all(h);
+  delete h;
+  return MPRW_OK;
+}
+
+const char *mprw_last_error(const mprw_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+}  // extern "C"

@@ -1,0 +1,95 @@
+// mprw_kernels.cuh -- kernel argument blocks and launch wrappers.
+#pragma once
+#include "mprw_common.cuh"
+
+namespace mprw {
+
+constexpr int kStepThreads = 256;
+
+template <typename R>
+struct AdvanceArgs {
+  const CellRec<R> *recs;
+  const int32_t *iboundts;
+  const uint8_t *cellflags;  // CellBase::flags
+  int32_t *cell;             // 0-based
+  int32_t *status;
+  R *x, *y, *z;
+  double *t;
+  uint64_t *ctr;
+  const uint64_t *id;        // may be null: id = index
+  const uint32_t *perm;      // processing order (cell-sorted) or null
+  unsigned long long *queue; // work counter, zeroed before launch
+  unsigned long long *steps; // particle-step counter
+  int64_t n;
+  double t_begin, t_end;
+  int ndim, d1, d2;
+  uint64_t seed;
+};
+
+template <typename R>
+cudaError_t launch_advance(const AdvanceArgs<R> &a, int blocks, int threads, cudaStream_t s);
+template <typename R>
+size_t advance_smem_bytes(int threads);
+
+// ---- prep (prep.cu) -------------------------------------------------------
+struct PrepInputs {
+  GridDims g;
+  const double *delr, *delc, *top, *botm;
+  const int32_t *ia, *ja;
+  const double *flowja, *bflow;
+  const double *porosity, *retardation;
+  const int32_t *iboundts, *icboundts;
+  int32_t default_icbound;
+  const double *heads;
+  const int32_t *celltype;
+  const double *source_flow, *sink_flow;
+  const int32_t *zones;
+  const double *alpha_l, *alpha_t, *dm_eff;
+  int32_t uniform_dispersion, steady_state;
+  // options
+  int32_t time_step_kind;
+  double ts_param0, ts_param1;
+  int32_t backward, stop_weak_sinks, stop_weak_sources, stop_zone, uniform_porosity;
+};
+
+cudaError_t launch_prep(const PrepInputs &in, CellBase base, uint8_t *massb, CellRec<double> *rec64,
+                        CellRec<float> *rec32, cudaStream_t s);
+
+// ---- geometry / histogram (hist.cu) --------------------------------------
+struct Geometry {
+  const double *col_left, *col_right;   // ncol  (GetLeft / GetRight)
+  const double *row_front, *row_back;   // nrow  (GetFront / GetBack)
+  const double *botm, *sattop;          // ncell
+  GridDims g;
+};
+
+template <typename R>
+cudaError_t launch_global_xyz(const Geometry &geo, int64_t n, const int32_t *cell, const R *x, const R *y,
+                              const R *z, double *gx, double *gy, double *gz, cudaStream_t s);
+
+struct HistArgs {
+  Geometry geo;
+  int64_t n;
+  const int32_t *cell, *status;
+  const void *x, *y, *z;  // R per precision
+  int mixed;
+  double origin[3], bin[3], inv_bin[3];
+  int32_t nb[3];
+  int active_dim[3];
+  unsigned int *counts32;  // unit-mass path (zeroed)
+  int64_t *bin_of;         // ordered path: per particle bin (or -1), may be null
+  unsigned long long *nbinned;
+};
+
+cudaError_t launch_hist_unit(const HistArgs &a, cudaStream_t s);
+cudaError_t launch_hist_bins(const HistArgs &a, cudaStream_t s);
+cudaError_t launch_u32_to_f64(const unsigned int *in, double *out, int64_t n, cudaStream_t s);
+
+// Ordered (order-preserving) weighted sums: sort.cu
+cudaError_t ordered_bin_sums(const int64_t *bin_of, const double *mass, const int32_t *status, int64_t n,
+                             int64_t nbins, double *counts, double *total_mass, double *sum_w2,
+                             void **scratch, size_t *scratch_bytes, cudaStream_t s);
+cudaError_t sort_cells(const int32_t *cell, uint32_t *perm, int64_t n, int ncell_bits, void **scratch,
+                       size_t *scratch_bytes, cudaStream_t s);
+
+}  // namespace mprw

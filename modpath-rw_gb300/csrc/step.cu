@@ -1,0 +1,592 @@
+// step.cu -- the random-walk particle-tracking step kernel.
+//
+// One persistent kernel advances every particle to the end of the tracking
+// interval.  Each lane runs a flat state machine, one time-loop pass per
+// iteration of its main loop:
+//   fetch particle -> release checks -> enter cell (stage the cell record in
+//   shared memory, entry checks) -> time-loop passes -> exit / stop / store
+// so lanes of a warp stay on the common step body no matter which particle,
+// cell or phase each one is in.  Particles are taken from an atomic queue in
+// cell-sorted order (perm[]), which keeps the records a warp reads in cache.
+//
+// Per-pass logic restates pr_ExecuteRandomWalkParticleTracking
+// (TrackSubCell.F90:812-1373) with the quadratic exit-face solver of the
+// EULERIAN advection model (TrackSubCell.F90:1576-1892); the cell-to-cell
+// logic restates pr_RWPTrackPath (ParticleTrackingEngine.f90:1051-1254),
+// TrackCell (TrackCell.f90:375-669) and ConvertFromNeighbor
+// (RectangularGridDisMf6.f90:50-108).  Interpolants are evaluated from the
+// monomial coefficients the prep kernel stores, with fused multiply-adds.
+#include "mprw_common.cuh"
+#include "mprw_kernels.cuh"
+
+namespace mprw {
+
+// Shared-memory view of one lane's record: field f at sm[f*stride + lane],
+// conflict-free for a warp reading the same field.
+enum : int {
+  F_V1 = 0, F_DV = 3, F_D = 6, F_INVD = 9, F_DIV = 12, F_VB = 33,
+  F_AL = 57, F_AT = 58, F_DM = 59, F_2R = 60, F_V2 = 61, NFIELDS = 64
+};
+
+template <typename R>
+struct Lane {
+  R *p;
+  int stride;
+  __device__ __forceinline__ R operator()(int f) const { return p[f * stride]; }
+};
+
+template <typename R>
+__device__ __forceinline__ void stage_record(const CellRec<R> *__restrict__ recs, int32_t c, R *sm,
+                                             int stride) {
+  const R *src = reinterpret_cast<const R *>(recs + c);
+#pragma unroll 8
+  for (int f = 0; f < NFIELDS; ++f) sm[f * stride] = __ldg(src + f);
+}
+
+template <typename R>
+__device__ __forceinline__ R tril(const Lane<R> &F, int base, R x, R y, R z, R xy, R xz, R yz, R xyz) {
+  R a = F(base + 0);
+  a = fma(F(base + 1), x, a);
+  a = fma(F(base + 2), y, a);
+  a = fma(F(base + 3), z, a);
+  a = fma(F(base + 4), xy, a);
+  a = fma(F(base + 5), xz, a);
+  a = fma(F(base + 6), yz, a);
+  a = fma(F(base + 7), xyz, a);
+  return a;
+}
+
+template <typename R>
+__device__ __forceinline__ R divc(const Lane<R> &F, int base, R x, R y, R z, R xy, R xz, R yz) {
+  R a = F(base + 0);
+  a = fma(F(base + 1), x, a);
+  a = fma(F(base + 2), y, a);
+  a = fma(F(base + 3), z, a);
+  a = fma(F(base + 4), xy, a);
+  a = fma(F(base + 5), xz, a);
+  a = fma(F(base + 6), yz, a);
+  return a;
+}
+
+template <typename R>
+__device__ __forceinline__ R rnorm_draw(uint64_t seed, uint64_t id, uint64_t &ctr) {
+  return (R)normal_ih12(seed, id, ctr);
+}
+
+// pr_DisplacementRandomDischarge (3-D :2821-2928, 2-D :2931-3028, 1-D :3031-3113)
+template <typename R>
+__device__ __forceinline__ void random_displacement(const Lane<R> &F, int ndim, int d1, int d2, R x, R y,
+                                                    R z, uint64_t seed, uint64_t id, uint64_t &ctr, R &bx,
+                                                    R &by, R &bz) {
+  const R zero = R(0);
+  R xy = x * y, xz = x * z, yz = y * z, xyz = xy * z;
+  R aL = F(F_AL), aT = F(F_AT), dm = F(F_DM), tr = F(F_2R);
+  if (ndim == 3) {
+    R vx = tril(F, F_VB + 0, x, y, z, xy, xz, yz, xyz);
+    R vy = tril(F, F_VB + 8, x, y, z, xy, xz, yz, xyz);
+    R vz = tril(F, F_VB + 16, x, y, z, xy, xz, yz, xyz);
+    R nxy2 = fma(vx, vx, vy * vy);
+    R n2 = fma(vz, vz, nxy2);
+    R B11 = zero, B12 = zero, B13 = zero, B21 = zero, B22 = zero, B23 = zero, B31 = zero, B32 = zero;
+    if (n2 > zero) {
+      R inv = rsqrt(n2);
+      R nrm = n2 * inv;
+      R sL = sqrt(tr * fma(aL, nrm, dm));
+      R sT = sqrt(tr * fma(aT, nrm, dm));
+      R sLi = sL * inv;
+      B11 = vx * sLi;
+      B21 = vy * sLi;
+      B31 = vz * sLi;
+      if (nxy2 > zero) {
+        R invxy = rsqrt(nxy2);
+        R nxy = nxy2 * invxy;
+        R sTi = sT * inv;
+        B32 = nxy * sTi;
+        R sTixy = sTi * invxy;
+        B12 = -(vx * vz) * sTixy;
+        B22 = -(vy * vz) * sTixy;
+        R sTxy = sT * invxy;
+        B13 = -vy * sTxy;
+        B23 = vx * sTxy;
+      }
+    }
+    R rx = rnorm_draw<R>(seed, id, ctr);
+    R ry = rnorm_draw<R>(seed, id, ctr);
+    R rz = rnorm_draw<R>(seed, id, ctr);
+    bx = fma(B13, rz, fma(B12, ry, B11 * rx));
+    by = fma(B23, rz, fma(B22, ry, B21 * rx));
+    bz = fma(B32, ry, B31 * rx);
+  } else if (ndim == 2) {
+    R v1 = tril(F, F_VB + 8 * d1, x, y, z, xy, xz, yz, xyz);
+    R v2 = tril(F, F_VB + 8 * d2, x, y, z, xy, xz, yz, xyz);
+    R n2 = fma(v1, v1, v2 * v2);
+    R B11 = zero, B12 = zero, B21 = zero, B22 = zero;
+    if (n2 > zero) {
+      R inv = rsqrt(n2);
+      R nrm = n2 * inv;
+      R sLi = sqrt(tr * fma(aL, nrm, dm)) * inv;
+      R sTi = sqrt(tr * fma(aT, nrm, dm)) * inv;
+      B11 = v1 * sLi;
+      B21 = v2 * sLi;
+      B12 = -v2 * sTi;
+      B22 = v1 * sTi;
+    }
+    R r1 = rnorm_draw<R>(seed, id, ctr);
+    R r2 = rnorm_draw<R>(seed, id, ctr);
+    R o1 = fma(B12, r2, B11 * r1), o2 = fma(B22, r2, B21 * r1);
+    bx = zero; by = zero; bz = zero;
+    if (d1 == 0) bx = o1; else if (d1 == 1) by = o1; else bz = o1;
+    if (d2 == 0) bx = o2; else if (d2 == 1) by = o2; else bz = o2;
+  } else {
+    R v1 = tril(F, F_VB + 8 * d1, x, y, z, xy, xz, yz, xyz);
+    R nrm = fabs(v1);
+    R B11 = zero;
+    if (nrm > zero) B11 = sqrt(tr * fma(aL, nrm, dm));
+    R r1 = rnorm_draw<R>(seed, id, ctr);
+    bx = zero; by = zero; bz = zero;
+    R o1 = B11 * r1;
+    if (d1 == 0) bx = o1; else if (d1 == 1) by = o1; else bz = o1;
+  }
+}
+
+// One axis of pr_DetectExitFaceAndUpdateTimeStepQuadratic (:1622-1710).
+// Returns true when the routine must return at once (exitFace, dt set).
+template <typename R>
+__device__ __forceinline__ bool quad_axis(R npos, R pos, R d, R v, R divD, R dB, int faceLo, int faceHi,
+                                          double dt, R &dtaxis, int &exitAxis, int &exitFace,
+                                          double &dtout) {
+  const R zero = R(0), one = R(1);
+  R dI;
+  if (npos > one) {
+    dI = d * (one - pos);
+    exitAxis = faceHi;
+  } else {
+    dI = -d * pos;
+    exitAxis = faceLo;
+  }
+  if (dI == zero) {
+    exitFace = exitAxis;
+    dtout = 0.0;
+    return true;
+  }
+  R A = v + divD, B = dB;
+  R arg = B * B + R(4) * dI * A;
+  if ((arg >= zero) && (A != zero)) {
+    R zs = sqrt(arg);
+    R z1 = (-B + zs) / (R(2) * A);
+    R z2 = (-B - zs) / (R(2) * A);
+    if (z1 > zero || z2 > zero) {
+      R zm = (z1 > zero && z2 > zero) ? (z1 < z2 ? z1 : z2) : (z1 > zero ? z1 : z2);
+      dtaxis = zm * zm;
+      if (dtaxis == zero) {
+        exitFace = exitAxis;
+        dtout = 0.0;
+        return true;
+      }
+    } else if (z1 == zero || z2 == zero) {
+      exitFace = exitAxis;
+      dtout = 0.0;
+      return true;
+    }
+  } else if (A == zero) {
+    if (B != zero) {
+      R q = dI / B;
+      dtaxis = q * q;
+      if (dtaxis == zero) {
+        exitFace = exitAxis;
+        dtout = 0.0;
+        return true;
+      }
+    }
+  }
+  if ((double)dtaxis > dt) dtaxis = zero;
+  return false;
+}
+
+template <typename R>
+struct Visit {
+  R x, y, z;     // current local position (TrackSubCell x,y,z)
+  R ix, iy, iz;  // cell-entry location (initialLocation)
+  double t, tinit, dtcell;
+  R sqrt_dtcell;
+  int exitFace, posRestart;
+  bool reachedMax;
+  int64_t passes;
+};
+
+enum : int { PASS_CONTINUE = 0, PASS_MAXTIME = 1, PASS_EXIT = 2, PASS_UNDEFINED = 3 };
+
+#define MPRW_OUTSIDE(a, b, c) \
+  (((a) > one) || ((a) < zero) || ((b) > one) || ((b) < zero) || ((c) > one) || ((c) < zero))
+
+// One pass of the `do while (continueTimeLoop)` body, TrackSubCell.F90:956-1368.
+// On PASS_MAXTIME / PASS_EXIT the final location is (ox,oy,oz,V.t); on
+// PASS_UNDEFINED the caller uses the last recorded point.
+template <typename R>
+__device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double maxTime, int ndim, int d1, int d2,
+                       uint64_t seed, uint64_t id, uint64_t &ctr, R &ox, R &oy, R &oz) {
+  const R zero = R(0), one = R(1), half = R(0.5);
+  const double dtRed = (double)0.1f;  // dtReductionFactor, a single-precision literal (:850)
+  double dt = V.dtcell;
+  V.t = V.t + dt;
+  if (maxTime < V.t) {
+    V.t = V.t - dt;
+    dt = fmax(maxTime - V.t, 0.0);
+    V.t = maxTime;
+    V.reachedMax = true;
+  }
+  R x = V.x, y = V.y, z = V.z;
+  R dX = F(F_D + 0), dY = F(F_D + 1), dZ = F(F_D + 2);
+  R iX = F(F_INVD + 0), iY = F(F_INVD + 1), iZ = F(F_INVD + 2);
+  // pr_RWPTDisplacementsLinear (:673-706)
+  R vx = fma(x, F(F_DV + 0), F(F_V1 + 0));
+  R vy = fma(y, F(F_DV + 1), F(F_V1 + 1));
+  R vz = fma(z, F(F_DV + 2), F(F_V1 + 2));
+  R xy = x * y, xz = x * z, yz = y * z;
+  R ddx = divc(F, F_DIV + 0, x, y, z, xy, xz, yz);
+  R ddy = divc(F, F_DIV + 7, x, y, z, xy, xz, yz);
+  R ddz = divc(F, F_DIV + 14, x, y, z, xy, xz, yz);
+  R bx, by, bz;
+  random_displacement(F, ndim, d1, d2, x, y, z, seed, id, ctr, bx, by, bz);
+  R rdt = (R)dt;
+  R sdt = (dt == V.dtcell) ? V.sqrt_dtcell : sqrt(rdt);
+  R ax = vx * rdt, ay = vy * rdt, az = vz * rdt;
+  R dxrw = ax + ddx * rdt + bx * sdt;
+  R dyrw = ay + ddy * rdt + by * sdt;
+  R dzrw = az + ddz * rdt + bz * sdt;
+  // jump limiter (:989-1013)
+  while ((fabs(dxrw * iX) > half) || (fabs(dyrw * iY) > half) || (fabs(dzrw * iZ) > half)) {
+    V.t = V.t - dt;
+    dt = dtRed * dt;
+    rdt = (R)dt;
+    sdt = sqrt(rdt);
+    ax = vx * rdt; ay = vy * rdt; az = vz * rdt;
+    dxrw = ax + ddx * rdt + bx * sdt;
+    dyrw = ay + ddy * rdt + by * sdt;
+    dzrw = az + ddz * rdt + bz * sdt;
+    V.t = V.t + dt;
+    V.reachedMax = false;
+  }
+  R nx = x + dxrw * iX, ny = y + dyrw * iY, nz = z + dzrw * iZ;
+  // particleLeavingCell (:1025-1316)
+  int intLoop = 0;
+  while (MPRW_OUTSIDE(nx, ny, nz)) {
+    ++intLoop;
+    R dtx = zero, dty = zero, dtz = zero;
+    {
+      // ExitFaceAndUpdateTimeStep (quadratic, :1576-1892)
+      int efx = 0, efy = 0, efz = 0;
+      bool ret = false;
+      V.t = V.t - dt;
+      if (!ret && ((nx > one) || (nx < zero)))
+        ret = quad_axis(nx, x, dX, vx, ddx, bx, 1, 2, dt, dtx, efx, V.exitFace, dt);
+      if (!ret && ((ny > one) || (ny < zero)))
+        ret = quad_axis(ny, y, dY, vy, ddy, by, 3, 4, dt, dty, efy, V.exitFace, dt);
+      if (!ret && ((nz > one) || (nz < zero)))
+        ret = quad_axis(nz, z, dZ, vz, ddz, bz, 5, 6, dt, dtz, efz, V.exitFace, dt);
+      if (!ret) {
+        if (dtx == zero && dty == zero && dtz == zero) {
+          V.t = V.t + dt;
+        } else {
+          int im = -1;
+          R best = zero;
+          if (dtx > zero) { im = 0; best = dtx; }
+          if (dty > zero && (im < 0 || dty < best)) { im = 1; best = dty; }
+          if (dtz > zero && (im < 0 || dtz < best)) { im = 2; best = dtz; }
+          dt = (double)best;
+          V.exitFace = (im == 0) ? efx : (im == 1 ? efy : efz);
+          V.t = V.t + dt;
+        }
+      }
+    }
+    if (intLoop > 5) {
+      nx = V.ix; ny = V.iy; nz = V.iz;
+      V.t = V.tinit;
+      dt = V.dtcell;
+      if (++V.posRestart > 10) {
+        V.x = x; V.y = y; V.z = z;
+        return PASS_UNDEFINED;
+      }
+      break;
+    }
+    rdt = (R)dt;
+    sdt = sqrt(rdt);
+    ax = vx * rdt; ay = vy * rdt; az = vz * rdt;
+    V.reachedMax = false;
+    int ef = V.exitFace;
+    if (ef == 1 || ef == 2) {
+      nx = (ef == 1) ? zero : one;
+      dyrw = ay + ddy * rdt + by * sdt;
+      ny = y + dyrw * iY;
+      dzrw = az + ddz * rdt + bz * sdt;
+      nz = z + dzrw * iZ;
+    } else if (ef == 3 || ef == 4) {
+      dxrw = ax + ddx * rdt + bx * sdt;
+      nx = x + dxrw * iX;
+      ny = (ef == 3) ? zero : one;
+      dzrw = az + ddz * rdt + bz * sdt;
+      nz = z + dzrw * iZ;
+    } else if (ef == 5 || ef == 6) {
+      dxrw = ax + ddx * rdt + bx * sdt;
+      nx = x + dxrw * iX;
+      dyrw = ay + ddy * rdt + by * sdt;
+      ny = y + dyrw * iY;
+      nz = (ef == 5) ? zero : one;
+    } else {
+      nx = V.ix; ny = V.iy; nz = V.iz;
+      V.t = V.tinit;
+      dt = V.dtcell;
+      if (++V.posRestart > 10) {
+        V.x = x; V.y = y; V.z = z;
+        return PASS_UNDEFINED;
+      }
+      break;
+    }
+    if (MPRW_OUTSIDE(nx, ny, nz)) continue;
+    // elasticRebound (:1157-1312)
+    int rebound = 0;
+    while (V.exitFace > 0) {
+      if (!((massb >> (V.exitFace - 1)) & 1u)) break;
+      if (++rebound > 10) {
+        V.x = x; V.y = y; V.z = z;
+        return PASS_UNDEFINED;
+      }
+      R xi = nx, yi = ny, zi = nz;
+      if (dt == 0.0) {
+        nx = V.ix; ny = V.iy; nz = V.iz;
+        V.t = V.t - dt;
+        dt = V.dtcell;
+        V.exitFace = 0;
+        ++V.posRestart;
+        break;
+      }
+      V.t = V.t + dt;
+      if (maxTime < V.t) {
+        V.t = V.t - dt;
+        dt = fmax(maxTime - V.t, 0.0);
+        V.t = maxTime;
+        V.reachedMax = true;
+        rdt = (R)dt;
+        sdt = sqrt(rdt);
+        ax = vx * rdt; ay = vy * rdt; az = vz * rdt;
+        dxrw = ax + ddx * rdt + bx * sdt;
+        dyrw = ay + ddy * rdt + by * sdt;
+        dzrw = az + ddz * rdt + bz * sdt;
+      }
+      ef = V.exitFace;
+      if (ef == 1 || ef == 2) {
+        nx = nx - dxrw * iX; ny = ny + dyrw * iY; nz = nz + dzrw * iZ;
+      } else if (ef == 3 || ef == 4) {
+        nx = nx + dxrw * iX; ny = ny - dyrw * iY; nz = nz + dzrw * iZ;
+      } else {
+        nx = nx + dxrw * iX; ny = ny + dyrw * iY; nz = nz - dzrw * iZ;
+      }
+      if (MPRW_OUTSIDE(nx, ny, nz)) {
+        x = xi; y = yi; z = zi;
+        if (ef == 1 || ef == 2) { vx = -vx; ddx = -ddx; bx = -bx; }
+        else if (ef == 3 || ef == 4) { vy = -vy; ddy = -ddy; by = -by; }
+        else { vz = -vz; ddz = -ddz; bz = -bz; }
+        V.exitFace = 0;
+      } else {
+        dt = V.dtcell;
+        V.exitFace = 0;
+        if (nx == zero) V.exitFace = 1;
+        if (nx == one) V.exitFace = 2;
+        if (ny == zero) V.exitFace = 3;
+        if (ny == one) V.exitFace = 4;
+        if (nz == zero) V.exitFace = 5;
+        if (nz == one) V.exitFace = 6;
+      }
+    }
+  }
+  if (V.reachedMax) {
+    ox = nx; oy = ny; oz = nz;
+    return PASS_MAXTIME;
+  }
+  if (V.exitFace > 0) {
+    ox = nx; oy = ny; oz = nz;
+    return PASS_EXIT;
+  }
+  V.x = nx; V.y = ny; V.z = nz;
+  return PASS_CONTINUE;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kStepThreads) rwpt_advance_kernel(AdvanceArgs<R> a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  R *sm = reinterpret_cast<R *>(smraw) + threadIdx.x;
+  const int stride = blockDim.x;
+  Lane<R> F{sm, stride};
+  const R zero = R(0), one = R(1);
+
+  int64_t my_passes = 0;
+  int64_t p = -1;        // particle being tracked (index into the state arrays)
+  int32_t c = 0;         // current cell (0-based)
+  bool need_cell = false;
+  int32_t status = 0;
+  uint64_t id = 0, ctr = 0;
+  // last point of the pathline (cell, local coords, time)
+  int32_t lc = 0;
+  R lx = zero, ly = zero, lz = zero;
+  double lt = 0.0;
+  // location at cell entry
+  R ex = zero, ey = zero, ez = zero;
+  double et = 0.0;
+  Visit<R> V;
+  uint32_t massb = 0;
+  int32_t conn6[6];
+
+  for (;;) {
+    if (p < 0) {
+      int64_t q = (int64_t)atomicAdd(reinterpret_cast<unsigned long long *>(a.queue), 1ULL);
+      if (q >= a.n) break;
+      p = a.perm ? (int64_t)a.perm[q] : q;
+      status = a.status[p];
+      c = a.cell[p];
+      ex = a.x[p]; ey = a.y[p]; ez = a.z[p];
+      et = a.t[p];
+      // release checks, MPathRW.F90:1256-1302
+      if (status == ST_PENDING) {
+        if (et < a.t_begin) status = ST_UNRELEASED;
+        else if (et <= a.t_end) {
+          status = ST_ACTIVE;
+          if (a.iboundts[c] == 0) status = ST_INACTIVE;
+        }
+      }
+      if (status == ST_INACTIVE && (a.cellflags[c] & 2u)) status = ST_ACTIVE;  // partially dry
+      if (status != ST_ACTIVE) {
+        a.status[p] = status;
+        p = -1;
+        continue;
+      }
+      id = a.id ? a.id[p] : (uint64_t)p;
+      ctr = a.ctr[p];
+      lc = c; lx = ex; ly = ey; lz = ez; lt = et;
+      need_cell = true;
+    }
+    if (need_cell) {
+      need_cell = false;
+      int32_t fin = 0;  // 0 track, else final status
+      bool use_last = false;
+      if (ex < zero || ex > one || ey < zero || ey > one || ez < zero || ez > one) {
+        fin = ST_UNDEFINED;  // InvalidLocation (TrackCell.f90:410-413)
+        use_last = true;
+      } else {
+        const CellRec<R> *rec = a.recs + c;
+        int32_t es = rec->entry_status;
+        if (es != 0) {
+          fin = es;
+          use_last = (es == ST_UNDEFINED);
+        } else {
+          stage_record(a.recs, c, sm, stride);
+          massb = rec->massb;
+#pragma unroll
+          for (int f = 0; f < 6; ++f) conn6[f] = rec->conn[f];
+          V.x = ex; V.y = ey; V.z = ez;
+          V.ix = ex; V.iy = ey; V.iz = ez;
+          V.t = et; V.tinit = et;
+          V.dtcell = rec->dtcell;
+          V.sqrt_dtcell = (R)rec->sqrt_dtcell;
+          V.exitFace = 0;
+          V.posRestart = 0;
+          V.reachedMax = false;
+          V.passes = 0;
+        }
+      }
+      if (fin != 0) {
+        if (use_last) {
+          a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
+        } else {
+          a.cell[p] = c; a.x[p] = ex; a.y[p] = ey; a.z[p] = ez; a.t[p] = et;
+        }
+        a.status[p] = fin;
+        a.ctr[p] = ctr;
+        p = -1;
+        continue;
+      }
+    }
+    // one time-loop pass (with the per-visit safety cap)
+    R ox, oy, oz;
+    int r;
+    if (++V.passes > kMaxStepsPerVisit) {
+      r = PASS_UNDEFINED;
+    } else {
+      r = rw_pass(V, F, massb, a.t_end, a.ndim, a.d1, a.d2, a.seed, id, ctr, ox, oy, oz);
+      ++my_passes;
+    }
+    if (r == PASS_CONTINUE) continue;
+    if (r == PASS_MAXTIME) {
+      a.cell[p] = c; a.x[p] = ox; a.y[p] = oy; a.z[p] = oz; a.t[p] = V.t;
+      a.status[p] = ST_ACTIVE;
+      a.ctr[p] = ctr;
+      p = -1;
+      continue;
+    }
+    if (r == PASS_UNDEFINED) {
+      a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
+      a.status[p] = ST_UNDEFINED;
+      a.ctr[p] = ctr;
+      p = -1;
+      continue;
+    }
+    // PASS_EXIT: the exit point becomes the last pathline point
+    int face = V.exitFace;
+    lc = c; lx = ox; ly = oy; lz = oz; lt = V.t;
+    int32_t nc = conn6[face - 1];
+    if (nc < 0) {
+      a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
+      a.status[p] = ST_BOUNDARY;
+      a.ctr[p] = ctr;
+      p = -1;
+      continue;
+    }
+    // ConvertFromNeighbor: the exit coordinate must sit exactly on the face
+    bool bad = (face == 2 && ox != one) || (face == 1 && ox != zero) || (face == 4 && oy != one) ||
+               (face == 3 && oy != zero) || (face == 6 && oz != one) || (face == 5 && oz != zero);
+    if (bad) {
+      a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
+      a.status[p] = ST_UNDEFINED;
+      a.ctr[p] = ctr;
+      p = -1;
+      continue;
+    }
+    ex = ox; ey = oy; ez = oz; et = V.t;
+    if (face == 2) ex = zero;
+    if (face == 1) ex = one;
+    if (face == 4) ey = zero;
+    if (face == 3) ey = one;
+    if (face == 6) ez = zero;
+    if (face == 5) ez = one;
+    c = nc;
+    need_cell = true;
+  }
+  // block-level sum of passes, one atomic per block
+  __shared__ unsigned long long blk;
+  if (threadIdx.x == 0) blk = 0;
+  __syncthreads();
+  atomicAdd(&blk, (unsigned long long)my_passes);
+  __syncthreads();
+  if (threadIdx.x == 0) atomicAdd(reinterpret_cast<unsigned long long *>(a.steps), blk);
+}
+
+template <typename R>
+size_t advance_smem_bytes(int threads) {
+  return (size_t)NFIELDS * sizeof(R) * threads;
+}
+
+template <typename R>
+cudaError_t launch_advance(const AdvanceArgs<R> &a, int blocks, int threads, cudaStream_t s) {
+  size_t smem = advance_smem_bytes<R>(threads);
+  cudaError_t e = cudaFuncSetAttribute(rwpt_advance_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  rwpt_advance_kernel<R><<<blocks, threads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_advance<double>(const AdvanceArgs<double> &, int, int, cudaStream_t);
+template cudaError_t launch_advance<float>(const AdvanceArgs<float> &, int, int, cudaStream_t);
+template size_t advance_smem_bytes<double>(int);
+template size_t advance_smem_bytes<float>(int);
+
+}  // namespace mprw

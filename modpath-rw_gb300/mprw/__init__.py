@@ -1,0 +1,245 @@
+"""GB300 random-walk particle tracking (host side).
+
+``Tracker`` wraps the C ABI of ``libmprw_gpu.so`` (include/mprw_gpu.h) with
+ctypes, mirroring the reference's calls on the tracking path:
+
+=====================  ==========================================================
+``Tracker(grid, opt)``  trackingEngine%Initialize (ParticleTrackingEngine.f90:393)
+``load_flow(flow)``     FlowModelData%LoadTimeStep + per-cell buffers
+``set_particles(p)``    particle group arrays (Particle.f90:7-17)
+``advance(t0, t1)``     the OpenMP particle loop of MPathRW.F90:1207-1539
+``get_particles()``     particle state + ConvertToModelXYZ
+``histogram(...)``      Histogram%ComputeCountsWeighted (Histogram.F90:276-350)
+=====================  ==========================================================
+
+There is no CPU fallback: constructing a Tracker without the built library
+or without a CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .model import (ACTIVE, ADV, BOUNDARY, DISP, EULERIAN, EXPONENTIAL, FIXED, FP64, INACTIVE, MIN_ADV_DISP,
+                    MIXED, NO_EXIT, PENDING, STOP_ZONE, UNDEFINED, UNRELEASED, WEAK_SINK, WEAK_SOURCE, Flow,
+                    Grid, Options, Particles)
+
+LIB_PATH = Path(__file__).resolve().parent / "libmprw_gpu.so"
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_up = C.POINTER(C.c_uint64)
+
+
+class MprwError(RuntimeError):
+    pass
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("nlay", C.c_int32), ("nrow", C.c_int32), ("ncol", C.c_int32),
+                ("delr", _dp), ("delc", _dp), ("top", _dp), ("botm", _dp)]
+
+
+class OptionsDesc(C.Structure):
+    _fields_ = [("time_step_kind", C.c_int32), ("ts_param", C.c_double * 2), ("advection_kind", C.c_int32),
+                ("dim_mask", C.c_int32 * 3), ("dispersion_model", C.c_int32), ("stop_weak_sinks", C.c_int32),
+                ("stop_weak_sources", C.c_int32), ("backward", C.c_int32), ("stop_zone", C.c_int32),
+                ("uniform_porosity", C.c_int32), ("rng_seed", C.c_uint64), ("precision", C.c_int32)]
+
+
+class FlowDesc(C.Structure):
+    _fields_ = [("ia", _ip), ("ja", _ip), ("nja", C.c_int64), ("flowja", _dp), ("boundary_flows", _dp),
+                ("porosity", _dp), ("retardation", _dp), ("iboundts", _ip), ("icboundts", _ip),
+                ("default_icbound", C.c_int32), ("heads", _dp), ("celltype", _ip), ("source_flow", _dp),
+                ("sink_flow", _dp), ("zones", _ip), ("alpha_l", _dp), ("alpha_t", _dp), ("dm_eff", _dp),
+                ("uniform_dispersion", C.c_int32), ("steady_state", C.c_int32)]
+
+
+_lib = None
+
+
+def load_library() -> C.CDLL:
+    """Load libmprw_gpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise MprwError(f"{LIB_PATH} is missing: build it with mprw.build.build()")
+    lib = C.CDLL(str(LIB_PATH))
+    H = C.c_void_p
+    sig = {
+        "mprw_create": (C.c_int, [C.POINTER(H), C.POINTER(GridDesc), C.POINTER(OptionsDesc)]),
+        "mprw_load_flow": (C.c_int, [H, C.POINTER(FlowDesc)]),
+        "mprw_set_particles": (C.c_int, [H, C.c_int64, _ip, _dp, _dp, _dp, _dp, _ip, _dp, _up, _up]),
+        "mprw_advance": (C.c_int, [H, C.c_double, C.c_double, C.POINTER(C.c_int64)]),
+        "mprw_get_particles": (C.c_int, [H, _ip, _dp, _dp, _dp, _dp, _ip, _up, _dp, _dp, _dp]),
+        "mprw_histogram": (C.c_int, [H, _dp, _dp, _ip, _dp, C.POINTER(C.c_int64), _dp]),
+        "mprw_set_stream": (C.c_int, [H, C.c_void_p]),
+        "mprw_last_timings": (C.c_int, [H, _dp, _dp, _dp, C.POINTER(C.c_int64)]),
+        "mprw_destroy": (C.c_int, [H]),
+        "mprw_last_error": (C.c_char_p, [H]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _u64(a):
+    return np.ascontiguousarray(a, dtype=np.uint64)
+
+
+def _p(a, ptype):
+    return None if a is None else a.ctypes.data_as(ptype)
+
+
+class Tracker:
+    """One device-resident tracking engine (one C-ABI handle)."""
+
+    def __init__(self, grid: Grid, opt: Options):
+        self.lib = load_library()
+        self.grid = grid
+        self.opt = opt
+        self._keep = []
+        self._g = dict(delr=_f64(grid.delr), delc=_f64(grid.delc), top=_f64(grid.top), botm=_f64(grid.botm))
+        gd = GridDesc(grid.nlay, grid.nrow, grid.ncol, _p(self._g["delr"], _dp), _p(self._g["delc"], _dp),
+                      _p(self._g["top"], _dp), _p(self._g["botm"], _dp))
+        od = OptionsDesc()
+        od.time_step_kind = opt.time_step_kind
+        od.ts_param[0], od.ts_param[1] = float(opt.ts_param[0]), float(opt.ts_param[1])
+        od.advection_kind = opt.advection_kind
+        for d in range(3):
+            od.dim_mask[d] = int(opt.dim_mask[d])
+        od.dispersion_model = opt.dispersion_model
+        od.stop_weak_sinks = int(opt.stop_weak_sinks)
+        od.stop_weak_sources = int(opt.stop_weak_sources)
+        od.backward = int(opt.backward)
+        od.stop_zone = int(opt.stop_zone)
+        od.uniform_porosity = int(opt.uniform_porosity)
+        od.rng_seed = int(opt.rng_seed) & 0xFFFFFFFFFFFFFFFF
+        od.precision = int(opt.precision)
+        self.h = C.c_void_p()
+        rc = self.lib.mprw_create(C.byref(self.h), C.byref(gd), C.byref(od))
+        if rc != 0:
+            msg = self.lib.mprw_last_error(self.h).decode() if self.h.value else "mprw_create failed"
+            if self.h.value:
+                self.lib.mprw_destroy(self.h)
+                self.h = C.c_void_p()
+            raise MprwError(f"mprw_create: rc={rc}: {msg}")
+        self.n = 0
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise MprwError(f"{what}: rc={rc}: {self.lib.mprw_last_error(self.h).decode()}")
+
+    def load_flow(self, f: Flow):
+        keep = dict(ia=_i32(f.ia), ja=_i32(f.ja), flowja=_f64(f.flowja), por=_f64(f.porosity),
+                    ret=_f64(f.retardation), ibts=_i32(f.iboundts), aL=_f64(f.alpha_l), aT=_f64(f.alpha_t),
+                    dm=_f64(f.dm_eff))
+        opt = dict(icb=(f.icboundts, _i32, _ip), bf=(f.boundary_flows, _f64, _dp), hd=(f.heads, _f64, _dp),
+                   ct=(f.celltype, _i32, _ip), src=(f.source_flow, _f64, _dp), snk=(f.sink_flow, _f64, _dp),
+                   zn=(f.zones, _i32, _ip))
+        ptrs = {}
+        for k, (arr, conv, pt) in opt.items():
+            keep[k] = None if arr is None else conv(arr)
+            ptrs[k] = _p(keep[k], pt)
+        fd = FlowDesc()
+        fd.ia = _p(keep["ia"], _ip)
+        fd.ja = _p(keep["ja"], _ip)
+        fd.nja = keep["ja"].shape[0]
+        fd.flowja = _p(keep["flowja"], _dp)
+        fd.boundary_flows = ptrs["bf"]
+        fd.porosity = _p(keep["por"], _dp)
+        fd.retardation = _p(keep["ret"], _dp)
+        fd.iboundts = _p(keep["ibts"], _ip)
+        fd.icboundts = ptrs["icb"]
+        fd.default_icbound = int(f.default_icbound)
+        fd.heads = ptrs["hd"]
+        fd.celltype = ptrs["ct"]
+        fd.source_flow = ptrs["src"]
+        fd.sink_flow = ptrs["snk"]
+        fd.zones = ptrs["zn"]
+        fd.alpha_l = _p(keep["aL"], _dp)
+        fd.alpha_t = _p(keep["aT"], _dp)
+        fd.dm_eff = _p(keep["dm"], _dp)
+        fd.uniform_dispersion = int(f.uniform_dispersion)
+        fd.steady_state = int(f.steady_state)
+        self._check(self.lib.mprw_load_flow(self.h, C.byref(fd)), "mprw_load_flow")
+
+    def set_particles(self, p: Particles):
+        arrs = dict(cell=_i32(p.cell), lx=_f64(p.lx), ly=_f64(p.ly), lz=_f64(p.lz), t=_f64(p.t),
+                    st=_i32(p.status), m=None if p.mass is None else _f64(p.mass),
+                    id=None if p.id is None else _u64(p.id), rc=None if p.rng_ctr is None else _u64(p.rng_ctr))
+        self._check(self.lib.mprw_set_particles(
+            self.h, p.n, _p(arrs["cell"], _ip), _p(arrs["lx"], _dp), _p(arrs["ly"], _dp), _p(arrs["lz"], _dp),
+            _p(arrs["t"], _dp), _p(arrs["st"], _ip), _p(arrs["m"], _dp), _p(arrs["id"], _up),
+            _p(arrs["rc"], _up)), "mprw_set_particles")
+        self.n = p.n
+
+    def advance(self, t_begin: float, t_end: float) -> int:
+        steps = C.c_int64(0)
+        self._check(self.lib.mprw_advance(self.h, float(t_begin), float(t_end), C.byref(steps)), "mprw_advance")
+        return steps.value
+
+    def get_particles(self, global_xyz: bool = True) -> dict:
+        n = self.n
+        out = dict(cell=np.empty(n, np.int32), lx=np.empty(n), ly=np.empty(n), lz=np.empty(n), t=np.empty(n),
+                   status=np.empty(n, np.int32), rng_ctr=np.empty(n, np.uint64))
+        g = [np.empty(n) for _ in range(3)] if global_xyz else [None] * 3
+        self._check(self.lib.mprw_get_particles(
+            self.h, _p(out["cell"], _ip), _p(out["lx"], _dp), _p(out["ly"], _dp), _p(out["lz"], _dp),
+            _p(out["t"], _dp), _p(out["status"], _ip), _p(out["rng_ctr"], _up), _p(g[0], _dp), _p(g[1], _dp),
+            _p(g[2], _dp)), "mprw_get_particles")
+        if global_xyz:
+            out["gx"], out["gy"], out["gz"] = g
+        return out
+
+    def histogram(self, origin, bin_size, n_bins):
+        """Weighted counts of the active particles, shape (nz, ny, nx), plus (n_binned, eff_mass)."""
+        o, b = _f64(origin), _f64(bin_size)
+        nb = _i32(n_bins)
+        counts = np.empty(int(np.prod(nb)), np.float64)
+        nbinned = C.c_int64(0)
+        eff = C.c_double(0)
+        self._check(self.lib.mprw_histogram(self.h, _p(o, _dp), _p(b, _dp), _p(nb, _ip), _p(counts, _dp),
+                                            C.byref(nbinned), C.byref(eff)), "mprw_histogram")
+        return counts.reshape(int(nb[2]), int(nb[1]), int(nb[0])), nbinned.value, eff.value
+
+    def set_stream(self, stream_ptr: int):
+        self._check(self.lib.mprw_set_stream(self.h, C.c_void_p(stream_ptr)), "mprw_set_stream")
+
+    def timings(self) -> dict:
+        s, p, h = C.c_double(), C.c_double(), C.c_double()
+        n = C.c_int64()
+        self._check(self.lib.mprw_last_timings(self.h, C.byref(s), C.byref(p), C.byref(h), C.byref(n)),
+                    "mprw_last_timings")
+        return dict(step_ms=s.value, prep_ms=p.value, hist_ms=h.value, launches=n.value)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.mprw_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
