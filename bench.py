@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="precision of the headline run (mixed: for profiling the MIXED kernel alone)")
     return ap.parse_args()
 
 
@@ -209,7 +211,7 @@ def run_gpu_arm(args, rank, world, local):
                     launches=launches, out=out, t_end=t)
 
     with ClockSampler(local) as clk:
-        fp64 = timed_run(0, args.steps, args.warmup)
+        fp64 = timed_run(MIXED if args.precision == "mixed" else 0, args.steps, args.warmup)
     res = dict(fp64=fp64, clocks=clk.summary())
     if not args.no_mixed:
         res["mixed"] = timed_run(MIXED, args.steps, args.warmup)

@@ -19,6 +19,9 @@ BUILD_DIR = PKG_DIR.parent / "build"
 LIB_PATH = PKG_DIR / "libmprw_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "prep.cu", "step.cu", "hist.cu", "sort.cu"]
+# The per-cell records and model coordinates follow the reference's operation
+# order exactly, so these units are compiled without multiply-add contraction.
+NO_FMAD = {"prep.cu", "hist.cu"}
 
 
 def nvcc() -> str:
@@ -47,7 +50,8 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
         s = SRC_DIR / src
         o = BUILD_DIR / (src + ".o")
         if _stale(o, [s] + headers) or extra_flags:
-            jobs.append([cc, *flags, "-c", str(s), "-o", str(o)])
+            fl = flags + (["-fmad=false"] if src in NO_FMAD else [])
+            jobs.append([cc, *fl, "-c", str(s), "-o", str(o)])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -99,7 +99,7 @@ def _cg(apply, b, diag, rtol=1e-12, maxiter=200000, xp=np):
     x = xp.zeros_like(b)
     r = b - apply(x)
     z = r / diag
-    p = z.copy()
+    p = z.clone() if hasattr(z, "clone") else z.copy()
     rz = float((r * z).sum())
     bn = float(xp.sqrt((b * b).sum()))
     if bn == 0:

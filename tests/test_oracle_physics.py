@@ -1,0 +1,100 @@
+"""The oracle against known answers (CPU).
+
+* cell records of uniform flow in closed form (ModpathCellData.f90:2557-2564,
+  TrackSubCell.F90:2557-2691, 4016-4138);
+* pure advection is exact: a particle moves v*t and sits on cell faces
+  exactly (ConvertFromNeighbor, RectangularGridDisMf6.f90:50-108);
+* the plume of config 1 against the analytic 1-D Gaussian ADE solution,
+  with the tolerance the reference's interface-forcing scheme needs;
+* release / status logic of the driver (MPathRW.F90:1256-1302);
+* counter-based streams make results independent of the thread count.
+"""
+import numpy as np
+import pytest
+
+from mprw import workloads as W
+from mprw.model import ACTIVE, INACTIVE, PENDING, UNRELEASED, WEAK_SINK, Particles
+from oracle import oracle as O
+
+
+def test_uniform_flow_cell_record():
+    g, f, p, opt = W.config1(n_particles=1)
+    r = O.cell_record(g, f, opt, 50)
+    np.testing.assert_allclose(r["vface"], [1, 1, 0, 0, 0, 0], rtol=0, atol=1e-15)
+    assert r["dtcell"] == pytest.approx(0.1, rel=1e-15)
+    np.testing.assert_allclose(r["qcorner"], np.tile([0.3, 0.0, 0.0, 0.3], (8, 1)), rtol=1e-15, atol=0)
+    np.testing.assert_allclose(r["phicorner"], 0.3)
+    D = r["D"]
+    np.testing.assert_allclose(D[0], 0.01 * 0.3 + 0.09 * 0.3, rtol=1e-14)  # Dxx
+    np.testing.assert_allclose(D[1], 0.01 * 0.3, rtol=1e-14)               # Dyy
+    np.testing.assert_allclose(D[2], 0.01 * 0.3, rtol=1e-14)               # Dzz
+    assert np.all(D[3:] == 0.0)
+    # interior x faces connect, y/z faces are domain edges (defaultICBound = 1 reflects)
+    assert list(r["conn"]) == [49, 51, 0, 0, 0, 0]
+    assert list(r["massb"]) == [0, 0, 1, 1, 1, 1]
+
+
+def test_pure_advection_exact():
+    g, f, p, opt = W.config1(n_particles=3, pure_advection=True)
+    p.lx[:] = [0.0, 0.25, 0.5]
+    q, steps = O.advance(g, f, opt, p, 0.0, 25.0)
+    gx, gy, gz = O.global_xyz(g, f, q)
+    np.testing.assert_allclose(gx, np.array([10.0, 10.25, 10.5]) + 25.0, rtol=0, atol=1e-9)
+    assert np.all(q.t == 25.0) and np.all(q.status == ACTIVE)
+    np.testing.assert_allclose(gy, 0.5)
+    # one pass per 0.1 d plus one face-truncated pass per crossed face
+    assert steps >= 3 * 250
+
+
+def test_analytic_gaussian_config1():
+    n = 6000
+    g, f, p, opt = W.config1(n_particles=n)
+    q, _ = O.advance(g, f, opt, p, 0.0, 50.0, rng_kind=O.RNG_PHILOX, nthreads=8)
+    gx, _, _ = O.global_xyz(g, f, q)
+    mean, var = 10.0 + 50.0, 2.0 * 0.1 * 1.0 * 50.0
+    assert np.all(q.status == ACTIVE)
+    # the scheme's interface forcing biases the drift by a few tenths of a metre
+    assert abs(gx.mean() - mean) < 0.5
+    assert abs(gx.var() - var) / var < 0.12
+
+
+def test_release_and_status_logic():
+    g, f, p, opt = W.config1(n_particles=4, pure_advection=True)
+    p.t[:] = [0.0, 5.0, 50.0, -1.0]      # released now, later in interval, after, before interval
+    p.status[:] = PENDING
+    q, _ = O.advance(g, f, opt, p, 0.0, 10.0)
+    assert list(q.status) == [ACTIVE, ACTIVE, PENDING, UNRELEASED]
+    gx, _, _ = O.global_xyz(g, f, q)
+    assert gx[0] == pytest.approx(20.0, abs=1e-9) and gx[1] == pytest.approx(15.0, abs=1e-9)
+    # inactive release cell
+    f.iboundts = f.iboundts.copy()
+    f.iboundts[10] = 0
+    q, _ = O.advance(g, f, opt, p, 0.0, 10.0)
+    assert q.status[0] == INACTIVE
+
+
+def test_empty_particle_set():
+    g, f, p, opt = W.config1(n_particles=0)
+    q, steps = O.advance(g, f, opt, p, 0.0, 10.0)
+    assert q.n == 0 and steps == 0
+
+
+def test_thread_count_invariance_with_counter_based_rng():
+    g, f, p, opt, _ = W.config2(n_particles=400, nlay=3, nrow=8, ncol=20, seed=2, use_torch=False)
+    a, sa = O.advance(g, f, opt, p, 0.0, 30.0, rng_kind=O.RNG_PHILOX, nthreads=1)
+    b, sb = O.advance(g, f, opt, p, 0.0, 30.0, rng_kind=O.RNG_PHILOX, nthreads=8)
+    assert sa == sb
+    for x, y in ((a.cell, b.cell), (a.lx, b.lx), (a.ly, b.ly), (a.lz, b.lz), (a.t, b.t), (a.status, b.status),
+                 (a.rng_ctr, b.rng_ctr)):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_heterogeneous_weak_sink_stops():
+    g, f, p, opt, info = W.config2(n_particles=600, nlay=3, nrow=8, ncol=20, seed=1, use_torch=False)
+    q, _ = O.advance(g, f, opt, p, 0.0, 200.0, rng_kind=O.RNG_PHILOX, nthreads=8)
+    counts = np.bincount(q.status, minlength=10)
+    assert counts[WEAK_SINK] > 0
+    assert counts.sum() == p.n
+    # particles that stopped at the outlet sit in the last column
+    col = (q.cell[q.status == WEAK_SINK] - 1) % g.ncol
+    assert np.all(col == g.ncol - 1)
