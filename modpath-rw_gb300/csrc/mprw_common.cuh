@@ -87,6 +87,9 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t
 }
 
 // Exact Irwin-Hall(12) normal from three Philox blocks; advances ctr by 3.
+// The 36-bit word sum S is placed in the mantissa of 2^20 + S*2^-32 (exponent
+// field 0x413, mantissa LSB 2^-32), so the normal S*2^-32 - 6 costs one exact
+// FP64 subtraction instead of an int64 conversion.
 __device__ __forceinline__ double normal_ih12(uint64_t seed, uint64_t id, uint64_t &ctr) {
   uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
   uint32_t i0 = (uint32_t)id, i1 = (uint32_t)(id >> 32);
@@ -98,8 +101,38 @@ __device__ __forceinline__ double normal_ih12(uint64_t seed, uint64_t id, uint64
     philox4x32_10((uint32_t)n, (uint32_t)(n >> 32), i0, i1, k0, k1, o);
     sum += (uint64_t)o[0] + o[1] + o[2] + o[3];
   }
-  int64_t centred = (int64_t)sum - 25769803776LL;  // 6 * 2^32
-  return (double)centred * 0x1p-32;
+  double d = __longlong_as_double((long long)(0x4130000000000000ULL | sum));
+  return d - 1048582.0;  // 2^20 + 6
+}
+
+// MIXED-precision normals: the same Irwin-Hall(12) distribution on 8-bit
+// uniforms.  One 32-bit word holds four bytes b_i; a normal sums the 12 bytes
+// of three words with dp4a: xi = (sum + 6)/256 - 6, i.e. sum_i (b_i+0.5)/256 - 6,
+// exactly representable in FP32.  Three normals use 9 words of 3 Philox
+// blocks (ctr advances by ceil(3*ndim/4)).
+__device__ __forceinline__ void normals_ih12_u8(int ndim, uint64_t seed, uint64_t id, uint64_t &ctr,
+                                                float out[3]) {
+  uint32_t w[12];
+  const int nblk = (3 * ndim + 3) / 4;
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    if (b < nblk) {
+      uint64_t n = ctr++;
+      philox4x32_10((uint32_t)n, (uint32_t)(n >> 32), (uint32_t)id, (uint32_t)(id >> 32), (uint32_t)seed,
+                    (uint32_t)(seed >> 32), &w[4 * b]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (k < ndim) {
+      unsigned s = __dp4a(w[3 * k], 0x01010101u, 0u);  // unsigned bytes
+      s = __dp4a(w[3 * k + 1], 0x01010101u, s);
+      s = __dp4a(w[3 * k + 2], 0x01010101u, s);
+      out[k] = fmaf((float)s, 0.00390625f, -5.9765625f);  // (s + 6)/256 - 6
+    } else {
+      out[k] = 0.0f;
+    }
+  }
 }
 
 // Driver status codes (MPathRW.F90:1337-1403).

@@ -68,10 +68,31 @@ __device__ __forceinline__ R divc(const Lane<R> &F, int base, R x, R y, R z, R x
   return a;
 }
 
+// The step's standard normals, the reference's Irwin-Hall(12) distribution
+// in both paths: FP64 -- exact 32-bit uniforms (3 Philox blocks per normal);
+// MIXED -- 8-bit uniforms summed with dp4a (3 blocks per 3-D step).
 template <typename R>
-__device__ __forceinline__ R rnorm_draw(uint64_t seed, uint64_t id, uint64_t &ctr) {
-  return (R)normal_ih12(seed, id, ctr);
-}
+struct Normals;
+template <>
+struct Normals<double> {
+  __device__ __forceinline__ static void draw(int ndim, uint64_t seed, uint64_t id, uint64_t &ctr, double &r0,
+                                              double &r1, double &r2) {
+    r0 = normal_ih12(seed, id, ctr);
+    r1 = (ndim > 1) ? normal_ih12(seed, id, ctr) : 0.0;
+    r2 = (ndim > 2) ? normal_ih12(seed, id, ctr) : 0.0;
+  }
+};
+template <>
+struct Normals<float> {
+  __device__ __forceinline__ static void draw(int ndim, uint64_t seed, uint64_t id, uint64_t &ctr, float &r0,
+                                              float &r1, float &r2) {
+    float v[3];
+    normals_ih12_u8(ndim, seed, id, ctr, v);
+    r0 = v[0];
+    r1 = v[1];
+    r2 = v[2];
+  }
+};
 
 // pr_DisplacementRandomDischarge (3-D :2821-2928, 2-D :2931-3028, 1-D :3031-3113)
 template <typename R>
@@ -110,9 +131,8 @@ __device__ __forceinline__ void random_displacement(const Lane<R> &F, int ndim, 
         B23 = vx * sTxy;
       }
     }
-    R rx = rnorm_draw<R>(seed, id, ctr);
-    R ry = rnorm_draw<R>(seed, id, ctr);
-    R rz = rnorm_draw<R>(seed, id, ctr);
+    R rx, ry, rz;
+    Normals<R>::draw(3, seed, id, ctr, rx, ry, rz);
     bx = fma(B13, rz, fma(B12, ry, B11 * rx));
     by = fma(B23, rz, fma(B22, ry, B21 * rx));
     bz = fma(B32, ry, B31 * rx);
@@ -131,8 +151,8 @@ __device__ __forceinline__ void random_displacement(const Lane<R> &F, int ndim, 
       B12 = -v2 * sTi;
       B22 = v1 * sTi;
     }
-    R r1 = rnorm_draw<R>(seed, id, ctr);
-    R r2 = rnorm_draw<R>(seed, id, ctr);
+    R r1, r2, r3;
+    Normals<R>::draw(2, seed, id, ctr, r1, r2, r3);
     R o1 = fma(B12, r2, B11 * r1), o2 = fma(B22, r2, B21 * r1);
     bx = zero; by = zero; bz = zero;
     if (d1 == 0) bx = o1; else if (d1 == 1) by = o1; else bz = o1;
@@ -142,7 +162,8 @@ __device__ __forceinline__ void random_displacement(const Lane<R> &F, int ndim, 
     R nrm = fabs(v1);
     R B11 = zero;
     if (nrm > zero) B11 = sqrt(tr * fma(aL, nrm, dm));
-    R r1 = rnorm_draw<R>(seed, id, ctr);
+    R r1, r2, r3;
+    Normals<R>::draw(1, seed, id, ctr, r1, r2, r3);
     bx = zero; by = zero; bz = zero;
     R o1 = B11 * r1;
     if (d1 == 0) bx = o1; else if (d1 == 1) by = o1; else bz = o1;
@@ -173,8 +194,17 @@ __device__ __forceinline__ bool quad_axis(R npos, R pos, R d, R v, R divD, R dB,
   R arg = B * B + R(4) * dI * A;
   if ((arg >= zero) && (A != zero)) {
     R zs = sqrt(arg);
-    R z1 = (-B + zs) / (R(2) * A);
-    R z2 = (-B - zs) / (R(2) * A);
+    R z1, z2;
+    if constexpr (sizeof(R) == 4) {
+      // the same two roots without cancellation: q = -(B + sign(B) sqrt(arg))/2,
+      // roots q/A and -dI/q
+      R q = (B >= zero) ? -(B + zs) * R(0.5) : (zs - B) * R(0.5);
+      z1 = q / A;
+      z2 = (q != zero) ? -dI / q : zero;
+    } else {
+      z1 = (-B + zs) / (R(2) * A);
+      z2 = (-B - zs) / (R(2) * A);
+    }
     if (z1 > zero || z2 > zero) {
       R zm = (z1 > zero && z2 > zero) ? (z1 < z2 ? z1 : z2) : (z1 > zero ? z1 : z2);
       dtaxis = zm * zm;
@@ -208,7 +238,7 @@ struct Visit {
   R x, y, z;     // current local position (TrackSubCell x,y,z)
   R ix, iy, iz;  // cell-entry location (initialLocation)
   double t, tinit, dtcell;
-  R sqrt_dtcell;
+  R sqrt_dtcell, rdt_cell;
   int exitFace, posRestart;
   bool reachedMax;
   int64_t passes;
@@ -228,12 +258,15 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
   const R zero = R(0), one = R(1), half = R(0.5);
   const double dtRed = (double)0.1f;  // dtReductionFactor, a single-precision literal (:850)
   double dt = V.dtcell;
+  R rdt = V.rdt_cell, sdt = V.sqrt_dtcell;  // FP32 copies: no conversion on the common pass
   V.t = V.t + dt;
   if (maxTime < V.t) {
     V.t = V.t - dt;
     dt = fmax(maxTime - V.t, 0.0);
     V.t = maxTime;
     V.reachedMax = true;
+    rdt = (R)dt;
+    sdt = sqrt(rdt);
   }
   R x = V.x, y = V.y, z = V.z;
   R dX = F(F_D + 0), dY = F(F_D + 1), dZ = F(F_D + 2);
@@ -248,8 +281,6 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
   R ddz = divc(F, F_DIV + 14, x, y, z, xy, xz, yz);
   R bx, by, bz;
   random_displacement(F, ndim, d1, d2, x, y, z, seed, id, ctr, bx, by, bz);
-  R rdt = (R)dt;
-  R sdt = (dt == V.dtcell) ? V.sqrt_dtcell : sqrt(rdt);
   R ax = vx * rdt, ay = vy * rdt, az = vz * rdt;
   R dxrw = ax + ddx * rdt + bx * sdt;
   R dyrw = ay + ddy * rdt + by * sdt;
@@ -411,6 +442,13 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
   return PASS_CONTINUE;
 }
 
+// Persistent kernel: every lane owns one particle at a time.  Each iteration of
+// the main loop (a) refills lanes without a particle from the atomic queue
+// (one atomic per warp), (b) runs the cell-entry phase for lanes that changed
+// cell, (c) runs one time-loop pass for every tracking lane.  All phases are
+// structured and the loop head re-converges the warp, so the common pass body
+// runs with every tracking lane active; the loop ends when no lane of the warp
+// has work.
 template <typename R>
 __global__ void __launch_bounds__(kStepThreads) rwpt_advance_kernel(AdvanceArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -418,12 +456,14 @@ __global__ void __launch_bounds__(kStepThreads) rwpt_advance_kernel(AdvanceArgs<
   const int stride = blockDim.x;
   Lane<R> F{sm, stride};
   const R zero = R(0), one = R(1);
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
 
   int64_t my_passes = 0;
   int64_t p = -1;        // particle being tracked (index into the state arrays)
+  bool open = true;      // the queue may still have particles for this lane
   int32_t c = 0;         // current cell (0-based)
   bool need_cell = false;
-  int32_t status = 0;
   uint64_t id = 0, ctr = 0;
   // last point of the pathline (cell, local coords, time)
   int32_t lc = 0;
@@ -433,38 +473,62 @@ __global__ void __launch_bounds__(kStepThreads) rwpt_advance_kernel(AdvanceArgs<
   R ex = zero, ey = zero, ez = zero;
   double et = 0.0;
   Visit<R> V;
+  V.x = V.y = V.z = V.ix = V.iy = V.iz = zero;
+  V.t = V.tinit = V.dtcell = 0.0;
+  V.sqrt_dtcell = zero;
+  V.rdt_cell = zero;
+  V.exitFace = V.posRestart = 0;
+  V.reachedMax = false;
+  V.passes = 0;
   uint32_t massb = 0;
-  int32_t conn6[6];
+  int32_t conn6[6] = {-1, -1, -1, -1, -1, -1};
 
   for (;;) {
-    if (p < 0) {
-      int64_t q = (int64_t)atomicAdd(reinterpret_cast<unsigned long long *>(a.queue), 1ULL);
-      if (q >= a.n) break;
-      p = a.perm ? (int64_t)a.perm[q] : q;
-      status = a.status[p];
-      c = a.cell[p];
-      ex = a.x[p]; ey = a.y[p]; ez = a.z[p];
-      et = a.t[p];
-      // release checks, MPathRW.F90:1256-1302
-      if (status == ST_PENDING) {
-        if (et < a.t_begin) status = ST_UNRELEASED;
-        else if (et <= a.t_end) {
-          status = ST_ACTIVE;
-          if (a.iboundts[c] == 0) status = ST_INACTIVE;
+    __syncwarp(FULL);
+    // (a) refill
+    const bool want = (p < 0) && open;
+    const unsigned m = __ballot_sync(FULL, want);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if (lane == leader)
+        base = atomicAdd(reinterpret_cast<unsigned long long *>(a.queue), (unsigned long long)__popc(m));
+      base = __shfl_sync(FULL, base, leader);
+      if (want) {
+        const int64_t q = (int64_t)base + __popc(m & ((1u << lane) - 1u));
+        if (q >= a.n) {
+          open = false;
+        } else {
+          p = a.perm ? (int64_t)a.perm[q] : q;
+          int32_t status = a.status[p];
+          c = a.cell[p];
+          ex = a.x[p]; ey = a.y[p]; ez = a.z[p];
+          et = a.t[p];
+          // release checks, MPathRW.F90:1256-1302
+          if (status == ST_PENDING) {
+            if (et < a.t_begin) status = ST_UNRELEASED;
+            else if (et <= a.t_end) {
+              status = ST_ACTIVE;
+              if (a.iboundts[c] == 0) status = ST_INACTIVE;
+            }
+          }
+          if (status == ST_INACTIVE && (a.cellflags[c] & 2u)) status = ST_ACTIVE;  // partially dry
+          if (status != ST_ACTIVE) {
+            a.status[p] = status;
+            p = -1;
+          } else {
+            id = a.id ? a.id[p] : (uint64_t)p;
+            ctr = a.ctr[p];
+            lc = c; lx = ex; ly = ey; lz = ez; lt = et;
+            need_cell = true;
+          }
         }
       }
-      if (status == ST_INACTIVE && (a.cellflags[c] & 2u)) status = ST_ACTIVE;  // partially dry
-      if (status != ST_ACTIVE) {
-        a.status[p] = status;
-        p = -1;
-        continue;
-      }
-      id = a.id ? a.id[p] : (uint64_t)p;
-      ctr = a.ctr[p];
-      lc = c; lx = ex; ly = ey; lz = ez; lt = et;
-      need_cell = true;
     }
-    if (need_cell) {
+    if (!__any_sync(FULL, (p >= 0) || open)) break;
+
+    // (b) cell entry (TrackCell checks + sub-cell set-up)
+    if (p >= 0 && need_cell) {
       need_cell = false;
       int32_t fin = 0;  // 0 track, else final status
       bool use_last = false;
@@ -473,7 +537,7 @@ __global__ void __launch_bounds__(kStepThreads) rwpt_advance_kernel(AdvanceArgs<
         use_last = true;
       } else {
         const CellRec<R> *rec = a.recs + c;
-        int32_t es = rec->entry_status;
+        const int32_t es = rec->entry_status;
         if (es != 0) {
           fin = es;
           use_last = (es == ST_UNDEFINED);
@@ -487,6 +551,7 @@ __global__ void __launch_bounds__(kStepThreads) rwpt_advance_kernel(AdvanceArgs<
           V.t = et; V.tinit = et;
           V.dtcell = rec->dtcell;
           V.sqrt_dtcell = (R)rec->sqrt_dtcell;
+          V.rdt_cell = (R)rec->dtcell;
           V.exitFace = 0;
           V.posRestart = 0;
           V.reachedMax = false;
@@ -502,63 +567,55 @@ __global__ void __launch_bounds__(kStepThreads) rwpt_advance_kernel(AdvanceArgs<
         a.status[p] = fin;
         a.ctr[p] = ctr;
         p = -1;
-        continue;
       }
     }
-    // one time-loop pass (with the per-visit safety cap)
-    R ox, oy, oz;
-    int r;
-    if (++V.passes > kMaxStepsPerVisit) {
-      r = PASS_UNDEFINED;
-    } else {
-      r = rw_pass(V, F, massb, a.t_end, a.ndim, a.d1, a.d2, a.seed, id, ctr, ox, oy, oz);
-      ++my_passes;
+
+    // (c) one time-loop pass (with the per-visit safety cap)
+    if (p >= 0 && !need_cell) {
+      R ox = zero, oy = zero, oz = zero;
+      int r;
+      if (++V.passes > kMaxStepsPerVisit) {
+        r = PASS_UNDEFINED;
+      } else {
+        r = rw_pass(V, F, massb, a.t_end, a.ndim, a.d1, a.d2, a.seed, id, ctr, ox, oy, oz);
+        ++my_passes;
+      }
+      if (r == PASS_MAXTIME) {
+        a.cell[p] = c; a.x[p] = ox; a.y[p] = oy; a.z[p] = oz; a.t[p] = V.t;
+        a.status[p] = ST_ACTIVE;
+        a.ctr[p] = ctr;
+        p = -1;
+      } else if (r == PASS_UNDEFINED) {
+        a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
+        a.status[p] = ST_UNDEFINED;
+        a.ctr[p] = ctr;
+        p = -1;
+      } else if (r == PASS_EXIT) {
+        // the exit point becomes the last pathline point
+        const int face = V.exitFace;
+        lc = c; lx = ox; ly = oy; lz = oz; lt = V.t;
+        const int32_t nc = conn6[face - 1];
+        // ConvertFromNeighbor: the exit coordinate must sit exactly on the face
+        const bool bad = (face == 2 && ox != one) || (face == 1 && ox != zero) || (face == 4 && oy != one) ||
+                         (face == 3 && oy != zero) || (face == 6 && oz != one) || (face == 5 && oz != zero);
+        if (nc < 0 || bad) {
+          a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
+          a.status[p] = (nc < 0) ? ST_BOUNDARY : ST_UNDEFINED;
+          a.ctr[p] = ctr;
+          p = -1;
+        } else {
+          ex = ox; ey = oy; ez = oz; et = V.t;
+          if (face == 2) ex = zero;
+          if (face == 1) ex = one;
+          if (face == 4) ey = zero;
+          if (face == 3) ey = one;
+          if (face == 6) ez = zero;
+          if (face == 5) ez = one;
+          c = nc;
+          need_cell = true;
+        }
+      }
     }
-    if (r == PASS_CONTINUE) continue;
-    if (r == PASS_MAXTIME) {
-      a.cell[p] = c; a.x[p] = ox; a.y[p] = oy; a.z[p] = oz; a.t[p] = V.t;
-      a.status[p] = ST_ACTIVE;
-      a.ctr[p] = ctr;
-      p = -1;
-      continue;
-    }
-    if (r == PASS_UNDEFINED) {
-      a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
-      a.status[p] = ST_UNDEFINED;
-      a.ctr[p] = ctr;
-      p = -1;
-      continue;
-    }
-    // PASS_EXIT: the exit point becomes the last pathline point
-    int face = V.exitFace;
-    lc = c; lx = ox; ly = oy; lz = oz; lt = V.t;
-    int32_t nc = conn6[face - 1];
-    if (nc < 0) {
-      a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
-      a.status[p] = ST_BOUNDARY;
-      a.ctr[p] = ctr;
-      p = -1;
-      continue;
-    }
-    // ConvertFromNeighbor: the exit coordinate must sit exactly on the face
-    bool bad = (face == 2 && ox != one) || (face == 1 && ox != zero) || (face == 4 && oy != one) ||
-               (face == 3 && oy != zero) || (face == 6 && oz != one) || (face == 5 && oz != zero);
-    if (bad) {
-      a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
-      a.status[p] = ST_UNDEFINED;
-      a.ctr[p] = ctr;
-      p = -1;
-      continue;
-    }
-    ex = ox; ey = oy; ez = oz; et = V.t;
-    if (face == 2) ex = zero;
-    if (face == 1) ex = one;
-    if (face == 4) ey = zero;
-    if (face == 3) ey = one;
-    if (face == 6) ez = zero;
-    if (face == 5) ez = one;
-    c = nc;
-    need_cell = true;
   }
   // block-level sum of passes, one atomic per block
   __shared__ unsigned long long blk;
