@@ -151,6 +151,35 @@ int mprw_histogram(mprw_handle *h, const double origin[3], const double bin_size
                    const int32_t n_bins[3], double *counts, int64_t *n_binned,
                    double *eff_mass);
 
+/* GPKDE reconstruction options (the GPKDE input file, read at
+ * ModpathSimulationData.f90:772-1289, passed to gpkde%Initialize at
+ * MPathRW.F90:556-574 and to ComputeDensity at MPathRW.F90:1626-1642). */
+typedef struct {
+  double origin[3];            /* gpkdeDomainOrigin                            */
+  double domain_size[3];       /* gpkdeDomainSize                              */
+  double bin_size[3];          /* gpkdeBinSize                                 */
+  int32_t n_opt_loops;         /* gpkdeNOptLoops (10)                          */
+  double min_hover_delta;      /* kernel database: minHOverDelta (0.3)         */
+  double delta_hover_delta;    /*                  deltaHOverDelta (0.3)       */
+  double max_hover_delta;      /*                  maxHOverDelta (15)          */
+  double rel_err_convergence;  /* gpkdeRelErrorConvergence (0.02)              */
+  int32_t skip_error_convergence;
+  int32_t unit_volume;         /* ComputeDensity(unitVolume=.true.)            */
+  double scaling_factor;       /* gpkdeScalingFactor, e.g. 1/binVolume         */
+} mprw_gpkde_options;
+
+/* GPKDE reconstruction of the ACTIVE particles (weights = particle masses).
+ * Replaces gpkde%ComputeDensity (GridProjectedKDE.F90:3598-4392) with the
+ * kernel database on, bounded kernel sizes, Kish effective weights and
+ * anisotropic kernels, for 1-D and 3-D grids (a grid whose three
+ * dimensions all have more than one bin, or exactly one).
+ * density: nx*ny*nz doubles, x fastest (nx = int(domain/bin + 0.5)),
+ * scaled as the reference exports it (x binVolume if unit_volume, x
+ * scaling_factor); histogram (may be NULL): mass per bin; n_bins_out (may be
+ * NULL): the grid; loops_done (may be NULL): optimisation loops run. */
+int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *opt, double *density, double *histogram,
+               int32_t n_bins_out[3], int32_t *loops_done);
+
 /* Optional: launch on a caller-provided cudaStream_t (NULL = the handle's). */
 int mprw_set_stream(mprw_handle *h, void *stream);
 

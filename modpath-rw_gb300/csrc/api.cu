@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/mprw_gpu.h"
+#include "gpkde.cuh"
 #include "mprw_kernels.cuh"
 
 using namespace mprw;
@@ -53,7 +54,10 @@ struct mprw_handle {
   void *hscratch = nullptr;
   size_t hscratch_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
-  double step_ms = 0, prep_ms = 0, hist_ms = 0;
+  double step_ms = 0, prep_ms = 0, hist_ms = 0, kde_ms = 0;
+  KdeState kde;
+  double *d_counts = nullptr;
+  int64_t counts_cap = 0;
   int64_t launches = 0;
   int sms = 152;
   int sort_enabled = 1;
@@ -100,6 +104,8 @@ void free_all(mprw_handle *h) {
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->h_counters) cudaFreeHost(h->h_counters);
+  if (h->d_counts) cudaFree(h->d_counts);
+  h->kde.release();
   if (h->hscratch) cudaFreeHost(h->hscratch);
   cudaEvent_t evs[] = {h->ev0, h->ev1, h->ev2, h->ev3};
   for (auto e : evs)
@@ -118,6 +124,10 @@ __global__ void f32_to_f64_kernel(const float *in, double *out, int64_t n) {
 __global__ void cell_shift_kernel(int32_t *cell, int64_t n, int32_t delta) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     cell[i] += delta;
+}
+__global__ void mul2_kernel(double *x, int64_t n, double a, double b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = (x[i] * a) * b;
 }
 __global__ void div_kernel(double *x, int64_t n, double d) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -522,15 +532,19 @@ int mprw_get_particles(mprw_handle *h, int32_t *cell, double *lx, double *ly, do
   return MPRW_OK;
 }
 
-int mprw_histogram(mprw_handle *h, const double origin[3], const double bin_size[3], const int32_t n_bins[3],
-                   double *counts, int64_t *n_binned, double *eff_mass) {
-  if (!h) return MPRW_E_INVAL;
-  if (!origin || !bin_size || !n_bins || !counts) return fail(h, MPRW_E_INVAL, "mprw_histogram: null argument");
+}  // extern "C"
+
+namespace {
+
+// Histogram of the active particles into h->d_counts (counts / effMass, the
+// reference's histogram%counts after ComputeCountsWeighted).
+int histogram_device(mprw_handle *h, const double origin[3], const double bin_size[3], const int32_t n_bins[3],
+                     int64_t *n_binned, double *eff_mass, double *n_active) {
   int64_t nbins = 1;
   HistArgs a{};
   for (int d = 0; d < 3; ++d) {
-    if (n_bins[d] < 1) return fail(h, MPRW_E_INVAL, "mprw_histogram: n_bins must be >= 1");
-    if (bin_size[d] < 0.0) return fail(h, MPRW_E_INVAL, "mprw_histogram: bin_size must be >= 0");
+    if (n_bins[d] < 1) return fail(h, MPRW_E_INVAL, "histogram: n_bins must be >= 1");
+    if (bin_size[d] < 0.0) return fail(h, MPRW_E_INVAL, "histogram: bin_size must be >= 0");
     nbins *= n_bins[d];
     a.origin[d] = origin[d];
     a.bin[d] = bin_size[d];
@@ -538,9 +552,16 @@ int mprw_histogram(mprw_handle *h, const double origin[3], const double bin_size
     a.nb[d] = n_bins[d];
     a.active_dim[d] = bin_size[d] != 0.0;
   }
-  if (nbins > ((int64_t)1 << 31)) return fail(h, MPRW_E_INVAL, "mprw_histogram: too many bins");
+  if (nbins > ((int64_t)1 << 31)) return fail(h, MPRW_E_INVAL, "histogram: too many bins");
   cudaStream_t s = h->stream;
   const int64_t n = h->n;
+  if (nbins > h->counts_cap) {
+    if (h->d_counts) cudaFree(h->d_counts);
+    h->d_counts = nullptr;
+    h->counts_cap = 0;
+    CK(cudaMalloc(&h->d_counts, sizeof(double) * nbins + sizeof(unsigned int) * nbins));
+    h->counts_cap = nbins;
+  }
   a.geo = geometry(h);
   a.n = n;
   a.cell = h->d_cell;
@@ -550,67 +571,252 @@ int mprw_histogram(mprw_handle *h, const double origin[3], const double bin_size
   a.z = h->d_z;
   a.mixed = h->opt.precision == MPRW_MIXED;
   a.nbinned = h->d_counters + 2;
-  h->launches = 0;
-  // device output buffer
-  size_t cbytes = ((size_t)nbins * 8 + 255) / 256 * 256;
-  CK(cudaEventRecord(h->ev2, s));
   double total = 0, sw2 = 0, eff = 1.0;
   int64_t nb_out = 0;
   if (h->unit_mass) {
-    size_t need = cbytes + (size_t)nbins * 4 + 256;
-    if (h->scratch_bytes < need) {
-      if (h->scratch) cudaFree(h->scratch);
-      h->scratch = nullptr;
-      h->scratch_bytes = 0;
-      CK(cudaMalloc(&h->scratch, need));
-      h->scratch_bytes = need;
-    }
-    double *dcounts = (double *)h->scratch;
-    unsigned int *c32 = (unsigned int *)((char *)h->scratch + cbytes);
+    unsigned int *c32 = (unsigned int *)(h->d_counts + nbins);
     CK(cudaMemsetAsync(c32, 0, (size_t)nbins * 4, s));
-    CK(cudaMemsetAsync(h->d_counters + 2, 0, sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(h->d_counters + 2, 0, 2 * sizeof(unsigned long long), s));
     a.counts32 = c32;
     CK(launch_hist_unit(a, s));
-    CK(launch_u32_to_f64(c32, dcounts, nbins, s));
+    CK(launch_u32_to_f64(c32, h->d_counts, nbins, s));
     h->launches += 2;
-    CK(cudaMemcpyAsync(counts, dcounts, 8 * (size_t)nbins, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(h->h_counters + 2, h->d_counters + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-    CK(cudaEventRecord(h->ev3, s));
     CK(cudaStreamSynchronize(s));
     nb_out = (int64_t)h->h_counters[2];
-    // active count: unit weights => totalMass = nActive, Kish nEff = nActive, effMass = 1
-    eff = 1.0;
+    eff = 1.0;  // unit weights: Kish nEffective = totalMass, effective mass 1
   } else {
-    // per-particle bins, then order-preserving sums
     size_t arr = ((size_t)n * 8 + 255) / 256 * 256;
     void *tmp = nullptr;
-    CK(cudaMalloc(&tmp, arr + cbytes));
+    CK(cudaMalloc(&tmp, arr));
     int64_t *bin_of = (int64_t *)tmp;
-    double *dcounts = (double *)((char *)tmp + arr);
     a.bin_of = bin_of;
     cudaError_t e = launch_hist_bins(a, s);
     if (e == cudaSuccess)
-      e = ordered_bin_sums(bin_of, h->d_mass, h->d_status, n, nbins, dcounts, &total, &sw2, &h->scratch,
+      e = ordered_bin_sums(bin_of, h->d_mass, h->d_status, n, nbins, h->d_counts, &total, &sw2, &h->scratch,
                            &h->scratch_bytes, s);
     if (e == cudaSuccess && total != 0.0) {
       double neff = total * total / sw2;  // Kish (Histogram.F90:338-340)
       eff = total / neff;
-      div_kernel<<<grid1d(nbins), 256, 0, s>>>(dcounts, nbins, eff);
+      div_kernel<<<grid1d(nbins), 256, 0, s>>>(h->d_counts, nbins, eff);
       e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(counts, dcounts, 8 * (size_t)nbins, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaEventRecord(h->ev3, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaFree(tmp);
     CK(e);
     h->launches += 5;
     nb_out = -1;
   }
+  if (n_binned) *n_binned = nb_out;
+  if (eff_mass) *eff_mass = eff;
+  (void)n_active;
+  return MPRW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mprw_histogram(mprw_handle *h, const double origin[3], const double bin_size[3], const int32_t n_bins[3],
+                   double *counts, int64_t *n_binned, double *eff_mass) {
+  if (!h) return MPRW_E_INVAL;
+  if (!origin || !bin_size || !n_bins || !counts) return fail(h, MPRW_E_INVAL, "mprw_histogram: null argument");
+  h->launches = 0;
+  cudaStream_t s = h->stream;
+  CK(cudaEventRecord(h->ev2, s));
+  int rc = histogram_device(h, origin, bin_size, n_bins, n_binned, eff_mass, nullptr);
+  if (rc != MPRW_OK) return rc;
+  const int64_t nbins = (int64_t)n_bins[0] * n_bins[1] * n_bins[2];
+  CK(cudaMemcpyAsync(counts, h->d_counts, 8 * (size_t)nbins, cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(h->ev3, s));
+  CK(cudaStreamSynchronize(s));
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, h->ev2, h->ev3));
   h->hist_ms = ms;
-  if (n_binned) *n_binned = nb_out;
-  if (eff_mass) *eff_mass = eff;
+  return MPRW_OK;
+}
+
+int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, double *histogram,
+               int32_t n_bins_out[3], int32_t *loops_done) {
+  if (!h) return MPRW_E_INVAL;
+  if (!o || !density) return fail(h, MPRW_E_INVAL, "mprw_gpkde: null argument");
+  // prInitialize (GridProjectedKDE.F90:354-998)
+  KdeParams P{};
+  int32_t nb[3];
+  for (int d = 0; d < 3; ++d) {
+    if (o->bin_size[d] < 0.0 || o->domain_size[d] < 0.0) return fail(h, MPRW_E_INVAL, "mprw_gpkde: negative size");
+    nb[d] = (o->bin_size[d] != 0.0) ? (int32_t)(o->domain_size[d] / o->bin_size[d] + 0.5) : 1;
+    if (nb[d] < 1) return fail(h, MPRW_E_INVAL, "mprw_gpkde: grid size < 1");
+    P.nb[d] = nb[d];
+    P.bin[d] = o->bin_size[d];
+    P.mask[d] = (nb[d] != 1) ? 1 : 0;
+  }
+  P.ndim = P.mask[0] + P.mask[1] + P.mask[2];
+  if (P.ndim != 1 && P.ndim != 3)
+    return fail(h, MPRW_E_INVAL, "mprw_gpkde: only 1-D and 3-D reconstruction grids are supported");
+  if (!(o->min_hover_delta > 0.0) || !(o->max_hover_delta > o->min_hover_delta) || !(o->delta_hover_delta > 0.0))
+    return fail(h, MPRW_E_INVAL, "mprw_gpkde: invalid kernel database parameters");
+  if (n_bins_out)
+    for (int d = 0; d < 3; ++d) n_bins_out[d] = nb[d];
+  double binvol = 1.0;
+  int hd = 0;
+  for (int d = 0; d < 3; ++d)
+    if (P.bin[d] > 0.0) {
+      binvol *= P.bin[d];
+      ++hd;
+    }
+  P.binvol = binvol;
+  P.bin_distance = std::pow(binvol, 1.0 / (double)hd);
+  const double nd = (double)P.ndim;
+  P.support_c = std::pow((nd + 2.0) * std::pow(8.0 * PI_D, 0.5 * nd), 0.25);
+  P.alpha_c = std::pow((1.0 + std::pow(2.0, 0.5 * nd + 2.0)) / (3.0 * std::pow(2.0, 4.0 / (nd + 4.0))),
+                       1.0 / (nd + 6.0)) *
+              std::pow(nd + 2.0, 1.0 / (nd + 4.0)) / (std::pow(nd + 4.0, 1.0 / (nd + 6.0)));
+  P.beta_c = 2.0 / (nd + 4.0) / (nd + 6.0);
+  P.one_over_nd4 = 1.0 / (nd + 4.0);
+  P.minus_one_over_nd6 = -1.0 / (nd + 6.0);
+  P.one_plus_nd_q = 1.0 + 0.25 * nd;
+  P.max_sigma_growth = 1.5;
+  P.iso_threshold = 0.85;
+  // logarithmic database (prInitializeKernelDatabaseFlat, prGenerateLogSpaceData)
+  const int ndelta = (int)std::ceil(std::log10(o->max_hover_delta / o->min_hover_delta) /
+                                    std::log10(1 + o->delta_hover_delta)) + 1;
+  if (ndelta > KDE_MAXDB || ndelta < 2) return fail(h, MPRW_E_INVAL, "mprw_gpkde: kernel database too large");
+  P.ndelta = ndelta;
+  {
+    const double li = std::log10(o->min_hover_delta), le = std::log10(o->max_hover_delta);
+    const double de = (le - li) / (ndelta - 1);
+    double acc = 0.0;
+    for (int n = 0; n < ndelta; ++n) {
+      P.hod[n] = std::pow(10.0, li + acc);
+      acc = acc + de;
+    }
+  }
+  if (o->max_hover_delta * 4 * 2 + 1 > KDE_MAXLEN) return fail(h, MPRW_E_INVAL, "mprw_gpkde: maxHOverDelta too large");
+  P.min_hod = o->min_hover_delta;
+  P.dlog = std::log(P.hod[1] / P.hod[0]);
+  // bounded kernel sizes (boundKernelSizeFormat 0)
+  int maxd = -1, mind = -1;
+  for (int d = 0; d < 3; ++d) {
+    if (!P.mask[d]) continue;
+    P.max_k[d] = P.bin[d] * (0.9 * nb[d] - 1) / 3.0;
+    P.max_sd[d] = P.bin[d] * (0.9 * nb[d] - 1) / 4.0;
+    P.min_k[d] = 1.2 * P.bin[d] / 3.0;
+    P.min_sd[d] = 1.2 * P.bin[d] / 4.0;
+  }
+  for (int d = 0; d < 3; ++d)
+    if (P.max_k[d] > 0.0 && (maxd < 0 || P.max_k[d] < P.max_k[maxd])) maxd = d;
+  for (int d = 0; d < 3; ++d)
+    if (P.min_k[d] > 0.0 && (mind < 0 || P.min_k[d] > P.min_k[mind])) mind = d;
+  if (maxd < 0 || mind < 0) return fail(h, MPRW_E_INVAL, "mprw_gpkde: grid too small for bounded kernels");
+  P.max_dim = maxd;
+  P.min_dim = mind;
+
+  cudaStream_t s = h->stream;
+  h->launches = 0;
+  h->kde.launches = 0;
+  CK(cudaEventRecord(h->ev2, s));
+  // histogram (counts / effective mass)
+  int64_t nbinned = 0;
+  double eff = 1.0;
+  int rc = histogram_device(h, o->origin, o->bin_size, nb, &nbinned, &eff, nullptr);
+  if (rc != MPRW_OK) return rc;
+  const int64_t ngrid = (int64_t)nb[0] * nb[1] * nb[2];
+  // statistics of the active particles' coordinates (GridProjectedKDE.F90:4023-4030)
+  CK(h->kde.ensure_grid(ngrid));
+  double mean[3] = {0, 0, 0}, sd[3] = {0, 0, 0}, npts = 0.0;
+  {
+    std::vector<double> part;
+    int nblk = 0;
+    double *dpart = nullptr;
+    CK(cudaMalloc(&dpart, sizeof(double) * 4 * 152 * 4));
+    cudaError_t e = launch_coord_sums(geometry(h), h->n, h->d_cell, h->d_status, h->d_x, h->d_y, h->d_z,
+                                      h->opt.precision == MPRW_MIXED, 0, mean, dpart, &nblk, s);
+    part.resize(4 * nblk);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), dpart, sizeof(double) * 4 * nblk, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    double acc[4] = {0, 0, 0, 0};
+    for (int i = 0; i < nblk && e == cudaSuccess; ++i)
+      for (int k = 0; k < 4; ++k) acc[k] += part[4 * i + k];
+    npts = acc[3];
+    if (npts > 0)
+      for (int d = 0; d < 3; ++d) mean[d] = acc[d] / npts;
+    if (e == cudaSuccess)
+      e = launch_coord_sums(geometry(h), h->n, h->d_cell, h->d_status, h->d_x, h->d_y, h->d_z,
+                            h->opt.precision == MPRW_MIXED, 1, mean, dpart, &nblk, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), dpart, sizeof(double) * 4 * nblk, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    double sq[3] = {0, 0, 0};
+    for (int i = 0; i < nblk && e == cudaSuccess; ++i)
+      for (int k = 0; k < 3; ++k) sq[k] += part[4 * i + k];
+    for (int d = 0; d < 3; ++d) sd[d] = (P.mask[d] && npts > 0) ? std::sqrt(sq[d] / npts) : 0.0;
+    cudaFree(dpart);
+    h->launches += 2;
+    CK(e);
+  }
+  // active bins
+  int nactive = 0;
+  CK(kde_collect_active(h->kde, P, h->d_counts, s, &nactive));
+  int loops = 0;
+  if (nactive > 0) {
+    // initial smoothing (initialSmoothingSelection 0: Silverman-type scale)
+    double prod = 1.0;
+    for (int d = 0; d < 3; ++d)
+      if (P.mask[d]) prod *= sd[d];
+    const double ss = std::pow(prod, 1.0 / nd);
+    double hs = ss * std::pow(4.0 / ((nd + 2.0) * npts), 1.0 / (nd + 4.0));
+    if (ss == 0.0) hs = 2.0 * P.bin_distance;
+    // factor tables
+    std::vector<double> val;
+    std::vector<int> wm, wofs, sm[3], sofs[3];
+    kde_build_tables(P, val, wm, wofs, sm, sofs);
+    if (h->kde.d_val) cudaFree(h->kde.d_val);
+    if (h->kde.d_meta) cudaFree(h->kde.d_meta);
+    h->kde.d_val = nullptr;
+    h->kde.d_meta = nullptr;
+    CK(cudaMalloc(&h->kde.d_val, sizeof(double) * val.size()));
+    CK(cudaMalloc(&h->kde.d_meta, sizeof(int) * 8 * 3 * KDE_MAXDB));
+    std::vector<int> meta;
+    meta.insert(meta.end(), wm.begin(), wm.end());
+    meta.insert(meta.end(), wofs.begin(), wofs.end());
+    for (int a = 0; a < 3; ++a) {
+      meta.insert(meta.end(), sm[a].begin(), sm[a].end());
+      meta.insert(meta.end(), sofs[a].begin(), sofs[a].end());
+    }
+    CK(cudaMemcpyAsync(h->kde.d_val, val.data(), sizeof(double) * val.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->kde.d_meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, s));
+    const int L = 3 * KDE_MAXDB;
+    h->kde.wtab = KdeTable{h->kde.d_val, h->kde.d_meta, h->kde.d_meta + L};
+    for (int a = 0; a < 3; ++a)
+      h->kde.sdtab[a] = KdeTable{h->kde.d_val, h->kde.d_meta + (2 + 2 * a) * L, h->kde.d_meta + (3 + 2 * a) * L};
+    cudaError_t e = kde_run(h->kde, P, hs, npts, o->n_opt_loops, o->rel_err_convergence,
+                            o->skip_error_convergence != 0, s, &loops);
+    if (e == cudaErrorInvalidValue) return fail(h, MPRW_E_INVAL, "mprw_gpkde: net roughness is zero everywhere");
+    CK(e);
+    // effective mass, unit volume, scaling (GridProjectedKDE.F90:4292-4306, 5080-5084)
+    double f = eff;
+    double scale = 1.0;
+    if (o->unit_volume) scale *= binvol;
+    if (o->scaling_factor != 0.0) scale *= o->scaling_factor;
+    mul2_kernel<<<grid1d(ngrid), 256, 0, s>>>(h->kde.dens_grid, ngrid, f, scale);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(density, h->kde.dens_grid, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
+  } else {
+    CK(cudaMemsetAsync(h->kde.dens_grid, 0, sizeof(double) * ngrid, s));
+    CK(cudaMemcpyAsync(density, h->kde.dens_grid, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
+  }
+  if (histogram) {
+    mul2_kernel<<<grid1d(ngrid), 256, 0, s>>>(h->d_counts, ngrid, eff, 1.0);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(histogram, h->d_counts, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaEventRecord(h->ev3, s));
+  CK(cudaStreamSynchronize(s));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, h->ev2, h->ev3));
+  h->kde_ms = ms;
+  h->launches += h->kde.launches + 2;
+  if (loops_done) *loops_done = loops;
   return MPRW_OK;
 }
 

@@ -1,0 +1,69 @@
+// gpkde.cuh -- types of the device GPKDE reconstruction (gpkde.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+namespace mprw {
+
+constexpr int KDE_MAXDB = 64;    // h/delta database entries (16 at the defaults)
+constexpr int KDE_MAXLEN = 256;  // longest 1-D factor, 2*ceil(4*maxHOverDelta)+1
+constexpr double PI_D = 3.14159265358979323846;
+constexpr double SQRT8PI_D = 5.01325654926724104;  // sqrt(8*pi)
+
+// Constants of one reconstruction grid (GridProjectedKDE.F90 prInitialize,
+// prInitializeModuleConstants 1582-1611).
+struct KdeParams {
+  int ndim, mask[3], nb[3];
+  double bin[3], binvol, bin_distance;
+  int ndelta;
+  double hod[KDE_MAXDB];
+  double min_hod, dlog;  // log database: index = floor(log(h/bin/min)/dlog)+1
+  double max_k[3], min_k[3], max_sd[3], min_sd[3];
+  int max_dim, min_dim;
+  double support_c, alpha_c, beta_c, one_over_nd4, minus_one_over_nd6, one_plus_nd_q;
+  double max_sigma_growth, iso_threshold;
+};
+
+// 1-D factor table: for dimension d and database index n (0-based),
+// m[d*KDE_MAXDB+n] is the half width and val[ofs[...] + k], k = 0..2m, the
+// full symmetric factor.
+struct KdeTable {
+  const double *val;
+  const int *m, *ofs;
+};
+
+// Per active bin state (SoA).  3-vectors are stored dimension-major: v[d*n + b].
+struct KdeBins {
+  int n;
+  int *gx, *gy, *gz;  // 1-based bin indexes
+  double *count;
+  double *ks, *scale, *shape, *support, *nest, *dens, *cb, *rxx, *ryy, *rzz, *net, *dens_old, *scale_old;
+};
+
+struct KdeState {
+  KdeBins bins{};
+  int cap = 0;
+  double *dens_grid = nullptr, *cx = nullptr, *cy = nullptr, *cz = nullptr;
+  int64_t grid_cap = 0;
+  double *tmp = nullptr, *partial = nullptr, *d_scalars = nullptr, *h_scalars = nullptr;
+  int *d_flag = nullptr, *h_flag = nullptr, *d_blockcnt = nullptr;
+  KdeTable wtab{}, sdtab[3]{};
+  double *d_val = nullptr;
+  int *d_meta = nullptr;  // wm, wofs, sm[3], sofs[3]
+  int64_t launches = 0;
+
+  cudaError_t ensure_bins(int n);
+  cudaError_t ensure_grid(int64_t ngrid);
+  void release();
+};
+
+void kde_build_tables(const KdeParams &P, std::vector<double> &val, std::vector<int> &wm, std::vector<int> &wofs,
+                      std::vector<int> (&sm)[3], std::vector<int> (&sofs)[3]);
+cudaError_t kde_collect_active(KdeState &st, const KdeParams &P, const double *counts, cudaStream_t s,
+                               int *nactive);
+cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, int n_opt_loops, double rel_err,
+                    bool skip_error, cudaStream_t s, int *loops_done);
+
+}  // namespace mprw

@@ -65,6 +65,57 @@ template cudaError_t launch_global_xyz<float>(const Geometry &, int64_t, const i
                                               const float *, const float *, double *, double *, double *,
                                               cudaStream_t);
 
+// Per-block sums over the active particles of the model coordinates
+// (pass 0: x, y, z, count) or of squared deviations from `mean` (pass 1);
+// the host adds the block partials in order.
+template <typename R>
+__global__ void coord_sums_kernel(Geometry geo, int64_t n, const int32_t *cell, const int32_t *status, const R *x,
+                                  const R *y, const R *z, int pass, double m0, double m1, double m2, double *partial) {
+  __shared__ double red[4][32];
+  double a[4] = {0, 0, 0, 0};
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    if (status[p] != ST_ACTIVE) continue;
+    double X, Y, Z;
+    model_xyz<R>(geo, cell[p], x[p], y[p], z[p], X, Y, Z);
+    if (pass == 0) {
+      a[0] += X; a[1] += Y; a[2] += Z; a[3] += 1.0;
+    } else {
+      a[0] += (X - m0) * (X - m0); a[1] += (Y - m1) * (Y - m1); a[2] += (Z - m2) * (Z - m2);
+    }
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  for (int k = 0; k < 4; ++k) {
+    double v = a[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (l == 0) red[k][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 4; ++k) {
+      double s = 0.0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[k][i];
+      partial[4 * blockIdx.x + k] = s;
+    }
+  }
+}
+
+cudaError_t launch_coord_sums(const Geometry &geo, int64_t n, const int32_t *cell, const int32_t *status,
+                              const void *x, const void *y, const void *z, int mixed, int pass, const double mean[3],
+                              double *partial, int *nblocks, cudaStream_t s) {
+  const int threads = 256;
+  int64_t b = (n + threads - 1) / threads;
+  if (b > 152 * 4) b = 152 * 4;
+  if (b < 1) b = 1;
+  *nblocks = (int)b;
+  if (mixed)
+    coord_sums_kernel<float><<<(int)b, threads, 0, s>>>(geo, n, cell, status, (const float *)x, (const float *)y,
+                                                         (const float *)z, pass, mean[0], mean[1], mean[2], partial);
+  else
+    coord_sums_kernel<double><<<(int)b, threads, 0, s>>>(geo, n, cell, status, (const double *)x, (const double *)y,
+                                                          (const double *)z, pass, mean[0], mean[1], mean[2], partial);
+  return cudaGetLastError();
+}
+
 // bin index (0-based linear, x fastest) of an active particle, or -1
 template <typename R>
 __device__ __forceinline__ int64_t bin_index(const HistArgs &a, int64_t p) {

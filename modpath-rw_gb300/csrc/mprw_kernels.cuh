@@ -84,6 +84,9 @@ struct HistArgs {
 cudaError_t launch_hist_unit(const HistArgs &a, cudaStream_t s);
 cudaError_t launch_hist_bins(const HistArgs &a, cudaStream_t s);
 cudaError_t launch_u32_to_f64(const unsigned int *in, double *out, int64_t n, cudaStream_t s);
+cudaError_t launch_coord_sums(const Geometry &geo, int64_t n, const int32_t *cell, const int32_t *status,
+                              const void *x, const void *y, const void *z, int mixed, int pass, const double mean[3],
+                              double *partial, int *nblocks, cudaStream_t s);
 
 // Ordered (order-preserving) weighted sums: sort.cu
 cudaError_t ordered_bin_sums(const int64_t *bin_of, const double *mass, const int32_t *status, int64_t n,

@@ -49,6 +49,13 @@ class OptionsDesc(C.Structure):
                 ("uniform_porosity", C.c_int32), ("rng_seed", C.c_uint64), ("precision", C.c_int32)]
 
 
+class GpkdeOptions(C.Structure):
+    _fields_ = [("origin", C.c_double * 3), ("domain_size", C.c_double * 3), ("bin_size", C.c_double * 3),
+                ("n_opt_loops", C.c_int32), ("min_hover_delta", C.c_double), ("delta_hover_delta", C.c_double),
+                ("max_hover_delta", C.c_double), ("rel_err_convergence", C.c_double),
+                ("skip_error_convergence", C.c_int32), ("unit_volume", C.c_int32), ("scaling_factor", C.c_double)]
+
+
 class FlowDesc(C.Structure):
     _fields_ = [("ia", _ip), ("ja", _ip), ("nja", C.c_int64), ("flowja", _dp), ("boundary_flows", _dp),
                 ("porosity", _dp), ("retardation", _dp), ("iboundts", _ip), ("icboundts", _ip),
@@ -76,6 +83,7 @@ def load_library() -> C.CDLL:
         "mprw_advance": (C.c_int, [H, C.c_double, C.c_double, C.POINTER(C.c_int64)]),
         "mprw_get_particles": (C.c_int, [H, _ip, _dp, _dp, _dp, _dp, _ip, _up, _dp, _dp, _dp]),
         "mprw_histogram": (C.c_int, [H, _dp, _dp, _ip, _dp, C.POINTER(C.c_int64), _dp]),
+        "mprw_gpkde": (C.c_int, [H, C.POINTER(GpkdeOptions), _dp, _dp, _ip, _ip]),
         "mprw_set_stream": (C.c_int, [H, C.c_void_p]),
         "mprw_last_timings": (C.c_int, [H, _dp, _dp, _dp, C.POINTER(C.c_int64)]),
         "mprw_destroy": (C.c_int, [H]),
@@ -216,6 +224,29 @@ class Tracker:
         self._check(self.lib.mprw_histogram(self.h, _p(o, _dp), _p(b, _dp), _p(nb, _ip), _p(counts, _dp),
                                             C.byref(nbinned), C.byref(eff)), "mprw_histogram")
         return counts.reshape(int(nb[2]), int(nb[1]), int(nb[0])), nbinned.value, eff.value
+
+    def gpkde(self, domain_size, bin_size, origin=(0.0, 0.0, 0.0), n_opt_loops=10, kdb=(0.3, 0.3, 15.0),
+              rel_err=0.02, skip_error=False, unit_volume=True, scaling_factor=1.0):
+        """GPKDE reconstruction of the active particles.  Returns (density, histogram,
+        loops) with the grids shaped (nz, ny, nx)."""
+        o = GpkdeOptions()
+        for d in range(3):
+            o.origin[d], o.domain_size[d], o.bin_size[d] = float(origin[d]), float(domain_size[d]), float(bin_size[d])
+        o.n_opt_loops = int(n_opt_loops)
+        o.min_hover_delta, o.delta_hover_delta, o.max_hover_delta = (float(v) for v in kdb)
+        o.rel_err_convergence = float(rel_err)
+        o.skip_error_convergence = int(skip_error)
+        o.unit_volume = int(unit_volume)
+        o.scaling_factor = float(scaling_factor)
+        nb = [int(domain_size[d] / bin_size[d] + 0.5) if bin_size[d] != 0 else 1 for d in range(3)]
+        dens = np.empty(int(np.prod(nb)))
+        hist = np.empty(int(np.prod(nb)))
+        nbo = np.zeros(3, np.int32)
+        loops = C.c_int32(0)
+        self._check(self.lib.mprw_gpkde(self.h, C.byref(o), _p(dens, _dp), _p(hist, _dp), _p(nbo, _ip),
+                                        C.byref(loops)), "mprw_gpkde")
+        shp = (nb[2], nb[1], nb[0])
+        return dens.reshape(shp), hist.reshape(shp), loops.value
 
     def set_stream(self, stream_ptr: int):
         self._check(self.lib.mprw_set_stream(self.h, C.c_void_p(stream_ptr)), "mprw_set_stream")
