@@ -180,6 +180,33 @@ typedef struct {
 int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *opt, double *density, double *histogram,
                int32_t n_bins_out[3], int32_t *loops_done);
 
+/* Allocation-free unit-mass histogram.  No counterpart in the reference: it
+ * exists for callers that cannot allocate device memory when they bin -- a
+ * host code that owns a fixed device-memory budget and hands the library only
+ * pre-sized buffers, or one running where cudaMalloc would synchronise the
+ * device or is forbidden.  It needs no handle and calls no cudaMalloc,
+ * cudaFree or allocating library routine.
+ *
+ * All pointers are DEVICE pointers: gx/gy/gz are model coordinates (as
+ * mprw_get_particles returns them), status the particle statuses; only
+ * ACTIVE (1) particles are counted.  counts (prod n_bins doubles, x fastest)
+ * receives the particle count per bin, identical to mprw_histogram's with
+ * unit masses; n_binned (one int64, may be NULL) the particles binned.  The
+ * work is queued on `stream` (a cudaStream_t, NULL = the default stream) and
+ * the call returns without waiting for it.
+ *
+ * Limit: prod(n_bins) <= MPRW_NOALLOC_MAX_BINS, else MPRW_E_INVAL.  The
+ * scratch (MPRW_NOALLOC_MAX_BINS + 2 32-bit words, about 4 MiB) is a fixed
+ * array in the library's device image that every GPU loading the library
+ * holds until the process exits.  The first call on each device looks up the
+ * array's device address (with that device current), so make that first
+ * call before any stream capture.  All calls share the array and each clears
+ * it before counting; calls that overlap on the GPU race on it. */
+#define MPRW_NOALLOC_MAX_BINS (1 << 20)
+int mprw_histogram_noalloc(const double *gx, const double *gy, const double *gz, const int32_t *status,
+                           int64_t n, const double origin[3], const double bin_size[3],
+                           const int32_t n_bins[3], double *counts, int64_t *n_binned, void *stream);
+
 /* Optional: launch on a caller-provided cudaStream_t (NULL = the handle's). */
 int mprw_set_stream(mprw_handle *h, void *stream);
 
