@@ -19,6 +19,7 @@
 // bins are two-stage with a fixed order, so runs are repeatable; the host
 // takes the per-loop convergence decision from four scalars.
 #include <cfloat>
+#include <climits>
 #include <cmath>
 #include <vector>
 
@@ -58,36 +59,6 @@ struct Span {
   int g0[3], n[3], k0[3];
 };
 
-// Load the three factors of one kernel (table `tab`, per-dimension indexes
-// idx[d] 1-based) for bin `gid`, fold them, and return the grid span.
-__device__ void load_kernel(const KdeParams &P, const KdeTable &tab, const int idx[3], const int gid[3],
-                            double *sv, Span &S) {
-  __shared__ int s_m[3], s_ofs[3];
-  if (threadIdx.x < 3) {
-    const int d = threadIdx.x;
-    s_m[d] = tab.m[d * KDE_MAXDB + idx[d] - 1];
-    s_ofs[d] = tab.ofs[d * KDE_MAXDB + idx[d] - 1];
-  }
-  __syncthreads();
-  for (int d = 0; d < 3; ++d) {
-    const int m = s_m[d];
-    for (int k = threadIdx.x; k < 2 * m + 1; k += blockDim.x) sv[d * KDE_MAXLEN + k] = tab.val[s_ofs[d] + k];
-  }
-  __syncthreads();
-  if (threadIdx.x < 3) {
-    const int d = threadIdx.x;
-    if (P.mask[d]) fold_factor(sv + d * KDE_MAXLEN, s_m[d], gid[d], P.nb[d]);
-  }
-  __syncthreads();
-  for (int d = 0; d < 3; ++d) {
-    const int m = s_m[d];
-    const int g0 = max(gid[d] - m, 1), g1 = min(gid[d] + m, P.nb[d]);
-    S.g0[d] = g0;
-    S.n[d] = g1 - g0 + 1;
-    S.k0[d] = g0 - gid[d] + m;
-  }
-}
-
 __device__ __forceinline__ double block_sum(double v, double *red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -100,97 +71,292 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
   return s;  // valid in thread 0
 }
 
-// kind: 0 = W kernel from ks (3 per-dim smoothings), 1 = isotropic kernel
-// from a per-bin scale (sigma support), 2 = second-derivative kernel of
-// axis `axis` from cb[axis]
-__device__ void bin_indexes(const KdeParams &P, const KdeBins &B, int b, int kind, int axis, int idx[3]) {
-  idx[0] = idx[1] = idx[2] = 1;
-  if (kind == 0) {
-    for (int d = 0; d < 3; ++d)
-      if (P.mask[d]) idx[d] = log_index(P, B.ks[d * B.n + b], d);
-  } else if (kind == 1) {
-    const double s = B.support[b];
-    for (int d = 0; d < 3; ++d)
-      if (P.mask[d]) idx[d] = log_index(P, s, d);
-  } else {
-    const int n = log_index(P, B.cb[axis * B.n + b], axis);
-    for (int d = 0; d < 3; ++d) idx[d] = n;  // the second-derivative database is isotropic
-  }
-}
+// ---- density scatter: one warp per bin --------------------------------------
+// The W kernel of a bin is anisotropic (one database level per dimension), so
+// bins share no kernel and each warp folds its bin's three factors in shared
+// memory and adds count * fx fy fz over the span (FP64 atomics).
+constexpr int kWarpsW = 4;
 
-__global__ void scatter_kernel(KdeParams P, KdeBins B, KdeTable tab, int kind, int axis, double *grid) {
-  __shared__ double sv[3 * KDE_MAXLEN];
-  const int b = blockIdx.x;
-  if (b >= B.n) return;
-  int idx[3], gid[3] = {B.gx[b], B.gy[b], B.gz[b]};
-  bin_indexes(P, B, b, kind, axis, idx);
+__global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, KdeBins B, KdeTable tab,
+                                                                double *grid) {
+  __shared__ double sv_all[kWarpsW][3 * KDE_MAXLEN];
+  __shared__ int sm_all[kWarpsW][3], sofs_all[kWarpsW][3];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int b = blockIdx.x * kWarpsW + w;
+  if (b >= B.n) return;  // warp-uniform
+  double *sv = sv_all[w];
+  const int gid[3] = {B.gx[b], B.gy[b], B.gz[b]};
+  if (lane < 3) {
+    const int d = lane;
+    const int idx = P.mask[d] ? log_index(P, B.ks[d * B.n + b], d) : 1;
+    sm_all[w][d] = tab.m[d * KDE_MAXDB + idx - 1];
+    sofs_all[w][d] = tab.ofs[d * KDE_MAXDB + idx - 1];
+  }
+  __syncwarp();
+  for (int d = 0; d < 3; ++d) {
+    const int m = sm_all[w][d], o = sofs_all[w][d];
+    for (int k = lane; k < 2 * m + 1; k += 32) sv[d * KDE_MAXLEN + k] = tab.val[o + k];
+  }
+  __syncwarp();
+  if (lane < 3 && P.mask[lane]) fold_factor(sv + lane * KDE_MAXLEN, sm_all[w][lane], gid[lane], P.nb[lane]);
+  __syncwarp();
   Span S;
-  load_kernel(P, tab, idx, gid, sv, S);
+  for (int d = 0; d < 3; ++d) {
+    const int m = sm_all[w][d];
+    const int g0 = max(gid[d] - m, 1), g1 = min(gid[d] + m, P.nb[d]);
+    S.g0[d] = g0;
+    S.n[d] = g1 - g0 + 1;
+    S.k0[d] = g0 - gid[d] + m;
+  }
   const double cnt = B.count[b];
-  const int tot = S.n[0] * S.n[1] * S.n[2];
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int ix = t % S.n[0], r = t / S.n[0], iy = r % S.n[1], iz = r / S.n[1];
-    const double w = sv[S.k0[0] + ix] * sv[KDE_MAXLEN + S.k0[1] + iy] * sv[2 * KDE_MAXLEN + S.k0[2] + iz];
+  const int n0 = S.n[0], n01 = S.n[0] * S.n[1], tot = n01 * S.n[2];
+  for (int t = lane; t < tot; t += 32) {
+    const int iz = t / n01, r = t - iz * n01, iy = r / n0, ix = r - iy * n0;
+    const double wv = sv[S.k0[0] + ix] * sv[KDE_MAXLEN + S.k0[1] + iy] * sv[2 * KDE_MAXLEN + S.k0[2] + iz];
     const int64_t g = (int64_t)(S.g0[0] - 1 + ix) +
                       (int64_t)P.nb[0] * ((S.g0[1] - 1 + iy) + (int64_t)P.nb[1] * (S.g0[2] - 1 + iz));
-    atomicAdd(&grid[g], cnt * w);
+    atomicAdd(&grid[g], cnt * wv);
   }
 }
 
-// nEstimate-type gather with the isotropic kernel of scale `support` (kind 1)
-__global__ void gather_kernel(KdeParams P, KdeBins B, KdeTable tab, const double *grid, double *out) {
-  __shared__ double sv[3 * KDE_MAXLEN];
-  __shared__ double red[32];
-  const int b = blockIdx.x;
-  if (b >= B.n) return;
-  int idx[3], gid[3] = {B.gx[b], B.gy[b], B.gz[b]};
-  bin_indexes(P, B, b, 1, 0, idx);
-  Span S;
-  load_kernel(P, tab, idx, gid, sv, S);
-  const int tot = S.n[0] * S.n[1] * S.n[2];
-  double acc = 0.0;
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int ix = t % S.n[0], r = t / S.n[0], iy = r % S.n[1], iz = r / S.n[1];
-    const double w = sv[S.k0[0] + ix] * sv[KDE_MAXLEN + S.k0[1] + iy] * sv[2 * KDE_MAXLEN + S.k0[2] + iz];
-    const int64_t g = (int64_t)(S.g0[0] - 1 + ix) +
-                      (int64_t)P.nb[0] * ((S.g0[1] - 1 + iy) + (int64_t)P.nb[1] * (S.g0[2] - 1 + iz));
-    acc += grid[g] * w;
-  }
-  const double s = block_sum(acc, red);
-  if (threadIdx.x == 0) out[b] = s;
+// ---- separable passes -------------------------------------------------------
+// The reference folds a kernel that crosses a grid edge back into the grid:
+// first the part below cell 1 (mirrored about the lower face), then the part
+// above cell n (mirrored about the upper face), and drops what still lies
+// outside.  Unfolded kernel position p (1-based) therefore lands on
+// reflect_pos(p, n), or nowhere when that is < 1; for kernels narrower than
+// the grid this is the plain mirror image.
+__device__ __forceinline__ int reflect_pos(int p, int n) {
+  if (p < 1) p = 1 - p;
+  if (p > n) p = 2 * n + 1 - p;
+  return p;
 }
 
-// roughness gathers of the squared curvatures (3-D: XX, YY, ZZ and the
-// cross products of squares, GridProjectedKDE.F90:2470-2600)
-__global__ void gather_roughness3_kernel(KdeParams P, KdeBins B, KdeTable tab, const double *cx, const double *cy,
-                                         const double *cz) {
-  __shared__ double sv[3 * KDE_MAXLEN];
-  __shared__ double red[32];
-  const int b = blockIdx.x;
-  if (b >= B.n) return;
-  int idx[3], gid[3] = {B.gx[b], B.gy[b], B.gz[b]};
-  bin_indexes(P, B, b, 1, 0, idx);
-  Span S;
-  load_kernel(P, tab, idx, gid, sv, S);
-  const int tot = S.n[0] * S.n[1] * S.n[2];
-  double a[6] = {0, 0, 0, 0, 0, 0};
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int ix = t % S.n[0], r = t / S.n[0], iy = r % S.n[1], iz = r / S.n[1];
-    const double w = sv[S.k0[0] + ix] * sv[KDE_MAXLEN + S.k0[1] + iy] * sv[2 * KDE_MAXLEN + S.k0[2] + iz];
-    const int64_t g = (int64_t)(S.g0[0] - 1 + ix) +
-                      (int64_t)P.nb[0] * ((S.g0[1] - 1 + iy) + (int64_t)P.nb[1] * (S.g0[2] - 1 + iz));
-    const double x = cx[g], y = cy[g], z = cz[g];
-    a[0] += x * w;
-    a[1] += y * w;
-    a[2] += z * w;
-    a[3] += (x * y) * w;
-    a[4] += (x * z) * w;
-    a[5] += (y * z) * w;
+__global__ void key_init_kernel(KeyAcc *K) {
+  for (int k = threadIdx.x; k < KDE_KMAX; k += blockDim.x) {
+    K->box[k][0] = K->box[k][2] = K->box[k][4] = INT_MAX;
+    K->box[k][1] = K->box[k][3] = K->box[k][5] = INT_MIN;
+    K->cnt[k] = 0;
   }
-  double s[6];
-  for (int k = 0; k < 6; ++k) s[k] = block_sum(a[k], red);
-  if (threadIdx.x == 0) {
-    const double rxx = s[0], ryy = s[1], rzz = s[2], rxy = s[3], rxz = s[4], ryz = s[5];
+}
+
+__device__ __forceinline__ void key_record(KeyAcc *K, int key, const int lev[3], const int g[3]) {
+  for (int d = 0; d < 3; ++d) {
+    atomicMin(&K->box[key][2 * d], g[d]);
+    atomicMax(&K->box[key][2 * d + 1], g[d]);
+    K->lev[key][d] = lev[d];  // every bin of the key writes the same levels
+  }
+  atomicAdd(&K->cnt[key], 1);
+}
+
+// kind 1: the smoothing (sigma) kernel of scale support[b]; its level per
+// dimension is non-decreasing in the scale, so the sum of the three levels
+// (minus 3, each level is >= 1) identifies the triple.  kind 2: the second-derivative kernel of each
+// active axis a from cb[a] (the database is isotropic: one level), key
+// a*KDE_MAXDB + level-1; a NaN bandwidth has no kernel and is skipped, as the
+// reference's 1-D path does (GridProjectedKDE.F90:2340-2345).
+__global__ void key_assign_kernel(KdeParams P, KdeBins B, int kind, int *bin_key, KeyAcc *K) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B.n) return;
+  const int g[3] = {B.gx[b], B.gy[b], B.gz[b]};
+  if (kind == 1) {
+    const double s = B.support[b];
+    int lev[3] = {1, 1, 1};
+    for (int d = 0; d < 3; ++d)
+      if (P.mask[d]) lev[d] = log_index(P, s, d);
+    const int key = lev[0] + lev[1] + lev[2] - 3;
+    bin_key[b] = key;
+    key_record(K, key, lev, g);
+  } else {
+    for (int a = 0; a < 3; ++a) {
+      int key = -1;
+      const double h = B.cb[a * B.n + b];
+      if (P.mask[a] && h == h) {
+        const int n = log_index(P, h, a);
+        const int lev[3] = {n, n, n};
+        key = a * KDE_MAXDB + n - 1;
+        key_record(K, key, lev, g);
+      }
+      bin_key[a * B.n + b] = key;
+    }
+  }
+}
+
+// Compact the keys present and lay out the pass regions.  Gather: pass 1
+// (x) covers the bins' x range and the y, z ranges widened by the half
+// widths; pass 2 (y) the bins' x, y ranges and the widened z range; the z
+// pass runs per bin.  Scatter: pass 1 widens x, pass 2 widens y, the z pass
+// writes the grid.  out[0..3]: keys present, pass-1 and pass-2 elements,
+// largest region.
+__global__ void plan_kernel(KdeParams P, const KeyAcc *K, KdeTable t0, KdeTable t1, KdeTable t2, int scatter,
+                            SepPlan *pl, long long *out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int np = 0;
+  long long o1 = 0, o2 = 0, mx = 0;
+  for (int k = 0; k < KDE_KMAX; ++k) {
+    pl->slot_of[k] = -1;
+    if (K->cnt[k] == 0) continue;
+    const int axis = k / KDE_MAXDB;
+    const KdeTable T = !scatter ? t0 : (axis == 0 ? t0 : (axis == 1 ? t1 : t2));
+    int m[3];
+    for (int d = 0; d < 3; ++d) {
+      const int li = d * KDE_MAXDB + K->lev[k][d] - 1;
+      m[d] = T.m[li];
+      pl->m[np][d] = m[d];
+      pl->f[np][d] = T.val + T.ofs[li];
+    }
+    int bx[6], r1[6], r2[6];
+    for (int i = 0; i < 6; ++i) bx[i] = K->box[k][i];
+    for (int i = 0; i < 6; ++i) r1[i] = r2[i] = bx[i];
+    if (!scatter) {
+      r1[2] = max(1, bx[2] - m[1]);
+      r1[3] = min(P.nb[1], bx[3] + m[1]);
+      r1[4] = r2[4] = max(1, bx[4] - m[2]);
+      r1[5] = r2[5] = min(P.nb[2], bx[5] + m[2]);
+    } else {
+      r1[0] = r2[0] = max(1, bx[0] - m[0]);
+      r1[1] = r2[1] = min(P.nb[0], bx[1] + m[0]);
+      r2[2] = max(1, bx[2] - m[1]);
+      r2[3] = min(P.nb[1], bx[3] + m[1]);
+    }
+    const long long v1 = (long long)(r1[1] - r1[0] + 1) * (r1[3] - r1[2] + 1) * (r1[5] - r1[4] + 1);
+    const long long v2 = (long long)(r2[1] - r2[0] + 1) * (r2[3] - r2[2] + 1) * (r2[5] - r2[4] + 1);
+    for (int i = 0; i < 6; ++i) {
+      pl->box[np][i] = bx[i];
+      pl->r1[np][i] = r1[i];
+      pl->r2[np][i] = r2[i];
+    }
+    pl->o1[np] = o1;
+    pl->o2[np] = o2;
+    o1 += v1;
+    o2 += v2;
+    mx = max(mx, max(v1, v2));
+    pl->key[np] = k;
+    pl->slot_of[k] = np;
+    ++np;
+  }
+  pl->np = np;
+  out[0] = np;
+  out[1] = o1;
+  out[2] = o2;
+  out[3] = mx;
+}
+
+__device__ __forceinline__ void region_xyz(const int r[6], long long i, int &x, int &y, int &z) {
+  const int nx = r[1] - r[0] + 1, ny = r[3] - r[2] + 1;
+  const long long q = i / nx;
+  x = r[0] + (int)(i - q * nx);
+  y = r[2] + (int)(q % ny);
+  z = r[4] + (int)(q / ny);
+}
+
+__device__ __forceinline__ long long region_vol(const int r[6]) {
+  return (long long)(r[1] - r[0] + 1) * (r[3] - r[2] + 1) * (r[5] - r[4] + 1);
+}
+
+__device__ __forceinline__ long long region_loc(const int r[6], int x, int y, int z) {
+  return (long long)(x - r[0]) + (long long)(r[1] - r[0] + 1) * ((y - r[2]) + (long long)(r[3] - r[2] + 1) * (z - r[4]));
+}
+
+// Gather pass 1: T1 = sum_t fx[t] F(reflect(x - m + t), y, z) over region 1.
+// NC = 1: one field; NC = 6: the squared curvatures cx, cy, cz and their
+// pairwise products (the roughness terms, GridProjectedKDE.F90:2470-2600).
+template <int NC>
+__global__ void gather_x_kernel(KdeParams P, const SepPlan *pl, const double *F0, const double *F1,
+                                const double *F2, double *T1) {
+  const int j = blockIdx.y;
+  if (j >= pl->np) return;
+  int r[6];
+  for (int i = 0; i < 6; ++i) r[i] = pl->r1[j][i];
+  const int m = pl->m[j][0], n = P.nb[0];
+  const double *f = pl->f[j][0];
+  double *out = T1 + pl->o1[j] * NC;
+  const long long vol = region_vol(r);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
+    int x, y, z;
+    region_xyz(r, i, x, y, z);
+    const long long row = (long long)P.nb[0] * ((y - 1) + (long long)P.nb[1] * (z - 1)) - 1;
+    double acc[NC];
+    for (int c = 0; c < NC; ++c) acc[c] = 0.0;
+    for (int t = 0; t <= 2 * m; ++t) {
+      const int p = reflect_pos(x - m + t, n);
+      if (p < 1) continue;
+      const double w = f[t];
+      if constexpr (NC == 1) {
+        acc[0] += w * F0[row + p];
+      } else {
+        const double a = F0[row + p], bb = F1[row + p], c = F2[row + p];
+        acc[0] += w * a;
+        acc[1] += w * bb;
+        acc[2] += w * c;
+        acc[3] += w * (a * bb);
+        acc[4] += w * (a * c);
+        acc[5] += w * (bb * c);
+      }
+    }
+    for (int c = 0; c < NC; ++c) out[i * NC + c] = acc[c];
+  }
+}
+
+// Gather pass 2: T2 = sum_t fy[t] T1(x, reflect(y - m + t), z) over region 2.
+template <int NC>
+__global__ void gather_y_kernel(KdeParams P, const SepPlan *pl, const double *T1, double *T2) {
+  const int j = blockIdx.y;
+  if (j >= pl->np) return;
+  int r1[6], r2[6];
+  for (int i = 0; i < 6; ++i) {
+    r1[i] = pl->r1[j][i];
+    r2[i] = pl->r2[j][i];
+  }
+  const int m = pl->m[j][1], n = P.nb[1];
+  const double *f = pl->f[j][1];
+  const double *in = T1 + pl->o1[j] * NC;
+  double *out = T2 + pl->o2[j] * NC;
+  const long long vol = region_vol(r2);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
+    int x, y, z;
+    region_xyz(r2, i, x, y, z);
+    double acc[NC];
+    for (int c = 0; c < NC; ++c) acc[c] = 0.0;
+    for (int t = 0; t <= 2 * m; ++t) {
+      const int p = reflect_pos(y - m + t, n);
+      if (p < 1) continue;
+      const double w = f[t];
+      const long long l = region_loc(r1, x, p, z) * NC;
+      for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
+    }
+    for (int c = 0; c < NC; ++c) out[i * NC + c] = acc[c];
+  }
+}
+
+// Gather pass 3 at every bin: sum_t fz[t] T2(bx, by, reflect(bz - m + t)).
+// NC = 1 writes out[b] (and out2[b] when given); NC = 6 the roughness terms
+// and the net roughness (GridProjectedKDE.F90:2594-2600).
+template <int NC>
+__global__ void gather_z_kernel(KdeParams P, KdeBins B, const SepPlan *pl, const int *bin_key, const double *T2,
+                                double *out, double *out2) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B.n) return;
+  const int j = pl->slot_of[bin_key[b]];
+  const int m = pl->m[j][2], n = P.nb[2];
+  const double *f = pl->f[j][2];
+  const int *r2 = pl->r2[j];
+  const double *in = T2 + pl->o2[j] * NC;
+  const int bx = B.gx[b], by = B.gy[b], bz = B.gz[b];
+  double acc[NC];
+  for (int c = 0; c < NC; ++c) acc[c] = 0.0;
+  for (int t = 0; t <= 2 * m; ++t) {
+    const int p = reflect_pos(bz - m + t, n);
+    if (p < 1) continue;
+    const double w = f[t];
+    const long long l = region_loc(r2, bx, by, p) * NC;
+    for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
+  }
+  if constexpr (NC == 1) {
+    out[b] = acc[0];
+    if (out2) out2[b] = acc[0];
+  } else {
+    const double rxx = acc[0], ryy = acc[1], rzz = acc[2], rxy = acc[3], rxz = acc[4], ryz = acc[5];
     B.rxx[b] = rxx;
     B.ryy[b] = ryy;
     B.rzz[b] = rzz;
@@ -199,6 +365,117 @@ __global__ void gather_roughness3_kernel(KdeParams P, KdeBins B, KdeTable tab, c
     if (rxz > 0.0) v = v + 2.0 * rxz * pow(ryy * ryy / rxx / rzz, 1.0 / 6.0);
     if (rxy > 0.0) v = v + 2.0 * rxy * pow(rzz * rzz / rxx / ryy, 1.0 / 6.0);
     B.net[b] = v;
+  }
+}
+
+// Scatter = transpose of the folded gather.  Cell x (1-based, 1..n) receives
+// the kernel positions whose fold lands on it: x itself, 1-x (mirrored at the
+// lower face), x-2n (mirrored at the lower, then the upper face) and
+// 2n+1-x (mirrored at the upper face).  acc += f[t] * V(q + m - t) for each
+// such q, V read where it is non-zero: source positions in [lo, hi].
+__device__ __forceinline__ double scatter_taps(const double *f, int m, int x, int n, int lo, int hi,
+                                               const double *V, long long stride, long long base,
+                                               const int *cell_bin, const int *keys, int key, const double *cnt) {
+  const int q4[4] = {x, 1 - x, x - 2 * n, 2 * n + 1 - x};
+  double acc = 0.0;
+  for (int k = 0; k < 4; ++k) {
+    const int q = q4[k];
+    const int t0 = max(0, q + m - hi), t1 = min(2 * m, q + m - lo);
+    for (int t = t0; t <= t1; ++t) {
+      const int src = q + m - t;
+      const long long l = base + (long long)src * stride;
+      double v;
+      if (cell_bin) {
+        const int cb = cell_bin[l];
+        if (cb < 0 || keys[cb] != key) continue;
+        v = cnt[cb];
+      } else {
+        v = V[l];
+      }
+      acc += f[t] * v;
+    }
+  }
+  return acc;
+}
+
+// Scatter pass 1 (x) from the bins of each key (count per bin) over region 1.
+__global__ void scatter_x_kernel(KdeParams P, KdeBins B, const SepPlan *pl, const int *cell_bin, const int *bin_key,
+                                 double *V1) {
+  const int j = blockIdx.y;
+  if (j >= pl->np) return;
+  int r[6], bx[6];
+  for (int i = 0; i < 6; ++i) {
+    r[i] = pl->r1[j][i];
+    bx[i] = pl->box[j][i];
+  }
+  const int key = pl->key[j], axis = key / KDE_MAXDB;
+  const int *keys = bin_key + (long long)axis * B.n;
+  const int m = pl->m[j][0], n = P.nb[0];
+  const double *f = pl->f[j][0];
+  double *out = V1 + pl->o1[j];
+  const long long vol = region_vol(r);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
+    int x, y, z;
+    region_xyz(r, i, x, y, z);
+    const long long row = (long long)P.nb[0] * ((y - 1) + (long long)P.nb[1] * (z - 1)) - 1;
+    out[i] = scatter_taps(f, m, x, n, bx[0], bx[1], nullptr, 1, row, cell_bin, keys, key, B.count);
+  }
+}
+
+// Scatter pass 2 (y) over region 2.
+__global__ void scatter_y_kernel(KdeParams P, const SepPlan *pl, const double *V1, double *V2) {
+  const int j = blockIdx.y;
+  if (j >= pl->np) return;
+  int r1[6], r2[6];
+  for (int i = 0; i < 6; ++i) {
+    r1[i] = pl->r1[j][i];
+    r2[i] = pl->r2[j][i];
+  }
+  const int m = pl->m[j][1], n = P.nb[1];
+  const double *f = pl->f[j][1];
+  const double *in = V1 + pl->o1[j];
+  double *out = V2 + pl->o2[j];
+  const long long vol = region_vol(r2);
+  const long long sy = r1[1] - r1[0] + 1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
+    int x, y, z;
+    region_xyz(r2, i, x, y, z);
+    const long long base = region_loc(r1, x, r1[2], z) - (long long)r1[2] * sy;
+    out[i] = scatter_taps(f, m, y, n, r1[2], r1[3], in, sy, base, nullptr, nullptr, 0, nullptr);
+  }
+}
+
+// Scatter pass 3 (z) of every key of one axis into that axis's curvature
+// grid, keys in increasing order, then the normalisation
+// ((c / binVolume) / binSize^2)^2 (GridProjectedKDE.F90:2366-2461).
+__global__ void scatter_z_kernel(KdeParams P, const SepPlan *pl, const double *V2, double *c0, double *c1,
+                                 double *c2) {
+  const int axis = blockIdx.y;
+  if (!P.mask[axis]) return;
+  double *out = axis == 0 ? c0 : (axis == 1 ? c1 : c2);
+  const double bs2 = P.bin[axis] * P.bin[axis];
+  const long long ngrid = (long long)P.nb[0] * P.nb[1] * P.nb[2];
+  const int np = pl->np, n = P.nb[2];
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ngrid; g += (long long)gridDim.x * blockDim.x) {
+    const int x = 1 + (int)(g % P.nb[0]);
+    const long long q = g / P.nb[0];
+    const int y = 1 + (int)(q % P.nb[1]);
+    const int z = 1 + (int)(q / P.nb[1]);
+    double acc = 0.0;
+    for (int j = 0; j < np; ++j) {
+      if (pl->key[j] / KDE_MAXDB != axis) continue;
+      const int *r2 = pl->r2[j];
+      if (x < r2[0] || x > r2[1] || y < r2[2] || y > r2[3]) continue;
+      const int m = pl->m[j][2];
+      if (z < r2[4] - m || z > r2[5] + m) continue;
+      const long long sz = (long long)(r2[1] - r2[0] + 1) * (r2[3] - r2[2] + 1);
+      const long long base = region_loc(r2, x, y, r2[4]) - (long long)r2[4] * sz;
+      acc += scatter_taps(pl->f[j][2], m, z, n, r2[4], r2[5], V2 + pl->o2[j], sz, base, nullptr, nullptr, 0,
+                          nullptr);
+    }
+    double c = acc / P.binvol;
+    c = c / bs2;
+    out[g] = c * c;
   }
 }
 
@@ -232,15 +509,6 @@ __global__ void init_bins_kernel(KdeParams P, KdeBins B, double hs) {
 __global__ void grid_scale_kernel(double *g, int64_t n, double div) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     g[i] = g[i] / div;
-}
-
-// curvature normalisation: c = ((c / binVolume) / binSize^2)^2
-__global__ void curvature_square_kernel(double *g, int64_t n, double binvol, double bs2) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double c = g[i] / binvol;
-    c = c / bs2;
-    g[i] = c * c;
-  }
 }
 
 __global__ void pick_kernel(KdeParams P, KdeBins B, const double *grid, double *out) {
@@ -297,7 +565,6 @@ __global__ void curvature_bandwidth_kernel(KdeParams P, KdeBins B) {
 __global__ void reduce_stage1_kernel(KdeBins B, int what, double aux0, double aux1, double *partial) {
   __shared__ double red[32];
   double v0 = 0.0, v1 = 0.0, v2 = 0.0;
-  bool isMax = (what == 0 || what == 2);
   double mx0 = -DBL_MAX, mx1 = -DBL_MAX, mn0 = DBL_MAX;
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
     if (what == 0) {  // max(net), min(net > 0)
@@ -321,7 +588,6 @@ __global__ void reduce_stage1_kernel(KdeBins B, int what, double aux0, double au
       if (B.scale[b] > 0.0) mn0 = fmin(mn0, -B.scale[b]);  // -max(scale)
     }
   }
-  (void)isMax;
   // write per-thread values through a block reduction in fixed order
   if (what == 1) {
     const double s0 = block_sum(v0, red);
@@ -494,7 +760,7 @@ __global__ void active_count_kernel(const double *counts, int64_t nbins, int chu
 }
 
 __global__ void active_write_kernel(const double *counts, int64_t nbins, int chunk, const int *blockofs,
-                                    KdeParams P, KdeBins B) {
+                                    KdeParams P, KdeBins B, int *cell_bin) {
   if (threadIdx.x != 0) return;
   const int64_t beg = (int64_t)blockIdx.x * chunk;
   const int64_t end = min(beg + chunk, nbins);
@@ -510,6 +776,7 @@ __global__ void active_write_kernel(const double *counts, int64_t nbins, int chu
     B.gy[o] = iy + 1;
     B.gz[o] = iz + 1;
     B.count[o] = c;
+    cell_bin[i] = o;
     ++o;
   }
 }
@@ -532,7 +799,7 @@ cudaError_t KdeState::ensure_bins(int n) {
   }
   void *old[] = {bins.gx, bins.gy, bins.gz, bins.count, bins.ks, bins.scale, bins.shape, bins.support, bins.nest,
                  bins.dens, bins.cb, bins.rxx, bins.ryy, bins.rzz, bins.net, bins.dens_old, bins.scale_old, tmp,
-                 partial};
+                 partial, bin_key};
   for (void *p : old)
     if (p) cudaFree(p);
   const size_t c = (size_t)n;
@@ -543,7 +810,7 @@ cudaError_t KdeState::ensure_bins(int n) {
   auto D = [&](double **p, size_t k) {
     if (e == cudaSuccess) e = cudaMalloc((void **)p, sizeof(double) * k);
   };
-  I(&bins.gx, c); I(&bins.gy, c); I(&bins.gz, c);
+  I(&bins.gx, c); I(&bins.gy, c); I(&bins.gz, c); I(&bin_key, 4 * c);
   D(&bins.count, c); D(&bins.ks, 3 * c); D(&bins.scale, c); D(&bins.shape, 3 * c); D(&bins.support, c);
   D(&bins.nest, c); D(&bins.dens, c); D(&bins.cb, 3 * c); D(&bins.rxx, c); D(&bins.ryy, c); D(&bins.rzz, c);
   D(&bins.net, c); D(&bins.dens_old, c); D(&bins.scale_old, c); D(&tmp, c);
@@ -560,6 +827,9 @@ cudaError_t KdeState::ensure_grid(int64_t ngrid) {
     if (e == cudaSuccess) e = cudaMallocHost((void **)&h_scalars, 8 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&h_flag, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_keys, sizeof(KeyAcc));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_plan, 2 * sizeof(SepPlan) + 8 * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&h_plan, 8 * sizeof(long long));
     if (e != cudaSuccess) return e;
   }
   if (ngrid <= grid_cap) return cudaSuccess;
@@ -567,7 +837,9 @@ cudaError_t KdeState::ensure_grid(int64_t ngrid) {
   for (double *p : old)
     if (p) cudaFree(p);
   if (d_blockcnt) cudaFree(d_blockcnt);
+  if (cell_bin) cudaFree(cell_bin);
   cudaError_t e = cudaMalloc((void **)&dens_grid, sizeof(double) * ngrid);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&cell_bin, sizeof(int) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&cx, sizeof(double) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&cy, sizeof(double) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&cz, sizeof(double) * ngrid);
@@ -577,14 +849,38 @@ cudaError_t KdeState::ensure_grid(int64_t ngrid) {
   return cudaSuccess;
 }
 
+cudaError_t KdeState::ensure_pass(int64_t n1, int64_t n2) {
+  if (n1 > t1_cap) {
+    if (t1) cudaFree(t1);
+    t1 = nullptr;
+    t1_cap = 0;
+    const int64_t c = n1 + n1 / 4;
+    cudaError_t e = cudaMalloc((void **)&t1, sizeof(double) * c);
+    if (e != cudaSuccess) return e;
+    t1_cap = c;
+  }
+  if (n2 > t2_cap) {
+    if (t2) cudaFree(t2);
+    t2 = nullptr;
+    t2_cap = 0;
+    const int64_t c = n2 + n2 / 4;
+    cudaError_t e = cudaMalloc((void **)&t2, sizeof(double) * c);
+    if (e != cudaSuccess) return e;
+    t2_cap = c;
+  }
+  return cudaSuccess;
+}
+
 void KdeState::release() {
   void *ptrs[] = {bins.gx, bins.gy, bins.gz, bins.count, bins.ks, bins.scale, bins.shape, bins.support, bins.nest,
                   bins.dens, bins.cb, bins.rxx, bins.ryy, bins.rzz, bins.net, bins.dens_old, bins.scale_old, tmp,
-                  partial, dens_grid, cx, cy, cz, d_scalars, d_flag, d_blockcnt, d_val, d_meta};
+                  partial, dens_grid, cx, cy, cz, d_scalars, d_flag, d_blockcnt, d_val, d_meta, cell_bin, bin_key,
+                  d_keys, d_plan, t1, t2};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_scalars) cudaFreeHost(h_scalars);
   if (h_flag) cudaFreeHost(h_flag);
+  if (h_plan) cudaFreeHost(h_plan);
   *this = KdeState();
 }
 static double erf_diff(double i, double hd) {
@@ -698,9 +994,41 @@ cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, in
   double *h = st.h_scalars;
   auto density = [&](void) -> cudaError_t {
     KCK(cudaMemsetAsync(st.dens_grid, 0, sizeof(double) * ngrid, s));
-    scatter_kernel<<<nb, kThreads, 0, s>>>(P, B, st.wtab, 0, 0, st.dens_grid);
+    wscatter_kernel<<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, st.wtab, st.dens_grid);
     grid_scale_kernel<<<gb, kThreads, 0, s>>>(st.dens_grid, ngrid, P.binvol);
     pick_kernel<<<bb, kThreads, 0, s>>>(P, B, st.dens_grid, B.dens);
+    st.launches += 3;
+    return cudaGetLastError();
+  };
+  // plans: [0] smoothing kernels (kind 1), [1] second-derivative kernels (kind 2)
+  SepPlan *plan1 = st.d_plan, *plan2 = st.d_plan + 1;
+  long long *plan_out = reinterpret_cast<long long *>(st.d_plan + 2);
+  int *key1 = st.bin_key, *key2 = st.bin_key + nb;
+  dim3 grid1(1, 1), grid2(1, 1);
+  auto plan = [&](int kind, int nc, dim3 &grid) -> cudaError_t {
+    SepPlan *pl = kind == 1 ? plan1 : plan2;
+    key_init_kernel<<<1, kThreads, 0, s>>>(st.d_keys);
+    key_assign_kernel<<<bb, kThreads, 0, s>>>(P, B, kind, kind == 1 ? key1 : key2, st.d_keys);
+    if (kind == 1)
+      plan_kernel<<<1, 32, 0, s>>>(P, st.d_keys, st.wtab, st.wtab, st.wtab, 0, pl, plan_out);
+    else
+      plan_kernel<<<1, 32, 0, s>>>(P, st.d_keys, st.sdtab[0], st.sdtab[1], st.sdtab[2], 1, pl, plan_out);
+    st.launches += 3;
+    KCK(cudaGetLastError());
+    KCK(cudaMemcpyAsync(st.h_plan, plan_out, 4 * sizeof(long long), cudaMemcpyDeviceToHost, s));
+    KCK(cudaStreamSynchronize(s));
+    const long long np = st.h_plan[0], mx = st.h_plan[3];
+    KCK(st.ensure_pass(st.h_plan[1] * nc, st.h_plan[2] * nc));
+    long long gx = (mx + kThreads - 1) / kThreads;
+    gx = gx < 1 ? 1 : (gx > 1024 ? 1024 : gx);
+    grid = dim3((unsigned)gx, (unsigned)(np < 1 ? 1 : np));
+    return cudaSuccess;
+  };
+  // sum over every bin's smoothing kernel of `field`, at the bins
+  auto gather1 = [&](const double *field, double *out, double *out2) -> cudaError_t {
+    gather_x_kernel<1><<<grid1, kThreads, 0, s>>>(P, plan1, field, nullptr, nullptr, st.t1);
+    gather_y_kernel<1><<<grid1, kThreads, 0, s>>>(P, plan1, st.t1, st.t2);
+    gather_z_kernel<1><<<bb, kThreads, 0, s>>>(P, B, plan1, key1, st.t2, out, out2);
     st.launches += 3;
     return cudaGetLastError();
   };
@@ -732,30 +1060,32 @@ cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, in
   int m = 0;
   for (m = 1; m <= n_opt_loops; ++m) {
     // nEstimate with the current support, support update, nEstimate again
-    gather_kernel<<<nb, kThreads, 0, s>>>(P, B, st.wtab, st.dens_grid, st.tmp);
+    KCK(plan(1, 1, grid1));
+    KCK(gather1(st.dens_grid, st.tmp, nullptr));
     support_update_kernel<<<bb, kThreads, 0, s>>>(P, B, st.tmp);
-    gather_kernel<<<nb, kThreads, 0, s>>>(P, B, st.wtab, st.dens_grid, B.nest);
+    st.launches += 1;
+    KCK(plan(1, P.ndim == 3 ? 6 : 1, grid1));
+    KCK(gather1(st.dens_grid, B.nest, nullptr));
     curvature_bandwidth_kernel<<<bb, kThreads, 0, s>>>(P, B);
-    st.launches += 4;
-    // net roughness
-    double *cg[3] = {st.cx, st.cy, st.cz};
-    for (int a = 0; a < 3; ++a) {
-      if (P.ndim == 1 && !P.mask[a]) continue;
-      KCK(cudaMemsetAsync(cg[a], 0, sizeof(double) * ngrid, s));
-      scatter_kernel<<<nb, kThreads, 0, s>>>(P, B, st.sdtab[a], 2, a, cg[a]);
-      curvature_square_kernel<<<gb, kThreads, 0, s>>>(cg[a], ngrid, P.binvol, P.bin[a] * P.bin[a]);
-      st.launches += 2;
-    }
+    st.launches += 1;
+    // curvatures: second-derivative scatters of the counts, squared
+    KCK(plan(2, 1, grid2));
+    scatter_x_kernel<<<grid2, kThreads, 0, s>>>(P, B, plan2, st.cell_bin, key2, st.t1);
+    scatter_y_kernel<<<grid2, kThreads, 0, s>>>(P, plan2, st.t1, st.t2);
+    scatter_z_kernel<<<dim3(gb, 3), kThreads, 0, s>>>(P, plan2, st.t2, st.cx, st.cy, st.cz);
+    st.launches += 3;
+    // net roughness: smoothing-kernel gathers of the squared curvatures
     if (P.ndim == 3) {
-      gather_roughness3_kernel<<<nb, kThreads, 0, s>>>(P, B, st.wtab, st.cx, st.cy, st.cz);
-      st.launches += 1;
+      gather_x_kernel<6><<<grid1, kThreads, 0, s>>>(P, plan1, st.cx, st.cy, st.cz, st.t1);
+      gather_y_kernel<6><<<grid1, kThreads, 0, s>>>(P, plan1, st.t1, st.t2);
+      gather_z_kernel<6><<<bb, kThreads, 0, s>>>(P, B, plan1, key1, st.t2, nullptr, nullptr);
+      st.launches += 3;
     } else {
       int a = 0;
       while (!P.mask[a]) ++a;
+      double *cg[3] = {st.cx, st.cy, st.cz};
       double *r1 = (a == 0) ? B.rxx : (a == 1 ? B.ryy : B.rzz);
-      gather_kernel<<<nb, kThreads, 0, s>>>(P, B, st.wtab, cg[a], r1);
-      copy_kernel<<<bb, kThreads, 0, s>>>(B.net, r1, nb);
-      st.launches += 2;
+      KCK(gather1(cg[a], r1, B.net));
     }
     KCK(cudaGetLastError());
     // optimal smoothing and shape
@@ -820,7 +1150,8 @@ cudaError_t kde_collect_active(KdeState &st, const KdeParams &P, const double *c
   if (tot == 0) return cudaSuccess;
   KCK(st.ensure_bins(tot));
   KCK(cudaMemcpyAsync(d_cnt, ofs.data(), sizeof(int) * nblk, cudaMemcpyHostToDevice, s));
-  active_write_kernel<<<nblk, 32, 0, s>>>(counts, ngrid, chunk, d_cnt, P, st.bins);
+  KCK(cudaMemsetAsync(st.cell_bin, 0xff, sizeof(int) * ngrid, s));  // -1: no active bin
+  active_write_kernel<<<nblk, 32, 0, s>>>(counts, ngrid, chunk, d_cnt, P, st.bins, st.cell_bin);
   st.launches += 2;
   return cudaGetLastError();
 }

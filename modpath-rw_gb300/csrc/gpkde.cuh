@@ -34,6 +34,34 @@ struct KdeTable {
   const int *m, *ofs;
 };
 
+// Separable passes.  The smoothing (sigma) and second-derivative kernels of
+// a bin are chosen from the database by one scalar, so the bins fall into at
+// most KDE_KMAX groups ("keys") that share one kernel; a gather or scatter
+// over all bins is then, per key, three one-dimensional passes over the key's
+// bounding box.
+constexpr int KDE_KMAX = 3 * KDE_MAXDB;
+
+// Bounding box (1-based, inclusive: x0,x1,y0,y1,z0,z1), database levels and
+// bin count of every key, accumulated with atomics.
+struct KeyAcc {
+  int box[KDE_KMAX][6];
+  int lev[KDE_KMAX][3];
+  int cnt[KDE_KMAX];
+};
+
+// The keys present, compacted: per key its half widths and factors per
+// dimension, the regions of the two intermediate passes and their offsets
+// (in elements) into the pass buffers.
+struct SepPlan {
+  int np;
+  int slot_of[KDE_KMAX];
+  int key[KDE_KMAX];
+  int m[KDE_KMAX][3];
+  const double *f[KDE_KMAX][3];
+  int box[KDE_KMAX][6], r1[KDE_KMAX][6], r2[KDE_KMAX][6];
+  long long o1[KDE_KMAX], o2[KDE_KMAX];
+};
+
 // Per active bin state (SoA).  3-vectors are stored dimension-major: v[d*n + b].
 struct KdeBins {
   int n;
@@ -49,12 +77,20 @@ struct KdeState {
   int64_t grid_cap = 0;
   double *tmp = nullptr, *partial = nullptr, *d_scalars = nullptr, *h_scalars = nullptr;
   int *d_flag = nullptr, *h_flag = nullptr, *d_blockcnt = nullptr;
+  int *cell_bin = nullptr;          // per grid cell: active bin index or -1
+  int *bin_key = nullptr;           // per bin: smoothing key (n) and SD keys per axis (3n)
+  KeyAcc *d_keys = nullptr;
+  SepPlan *d_plan = nullptr;
+  long long *h_plan = nullptr;      // pinned: keys present, pass-buffer sizes, largest region
+  double *t1 = nullptr, *t2 = nullptr;
+  int64_t t1_cap = 0, t2_cap = 0;
   KdeTable wtab{}, sdtab[3]{};
   double *d_val = nullptr;
   int *d_meta = nullptr;  // wm, wofs, sm[3], sofs[3]
   int64_t launches = 0;
 
   cudaError_t ensure_bins(int n);
+  cudaError_t ensure_pass(int64_t n1, int64_t n2);
   cudaError_t ensure_grid(int64_t ngrid);
   void release();
 };
