@@ -19,6 +19,7 @@
 // bins are two-stage with a fixed order, so runs are repeatable; the host
 // takes the per-loop convergence decision from four scalars.
 #include <cfloat>
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <vector>
@@ -58,18 +59,6 @@ __device__ void fold_factor(double *v, int m, int gid, int nb) {
 struct Span {
   int g0[3], n[3], k0[3];
 };
-
-__device__ __forceinline__ double block_sum(double v, double *red) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  __syncthreads();
-  if (l == 0) red[w] = v;
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
-  return s;  // valid in thread 0
-}
 
 // ---- density scatter: one warp per bin --------------------------------------
 // The W kernel of a bin is anisotropic (one database level per dimension), so
@@ -140,74 +129,103 @@ __global__ void key_init_kernel(KeyAcc *K) {
   }
 }
 
-__device__ __forceinline__ void key_record(KeyAcc *K, int key, const int lev[3], const int g[3]) {
-  for (int d = 0; d < 3; ++d) {
-    atomicMin(&K->box[key][2 * d], g[d]);
-    atomicMax(&K->box[key][2 * d + 1], g[d]);
-    K->lev[key][d] = lev[d];  // every bin of the key writes the same levels
-  }
-  atomicAdd(&K->cnt[key], 1);
-}
-
 // kind 1: the smoothing (sigma) kernel of scale support[b]; its level per
 // dimension is non-decreasing in the scale, so the sum of the three levels
-// (minus 3, each level is >= 1) identifies the triple.  kind 2: the second-derivative kernel of each
-// active axis a from cb[a] (the database is isotropic: one level), key
-// a*KDE_MAXDB + level-1; a NaN bandwidth has no kernel and is skipped, as the
-// reference's 1-D path does (GridProjectedKDE.F90:2340-2345).
+// (minus 3, each level is >= 1) identifies the triple.  kind 2: the
+// second-derivative kernel of each active axis a from cb[a] (the database is
+// isotropic: one level), key a*KDE_MAXDB + level-1; a NaN bandwidth has no
+// kernel and is skipped, as the reference's 1-D path does
+// (GridProjectedKDE.F90:1723-1724; its 3-D path has no such test and no
+// defined kernel for NaN).  Boxes and counts are accumulated per
+// block in shared memory and merged into K once per block and key.
 __global__ void key_assign_kernel(KdeParams P, KdeBins B, int kind, int *bin_key, KeyAcc *K) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B.n) return;
-  const int g[3] = {B.gx[b], B.gy[b], B.gz[b]};
-  if (kind == 1) {
-    const double s = B.support[b];
-    int lev[3] = {1, 1, 1};
-    for (int d = 0; d < 3; ++d)
-      if (P.mask[d]) lev[d] = log_index(P, s, d);
-    const int key = lev[0] + lev[1] + lev[2] - 3;
-    bin_key[b] = key;
-    key_record(K, key, lev, g);
-  } else {
-    for (int a = 0; a < 3; ++a) {
-      int key = -1;
-      const double h = B.cb[a * B.n + b];
-      if (P.mask[a] && h == h) {
-        const int n = log_index(P, h, a);
-        const int lev[3] = {n, n, n};
-        key = a * KDE_MAXDB + n - 1;
-        key_record(K, key, lev, g);
-      }
-      bin_key[a * B.n + b] = key;
+  __shared__ int sb[KDE_KMAX][6];
+  __shared__ int sl[KDE_KMAX][3];
+  __shared__ int sc[KDE_KMAX];
+  for (int k = threadIdx.x; k < KDE_KMAX; k += blockDim.x) {
+    sb[k][0] = sb[k][2] = sb[k][4] = INT_MAX;
+    sb[k][1] = sb[k][3] = sb[k][5] = INT_MIN;
+    sc[k] = 0;
+  }
+  __syncthreads();
+  auto record = [&](int key, const int lev[3], const int g[3]) {
+    for (int d = 0; d < 3; ++d) {
+      atomicMin(&sb[key][2 * d], g[d]);
+      atomicMax(&sb[key][2 * d + 1], g[d]);
+      sl[key][d] = lev[d];  // every bin of the key writes the same levels
     }
+    atomicAdd(&sc[key], 1);
+  };
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
+    const int g[3] = {B.gx[b], B.gy[b], B.gz[b]};
+    if (kind == 1) {
+      const double s = B.support[b];
+      int lev[3] = {1, 1, 1};
+      for (int d = 0; d < 3; ++d)
+        if (P.mask[d]) lev[d] = log_index(P, s, d);
+      const int key = lev[0] + lev[1] + lev[2] - 3;
+      bin_key[b] = key;
+      record(key, lev, g);
+    } else {
+      for (int a = 0; a < 3; ++a) {
+        int key = -1;
+        const double h = B.cb[a * B.n + b];
+        if (P.mask[a] && h == h) {
+          const int n = log_index(P, h, a);
+          const int lev[3] = {n, n, n};
+          key = a * KDE_MAXDB + n - 1;
+          record(key, lev, g);
+        }
+        bin_key[a * B.n + b] = key;
+      }
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < KDE_KMAX; k += blockDim.x) {
+    if (sc[k] == 0) continue;
+    for (int d = 0; d < 3; ++d) {
+      atomicMin(&K->box[k][2 * d], sb[k][2 * d]);
+      atomicMax(&K->box[k][2 * d + 1], sb[k][2 * d + 1]);
+      K->lev[k][d] = sl[k][d];
+    }
+    atomicAdd(&K->cnt[k], sc[k]);
   }
 }
 
-// Compact the keys present and lay out the pass regions.  Gather: pass 1
-// (x) covers the bins' x range and the y, z ranges widened by the half
-// widths; pass 2 (y) the bins' x, y ranges and the widened z range; the z
-// pass runs per bin.  Scatter: pass 1 widens x, pass 2 widens y, the z pass
-// writes the grid.  out[0..3]: keys present, pass-1 and pass-2 elements,
-// largest region.
-__global__ void plan_kernel(KdeParams P, const KeyAcc *K, KdeTable t0, KdeTable t1, KdeTable t2, int scatter,
-                            SepPlan *pl, long long *out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int np = 0;
-  long long o1 = 0, o2 = 0, mx = 0;
-  for (int k = 0; k < KDE_KMAX; ++k) {
-    pl->slot_of[k] = -1;
-    if (K->cnt[k] == 0) continue;
+// Compact the keys present and lay out the pass regions, one thread per
+// key (launched with kPlanThreads >= KDE_KMAX threads), offsets by a block
+// prefix sum in key order.  Gather: pass 1 (x) covers the bins' x range and
+// the y, z ranges widened by the half widths; pass 2 (y) the bins' x, y
+// ranges and the widened z range; the z pass runs per bin.  Scatter: pass 1
+// widens x, pass 2 widens y, the z pass writes the grid over the union
+// region of each axis's keys.  out[0..3]: keys present, pass-1 and pass-2
+// elements, largest region.
+constexpr int kPlanThreads = 256;
+static_assert(kPlanThreads >= KDE_KMAX, "one plan thread per key");
+
+__global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, const KeyAcc *K, KdeTable t0, KdeTable t1,
+                                                            KdeTable t2, int scatter, SepPlan *pl, long long *out) {
+  __shared__ long long sv1[kPlanThreads], sv2[kPlanThreads];
+  __shared__ int sp[kPlanThreads];
+  __shared__ int su[3][6];
+  const int k = threadIdx.x;
+  if (k < 3) {
+    su[k][0] = su[k][2] = su[k][4] = INT_MAX;
+    su[k][1] = su[k][3] = su[k][5] = INT_MIN;
+  }
+  const bool present = k < KDE_KMAX && K->cnt[k] > 0;
+  int m[3] = {0, 0, 0}, bx[6], r1[6], r2[6];
+  const double *f[3] = {nullptr, nullptr, nullptr};
+  long long v1 = 0, v2 = 0;
+  if (present) {
     const int axis = k / KDE_MAXDB;
     const KdeTable T = !scatter ? t0 : (axis == 0 ? t0 : (axis == 1 ? t1 : t2));
-    int m[3];
     for (int d = 0; d < 3; ++d) {
       const int li = d * KDE_MAXDB + K->lev[k][d] - 1;
       m[d] = T.m[li];
-      pl->m[np][d] = m[d];
-      pl->f[np][d] = T.val + T.ofs[li];
+      f[d] = T.val + T.ofs[li];
     }
-    int bx[6], r1[6], r2[6];
-    for (int i = 0; i < 6; ++i) bx[i] = K->box[k][i];
-    for (int i = 0; i < 6; ++i) r1[i] = r2[i] = bx[i];
+    for (int i = 0; i < 6; ++i) bx[i] = r1[i] = r2[i] = K->box[k][i];
     if (!scatter) {
       r1[2] = max(1, bx[2] - m[1]);
       r1[3] = min(P.nb[1], bx[3] + m[1]);
@@ -219,27 +237,67 @@ __global__ void plan_kernel(KdeParams P, const KeyAcc *K, KdeTable t0, KdeTable 
       r2[2] = max(1, bx[2] - m[1]);
       r2[3] = min(P.nb[1], bx[3] + m[1]);
     }
-    const long long v1 = (long long)(r1[1] - r1[0] + 1) * (r1[3] - r1[2] + 1) * (r1[5] - r1[4] + 1);
-    const long long v2 = (long long)(r2[1] - r2[0] + 1) * (r2[3] - r2[2] + 1) * (r2[5] - r2[4] + 1);
-    for (int i = 0; i < 6; ++i) {
-      pl->box[np][i] = bx[i];
-      pl->r1[np][i] = r1[i];
-      pl->r2[np][i] = r2[i];
-    }
-    pl->o1[np] = o1;
-    pl->o2[np] = o2;
-    o1 += v1;
-    o2 += v2;
-    mx = max(mx, max(v1, v2));
-    pl->key[np] = k;
-    pl->slot_of[k] = np;
-    ++np;
+    v1 = (long long)(r1[1] - r1[0] + 1) * (r1[3] - r1[2] + 1) * (r1[5] - r1[4] + 1);
+    v2 = (long long)(r2[1] - r2[0] + 1) * (r2[3] - r2[2] + 1) * (r2[5] - r2[4] + 1);
   }
-  pl->np = np;
-  out[0] = np;
-  out[1] = o1;
-  out[2] = o2;
-  out[3] = mx;
+  sp[k] = present ? 1 : 0;
+  sv1[k] = v1;
+  sv2[k] = v2;
+  __syncthreads();
+  // inclusive Hillis-Steele scans
+  for (int o = 1; o < kPlanThreads; o <<= 1) {
+    const int a = (k >= o) ? sp[k - o] : 0;
+    const long long b1 = (k >= o) ? sv1[k - o] : 0, b2 = (k >= o) ? sv2[k - o] : 0;
+    __syncthreads();
+    sp[k] += a;
+    sv1[k] += b1;
+    sv2[k] += b2;
+    __syncthreads();
+  }
+  if (k < KDE_KMAX) pl->slot_of[k] = present ? sp[k] - 1 : -1;
+  if (present) {
+    const int j = sp[k] - 1;
+    for (int d = 0; d < 3; ++d) {
+      pl->m[j][d] = m[d];
+      pl->f[j][d] = f[d];
+    }
+    for (int i = 0; i < 6; ++i) {
+      pl->box[j][i] = bx[i];
+      pl->r1[j][i] = r1[i];
+      pl->r2[j][i] = r2[i];
+    }
+    pl->o1[j] = sv1[k] - v1;
+    pl->o2[j] = sv2[k] - v2;
+    pl->key[j] = k;
+    if (scatter) {
+      const int axis = k / KDE_MAXDB;
+      atomicMin(&su[axis][0], r2[0]);
+      atomicMax(&su[axis][1], r2[1]);
+      atomicMin(&su[axis][2], r2[2]);
+      atomicMax(&su[axis][3], r2[3]);
+      atomicMin(&su[axis][4], max(1, bx[4] - m[2]));
+      atomicMax(&su[axis][5], min(P.nb[2], bx[5] + m[2]));
+    }
+  }
+  // totals (inclusive scans end at the last key) and the largest region
+  const int np = sp[kPlanThreads - 1];
+  const long long tot1 = sv1[kPlanThreads - 1], tot2 = sv2[kPlanThreads - 1];
+  __shared__ long long smx[kPlanThreads];
+  smx[k] = max(v1, v2);
+  __syncthreads();
+  for (int o = kPlanThreads / 2; o > 0; o >>= 1) {
+    if (k < o) smx[k] = max(smx[k], smx[k + o]);
+    __syncthreads();
+  }
+  if (k < 3)
+    for (int i = 0; i < 6; ++i) pl->ur[k][i] = su[k][i];
+  if (k == 0) {
+    pl->np = np;
+    out[0] = np;
+    out[1] = tot1;
+    out[2] = tot2;
+    out[3] = smx[0];
+  }
 }
 
 __device__ __forceinline__ void region_xyz(const int r[6], long long i, int &x, int &y, int &z) {
@@ -446,7 +504,8 @@ __global__ void scatter_y_kernel(KdeParams P, const SepPlan *pl, const double *V
 }
 
 // Scatter pass 3 (z) of every key of one axis into that axis's curvature
-// grid, keys in increasing order, then the normalisation
+// grid (zeroed before; only the union of the keys' output regions is
+// written), keys in increasing order, then the normalisation
 // ((c / binVolume) / binSize^2)^2 (GridProjectedKDE.F90:2366-2461).
 __global__ void scatter_z_kernel(KdeParams P, const SepPlan *pl, const double *V2, double *c0, double *c1,
                                  double *c2) {
@@ -454,13 +513,15 @@ __global__ void scatter_z_kernel(KdeParams P, const SepPlan *pl, const double *V
   if (!P.mask[axis]) return;
   double *out = axis == 0 ? c0 : (axis == 1 ? c1 : c2);
   const double bs2 = P.bin[axis] * P.bin[axis];
-  const long long ngrid = (long long)P.nb[0] * P.nb[1] * P.nb[2];
+  int u[6];
+  for (int i = 0; i < 6; ++i) u[i] = pl->ur[axis][i];
+  if (u[0] > u[1]) return;  // no key on this axis: the grid stays zero
+  const long long vol = region_vol(u);
   const int np = pl->np, n = P.nb[2];
-  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ngrid; g += (long long)gridDim.x * blockDim.x) {
-    const int x = 1 + (int)(g % P.nb[0]);
-    const long long q = g / P.nb[0];
-    const int y = 1 + (int)(q % P.nb[1]);
-    const int z = 1 + (int)(q / P.nb[1]);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
+    int x, y, z;
+    region_xyz(u, i, x, y, z);
+    const long long g = (long long)(x - 1) + (long long)P.nb[0] * ((y - 1) + (long long)P.nb[1] * (z - 1));
     double acc = 0.0;
     for (int j = 0; j < np; ++j) {
       if (pl->key[j] / KDE_MAXDB != axis) continue;
@@ -561,117 +622,132 @@ __global__ void curvature_bandwidth_kernel(KdeParams P, KdeBins B) {
   }
 }
 
-// deterministic two-stage reductions: stage 1 writes per-block partials
-__global__ void reduce_stage1_kernel(KdeBins B, int what, double aux0, double aux1, double *partial) {
-  __shared__ double red[32];
-  double v0 = 0.0, v1 = 0.0, v2 = 0.0;
-  double mx0 = -DBL_MAX, mx1 = -DBL_MAX, mn0 = DBL_MAX;
+// Per-bin reductions of the optimisation loop, in two stages with a fixed
+// order (per-block partials, then one warp), results in the device scalars
+// S so that the next kernels read them without a host round trip:
+//   what 0: S[0] = max(net roughness), S[2] = min(net roughness > 0)
+//   what 2: S[3] = max(density), S[4] = max(previous density),
+//           S[5] = -max(smoothing scale > 0)
+//   what 1: S[6], S[7] = sums of the squared relative density and smoothing
+//           changes (GridProjectedKDE.F90:4976-5000; uses S[3], S[4])
+//   what 3: S[9] = sum of the squared ALMISE terms (4966-4972)
+constexpr int kRedBlocks = 152;
+enum { RED_NET = 0, RED_ERR = 1, RED_MAX = 2, RED_ALMISE = 3 };
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_min(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBins B, int what, double npts,
+                                                              const double *S, double *partial) {
+  __shared__ double red[kThreads / 32][3];
+  double a0, a1, a2;
+  if (what == RED_NET) {
+    a0 = -DBL_MAX, a1 = 0.0, a2 = DBL_MAX;
+  } else if (what == RED_MAX) {
+    a0 = -DBL_MAX, a1 = -DBL_MAX, a2 = DBL_MAX;
+  } else {
+    a0 = a1 = a2 = 0.0;
+  }
+  const double mx = (what == RED_ERR) ? S[3] : 0.0, mx_old = (what == RED_ERR) ? S[4] : 0.0;
+  const double nd = (double)P.ndim;
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
-    if (what == 0) {  // max(net), min(net > 0)
+    if (what == RED_NET) {
       const double r = B.net[b];
-      mx0 = fmax(mx0, r);
-      if (r > 0.0) mn0 = fmin(mn0, r);
-    } else if (what == 1) {  // error sums: density, smoothing, ALMISE
+      a0 = fmax(a0, r);
+      if (r > 0.0) a2 = fmin(a2, r);
+    } else if (what == RED_MAX) {
+      a0 = fmax(a0, B.dens[b]);
+      a1 = fmax(a1, B.dens_old[b]);
+      if (B.scale[b] > 0.0) a2 = fmin(a2, -B.scale[b]);
+    } else if (what == RED_ERR) {
       const double dn = B.dens[b], dold = B.dens_old[b];
       if (dold != 0.0) {
-        const double e = fabs(dn / aux0 - dold / aux1) / (dold / aux1);
-        v0 += e * e;
+        const double e = fabs(dn / mx - dold / mx_old) / (dold / mx_old);
+        a0 += e * e;
       }
       const double so = B.scale_old[b], sc = B.scale[b];
       if (so != 0.0) {
         const double e = fabs(sc - so) / so;
-        v1 += e * e;
+        a1 += e * e;
       }
-    } else if (what == 2) {  // max(dens), max(dens_old), max(scale > 0)
-      mx0 = fmax(mx0, B.dens[b]);
-      mx1 = fmax(mx1, B.dens_old[b]);
-      if (B.scale[b] > 0.0) mn0 = fmin(mn0, -B.scale[b]);  // -max(scale)
-    }
-  }
-  // write per-thread values through a block reduction in fixed order
-  if (what == 1) {
-    const double s0 = block_sum(v0, red);
-    const double s1 = block_sum(v1, red);
-    const double s2 = block_sum(v2, red);
-    if (threadIdx.x == 0) {
-      partial[3 * blockIdx.x + 0] = s0;
-      partial[3 * blockIdx.x + 1] = s1;
-      partial[3 * blockIdx.x + 2] = s2;
-    }
-  } else {
-    __shared__ double a[kThreads], c[kThreads], e[kThreads];
-    a[threadIdx.x] = mx0;
-    c[threadIdx.x] = mx1;
-    e[threadIdx.x] = mn0;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double A = -DBL_MAX, Cc = -DBL_MAX, E = DBL_MAX;
-      for (int i = 0; i < (int)blockDim.x; ++i) {
-        A = fmax(A, a[i]);
-        Cc = fmax(Cc, c[i]);
-        E = fmin(E, e[i]);
+    } else {
+      const double sc = B.scale[b];
+      if (sc != 0.0) {
+        const double e = (B.nest[b] / (pow(sc, nd) * pow(4.0 * PI_D, 0.5 * nd)) + 0.25 * B.net[b] * pow(sc, 4.0)) /
+                         pow(npts, 2.0);
+        a0 += e * e;
       }
-      partial[3 * blockIdx.x + 0] = A;
-      partial[3 * blockIdx.x + 1] = Cc;
-      partial[3 * blockIdx.x + 2] = E;
     }
+  }
+  const bool mm = (what == RED_NET || what == RED_MAX);
+  a0 = mm ? warp_max(a0) : warp_sum(a0);
+  a1 = (what == RED_MAX) ? warp_max(a1) : warp_sum(a1);
+  a2 = mm ? warp_min(a2) : warp_sum(a2);
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[w][0] = a0;
+    red[w][1] = a1;
+    red[w][2] = a2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b0 = red[0][0], b1 = red[0][1], b2 = red[0][2];
+    for (int i = 1; i < kThreads / 32; ++i) {
+      b0 = mm ? fmax(b0, red[i][0]) : b0 + red[i][0];
+      b1 = (what == RED_MAX) ? fmax(b1, red[i][1]) : b1 + red[i][1];
+      b2 = mm ? fmin(b2, red[i][2]) : b2 + red[i][2];
+    }
+    partial[3 * blockIdx.x + 0] = b0;
+    partial[3 * blockIdx.x + 1] = b1;
+    partial[3 * blockIdx.x + 2] = b2;
   }
 }
 
-__global__ void reduce_stage2_kernel(int what, int nblk, const double *partial, double *out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  if (what == 1) {
-    double s0 = 0, s1 = 0, s2 = 0;
-    for (int i = 0; i < nblk; ++i) {
-      s0 += partial[3 * i];
-      s1 += partial[3 * i + 1];
-      s2 += partial[3 * i + 2];
-    }
-    out[0] = s0;
-    out[1] = s1;
-    out[2] = s2;
+// one warp: lane l folds partials l, l+32, ... then a shuffle tree
+__global__ void bin_reduce_final_kernel(int what, int nblk, const double *partial, double *S) {
+  const int l = threadIdx.x;
+  const bool mm = (what == RED_NET || what == RED_MAX);
+  double a0 = mm ? -DBL_MAX : 0.0, a1 = (what == RED_MAX) ? -DBL_MAX : 0.0, a2 = mm ? DBL_MAX : 0.0;
+  for (int i = l; i < nblk; i += 32) {
+    a0 = mm ? fmax(a0, partial[3 * i]) : a0 + partial[3 * i];
+    a1 = (what == RED_MAX) ? fmax(a1, partial[3 * i + 1]) : a1 + partial[3 * i + 1];
+    a2 = mm ? fmin(a2, partial[3 * i + 2]) : a2 + partial[3 * i + 2];
+  }
+  a0 = mm ? warp_max(a0) : warp_sum(a0);
+  a1 = (what == RED_MAX) ? warp_max(a1) : warp_sum(a1);
+  a2 = mm ? warp_min(a2) : warp_sum(a2);
+  if (l != 0) return;
+  if (what == RED_NET) {
+    S[0] = a0;
+    S[2] = a2;
+  } else if (what == RED_MAX) {
+    S[3] = a0;
+    S[4] = a1;
+    S[5] = a2;
+  } else if (what == RED_ERR) {
+    S[6] = a0;
+    S[7] = a1;
   } else {
-    double A = -DBL_MAX, Cc = -DBL_MAX, E = DBL_MAX;
-    for (int i = 0; i < nblk; ++i) {
-      A = fmax(A, partial[3 * i]);
-      Cc = fmax(Cc, partial[3 * i + 1]);
-      E = fmin(E, partial[3 * i + 2]);
-    }
-    out[0] = A;
-    out[1] = Cc;
-    out[2] = E;
+    S[9] = a0;
   }
-}
-
-// ALMISE per-bin term sum (GridProjectedKDE.F90:4966-4972)
-__global__ void almise_stage1_kernel(KdeParams P, KdeBins B, double npts, double *partial) {
-  __shared__ double red[32];
-  double v = 0.0;
-  const double nd = (double)P.ndim;
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
-    const double sc = B.scale[b];
-    if (sc != 0.0) {
-      const double e = (B.nest[b] / (pow(sc, nd) * pow(4.0 * PI_D, 0.5 * nd)) + 0.25 * B.net[b] * pow(sc, 4.0)) /
-                       pow(npts, 2.0);
-      v += e * e;
-    }
-  }
-  const double s = block_sum(v, red);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s;
-}
-
-__global__ void sum_stage2_kernel(int nblk, const double *partial, double *out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double s = 0;
-  for (int i = 0; i < nblk; ++i) s += partial[i];
-  out[0] = s;
 }
 
 // prComputeOptimalSmoothingAndShape, per bin (GridProjectedKDE.F90:5404-5724).
 // phase 0: isotropy correction of the net roughness + scale where net > 0.
-__global__ void optimal_phase0_kernel(KdeParams P, KdeBins B, double min_pos_net) {
+__global__ void optimal_phase0_kernel(KdeParams P, KdeBins B, const double *S) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B.n) return;
+  const double min_pos_net = S[2];
   const double nd = (double)P.ndim;
   double net = B.net[b];
   if (P.ndim == 3) {
@@ -687,9 +763,10 @@ __global__ void optimal_phase0_kernel(KdeParams P, KdeBins B, double min_pos_net
 }
 
 // phase 1: scale for zero net roughness, shapes, bounded smoothing
-__global__ void optimal_phase1_kernel(KdeParams P, KdeBins B, double max_pos_scale, int *update_flag) {
+__global__ void optimal_phase1_kernel(KdeParams P, KdeBins B, const double *S, int *update_flag) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B.n) return;
+  const double max_pos_scale = -S[5];
   double sc = B.scale[b];
   if (B.net[b] == 0.0) {
     sc = max_pos_scale;
@@ -732,9 +809,9 @@ __global__ void optimal_phase1_kernel(KdeParams P, KdeBins B, double max_pos_sca
 }
 
 // phase 2: smoothing scale from the bounded smoothing (all bins)
-__global__ void rescale_kernel(KdeParams P, KdeBins B) {
+__global__ void rescale_kernel(KdeParams P, KdeBins B, const int *update_flag) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B.n) return;
+  if (b >= B.n || *update_flag == 0) return;
   double ks[3] = {B.ks[b], B.ks[B.n + b], B.ks[2 * B.n + b]};
   B.scale[b] = smoothing_scale(P, ks);
 }
@@ -759,24 +836,42 @@ __global__ void active_count_kernel(const double *counts, int64_t nbins, int chu
   if (threadIdx.x == 0) blockcnt[blockIdx.x] = s;
 }
 
-__global__ void active_write_kernel(const double *counts, int64_t nbins, int chunk, const int *blockofs,
-                                    KdeParams P, KdeBins B, int *cell_bin) {
-  if (threadIdx.x != 0) return;
-  const int64_t beg = (int64_t)blockIdx.x * chunk;
-  const int64_t end = min(beg + chunk, nbins);
-  int o = blockofs[blockIdx.x];
-  for (int64_t i = beg; i < end; ++i) {
-    const double c = counts[i];
-    if (c == 0.0) continue;
-    const int ix = (int)(i % P.nb[0]);
-    const int64_t r = i / P.nb[0];
+constexpr int kCompactChunk = 4096;  // cells per block of kThreads threads, 16 per thread
+
+__global__ void active_write_kernel(const double *counts, int64_t nbins, const int *blockofs, KdeParams P, KdeBins B,
+                                    int *cell_bin) {
+  __shared__ int sc[kThreads];
+  constexpr int per = kCompactChunk / kThreads;
+  const int t = threadIdx.x;
+  const int64_t beg = (int64_t)blockIdx.x * kCompactChunk + (int64_t)t * per;
+  int c = 0;
+  for (int i = 0; i < per; ++i) {
+    const int64_t g = beg + i;
+    c += (g < nbins && counts[g] != 0.0);
+  }
+  sc[t] = c;
+  __syncthreads();
+  for (int o = 1; o < kThreads; o <<= 1) {
+    const int a = (t >= o) ? sc[t - o] : 0;
+    __syncthreads();
+    sc[t] += a;
+    __syncthreads();
+  }
+  int o = blockofs[blockIdx.x] + sc[t] - c;
+  for (int i = 0; i < per; ++i) {
+    const int64_t g = beg + i;
+    if (g >= nbins) break;
+    const double v = counts[g];
+    if (v == 0.0) continue;
+    const int ix = (int)(g % P.nb[0]);
+    const int64_t r = g / P.nb[0];
     const int iy = (int)(r % P.nb[1]);
     const int iz = (int)(r / P.nb[1]);
     B.gx[o] = ix + 1;
     B.gy[o] = iy + 1;
     B.gz[o] = iz + 1;
-    B.count[o] = c;
-    cell_bin[i] = o;
+    B.count[o] = v;
+    cell_bin[g] = o;
     ++o;
   }
 }
@@ -823,8 +918,8 @@ cudaError_t KdeState::ensure_bins(int n) {
 
 cudaError_t KdeState::ensure_grid(int64_t ngrid) {
   if (!d_scalars) {
-    cudaError_t e = cudaMalloc((void **)&d_scalars, 8 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMallocHost((void **)&h_scalars, 8 * sizeof(double));
+    cudaError_t e = cudaMalloc((void **)&d_scalars, 16 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&h_scalars, 16 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&h_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_keys, sizeof(KeyAcc));
@@ -990,8 +1085,9 @@ cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, in
   const int64_t ngrid = (int64_t)P.nb[0] * P.nb[1] * P.nb[2];
   const int bb = (nb + kThreads - 1) / kThreads;
   const int gb = blocks_for(ngrid);
-  const int rb = blocks_for(nb);
-  double *h = st.h_scalars;
+  const int rb = std::min(blocks_for(nb), kRedBlocks);
+  const int kb = std::min(bb, 2 * kRedBlocks);
+  double *S = st.d_scalars, *h = st.h_scalars;
   auto density = [&](void) -> cudaError_t {
     KCK(cudaMemsetAsync(st.dens_grid, 0, sizeof(double) * ngrid, s));
     wscatter_kernel<<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, st.wtab, st.dens_grid);
@@ -1005,14 +1101,15 @@ cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, in
   long long *plan_out = reinterpret_cast<long long *>(st.d_plan + 2);
   int *key1 = st.bin_key, *key2 = st.bin_key + nb;
   dim3 grid1(1, 1), grid2(1, 1);
+  // the host needs the keys present and the pass-buffer sizes: one sync
   auto plan = [&](int kind, int nc, dim3 &grid) -> cudaError_t {
     SepPlan *pl = kind == 1 ? plan1 : plan2;
     key_init_kernel<<<1, kThreads, 0, s>>>(st.d_keys);
-    key_assign_kernel<<<bb, kThreads, 0, s>>>(P, B, kind, kind == 1 ? key1 : key2, st.d_keys);
+    key_assign_kernel<<<kb, kThreads, 0, s>>>(P, B, kind, kind == 1 ? key1 : key2, st.d_keys);
     if (kind == 1)
-      plan_kernel<<<1, 32, 0, s>>>(P, st.d_keys, st.wtab, st.wtab, st.wtab, 0, pl, plan_out);
+      plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.wtab, st.wtab, st.wtab, 0, pl, plan_out);
     else
-      plan_kernel<<<1, 32, 0, s>>>(P, st.d_keys, st.sdtab[0], st.sdtab[1], st.sdtab[2], 1, pl, plan_out);
+      plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.sdtab[0], st.sdtab[1], st.sdtab[2], 1, pl, plan_out);
     st.launches += 3;
     KCK(cudaGetLastError());
     KCK(cudaMemcpyAsync(st.h_plan, plan_out, 4 * sizeof(long long), cudaMemcpyDeviceToHost, s));
@@ -1032,27 +1129,22 @@ cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, in
     st.launches += 3;
     return cudaGetLastError();
   };
-  auto reduce = [&](int what, double a0, double a1) -> cudaError_t {
-    reduce_stage1_kernel<<<rb, kThreads, 0, s>>>(B, what, a0, a1, st.partial);
-    reduce_stage2_kernel<<<1, 1, 0, s>>>(what, rb, st.partial, st.d_scalars);
-    KCK(cudaMemcpyAsync(h, st.d_scalars, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  auto reduce = [&](int what) -> cudaError_t {
+    bin_reduce_kernel<<<rb, kThreads, 0, s>>>(P, B, what, npts, S, st.partial);
+    bin_reduce_final_kernel<<<1, 32, 0, s>>>(what, rb, st.partial, S);
     st.launches += 2;
-    return cudaStreamSynchronize(s);
+    return cudaGetLastError();
   };
-  auto almise = [&](double &out) -> cudaError_t {
-    almise_stage1_kernel<<<rb, kThreads, 0, s>>>(P, B, npts, st.partial);
-    sum_stage2_kernel<<<1, 1, 0, s>>>(rb, st.partial, st.d_scalars);
-    KCK(cudaMemcpyAsync(h, st.d_scalars, sizeof(double), cudaMemcpyDeviceToHost, s));
-    KCK(cudaStreamSynchronize(s));
-    st.launches += 2;
-    out = std::sqrt(h[0] / nb);
-    return cudaSuccess;
+  auto fetch = [&](void) -> cudaError_t {
+    KCK(cudaMemcpyAsync(h, S, 10 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    return cudaStreamSynchronize(s);
   };
   init_bins_kernel<<<bb, kThreads, 0, s>>>(P, B, hs);
   st.launches += 1;
   KCK(density());
-  double alm = 0.0;
-  KCK(almise(alm));  // nEstimate and net roughness are zero: 0
+  KCK(reduce(RED_ALMISE));  // nEstimate and net roughness are zero: 0
+  KCK(fetch());
+  double alm = std::sqrt(h[9] / nb);
   double alm_old = alm, cum = alm, cum_old = alm;
   copy_kernel<<<bb, kThreads, 0, s>>>(B.dens_old, B.dens, nb);
   copy_kernel<<<bb, kThreads, 0, s>>>(B.scale_old, B.scale, nb);
@@ -1070,6 +1162,7 @@ cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, in
     st.launches += 1;
     // curvatures: second-derivative scatters of the counts, squared
     KCK(plan(2, 1, grid2));
+    for (double *c : {st.cx, st.cy, st.cz}) KCK(cudaMemsetAsync(c, 0, sizeof(double) * ngrid, s));
     scatter_x_kernel<<<grid2, kThreads, 0, s>>>(P, B, plan2, st.cell_bin, key2, st.t1);
     scatter_y_kernel<<<grid2, kThreads, 0, s>>>(P, plan2, st.t1, st.t2);
     scatter_z_kernel<<<dim3(gb, 3), kThreads, 0, s>>>(P, plan2, st.t2, st.cx, st.cy, st.cz);
@@ -1087,32 +1180,24 @@ cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, in
       double *r1 = (a == 0) ? B.rxx : (a == 1 ? B.ryy : B.rzz);
       KCK(gather1(cg[a], r1, B.net));
     }
-    KCK(cudaGetLastError());
-    // optimal smoothing and shape
-    KCK(reduce(0, 0.0, 0.0));
-    if (h[0] == 0.0) return cudaErrorInvalidValue;  // maxval(netRoughness) == 0: the reference stops
-    const double min_pos_net = h[2];
-    optimal_phase0_kernel<<<bb, kThreads, 0, s>>>(P, B, min_pos_net);
-    st.launches += 1;
-    KCK(reduce(2, 0.0, 0.0));
-    const double max_pos_scale = -h[2];
+    // optimal smoothing and shape; the extremes stay on the device
+    KCK(reduce(RED_NET));
+    optimal_phase0_kernel<<<bb, kThreads, 0, s>>>(P, B, S);
+    KCK(reduce(RED_MAX));
     KCK(cudaMemsetAsync(st.d_flag, 0, sizeof(int), s));
-    optimal_phase1_kernel<<<bb, kThreads, 0, s>>>(P, B, max_pos_scale, st.d_flag);
-    KCK(cudaMemcpyAsync(st.h_flag, st.d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
-    KCK(cudaStreamSynchronize(s));
-    st.launches += 1;
-    if (*st.h_flag) {
-      rescale_kernel<<<bb, kThreads, 0, s>>>(P, B);
-      st.launches += 1;
-    }
-    // density with the new smoothing
+    optimal_phase1_kernel<<<bb, kThreads, 0, s>>>(P, B, S, st.d_flag);
+    rescale_kernel<<<bb, kThreads, 0, s>>>(P, B, st.d_flag);
+    st.launches += 3;
+    // density with the new smoothing, then the convergence measures
     KCK(density());
-    // errors (GridProjectedKDE.F90:4962-5038)
-    KCK(reduce(2, 0.0, 0.0));
-    const double mx = h[0], mx_old = h[1];
-    KCK(reduce(1, mx, mx_old));
-    const double err_dens = std::sqrt(h[0] / nb), err_smooth = std::sqrt(h[1] / nb);
-    KCK(almise(alm));
+    KCK(reduce(RED_MAX));
+    KCK(reduce(RED_ERR));
+    KCK(reduce(RED_ALMISE));
+    KCK(fetch());
+    // maxval(netRoughness) == 0: the reference stops (GridProjectedKDE.F90:5443-5446)
+    if (h[0] == 0.0) return cudaErrorInvalidValue;
+    const double err_dens = std::sqrt(h[6] / nb), err_smooth = std::sqrt(h[7] / nb);
+    alm = std::sqrt(h[9] / nb);
     cum = cum + alm;
     if (!skip_error) {
       if (alm_old > 0.0 && std::fabs(alm - alm_old) / alm_old < rel_err) break;
@@ -1133,7 +1218,7 @@ cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, in
 
 cudaError_t kde_collect_active(KdeState &st, const KdeParams &P, const double *counts, cudaStream_t s, int *nactive) {
   const int64_t ngrid = (int64_t)P.nb[0] * P.nb[1] * P.nb[2];
-  const int chunk = 4096;
+  const int chunk = kCompactChunk;
   const int nblk = (int)((ngrid + chunk - 1) / chunk);
   std::vector<int> cnt(nblk), ofs(nblk);
   int *d_cnt = st.d_blockcnt;
@@ -1151,7 +1236,7 @@ cudaError_t kde_collect_active(KdeState &st, const KdeParams &P, const double *c
   KCK(st.ensure_bins(tot));
   KCK(cudaMemcpyAsync(d_cnt, ofs.data(), sizeof(int) * nblk, cudaMemcpyHostToDevice, s));
   KCK(cudaMemsetAsync(st.cell_bin, 0xff, sizeof(int) * ngrid, s));  // -1: no active bin
-  active_write_kernel<<<nblk, 32, 0, s>>>(counts, ngrid, chunk, d_cnt, P, st.bins, st.cell_bin);
+  active_write_kernel<<<nblk, kThreads, 0, s>>>(counts, ngrid, d_cnt, P, st.bins, st.cell_bin);
   st.launches += 2;
   return cudaGetLastError();
 }

@@ -60,6 +60,7 @@ struct SepPlan {
   const double *f[KDE_KMAX][3];
   int box[KDE_KMAX][6], r1[KDE_KMAX][6], r2[KDE_KMAX][6];
   long long o1[KDE_KMAX], o2[KDE_KMAX];
+  int ur[3][6];  // scatter: union of the output regions of each axis's keys
 };
 
 // Per active bin state (SoA).  3-vectors are stored dimension-major: v[d*n + b].
