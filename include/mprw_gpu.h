@@ -210,10 +210,13 @@ int mprw_histogram_noalloc(const double *gx, const double *gy, const double *gz,
 /* Optional: launch on a caller-provided cudaStream_t (NULL = the handle's). */
 int mprw_set_stream(mprw_handle *h, void *stream);
 
-/* Device time (ms) of the last launch of each kernel family, and the number
- * of kernel launches issued by the last mprw_advance / mprw_histogram call. */
+/* Device time (ms) of the last launch of each kernel family, of the last
+ * whole mprw_gpkde call (stream time from its first to its last operation,
+ * host-side waits included), and the number of kernel launches issued by the
+ * last mprw_advance / mprw_histogram / mprw_gpkde call.  Any pointer may be
+ * NULL. */
 int mprw_last_timings(mprw_handle *h, double *step_ms, double *prep_ms, double *hist_ms,
-                      int64_t *launches);
+                      double *gpkde_ms, int64_t *launches);
 
 int mprw_destroy(mprw_handle *h);
 

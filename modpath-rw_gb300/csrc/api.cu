@@ -56,6 +56,10 @@ struct mprw_handle {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   double step_ms = 0, prep_ms = 0, hist_ms = 0, kde_ms = 0;
   KdeState kde;
+  double *d_kpart = nullptr;          // coordinate-statistics partials
+  double *h_kout = nullptr;           // pinned staging of the density / histogram grids
+  int64_t h_kout_cap = 0;
+  std::vector<double> kde_table_key;  // database parameters of the uploaded factor tables
   double *d_counts = nullptr;
   int64_t counts_cap = 0;
   int64_t launches = 0;
@@ -105,6 +109,8 @@ void free_all(mprw_handle *h) {
     if (p) cudaFree(p);
   if (h->h_counters) cudaFreeHost(h->h_counters);
   if (h->d_counts) cudaFree(h->d_counts);
+  if (h->d_kpart) cudaFree(h->d_kpart);
+  if (h->h_kout) cudaFreeHost(h->h_kout);
   h->kde.release();
   if (h->hscratch) cudaFreeHost(h->hscratch);
   cudaEvent_t evs[] = {h->ev0, h->ev1, h->ev2, h->ev3};
@@ -728,8 +734,8 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
   {
     std::vector<double> part;
     int nblk = 0;
-    double *dpart = nullptr;
-    CK(cudaMalloc(&dpart, sizeof(double) * 4 * 152 * 4));
+    if (!h->d_kpart) CK(cudaMalloc(&h->d_kpart, sizeof(double) * 4 * 152 * 4));
+    double *dpart = h->d_kpart;
     cudaError_t e = launch_coord_sums(geometry(h), h->n, h->d_cell, h->d_status, h->d_x, h->d_y, h->d_z,
                                       h->opt.precision == MPRW_MIXED, 0, mean, dpart, &nblk, s);
     part.resize(4 * nblk);
@@ -750,7 +756,6 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
     for (int i = 0; i < nblk && e == cudaSuccess; ++i)
       for (int k = 0; k < 3; ++k) sq[k] += part[4 * i + k];
     for (int d = 0; d < 3; ++d) sd[d] = (P.mask[d] && npts > 0) ? std::sqrt(sq[d] / npts) : 0.0;
-    cudaFree(dpart);
     h->launches += 2;
     CK(e);
   }
@@ -766,25 +771,34 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
     const double ss = std::pow(prod, 1.0 / nd);
     double hs = ss * std::pow(4.0 / ((nd + 2.0) * npts), 1.0 / (nd + 4.0));
     if (ss == 0.0) hs = 2.0 * P.bin_distance;
-    // factor tables
-    std::vector<double> val;
-    std::vector<int> wm, wofs, sm[3], sofs[3];
-    kde_build_tables(P, val, wm, wofs, sm, sofs);
-    if (h->kde.d_val) cudaFree(h->kde.d_val);
-    if (h->kde.d_meta) cudaFree(h->kde.d_meta);
-    h->kde.d_val = nullptr;
-    h->kde.d_meta = nullptr;
-    CK(cudaMalloc(&h->kde.d_val, sizeof(double) * val.size()));
-    CK(cudaMalloc(&h->kde.d_meta, sizeof(int) * 8 * 3 * KDE_MAXDB));
-    std::vector<int> meta;
-    meta.insert(meta.end(), wm.begin(), wm.end());
-    meta.insert(meta.end(), wofs.begin(), wofs.end());
-    for (int a = 0; a < 3; ++a) {
-      meta.insert(meta.end(), sm[a].begin(), sm[a].end());
-      meta.insert(meta.end(), sofs[a].begin(), sofs[a].end());
+    // factor tables, rebuilt only when the database or the bins change
+    std::vector<double> key = {(double)P.ndim, (double)P.ndelta, P.bin[0], P.bin[1], P.bin[2],
+                               (double)P.mask[0], (double)P.mask[1], (double)P.mask[2]};
+    key.insert(key.end(), P.hod, P.hod + P.ndelta);
+    if (!h->kde.d_val || key != h->kde_table_key) {
+      std::vector<double> val;
+      std::vector<int> wm, wofs, sm[3], sofs[3];
+      kde_build_tables(P, val, wm, wofs, sm, sofs);
+      CK(cudaStreamSynchronize(s));
+      if (h->kde.d_val) cudaFree(h->kde.d_val);
+      if (h->kde.d_meta) cudaFree(h->kde.d_meta);
+      h->kde.d_val = nullptr;
+      h->kde.d_meta = nullptr;
+      h->kde_table_key.clear();
+      CK(cudaMalloc(&h->kde.d_val, sizeof(double) * val.size()));
+      CK(cudaMalloc(&h->kde.d_meta, sizeof(int) * 8 * 3 * KDE_MAXDB));
+      std::vector<int> meta;
+      meta.insert(meta.end(), wm.begin(), wm.end());
+      meta.insert(meta.end(), wofs.begin(), wofs.end());
+      for (int a = 0; a < 3; ++a) {
+        meta.insert(meta.end(), sm[a].begin(), sm[a].end());
+        meta.insert(meta.end(), sofs[a].begin(), sofs[a].end());
+      }
+      CK(cudaMemcpyAsync(h->kde.d_val, val.data(), sizeof(double) * val.size(), cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(h->kde.d_meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, s));
+      CK(cudaStreamSynchronize(s));  // the host vectors go out of scope
+      h->kde_table_key = key;
     }
-    CK(cudaMemcpyAsync(h->kde.d_val, val.data(), sizeof(double) * val.size(), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->kde.d_meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, s));
     const int L = 3 * KDE_MAXDB;
     h->kde.wtab = KdeTable{h->kde.d_val, h->kde.d_meta, h->kde.d_meta + L};
     for (int a = 0; a < 3; ++a)
@@ -800,18 +814,29 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
     if (o->scaling_factor != 0.0) scale *= o->scaling_factor;
     mul2_kernel<<<grid1d(ngrid), 256, 0, s>>>(h->kde.dens_grid, ngrid, f, scale);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(density, h->kde.dens_grid, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
   } else {
     CK(cudaMemsetAsync(h->kde.dens_grid, 0, sizeof(double) * ngrid, s));
-    CK(cudaMemcpyAsync(density, h->kde.dens_grid, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
   }
+  // outputs through pinned staging (density, then histogram)
+  const int64_t nout = histogram ? 2 * ngrid : ngrid;
+  if (nout > h->h_kout_cap) {
+    CK(cudaStreamSynchronize(s));
+    if (h->h_kout) cudaFreeHost(h->h_kout);
+    h->h_kout = nullptr;
+    h->h_kout_cap = 0;
+    CK(cudaMallocHost(&h->h_kout, sizeof(double) * nout));
+    h->h_kout_cap = nout;
+  }
+  CK(cudaMemcpyAsync(h->h_kout, h->kde.dens_grid, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
   if (histogram) {
     mul2_kernel<<<grid1d(ngrid), 256, 0, s>>>(h->d_counts, ngrid, eff, 1.0);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(histogram, h->d_counts, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h->h_kout + ngrid, h->d_counts, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
   }
   CK(cudaEventRecord(h->ev3, s));
   CK(cudaStreamSynchronize(s));
+  std::memcpy(density, h->h_kout, sizeof(double) * ngrid);
+  if (histogram) std::memcpy(histogram, h->h_kout + ngrid, sizeof(double) * ngrid);
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, h->ev2, h->ev3));
   h->kde_ms = ms;
@@ -826,11 +851,13 @@ int mprw_set_stream(mprw_handle *h, void *stream) {
   return MPRW_OK;
 }
 
-int mprw_last_timings(mprw_handle *h, double *step_ms, double *prep_ms, double *hist_ms, int64_t *launches) {
+int mprw_last_timings(mprw_handle *h, double *step_ms, double *prep_ms, double *hist_ms, double *gpkde_ms,
+                      int64_t *launches) {
   if (!h) return MPRW_E_INVAL;
   if (step_ms) *step_ms = h->step_ms;
   if (prep_ms) *prep_ms = h->prep_ms;
   if (hist_ms) *hist_ms = h->hist_ms;
+  if (gpkde_ms) *gpkde_ms = h->kde_ms;
   if (launches) *launches = h->launches;
   return MPRW_OK;
 }

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <numeric>
 #include <vector>
 
 #include "gpkde.cuh"
@@ -31,6 +32,8 @@ namespace mprw {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kBinThreads = 64;   // per-bin elementwise kernels: spread few bins over all SMs
+constexpr int kPassBlocks = 64;   // blocks per key of a separable pass (grid-stride in the key's region)
 
 __device__ __forceinline__ int log_index(const KdeParams &P, double h, int d) {
   if (h <= 0.0) return 1;
@@ -63,16 +66,23 @@ struct Span {
 // ---- density scatter: one warp per bin --------------------------------------
 // The W kernel of a bin is anisotropic (one database level per dimension), so
 // bins share no kernel and each warp folds its bin's three factors in shared
-// memory and adds count * fx fy fz over the span (FP64 atomics).
+// memory and adds count * fy fz * fx over the span (FP64 atomics, one
+// multiply per cell with the row products cached).
 constexpr int kWarpsW = 4;
+constexpr int kRowCache = 256;
 
-__global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, KdeBins B, KdeTable tab,
+__global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, KdeBins B, KdeTable tab, int stride,
                                                                 double *grid) {
   __shared__ double sv_all[kWarpsW][3 * KDE_MAXLEN];
   __shared__ int sm_all[kWarpsW][3], sofs_all[kWarpsW][3];
+  __shared__ double crow_all[kWarpsW][kRowCache];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int b = blockIdx.x * kWarpsW + w;
-  if (b >= B.n) return;  // warp-uniform
+  const int wi = blockIdx.x * kWarpsW + w;
+  if (wi >= B.n) return;  // warp-uniform
+  // bins are stored x fastest, so neighbouring warps would add into nearly the
+  // same cells at once; warp wi takes bin (wi * stride) mod n instead
+  // (gcd(stride, n) = 1: a permutation), spreading the atomics over the grid
+  const int b = (int)(((long long)wi * stride) % B.n);
   double *sv = sv_all[w];
   const int gid[3] = {B.gx[b], B.gy[b], B.gz[b]};
   if (lane < 3) {
@@ -98,15 +108,59 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
     S.k0[d] = g0 - gid[d] + m;
   }
   const double cnt = B.count[b];
-  const int n0 = S.n[0], n01 = S.n[0] * S.n[1], tot = n01 * S.n[2];
-  for (int t = lane; t < tot; t += 32) {
-    const int iz = t / n01, r = t - iz * n01, iy = r / n0, ix = r - iy * n0;
-    const double wv = sv[S.k0[0] + ix] * sv[KDE_MAXLEN + S.k0[1] + iy] * sv[2 * KDE_MAXLEN + S.k0[2] + iz];
-    const int64_t g = (int64_t)(S.g0[0] - 1 + ix) +
-                      (int64_t)P.nb[0] * ((S.g0[1] - 1 + iy) + (int64_t)P.nb[1] * (S.g0[2] - 1 + iz));
-    atomicAdd(&grid[g], cnt * wv);
+  const int n0 = S.n[0], n1 = S.n[1], rows = S.n[1] * S.n[2];
+  const double *fx = sv + S.k0[0], *fy = sv + KDE_MAXLEN + S.k0[1], *fz = sv + 2 * KDE_MAXLEN + S.k0[2];
+  const int64_t sy = P.nb[0], sz = (int64_t)P.nb[0] * P.nb[1];
+  double *gbase = grid + (S.g0[0] - 1) + sy * (S.g0[1] - 1) + sz * (S.g0[2] - 1);
+  // count * fy * fz per row (y fastest), cached when the span has few rows
+  double *crow = crow_all[w];
+  const bool cached = rows <= kRowCache;
+  if (cached) {
+    for (int r = lane; r < rows; r += 32) {
+      const int iz = r / n1, iy = r - iz * n1;
+      crow[r] = cnt * (fy[iy] * fz[iz]);
+    }
+    __syncwarp();
+  }
+  if (n0 <= 32) {
+    // 32 / n0 rows per pass, lane -> (row offset, x)
+    const int rpi = 32 / n0, ix = lane % n0, r0 = lane / n0;
+    if (r0 >= rpi) return;
+    const double fxv = fx[ix];
+    int iz = r0 / n1, iy = r0 - iz * n1;
+    for (int r = r0; r < rows; r += rpi) {
+      const double c = cached ? crow[r] : cnt * (fy[iy] * fz[iz]);
+      atomicAdd(gbase + ix + sy * iy + sz * iz, c * fxv);
+      iy += rpi;
+      while (iy >= n1) {
+        iy -= n1;
+        ++iz;
+      }
+    }
+  } else {
+    for (int r = 0; r < rows; ++r) {
+      const int iz = r / n1, iy = r - iz * n1;
+      const double c = cached ? crow[r] : cnt * (fy[iy] * fz[iz]);
+      for (int ix = lane; ix < n0; ix += 32) atomicAdd(gbase + ix + sy * iy + sz * iz, c * fx[ix]);
+    }
   }
 }
+
+// density grid = raw scatter / binVolume, and the density at every bin
+// (GridProjectedKDE.F90:4662-4667), both from the raw grid
+__global__ void scale_pick_kernel(KdeParams P, KdeBins B, const double *raw, double *grid, int64_t ngrid) {
+  const int64_t n = ngrid > B.n ? ngrid : (int64_t)B.n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < ngrid) grid[i] = raw[i] / P.binvol;
+    if (i < B.n) {
+      const int64_t g = (int64_t)(B.gx[i] - 1) + (int64_t)P.nb[0] * ((B.gy[i] - 1) + (int64_t)P.nb[1] * (B.gz[i] - 1));
+      B.dens[i] = raw[g] / P.binvol;
+    }
+  }
+}
+
+__device__ void support_update(const KdeParams &P, const KdeBins &B, int b, double ne1);
+__device__ void curvature_bandwidth(const KdeParams &P, const KdeBins &B, int b);
 
 // ---- separable passes -------------------------------------------------------
 // The reference folds a kernel that crosses a grid edge back into the grid:
@@ -198,13 +252,17 @@ __global__ void key_assign_kernel(KdeParams P, KdeBins B, int kind, int *bin_key
 // the y, z ranges widened by the half widths; pass 2 (y) the bins' x, y
 // ranges and the widened z range; the z pass runs per bin.  Scatter: pass 1
 // widens x, pass 2 widens y, the z pass writes the grid over the union
-// region of each axis's keys.  out[0..3]: keys present, pass-1 and pass-2
-// elements, largest region.
+// region of each axis's keys.
 constexpr int kPlanThreads = 256;
 static_assert(kPlanThreads >= KDE_KMAX, "one plan thread per key");
 
+// Pass-buffer capacity is checked here, on the device: a plan that needs
+// more than cap1 / cap2 elements (nc per region cell) records the sizes it
+// needs in need[0..1], sets need[2] and presents no key, so the passes do
+// nothing and the host reruns the reconstruction with larger buffers.
 __global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, const KeyAcc *K, KdeTable t0, KdeTable t1,
-                                                            KdeTable t2, int scatter, SepPlan *pl, long long *out) {
+                                                            KdeTable t2, int scatter, SepPlan *pl, int nc,
+                                                            long long cap1, long long cap2, long long *need) {
   __shared__ long long sv1[kPlanThreads], sv2[kPlanThreads];
   __shared__ int sp[kPlanThreads];
   __shared__ int su[3][6];
@@ -279,24 +337,20 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, const K
       atomicMax(&su[axis][5], min(P.nb[2], bx[5] + m[2]));
     }
   }
-  // totals (inclusive scans end at the last key) and the largest region
+  // totals: the inclusive scans end at the last key
   const int np = sp[kPlanThreads - 1];
   const long long tot1 = sv1[kPlanThreads - 1], tot2 = sv2[kPlanThreads - 1];
-  __shared__ long long smx[kPlanThreads];
-  smx[k] = max(v1, v2);
-  __syncthreads();
-  for (int o = kPlanThreads / 2; o > 0; o >>= 1) {
-    if (k < o) smx[k] = max(smx[k], smx[k + o]);
-    __syncthreads();
-  }
+  __syncthreads();  // su complete
+  const bool fits = tot1 * nc <= cap1 && tot2 * nc <= cap2;
   if (k < 3)
-    for (int i = 0; i < 6; ++i) pl->ur[k][i] = su[k][i];
+    for (int i = 0; i < 6; ++i) pl->ur[k][i] = fits ? su[k][i] : (i & 1 ? INT_MIN : INT_MAX);
   if (k == 0) {
-    pl->np = np;
-    out[0] = np;
-    out[1] = tot1;
-    out[2] = tot2;
-    out[3] = smx[0];
+    pl->np = fits ? np : 0;
+    if (!fits) {
+      atomicMax(&need[0], tot1 * nc);
+      atomicMax(&need[1], tot2 * nc);
+      need[2] = 1;
+    }
   }
 }
 
@@ -388,13 +442,17 @@ __global__ void gather_y_kernel(KdeParams P, const SepPlan *pl, const double *T1
 }
 
 // Gather pass 3 at every bin: sum_t fz[t] T2(bx, by, reflect(bz - m + t)).
-// NC = 1 writes out[b] (and out2[b] when given); NC = 6 the roughness terms
-// and the net roughness (GridProjectedKDE.F90:2594-2600).
+// NC = 1, mode GZ_OUT: out[b] (and out2[b] when given); GZ_SUPPORT: the
+// sigma-support update from this first nEstimate; GZ_NEST: nEstimate, then
+// the curvature bandwidths.  NC = 6: the roughness terms and the net
+// roughness (GridProjectedKDE.F90:2594-2600).
+enum { GZ_OUT = 0, GZ_SUPPORT = 1, GZ_NEST = 2 };
+
 template <int NC>
 __global__ void gather_z_kernel(KdeParams P, KdeBins B, const SepPlan *pl, const int *bin_key, const double *T2,
-                                double *out, double *out2) {
+                                int mode, double *out, double *out2) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B.n) return;
+  if (b >= B.n || pl->np == 0) return;  // np == 0: the plan did not fit, the attempt is discarded
   const int j = pl->slot_of[bin_key[b]];
   const int m = pl->m[j][2], n = P.nb[2];
   const double *f = pl->f[j][2];
@@ -411,8 +469,15 @@ __global__ void gather_z_kernel(KdeParams P, KdeBins B, const SepPlan *pl, const
     for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
   }
   if constexpr (NC == 1) {
-    out[b] = acc[0];
-    if (out2) out2[b] = acc[0];
+    if (mode == GZ_SUPPORT) {
+      support_update(P, B, b, acc[0]);
+    } else if (mode == GZ_NEST) {
+      B.nest[b] = acc[0];
+      curvature_bandwidth(P, B, b);
+    } else {
+      out[b] = acc[0];
+      if (out2) out2[b] = acc[0];
+    }
   } else {
     const double rxx = acc[0], ryy = acc[1], rzz = acc[2], rxy = acc[3], rxz = acc[4], ryz = acc[5];
     B.rxx[b] = rxx;
@@ -567,34 +632,19 @@ __global__ void init_bins_kernel(KdeParams P, KdeBins B, double hs) {
   B.net[b] = 0.0;
 }
 
-__global__ void grid_scale_kernel(double *g, int64_t n, double div) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    g[i] = g[i] / div;
-}
-
-__global__ void pick_kernel(KdeParams P, KdeBins B, const double *grid, double *out) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B.n) return;
-  const int64_t g = (int64_t)(B.gx[b] - 1) + (int64_t)P.nb[0] * ((B.gy[b] - 1) + (int64_t)P.nb[1] * (B.gz[b] - 1));
-  out[b] = grid[g];
-}
-
 // second-half of the sigma-support update (GridProjectedKDE.F90:4836-4860)
-__global__ void support_update_kernel(KdeParams P, KdeBins B, const double *ne1) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B.n) return;
+__device__ void support_update(const KdeParams &P, const KdeBins &B, int b, double ne1) {
   const double dn = B.dens[b];
-  double ssc = pow(ne1[b], 0.5) * pow(B.scale[b], P.one_plus_nd_q) / pow(4.0 * dn, 0.25) * P.support_c;
+  double ssc = pow(ne1, 0.5) * pow(B.scale[b], P.one_plus_nd_q) / pow(4.0 * dn, 0.25) * P.support_c;
   if (ssc > P.max_sigma_growth * B.support[b]) ssc = P.max_sigma_growth * B.support[b];
   ssc = fmin(ssc, P.max_k[P.max_dim]);
   if (ssc < P.min_k[P.min_dim]) ssc = P.min_k[P.min_dim];
   B.support[b] = ssc;
 }
 
-// prComputeCurvatureKernelBandwidth (GridProjectedKDE.F90:5207-5275)
-__global__ void curvature_bandwidth_kernel(KdeParams P, KdeBins B) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B.n) return;
+// prComputeCurvatureKernelBandwidth (GridProjectedKDE.F90:5207-5275);
+// nEstimate**fTWO is the product nEstimate*nEstimate, as Fortran compiles it
+__device__ void curvature_bandwidth(const KdeParams &P, const KdeBins &B, int b) {
   double nvpb = 0.0;
   const double dn = B.dens[b];
   if (dn > 0.0) {
@@ -602,7 +652,8 @@ __global__ void curvature_bandwidth_kernel(KdeParams P, KdeBins B) {
     double p = 1.0;
     for (int k = 0; k < P.ndim; ++k) p = (k == 0) ? base : p * base;  // integer power, left to right
     if (P.ndim == 3) p = base * (base * base);
-    nvpb = pow(p * pow(B.nest[b], 2.0) / dn, P.beta_c);
+    const double ne = B.nest[b];
+    nvpb = pow(p * (ne * ne) / dn, P.beta_c);
   }
   for (int d = 0; d < 3; ++d) {
     if (!P.mask[d]) continue;
@@ -625,120 +676,112 @@ __global__ void curvature_bandwidth_kernel(KdeParams P, KdeBins B) {
 // Per-bin reductions of the optimisation loop, in two stages with a fixed
 // order (per-block partials, then one warp), results in the device scalars
 // S so that the next kernels read them without a host round trip:
-//   what 0: S[0] = max(net roughness), S[2] = min(net roughness > 0)
-//   what 2: S[3] = max(density), S[4] = max(previous density),
-//           S[5] = -max(smoothing scale > 0)
-//   what 1: S[6], S[7] = sums of the squared relative density and smoothing
-//           changes (GridProjectedKDE.F90:4976-5000; uses S[3], S[4])
-//   what 3: S[9] = sum of the squared ALMISE terms (4966-4972)
+//   RED_NET:    S[0] = max(net roughness), S[2] = min(net roughness > 0)
+//   RED_MAX:    S[3] = max(density), S[4] = max(previous density),
+//               S[5] = -max(smoothing scale > 0), and S[9] as RED_ALMISE
+//   RED_ERR:    S[6], S[7] = sums of the squared relative density and
+//               smoothing changes (GridProjectedKDE.F90:4976-5000; uses
+//               S[3], S[4])
+//   RED_ALMISE: S[9] = sum of the squared ALMISE terms (4966-4972)
 constexpr int kRedBlocks = 152;
 enum { RED_NET = 0, RED_ERR = 1, RED_MAX = 2, RED_ALMISE = 3 };
+enum { OP_SUM = 0, OP_MAX = 1, OP_MIN = 2 };
 
-__device__ __forceinline__ double warp_sum(double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
+__device__ __forceinline__ int red_op(int what, int slot) {
+  if (what == RED_NET) return slot == 0 ? OP_MAX : (slot == 2 ? OP_MIN : OP_SUM);
+  if (what == RED_MAX) return slot <= 1 ? OP_MAX : (slot == 2 ? OP_MIN : OP_SUM);
+  return OP_SUM;
 }
-__device__ __forceinline__ double warp_max(double v) {
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
-  return v;
+__device__ __forceinline__ double red_init(int op) { return op == OP_MAX ? -DBL_MAX : (op == OP_MIN ? DBL_MAX : 0.0); }
+__device__ __forceinline__ double red_apply(int op, double a, double b) {
+  return op == OP_MAX ? fmax(a, b) : (op == OP_MIN ? fmin(a, b) : a + b);
 }
-__device__ __forceinline__ double warp_min(double v) {
-  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+__device__ __forceinline__ double warp_red(int op, double v) {
+  for (int o = 16; o > 0; o >>= 1) v = red_apply(op, v, __shfl_down_sync(0xffffffffu, v, o));
   return v;
 }
 
 __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBins B, int what, double npts,
                                                               const double *S, double *partial) {
-  __shared__ double red[kThreads / 32][3];
-  double a0, a1, a2;
-  if (what == RED_NET) {
-    a0 = -DBL_MAX, a1 = 0.0, a2 = DBL_MAX;
-  } else if (what == RED_MAX) {
-    a0 = -DBL_MAX, a1 = -DBL_MAX, a2 = DBL_MAX;
-  } else {
-    a0 = a1 = a2 = 0.0;
+  __shared__ double red[kThreads / 32][4];
+  int op[4];
+  double a[4];
+  for (int k = 0; k < 4; ++k) {
+    op[k] = red_op(what, k);
+    a[k] = red_init(op[k]);
   }
   const double mx = (what == RED_ERR) ? S[3] : 0.0, mx_old = (what == RED_ERR) ? S[4] : 0.0;
   const double nd = (double)P.ndim;
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
     if (what == RED_NET) {
       const double r = B.net[b];
-      a0 = fmax(a0, r);
-      if (r > 0.0) a2 = fmin(a2, r);
-    } else if (what == RED_MAX) {
-      a0 = fmax(a0, B.dens[b]);
-      a1 = fmax(a1, B.dens_old[b]);
-      if (B.scale[b] > 0.0) a2 = fmin(a2, -B.scale[b]);
+      a[0] = fmax(a[0], r);
+      if (r > 0.0) a[2] = fmin(a[2], r);
     } else if (what == RED_ERR) {
       const double dn = B.dens[b], dold = B.dens_old[b];
       if (dold != 0.0) {
         const double e = fabs(dn / mx - dold / mx_old) / (dold / mx_old);
-        a0 += e * e;
+        a[0] += e * e;
       }
       const double so = B.scale_old[b], sc = B.scale[b];
       if (so != 0.0) {
         const double e = fabs(sc - so) / so;
-        a1 += e * e;
+        a[1] += e * e;
       }
     } else {
       const double sc = B.scale[b];
+      if (what == RED_MAX) {
+        a[0] = fmax(a[0], B.dens[b]);
+        a[1] = fmax(a[1], B.dens_old[b]);
+        if (sc > 0.0) a[2] = fmin(a[2], -sc);
+      }
       if (sc != 0.0) {
         const double e = (B.nest[b] / (pow(sc, nd) * pow(4.0 * PI_D, 0.5 * nd)) + 0.25 * B.net[b] * pow(sc, 4.0)) /
                          pow(npts, 2.0);
-        a0 += e * e;
+        a[3] += e * e;
       }
     }
   }
-  const bool mm = (what == RED_NET || what == RED_MAX);
-  a0 = mm ? warp_max(a0) : warp_sum(a0);
-  a1 = (what == RED_MAX) ? warp_max(a1) : warp_sum(a1);
-  a2 = mm ? warp_min(a2) : warp_sum(a2);
+  for (int k = 0; k < 4; ++k) a[k] = warp_red(op[k], a[k]);
   const int w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) {
-    red[w][0] = a0;
-    red[w][1] = a1;
-    red[w][2] = a2;
-  }
+  if ((threadIdx.x & 31) == 0)
+    for (int k = 0; k < 4; ++k) red[w][k] = a[k];
   __syncthreads();
   if (threadIdx.x == 0) {
-    double b0 = red[0][0], b1 = red[0][1], b2 = red[0][2];
-    for (int i = 1; i < kThreads / 32; ++i) {
-      b0 = mm ? fmax(b0, red[i][0]) : b0 + red[i][0];
-      b1 = (what == RED_MAX) ? fmax(b1, red[i][1]) : b1 + red[i][1];
-      b2 = mm ? fmin(b2, red[i][2]) : b2 + red[i][2];
+    for (int k = 0; k < 4; ++k) {
+      double v = red[0][k];
+      for (int i = 1; i < kThreads / 32; ++i) v = red_apply(op[k], v, red[i][k]);
+      partial[4 * blockIdx.x + k] = v;
     }
-    partial[3 * blockIdx.x + 0] = b0;
-    partial[3 * blockIdx.x + 1] = b1;
-    partial[3 * blockIdx.x + 2] = b2;
   }
 }
 
 // one warp: lane l folds partials l, l+32, ... then a shuffle tree
 __global__ void bin_reduce_final_kernel(int what, int nblk, const double *partial, double *S) {
   const int l = threadIdx.x;
-  const bool mm = (what == RED_NET || what == RED_MAX);
-  double a0 = mm ? -DBL_MAX : 0.0, a1 = (what == RED_MAX) ? -DBL_MAX : 0.0, a2 = mm ? DBL_MAX : 0.0;
-  for (int i = l; i < nblk; i += 32) {
-    a0 = mm ? fmax(a0, partial[3 * i]) : a0 + partial[3 * i];
-    a1 = (what == RED_MAX) ? fmax(a1, partial[3 * i + 1]) : a1 + partial[3 * i + 1];
-    a2 = mm ? fmin(a2, partial[3 * i + 2]) : a2 + partial[3 * i + 2];
+  double a[4];
+  int op[4];
+  for (int k = 0; k < 4; ++k) {
+    op[k] = red_op(what, k);
+    a[k] = red_init(op[k]);
   }
-  a0 = mm ? warp_max(a0) : warp_sum(a0);
-  a1 = (what == RED_MAX) ? warp_max(a1) : warp_sum(a1);
-  a2 = mm ? warp_min(a2) : warp_sum(a2);
+  for (int i = l; i < nblk; i += 32)
+    for (int k = 0; k < 4; ++k) a[k] = red_apply(op[k], a[k], partial[4 * i + k]);
+  for (int k = 0; k < 4; ++k) a[k] = warp_red(op[k], a[k]);
   if (l != 0) return;
   if (what == RED_NET) {
-    S[0] = a0;
-    S[2] = a2;
+    S[0] = a[0];
+    S[2] = a[2];
   } else if (what == RED_MAX) {
-    S[3] = a0;
-    S[4] = a1;
-    S[5] = a2;
+    S[3] = a[0];
+    S[4] = a[1];
+    S[5] = a[2];
+    S[9] = a[3];
   } else if (what == RED_ERR) {
-    S[6] = a0;
-    S[7] = a1;
+    S[6] = a[0];
+    S[7] = a[1];
   } else {
-    S[9] = a0;
+    S[9] = a[3];
   }
 }
 
@@ -909,7 +952,7 @@ cudaError_t KdeState::ensure_bins(int n) {
   D(&bins.count, c); D(&bins.ks, 3 * c); D(&bins.scale, c); D(&bins.shape, 3 * c); D(&bins.support, c);
   D(&bins.nest, c); D(&bins.dens, c); D(&bins.cb, 3 * c); D(&bins.rxx, c); D(&bins.ryy, c); D(&bins.rzz, c);
   D(&bins.net, c); D(&bins.dens_old, c); D(&bins.scale_old, c); D(&tmp, c);
-  D(&partial, 3 * 152 * 8 + 16);
+  D(&partial, 4 * 152 * 8 + 16);
   if (e != cudaSuccess) return e;
   cap = n;
   bins.n = n;
@@ -923,18 +966,20 @@ cudaError_t KdeState::ensure_grid(int64_t ngrid) {
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&h_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_keys, sizeof(KeyAcc));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&d_plan, 2 * sizeof(SepPlan) + 8 * sizeof(long long));
-    if (e == cudaSuccess) e = cudaMallocHost((void **)&h_plan, 8 * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_plan, 2 * sizeof(SepPlan));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_need, 4 * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&h_need, 4 * sizeof(long long));
     if (e != cudaSuccess) return e;
   }
   if (ngrid <= grid_cap) return cudaSuccess;
-  double *old[] = {dens_grid, cx, cy, cz};
+  double *old[] = {dens_grid, dens_raw, cx, cy, cz};
   for (double *p : old)
     if (p) cudaFree(p);
   if (d_blockcnt) cudaFree(d_blockcnt);
   if (cell_bin) cudaFree(cell_bin);
   cudaError_t e = cudaMalloc((void **)&dens_grid, sizeof(double) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&cell_bin, sizeof(int) * ngrid);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&dens_raw, sizeof(double) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&cx, sizeof(double) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&cy, sizeof(double) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&cz, sizeof(double) * ngrid);
@@ -970,12 +1015,12 @@ void KdeState::release() {
   void *ptrs[] = {bins.gx, bins.gy, bins.gz, bins.count, bins.ks, bins.scale, bins.shape, bins.support, bins.nest,
                   bins.dens, bins.cb, bins.rxx, bins.ryy, bins.rzz, bins.net, bins.dens_old, bins.scale_old, tmp,
                   partial, dens_grid, cx, cy, cz, d_scalars, d_flag, d_blockcnt, d_val, d_meta, cell_bin, bin_key,
-                  d_keys, d_plan, t1, t2};
+                  d_keys, d_plan, t1, t2, dens_raw, d_need};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_scalars) cudaFreeHost(h_scalars);
   if (h_flag) cudaFreeHost(h_flag);
-  if (h_plan) cudaFreeHost(h_plan);
+  if (h_need) cudaFreeHost(h_need);
   *this = KdeState();
 }
 static double erf_diff(double i, double hd) {
@@ -1078,54 +1123,51 @@ void kde_build_tables(const KdeParams &P, std::vector<double> &val, std::vector<
     if (e_ != cudaSuccess) return e_;     \
   } while (0)
 
-cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, int n_opt_loops, double rel_err,
-                    bool skip_error, cudaStream_t s, int *loops_done) {
+// One reconstruction attempt; *overflow is set when a plan found the pass
+// buffers too small (the sizes it needed are in st.h_need).
+static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, double npts, int n_opt_loops,
+                               double rel_err, bool skip_error, cudaStream_t s, int *loops_done, bool *overflow) {
   KdeBins &B = st.bins;
   const int nb = B.n;
   const int64_t ngrid = (int64_t)P.nb[0] * P.nb[1] * P.nb[2];
-  const int bb = (nb + kThreads - 1) / kThreads;
+  const int bb = (nb + kBinThreads - 1) / kBinThreads;
   const int gb = blocks_for(ngrid);
   const int rb = std::min(blocks_for(nb), kRedBlocks);
-  const int kb = std::min(bb, 2 * kRedBlocks);
+  const int kb = std::min((nb + kThreads - 1) / kThreads, 2 * kRedBlocks);
+  const int64_t npick = ngrid > nb ? ngrid : nb;
   double *S = st.d_scalars, *h = st.h_scalars;
+  *overflow = false;
+  // a stride near n/61 coprime with n (a permutation of the bins)
+  int wstride = nb / 61 + 1;
+  while (std::gcd(wstride, nb) != 1) ++wstride;
   auto density = [&](void) -> cudaError_t {
-    KCK(cudaMemsetAsync(st.dens_grid, 0, sizeof(double) * ngrid, s));
-    wscatter_kernel<<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, st.wtab, st.dens_grid);
-    grid_scale_kernel<<<gb, kThreads, 0, s>>>(st.dens_grid, ngrid, P.binvol);
-    pick_kernel<<<bb, kThreads, 0, s>>>(P, B, st.dens_grid, B.dens);
-    st.launches += 3;
+    KCK(cudaMemsetAsync(st.dens_raw, 0, sizeof(double) * ngrid, s));
+    wscatter_kernel<<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, st.wtab, wstride, st.dens_raw);
+    scale_pick_kernel<<<blocks_for(npick), kThreads, 0, s>>>(P, B, st.dens_raw, st.dens_grid, ngrid);
+    st.launches += 2;
     return cudaGetLastError();
   };
   // plans: [0] smoothing kernels (kind 1), [1] second-derivative kernels (kind 2)
   SepPlan *plan1 = st.d_plan, *plan2 = st.d_plan + 1;
-  long long *plan_out = reinterpret_cast<long long *>(st.d_plan + 2);
   int *key1 = st.bin_key, *key2 = st.bin_key + nb;
-  dim3 grid1(1, 1), grid2(1, 1);
-  // the host needs the keys present and the pass-buffer sizes: one sync
-  auto plan = [&](int kind, int nc, dim3 &grid) -> cudaError_t {
-    SepPlan *pl = kind == 1 ? plan1 : plan2;
+  const dim3 pgrid(kPassBlocks, KDE_KMAX);
+  auto plan = [&](int kind, int nc) -> cudaError_t {
     key_init_kernel<<<1, kThreads, 0, s>>>(st.d_keys);
     key_assign_kernel<<<kb, kThreads, 0, s>>>(P, B, kind, kind == 1 ? key1 : key2, st.d_keys);
     if (kind == 1)
-      plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.wtab, st.wtab, st.wtab, 0, pl, plan_out);
+      plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.wtab, st.wtab, st.wtab, 0, plan1, nc, st.t1_cap,
+                                             st.t2_cap, st.d_need);
     else
-      plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.sdtab[0], st.sdtab[1], st.sdtab[2], 1, pl, plan_out);
+      plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.sdtab[0], st.sdtab[1], st.sdtab[2], 1, plan2, nc,
+                                             st.t1_cap, st.t2_cap, st.d_need);
     st.launches += 3;
-    KCK(cudaGetLastError());
-    KCK(cudaMemcpyAsync(st.h_plan, plan_out, 4 * sizeof(long long), cudaMemcpyDeviceToHost, s));
-    KCK(cudaStreamSynchronize(s));
-    const long long np = st.h_plan[0], mx = st.h_plan[3];
-    KCK(st.ensure_pass(st.h_plan[1] * nc, st.h_plan[2] * nc));
-    long long gx = (mx + kThreads - 1) / kThreads;
-    gx = gx < 1 ? 1 : (gx > 1024 ? 1024 : gx);
-    grid = dim3((unsigned)gx, (unsigned)(np < 1 ? 1 : np));
-    return cudaSuccess;
+    return cudaGetLastError();
   };
   // sum over every bin's smoothing kernel of `field`, at the bins
-  auto gather1 = [&](const double *field, double *out, double *out2) -> cudaError_t {
-    gather_x_kernel<1><<<grid1, kThreads, 0, s>>>(P, plan1, field, nullptr, nullptr, st.t1);
-    gather_y_kernel<1><<<grid1, kThreads, 0, s>>>(P, plan1, st.t1, st.t2);
-    gather_z_kernel<1><<<bb, kThreads, 0, s>>>(P, B, plan1, key1, st.t2, out, out2);
+  auto gather1 = [&](const double *field, int mode, double *out, double *out2) -> cudaError_t {
+    gather_x_kernel<1><<<pgrid, kThreads, 0, s>>>(P, plan1, field, nullptr, nullptr, st.t1);
+    gather_y_kernel<1><<<pgrid, kThreads, 0, s>>>(P, plan1, st.t1, st.t2);
+    gather_z_kernel<1><<<bb, kBinThreads, 0, s>>>(P, B, plan1, key1, st.t2, mode, out, out2);
     st.launches += 3;
     return cudaGetLastError();
   };
@@ -1135,65 +1177,107 @@ cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, in
     st.launches += 2;
     return cudaGetLastError();
   };
-  auto fetch = [&](void) -> cudaError_t {
+  auto fetch_async = [&](void) -> cudaError_t {
     KCK(cudaMemcpyAsync(h, S, 10 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    return cudaStreamSynchronize(s);
+    return cudaMemcpyAsync(st.h_need, st.d_need, 3 * sizeof(long long), cudaMemcpyDeviceToHost, s);
   };
-  init_bins_kernel<<<bb, kThreads, 0, s>>>(P, B, hs);
-  st.launches += 1;
-  KCK(density());
-  KCK(reduce(RED_ALMISE));  // nEstimate and net roughness are zero: 0
-  KCK(fetch());
-  double alm = std::sqrt(h[9] / nb);
-  double alm_old = alm, cum = alm, cum_old = alm;
-  copy_kernel<<<bb, kThreads, 0, s>>>(B.dens_old, B.dens, nb);
-  copy_kernel<<<bb, kThreads, 0, s>>>(B.scale_old, B.scale, nb);
-  st.launches += 2;
-  int m = 0;
-  for (m = 1; m <= n_opt_loops; ++m) {
+  auto fetch_wait = [&](void) -> cudaError_t {
+    KCK(cudaStreamSynchronize(s));
+    *overflow = st.h_need[2] != 0;
+    return cudaSuccess;
+  };
+  // One optimisation loop (GridProjectedKDE.F90:4700-5040) up to the
+  // convergence measures, which it copies to the host.  It starts by saving
+  // the previous density and smoothing scale (the reference does that at the
+  // end of a loop that did not converge; nothing runs in between).  Every
+  // data-dependent choice inside is taken on the device, so one captured
+  // graph replays every loop.
+  auto body = [&](void) -> cudaError_t {
+    copy_kernel<<<bb, kBinThreads, 0, s>>>(B.dens_old, B.dens, nb);
+    copy_kernel<<<bb, kBinThreads, 0, s>>>(B.scale_old, B.scale, nb);
+    st.launches += 2;
     // nEstimate with the current support, support update, nEstimate again
-    KCK(plan(1, 1, grid1));
-    KCK(gather1(st.dens_grid, st.tmp, nullptr));
-    support_update_kernel<<<bb, kThreads, 0, s>>>(P, B, st.tmp);
-    st.launches += 1;
-    KCK(plan(1, P.ndim == 3 ? 6 : 1, grid1));
-    KCK(gather1(st.dens_grid, B.nest, nullptr));
-    curvature_bandwidth_kernel<<<bb, kThreads, 0, s>>>(P, B);
-    st.launches += 1;
+    // and the curvature bandwidths
+    KCK(plan(1, 1));
+    KCK(gather1(st.dens_grid, GZ_SUPPORT, nullptr, nullptr));
+    KCK(plan(1, P.ndim == 3 ? 6 : 1));
+    KCK(gather1(st.dens_grid, GZ_NEST, nullptr, nullptr));
     // curvatures: second-derivative scatters of the counts, squared
-    KCK(plan(2, 1, grid2));
+    KCK(plan(2, 1));
     for (double *c : {st.cx, st.cy, st.cz}) KCK(cudaMemsetAsync(c, 0, sizeof(double) * ngrid, s));
-    scatter_x_kernel<<<grid2, kThreads, 0, s>>>(P, B, plan2, st.cell_bin, key2, st.t1);
-    scatter_y_kernel<<<grid2, kThreads, 0, s>>>(P, plan2, st.t1, st.t2);
+    scatter_x_kernel<<<pgrid, kThreads, 0, s>>>(P, B, plan2, st.cell_bin, key2, st.t1);
+    scatter_y_kernel<<<pgrid, kThreads, 0, s>>>(P, plan2, st.t1, st.t2);
     scatter_z_kernel<<<dim3(gb, 3), kThreads, 0, s>>>(P, plan2, st.t2, st.cx, st.cy, st.cz);
     st.launches += 3;
     // net roughness: smoothing-kernel gathers of the squared curvatures
     if (P.ndim == 3) {
-      gather_x_kernel<6><<<grid1, kThreads, 0, s>>>(P, plan1, st.cx, st.cy, st.cz, st.t1);
-      gather_y_kernel<6><<<grid1, kThreads, 0, s>>>(P, plan1, st.t1, st.t2);
-      gather_z_kernel<6><<<bb, kThreads, 0, s>>>(P, B, plan1, key1, st.t2, nullptr, nullptr);
+      gather_x_kernel<6><<<pgrid, kThreads, 0, s>>>(P, plan1, st.cx, st.cy, st.cz, st.t1);
+      gather_y_kernel<6><<<pgrid, kThreads, 0, s>>>(P, plan1, st.t1, st.t2);
+      gather_z_kernel<6><<<bb, kBinThreads, 0, s>>>(P, B, plan1, key1, st.t2, GZ_OUT, nullptr, nullptr);
       st.launches += 3;
     } else {
       int a = 0;
       while (!P.mask[a]) ++a;
       double *cg[3] = {st.cx, st.cy, st.cz};
       double *r1 = (a == 0) ? B.rxx : (a == 1 ? B.ryy : B.rzz);
-      KCK(gather1(cg[a], r1, B.net));
+      KCK(gather1(cg[a], GZ_OUT, r1, B.net));
     }
     // optimal smoothing and shape; the extremes stay on the device
     KCK(reduce(RED_NET));
-    optimal_phase0_kernel<<<bb, kThreads, 0, s>>>(P, B, S);
+    optimal_phase0_kernel<<<bb, kBinThreads, 0, s>>>(P, B, S);
     KCK(reduce(RED_MAX));
     KCK(cudaMemsetAsync(st.d_flag, 0, sizeof(int), s));
-    optimal_phase1_kernel<<<bb, kThreads, 0, s>>>(P, B, S, st.d_flag);
-    rescale_kernel<<<bb, kThreads, 0, s>>>(P, B, st.d_flag);
+    optimal_phase1_kernel<<<bb, kBinThreads, 0, s>>>(P, B, S, st.d_flag);
+    rescale_kernel<<<bb, kBinThreads, 0, s>>>(P, B, st.d_flag);
     st.launches += 3;
     // density with the new smoothing, then the convergence measures
     KCK(density());
-    KCK(reduce(RED_MAX));
+    KCK(reduce(RED_MAX));  // with the ALMISE sum
     KCK(reduce(RED_ERR));
-    KCK(reduce(RED_ALMISE));
-    KCK(fetch());
+    return fetch_async();
+  };
+  KCK(cudaMemsetAsync(st.d_need, 0, 3 * sizeof(long long), s));
+  init_bins_kernel<<<bb, kBinThreads, 0, s>>>(P, B, hs);
+  st.launches += 1;
+  KCK(density());
+  KCK(reduce(RED_ALMISE));  // nEstimate and net roughness are zero: 0
+  KCK(fetch_async());
+  KCK(fetch_wait());
+  double alm = std::sqrt(h[9] / nb);
+  double alm_old = alm, cum = alm, cum_old = alm;
+  // capture the loop body once; a stream that cannot be captured (the legacy
+  // default stream) runs it directly
+  cudaGraphExec_t exec = nullptr;
+  int64_t body_launches = 0;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    const int64_t l0 = st.launches;
+    const cudaError_t eb = body();
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(s, &g);
+    body_launches = st.launches - l0;
+    st.launches = l0;
+    if (eb == cudaSuccess && ee == cudaSuccess && g) {
+      if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) exec = nullptr;
+    }
+    if (g) cudaGraphDestroy(g);
+    (void)cudaGetLastError();  // a failed capture leaves no sticky error
+  }
+  struct ExecGuard {
+    cudaGraphExec_t e;
+    ~ExecGuard() {
+      if (e) cudaGraphExecDestroy(e);
+    }
+  } guard{exec};
+  int m = 0;
+  for (m = 1; m <= n_opt_loops; ++m) {
+    if (exec) {
+      KCK(cudaGraphLaunch(exec, s));
+      st.launches += body_launches;
+    } else {
+      KCK(body());
+    }
+    KCK(fetch_wait());
+    if (*overflow) return cudaSuccess;
     // maxval(netRoughness) == 0: the reference stops (GridProjectedKDE.F90:5443-5446)
     if (h[0] == 0.0) return cudaErrorInvalidValue;
     const double err_dens = std::sqrt(h[6] / nb), err_smooth = std::sqrt(h[7] / nb);
@@ -1208,12 +1292,28 @@ cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, in
     }
     alm_old = alm;
     cum_old = cum;
-    copy_kernel<<<bb, kThreads, 0, s>>>(B.dens_old, B.dens, nb);
-    copy_kernel<<<bb, kThreads, 0, s>>>(B.scale_old, B.scale, nb);
-    st.launches += 2;
   }
   if (loops_done) *loops_done = (m > n_opt_loops) ? n_opt_loops : m;
   return cudaGetLastError();
+}
+
+// The pass buffers start small and grow: an attempt whose plans did not fit
+// is discarded and the reconstruction restarts from the histogram with the
+// buffers the plans asked for (every attempt re-derives all per-bin state,
+// so the result does not depend on how many attempts ran).
+cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, int n_opt_loops, double rel_err,
+                    bool skip_error, cudaStream_t s, int *loops_done) {
+  const int64_t ngrid = (int64_t)P.nb[0] * P.nb[1] * P.nb[2];
+  // eight grid volumes of the six roughness fields: enough for most plumes
+  KCK(st.ensure_pass(48 * ngrid, 48 * ngrid));
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    bool overflow = false;
+    KCK(kde_attempt(st, P, hs, npts, n_opt_loops, rel_err, skip_error, s, loops_done, &overflow));
+    if (!overflow) return cudaSuccess;
+    // what a discarded attempt asked for is a lower bound: grow geometrically
+    KCK(st.ensure_pass(std::max<int64_t>(st.h_need[0], 2 * st.t1_cap), std::max<int64_t>(st.h_need[1], 2 * st.t2_cap)));
+  }
+  return cudaErrorMemoryAllocation;
 }
 
 cudaError_t kde_collect_active(KdeState &st, const KdeParams &P, const double *counts, cudaStream_t s, int *nactive) {

@@ -74,7 +74,7 @@ struct KdeBins {
 struct KdeState {
   KdeBins bins{};
   int cap = 0;
-  double *dens_grid = nullptr, *cx = nullptr, *cy = nullptr, *cz = nullptr;
+  double *dens_grid = nullptr, *dens_raw = nullptr, *cx = nullptr, *cy = nullptr, *cz = nullptr;
   int64_t grid_cap = 0;
   double *tmp = nullptr, *partial = nullptr, *d_scalars = nullptr, *h_scalars = nullptr;
   int *d_flag = nullptr, *h_flag = nullptr, *d_blockcnt = nullptr;
@@ -82,9 +82,9 @@ struct KdeState {
   int *bin_key = nullptr;           // per bin: smoothing key (n) and SD keys per axis (3n)
   KeyAcc *d_keys = nullptr;
   SepPlan *d_plan = nullptr;
-  long long *h_plan = nullptr;      // pinned: keys present, pass-buffer sizes, largest region
   double *t1 = nullptr, *t2 = nullptr;
   int64_t t1_cap = 0, t2_cap = 0;
+  long long *d_need = nullptr, *h_need = nullptr;  // pass-buffer sizes a plan needed, overflow flag
   KdeTable wtab{}, sdtab[3]{};
   double *d_val = nullptr;
   int *d_meta = nullptr;  // wm, wofs, sm[3], sofs[3]

@@ -85,7 +85,7 @@ def load_library() -> C.CDLL:
         "mprw_histogram": (C.c_int, [H, _dp, _dp, _ip, _dp, C.POINTER(C.c_int64), _dp]),
         "mprw_gpkde": (C.c_int, [H, C.POINTER(GpkdeOptions), _dp, _dp, _ip, _ip]),
         "mprw_set_stream": (C.c_int, [H, C.c_void_p]),
-        "mprw_last_timings": (C.c_int, [H, _dp, _dp, _dp, C.POINTER(C.c_int64)]),
+        "mprw_last_timings": (C.c_int, [H, _dp, _dp, _dp, _dp, C.POINTER(C.c_int64)]),
         "mprw_destroy": (C.c_int, [H]),
         "mprw_last_error": (C.c_char_p, [H]),
     }
@@ -225,10 +225,10 @@ class Tracker:
                                             C.byref(nbinned), C.byref(eff)), "mprw_histogram")
         return counts.reshape(int(nb[2]), int(nb[1]), int(nb[0])), nbinned.value, eff.value
 
-    def gpkde(self, domain_size, bin_size, origin=(0.0, 0.0, 0.0), n_opt_loops=10, kdb=(0.3, 0.3, 15.0),
-              rel_err=0.02, skip_error=False, unit_volume=True, scaling_factor=1.0):
-        """GPKDE reconstruction of the active particles.  Returns (density, histogram,
-        loops) with the grids shaped (nz, ny, nx)."""
+    @staticmethod
+    def gpkde_options(domain_size, bin_size, origin=(0.0, 0.0, 0.0), n_opt_loops=10, kdb=(0.3, 0.3, 15.0),
+                      rel_err=0.02, skip_error=False, unit_volume=True, scaling_factor=1.0) -> "GpkdeOptions":
+        """The mprw_gpkde_options of a reconstruction grid (defaults: the reference's GPKDE input defaults)."""
         o = GpkdeOptions()
         for d in range(3):
             o.origin[d], o.domain_size[d], o.bin_size[d] = float(origin[d]), float(domain_size[d]), float(bin_size[d])
@@ -238,6 +238,14 @@ class Tracker:
         o.skip_error_convergence = int(skip_error)
         o.unit_volume = int(unit_volume)
         o.scaling_factor = float(scaling_factor)
+        return o
+
+    def gpkde(self, domain_size, bin_size, origin=(0.0, 0.0, 0.0), n_opt_loops=10, kdb=(0.3, 0.3, 15.0),
+              rel_err=0.02, skip_error=False, unit_volume=True, scaling_factor=1.0):
+        """GPKDE reconstruction of the active particles.  Returns (density, histogram,
+        loops) with the grids shaped (nz, ny, nx)."""
+        o = self.gpkde_options(domain_size, bin_size, origin, n_opt_loops, kdb, rel_err, skip_error, unit_volume,
+                               scaling_factor)
         nb = [int(domain_size[d] / bin_size[d] + 0.5) if bin_size[d] != 0 else 1 for d in range(3)]
         dens = np.empty(int(np.prod(nb)))
         hist = np.empty(int(np.prod(nb)))
@@ -252,11 +260,11 @@ class Tracker:
         self._check(self.lib.mprw_set_stream(self.h, C.c_void_p(stream_ptr)), "mprw_set_stream")
 
     def timings(self) -> dict:
-        s, p, h = C.c_double(), C.c_double(), C.c_double()
+        s, p, h, k = C.c_double(), C.c_double(), C.c_double(), C.c_double()
         n = C.c_int64()
-        self._check(self.lib.mprw_last_timings(self.h, C.byref(s), C.byref(p), C.byref(h), C.byref(n)),
+        self._check(self.lib.mprw_last_timings(self.h, C.byref(s), C.byref(p), C.byref(h), C.byref(k), C.byref(n)),
                     "mprw_last_timings")
-        return dict(step_ms=s.value, prep_ms=p.value, hist_ms=h.value, launches=n.value)
+        return dict(step_ms=s.value, prep_ms=p.value, hist_ms=h.value, gpkde_ms=k.value, launches=n.value)
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
