@@ -682,6 +682,7 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
   P.one_over_nd4 = 1.0 / (nd + 4.0);
   P.minus_one_over_nd6 = -1.0 / (nd + 6.0);
   P.one_plus_nd_q = 1.0 + 0.25 * nd;
+  P.four_pi_half_nd = std::pow(4.0 * PI_D, 0.5 * nd);
   P.max_sigma_growth = 1.5;
   P.iso_threshold = 0.85;
   // logarithmic database (prInitializeKernelDatabaseFlat, prGenerateLogSpaceData)

@@ -43,19 +43,26 @@ __device__ __forceinline__ int log_index(const KdeParams &P, double h, int d) {
   return i;
 }
 
-// Fold one dimension's factor in place (prKernelReflection, one axis).
-__device__ void fold_factor(double *v, int m, int gid, int nb) {
+// Fold one dimension's factor in place (prKernelReflection, one axis), the
+// lanes of a warp splitting each loop: the part below cell 1 is added onto its
+// mirror image and cleared, then the part above cell nb likewise (targets and
+// sources of each step are disjoint).  m, gid and nb are warp-uniform.
+__device__ void fold_factor_warp(double *v, int m, int gid, int nb, int lane) {
   const int len = 2 * m + 1;
   if (gid - m < 1) {
     const int b = 1 - gid + m;
-    for (int j = 0; j < b; ++j) v[b + j] = v[b + j] + v[b - 1 - j];
-    for (int j = 0; j < b; ++j) v[j] = 0.0;
+    for (int j = lane; j < b; j += 32) v[b + j] = v[b + j] + v[b - 1 - j];
+    __syncwarp();
+    for (int j = lane; j < b; j += 32) v[j] = 0.0;
+    __syncwarp();
   }
   if (gid + m > nb) {
     const int B = 2 * m + 1 - (gid + m - nb) + 1;  // 1-based
     const int lenb = len - B + 1;
-    for (int j = 0; j < lenb; ++j) v[B - lenb - 1 + j] = v[B - lenb - 1 + j] + v[2 * m - j];
-    for (int j = B - 1; j < len; ++j) v[j] = 0.0;
+    for (int j = lane; j < lenb; j += 32) v[B - lenb - 1 + j] = v[B - lenb - 1 + j] + v[2 * m - j];
+    __syncwarp();
+    for (int j = B - 1 + lane; j < len; j += 32) v[j] = 0.0;
+    __syncwarp();
   }
 }
 
@@ -71,8 +78,16 @@ struct Span {
 constexpr int kWarpsW = 4;
 constexpr int kRowCache = 256;
 
+// database level of every bin's W kernel per dimension (one thread per bin:
+// the logarithm and divisions run on full warps)
+__global__ void wlevel_kernel(KdeParams P, KdeBins B, int *wlev) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B.n) return;
+  for (int d = 0; d < 3; ++d) wlev[d * B.n + b] = P.mask[d] ? log_index(P, B.ks[d * B.n + b], d) : 1;
+}
+
 __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, KdeBins B, KdeTable tab, int stride,
-                                                                double *grid) {
+                                                                const int *wlev, double *grid) {
   __shared__ double sv_all[kWarpsW][3 * KDE_MAXLEN];
   __shared__ int sm_all[kWarpsW][3], sofs_all[kWarpsW][3];
   __shared__ double crow_all[kWarpsW][kRowCache];
@@ -87,7 +102,7 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
   const int gid[3] = {B.gx[b], B.gy[b], B.gz[b]};
   if (lane < 3) {
     const int d = lane;
-    const int idx = P.mask[d] ? log_index(P, B.ks[d * B.n + b], d) : 1;
+    const int idx = wlev[d * B.n + b];
     sm_all[w][d] = tab.m[d * KDE_MAXDB + idx - 1];
     sofs_all[w][d] = tab.ofs[d * KDE_MAXDB + idx - 1];
   }
@@ -97,8 +112,8 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
     for (int k = lane; k < 2 * m + 1; k += 32) sv[d * KDE_MAXLEN + k] = tab.val[o + k];
   }
   __syncwarp();
-  if (lane < 3 && P.mask[lane]) fold_factor(sv + lane * KDE_MAXLEN, sm_all[w][lane], gid[lane], P.nb[lane]);
-  __syncwarp();
+  for (int d = 0; d < 3; ++d)
+    if (P.mask[d]) fold_factor_warp(sv + d * KDE_MAXLEN, sm_all[w][d], gid[d], P.nb[d], lane);
   Span S;
   for (int d = 0; d < 3; ++d) {
     const int m = sm_all[w][d];
@@ -372,10 +387,14 @@ __device__ __forceinline__ long long region_loc(const int r[6], int x, int y, in
 
 // Gather pass 1: T1 = sum_t fx[t] F(reflect(x - m + t), y, z) over region 1.
 // NC = 1: one field; NC = 6: the squared curvatures cx, cy, cz and their
-// pairwise products (the roughness terms, GridProjectedKDE.F90:2470-2600).
+// pairwise products cx*cy, cx*cz, cy*cz (the roughness terms,
+// GridProjectedKDE.F90:2470-2600).
+struct Fields {
+  const double *f[6];
+};
+
 template <int NC>
-__global__ void gather_x_kernel(KdeParams P, const SepPlan *pl, const double *F0, const double *F1,
-                                const double *F2, double *T1) {
+__global__ void gather_x_kernel(KdeParams P, const SepPlan *pl, Fields F, double *T1) {
   const int j = blockIdx.y;
   if (j >= pl->np) return;
   int r[6];
@@ -394,19 +413,20 @@ __global__ void gather_x_kernel(KdeParams P, const SepPlan *pl, const double *F0
       const int p = reflect_pos(x - m + t, n);
       if (p < 1) continue;
       const double w = f[t];
-      if constexpr (NC == 1) {
-        acc[0] += w * F0[row + p];
-      } else {
-        const double a = F0[row + p], bb = F1[row + p], c = F2[row + p];
-        acc[0] += w * a;
-        acc[1] += w * bb;
-        acc[2] += w * c;
-        acc[3] += w * (a * bb);
-        acc[4] += w * (a * c);
-        acc[5] += w * (bb * c);
-      }
+      for (int c = 0; c < NC; ++c) acc[c] += w * F.f[c][row + p];
     }
     for (int c = 0; c < NC; ++c) out[i * NC + c] = acc[c];
+  }
+}
+
+// pairwise products of the squared curvatures (GridProjectedKDE.F90:2466-2468)
+__global__ void products_kernel(const double *cx, const double *cy, const double *cz, double *cxy, double *cxz,
+                                double *cyz, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double a = cx[i], b = cy[i], c = cz[i];
+    cxy[i] = a * b;
+    cxz[i] = a * c;
+    cyz[i] = b * c;
   }
 }
 
@@ -635,7 +655,8 @@ __global__ void init_bins_kernel(KdeParams P, KdeBins B, double hs) {
 // second-half of the sigma-support update (GridProjectedKDE.F90:4836-4860)
 __device__ void support_update(const KdeParams &P, const KdeBins &B, int b, double ne1) {
   const double dn = B.dens[b];
-  double ssc = pow(ne1, 0.5) * pow(B.scale[b], P.one_plus_nd_q) / pow(4.0 * dn, 0.25) * P.support_c;
+  // nEstimate**0.5: the correctly rounded square root (as the C library's pow)
+  double ssc = sqrt(ne1) * pow(B.scale[b], P.one_plus_nd_q) / pow(4.0 * dn, 0.25) * P.support_c;
   if (ssc > P.max_sigma_growth * B.support[b]) ssc = P.max_sigma_growth * B.support[b];
   ssc = fmin(ssc, P.max_k[P.max_dim]);
   if (ssc < P.min_k[P.min_dim]) ssc = P.min_k[P.min_dim];
@@ -701,7 +722,8 @@ __device__ __forceinline__ double warp_red(int op, double v) {
   return v;
 }
 
-__global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBins B, int what, double npts,
+// npts2: nPoints**fTWO, which Fortran evaluates as the product nPoints*nPoints
+__global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBins B, int what, double npts2,
                                                               const double *S, double *partial) {
   __shared__ double red[kThreads / 32][4];
   int op[4];
@@ -736,8 +758,7 @@ __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBi
         if (sc > 0.0) a[2] = fmin(a[2], -sc);
       }
       if (sc != 0.0) {
-        const double e = (B.nest[b] / (pow(sc, nd) * pow(4.0 * PI_D, 0.5 * nd)) + 0.25 * B.net[b] * pow(sc, 4.0)) /
-                         pow(npts, 2.0);
+        const double e = (B.nest[b] / (pow(sc, nd) * P.four_pi_half_nd) + 0.25 * B.net[b] * pow(sc, 4.0)) / npts2;
         a[3] += e * e;
       }
     }
@@ -801,7 +822,7 @@ __global__ void optimal_phase0_kernel(KdeParams P, KdeBins B, const double *S) {
     B.net[b] = net;
   }
   double sc = 0.0;
-  if (net > 0.0) sc = pow(nd * B.nest[b] / (pow(4.0 * PI_D, 0.5 * nd) * net), P.one_over_nd4);
+  if (net > 0.0) sc = pow(nd * B.nest[b] / (P.four_pi_half_nd * net), P.one_over_nd4);
   B.scale[b] = sc;
 }
 
@@ -937,7 +958,7 @@ cudaError_t KdeState::ensure_bins(int n) {
   }
   void *old[] = {bins.gx, bins.gy, bins.gz, bins.count, bins.ks, bins.scale, bins.shape, bins.support, bins.nest,
                  bins.dens, bins.cb, bins.rxx, bins.ryy, bins.rzz, bins.net, bins.dens_old, bins.scale_old, tmp,
-                 partial, bin_key};
+                 partial, bin_key, wlev};
   for (void *p : old)
     if (p) cudaFree(p);
   const size_t c = (size_t)n;
@@ -948,7 +969,7 @@ cudaError_t KdeState::ensure_bins(int n) {
   auto D = [&](double **p, size_t k) {
     if (e == cudaSuccess) e = cudaMalloc((void **)p, sizeof(double) * k);
   };
-  I(&bins.gx, c); I(&bins.gy, c); I(&bins.gz, c); I(&bin_key, 4 * c);
+  I(&bins.gx, c); I(&bins.gy, c); I(&bins.gz, c); I(&bin_key, 4 * c); I(&wlev, 3 * c);
   D(&bins.count, c); D(&bins.ks, 3 * c); D(&bins.scale, c); D(&bins.shape, 3 * c); D(&bins.support, c);
   D(&bins.nest, c); D(&bins.dens, c); D(&bins.cb, 3 * c); D(&bins.rxx, c); D(&bins.ryy, c); D(&bins.rzz, c);
   D(&bins.net, c); D(&bins.dens_old, c); D(&bins.scale_old, c); D(&tmp, c);
@@ -972,7 +993,7 @@ cudaError_t KdeState::ensure_grid(int64_t ngrid) {
     if (e != cudaSuccess) return e;
   }
   if (ngrid <= grid_cap) return cudaSuccess;
-  double *old[] = {dens_grid, dens_raw, cx, cy, cz};
+  double *old[] = {dens_grid, dens_raw, cx, cy, cz, cxy, cxz, cyz};
   for (double *p : old)
     if (p) cudaFree(p);
   if (d_blockcnt) cudaFree(d_blockcnt);
@@ -980,6 +1001,8 @@ cudaError_t KdeState::ensure_grid(int64_t ngrid) {
   cudaError_t e = cudaMalloc((void **)&dens_grid, sizeof(double) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&cell_bin, sizeof(int) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&dens_raw, sizeof(double) * ngrid);
+  for (double **p : {&cxy, &cxz, &cyz})
+    if (e == cudaSuccess) e = cudaMalloc((void **)p, sizeof(double) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&cx, sizeof(double) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&cy, sizeof(double) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&cz, sizeof(double) * ngrid);
@@ -1015,7 +1038,7 @@ void KdeState::release() {
   void *ptrs[] = {bins.gx, bins.gy, bins.gz, bins.count, bins.ks, bins.scale, bins.shape, bins.support, bins.nest,
                   bins.dens, bins.cb, bins.rxx, bins.ryy, bins.rzz, bins.net, bins.dens_old, bins.scale_old, tmp,
                   partial, dens_grid, cx, cy, cz, d_scalars, d_flag, d_blockcnt, d_val, d_meta, cell_bin, bin_key,
-                  d_keys, d_plan, t1, t2, dens_raw, d_need};
+                  d_keys, d_plan, t1, t2, dens_raw, d_need, wlev, cxy, cxz, cyz};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_scalars) cudaFreeHost(h_scalars);
@@ -1142,9 +1165,11 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   while (std::gcd(wstride, nb) != 1) ++wstride;
   auto density = [&](void) -> cudaError_t {
     KCK(cudaMemsetAsync(st.dens_raw, 0, sizeof(double) * ngrid, s));
-    wscatter_kernel<<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, st.wtab, wstride, st.dens_raw);
+    wlevel_kernel<<<bb, kBinThreads, 0, s>>>(P, B, st.wlev);
+    wscatter_kernel<<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, st.wtab, wstride, st.wlev,
+                                                                          st.dens_raw);
     scale_pick_kernel<<<blocks_for(npick), kThreads, 0, s>>>(P, B, st.dens_raw, st.dens_grid, ngrid);
-    st.launches += 2;
+    st.launches += 3;
     return cudaGetLastError();
   };
   // plans: [0] smoothing kernels (kind 1), [1] second-derivative kernels (kind 2)
@@ -1165,14 +1190,14 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   };
   // sum over every bin's smoothing kernel of `field`, at the bins
   auto gather1 = [&](const double *field, int mode, double *out, double *out2) -> cudaError_t {
-    gather_x_kernel<1><<<pgrid, kThreads, 0, s>>>(P, plan1, field, nullptr, nullptr, st.t1);
+    gather_x_kernel<1><<<pgrid, kThreads, 0, s>>>(P, plan1, Fields{{field}}, st.t1);
     gather_y_kernel<1><<<pgrid, kThreads, 0, s>>>(P, plan1, st.t1, st.t2);
     gather_z_kernel<1><<<bb, kBinThreads, 0, s>>>(P, B, plan1, key1, st.t2, mode, out, out2);
     st.launches += 3;
     return cudaGetLastError();
   };
   auto reduce = [&](int what) -> cudaError_t {
-    bin_reduce_kernel<<<rb, kThreads, 0, s>>>(P, B, what, npts, S, st.partial);
+    bin_reduce_kernel<<<rb, kThreads, 0, s>>>(P, B, what, npts * npts, S, st.partial);
     bin_reduce_final_kernel<<<1, 32, 0, s>>>(what, rb, st.partial, S);
     st.launches += 2;
     return cudaGetLastError();
@@ -1211,7 +1236,10 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     st.launches += 3;
     // net roughness: smoothing-kernel gathers of the squared curvatures
     if (P.ndim == 3) {
-      gather_x_kernel<6><<<pgrid, kThreads, 0, s>>>(P, plan1, st.cx, st.cy, st.cz, st.t1);
+      products_kernel<<<gb, kThreads, 0, s>>>(st.cx, st.cy, st.cz, st.cxy, st.cxz, st.cyz, ngrid);
+      gather_x_kernel<6><<<pgrid, kThreads, 0, s>>>(P, plan1, Fields{{st.cx, st.cy, st.cz, st.cxy, st.cxz, st.cyz}},
+                                                    st.t1);
+      st.launches += 1;
       gather_y_kernel<6><<<pgrid, kThreads, 0, s>>>(P, plan1, st.t1, st.t2);
       gather_z_kernel<6><<<bb, kBinThreads, 0, s>>>(P, B, plan1, key1, st.t2, GZ_OUT, nullptr, nullptr);
       st.launches += 3;

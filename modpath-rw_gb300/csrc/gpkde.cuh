@@ -23,6 +23,7 @@ struct KdeParams {
   double max_k[3], min_k[3], max_sd[3], min_sd[3];
   int max_dim, min_dim;
   double support_c, alpha_c, beta_c, one_over_nd4, minus_one_over_nd6, one_plus_nd_q;
+  double four_pi_half_nd;  // (4 pi)**(0.5 nDim)
   double max_sigma_growth, iso_threshold;
 };
 
@@ -75,11 +76,13 @@ struct KdeState {
   KdeBins bins{};
   int cap = 0;
   double *dens_grid = nullptr, *dens_raw = nullptr, *cx = nullptr, *cy = nullptr, *cz = nullptr;
+  double *cxy = nullptr, *cxz = nullptr, *cyz = nullptr;  // products of the squared curvatures
   int64_t grid_cap = 0;
   double *tmp = nullptr, *partial = nullptr, *d_scalars = nullptr, *h_scalars = nullptr;
   int *d_flag = nullptr, *h_flag = nullptr, *d_blockcnt = nullptr;
   int *cell_bin = nullptr;          // per grid cell: active bin index or -1
   int *bin_key = nullptr;           // per bin: smoothing key (n) and SD keys per axis (3n)
+  int *wlev = nullptr;              // per bin: W kernel database level per dimension (3n)
   KeyAcc *d_keys = nullptr;
   SepPlan *d_plan = nullptr;
   double *t1 = nullptr, *t2 = nullptr;
