@@ -73,7 +73,7 @@ typedef struct {
 typedef struct {
   int32_t time_step_kind;     /* 1 ADV, 2 DISP, 3 MIN_ADV_DISP, 4 FIXED      */
   double ts_param[2];         /* timeStepParameters(1:2)                     */
-  int32_t advection_kind;     /* 2 EULERIAN (1 EXPONENTIAL: not supported)   */
+  int32_t advection_kind;     /* 1 EXPONENTIAL (Newton exit time), 2 EULERIAN */
   int32_t dim_mask[3];        /* random-walk dimension mask                  */
   int32_t dispersion_model;   /* 0 linear isotropic                          */
   int32_t stop_weak_sinks;

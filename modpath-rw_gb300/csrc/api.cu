@@ -181,7 +181,8 @@ int mprw_create(mprw_handle **out, const mprw_grid_desc *gd, const mprw_options 
   if (ncell >= (int64_t)1 << 31) return MPRW_E_INVAL;
   mprw_handle *h = new mprw_handle();
   *out = h;
-  if (o->advection_kind != 2) return fail(h, MPRW_E_INVAL, "advection_kind: only EULERIAN (2) is supported");
+  if (o->advection_kind != 1 && o->advection_kind != 2)
+    return fail(h, MPRW_E_INVAL, "advection_kind: 1 (EXPONENTIAL) or 2 (EULERIAN)");
   if (o->dispersion_model != 0) return fail(h, MPRW_E_INVAL, "dispersion_model: only linear isotropic (0)");
   if (o->time_step_kind < 1 || o->time_step_kind > 4) return fail(h, MPRW_E_INVAL, "time_step_kind");
   if (o->precision != MPRW_FP64 && o->precision != MPRW_MIXED) return fail(h, MPRW_E_INVAL, "precision");
@@ -440,6 +441,7 @@ int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_do
     a.d1 = h->d1;
     a.d2 = h->d2;
     a.seed = h->opt.rng_seed;
+    a.exp_adv = h->opt.advection_kind == 1;
     int blocks = h->sms * 2;
     int64_t need = (h->n + threads - 1) / threads;
     if (need < blocks) blocks = (int)need;
@@ -467,6 +469,7 @@ int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_do
     a.d1 = h->d1;
     a.d2 = h->d2;
     a.seed = h->opt.rng_seed;
+    a.exp_adv = h->opt.advection_kind == 1;
     int blocks = h->sms * 1;
     int64_t need = (h->n + threads - 1) / threads;
     if (need < blocks) blocks = (int)need;

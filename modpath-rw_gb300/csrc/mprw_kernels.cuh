@@ -24,6 +24,7 @@ struct AdvanceArgs {
   double t_begin, t_end;
   int ndim, d1, d2;
   uint64_t seed;
+  int exp_adv;  // EXPONENTIAL advection with the Newton exit time (else EULERIAN)
 };
 
 template <typename R>

@@ -233,6 +233,199 @@ __device__ __forceinline__ bool quad_axis(R npos, R pos, R d, R v, R divD, R dB,
   return false;
 }
 
+// ---- EXPONENTIAL advection (TrackSubCell.F90:1487-1538) and its exit time by
+// Newton-Raphson (:1895-2554).  Both run in FP64 whatever the particle
+// precision: the displacement v (e^{dv dt} - 1)/dv and the exit-time solve
+// lose their digits to cancellation at small velocity gradients.
+__device__ __forceinline__ double adv_exponential(double v, double dvdx, double dt) {
+  const double dvtol = 1.0e-10;
+  return (fabs(dvdx) > dvtol) ? v * (exp(dvdx * dt) - 1.0) / dvdx : v * dt;
+}
+
+// pr_NewtonRaphsonVariablesExponentialAdvection (:2082-2120)
+__device__ void nr_vars(double dt, double v, double dvdx, double dI, double divD, double dB, double &f0, double &f1,
+                        double &f2, double &f3) {
+  if (dt == 0.0) return;
+  f0 = adv_exponential(v, dvdx, dt) + divD * dt + dB * sqrt(dt) - dI;
+  const double e = exp(dvdx * dt);
+  f1 = v * e + divD + 0.5 * dB / sqrt(dt);
+  f2 = dvdx * v * e - 0.25 * dB * pow(dt, -1.5);
+  f3 = dvdx * dvdx * v * e + 0.375 * dB * pow(dt, -2.5);
+}
+__device__ __forceinline__ double nr_conv_g(double f0, double f1, double f2) { return fabs(f2 * f0 / (f1 * f1)); }
+__device__ __forceinline__ double nr_conv_gder(double f0, double f1, double f2, double f3) {
+  const double gna = f2 * f0 / (f1 * f1);
+  const double gpp = -2.0 * (f0 * (f2 * f2)) / (f1 * f1 * f1) + (f1 * f2 + f0 * f3) / (f1 * f1);
+  return gna / fabs(gna) * gpp;
+}
+__device__ __forceinline__ double nr_p10(int e) {  // 10d0**e, exact for |e| <= 22
+  double r = 1.0;
+  for (int i = 0; i < (e < 0 ? -e : e); ++i) r *= 10.0;
+  return e < 0 ? 1.0 / r : r;
+}
+
+// pr_SetInitialGuess (:2162-2448); every loop is bounded (7, 50 and 8 passes)
+__device__ double nr_initial_guess(double dt, double v, double dvdx, double dI, double divD, double dB) {
+  const double gdtol = (double)1e-6f;
+  const int maxter = 50;
+  double f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+  double dtnew = 0.0, dtold, dt0, gprimdernew, gprimnew, gprimder, gprim, gprimmin, gamman;
+  double dtfraction = 0, dtoldfraction, mindtfrac = 0;
+  int counter, ccount, bcount, zcount, rcount, gcount;
+  if (dt == 0.0) return dtnew;
+  gprimmin = (double)1e10f;
+  gprim = (double)1e10f;
+  gcount = 0;
+  while ((gprim > 1) && (gcount < 7)) {
+    gcount = gcount + 1;
+    dtfraction = nr_p10(-8 + gcount);
+    dt0 = dt * dtfraction;
+    nr_vars(dt0, v, dvdx, dI, divD, dB, f0, f1, f2, f3);
+    gprim = nr_conv_g(f0, f1, f2);
+    if (gprim < gprimmin) {
+      gprimmin = gprim;
+      mindtfrac = dtfraction;
+    }
+  }
+  if ((gprim < 1) && (gcount == 1)) dtoldfraction = 1e-8;
+  else if (gprim < 1) dtoldfraction = nr_p10(-8 + gcount - 1);
+  else {
+    dtfraction = mindtfrac;
+    dtoldfraction = 0.5 * dtfraction / 10.0;
+  }
+  dtnew = dtfraction * dt;
+  dtold = dtoldfraction * dt;
+  nr_vars(dtnew, v, dvdx, dI, divD, dB, f0, f1, f2, f3);
+  gprim = nr_conv_g(f0, f1, f2);
+  if (gprim < 0.5) return dtnew;
+  gprimnew = 10.0;
+  gprim = 10.0;
+  ccount = bcount = zcount = rcount = counter = 0;
+  while (counter < maxter) {
+    counter = counter + 1;
+    nr_vars(dtold, v, dvdx, dI, divD, dB, f0, f1, f2, f3);
+    gprimder = nr_conv_gder(f0, f1, f2, f3);
+    nr_vars(dtnew, v, dvdx, dI, divD, dB, f0, f1, f2, f3);
+    gprimdernew = nr_conv_gder(f0, f1, f2, f3);
+    gprim = nr_conv_g(f0, f1, f2);
+    if ((gprimdernew - gprimder) > 0.0)
+      gamman = fabs((dtnew - dtold) * (gprimdernew - gprimder)) /
+               ((gprimdernew - gprimder) * (gprimdernew - gprimder));
+    else
+      gamman = 0.0;
+    dtold = dtnew;
+    dtnew = dtnew - gamman * gprimdernew;
+    if (isnan(dtnew)) {
+      dtnew = 0.0;
+      break;
+    }
+    if ((gprim < 1) && (dtnew / dt > 1)) {
+      dtnew = dtold;
+      return dtnew;
+    } else if (dtnew / dt > 1) {
+      dtnew = (double)0.99f * dt;
+    }
+    if ((gprim < 1) && (dtnew < 0) && (dtold > 0)) {
+      dtnew = dtold;
+      return dtnew;
+    } else if (dtnew < 0) {
+      dtnew = (double)1e-8f * dt;
+      zcount = zcount + 1;
+      if (zcount > 1) {
+        dtnew = 0.0;
+        break;
+      }
+    }
+    nr_vars(dtnew, v, dvdx, dI, divD, dB, f0, f1, f2, f3);
+    gprimnew = nr_conv_g(f0, f1, f2);
+    if ((gprimnew < 1) && (dtnew > 0) && (dtnew / dt < 1)) {
+      rcount = rcount + 1;
+      if (rcount > 1) return dtnew;
+    } else {
+      rcount = 0;
+    }
+    if ((gprim < 1) && (gprimnew > gprim)) {
+      dtnew = dtold;
+      return dtnew;
+    }
+    if ((fabs((dtold - dtnew) / dtold) < gdtol) && (gprim < 1)) {
+      ccount = ccount + 1;
+      if (ccount > 1) return dtnew;
+    } else {
+      ccount = 0;
+    }
+    if ((fabs((dtold - dtnew) / dtold) < gdtol) && (gprim > 1)) {
+      bcount = bcount + 1;
+      if (bcount > 1) break;
+    } else {
+      bcount = 0;
+    }
+  }
+  if (gprim < 1) return dtnew;
+  gprim = (double)1e10f;
+  gprimmin = (double)1e10f;
+  mindtfrac = 0.0;
+  gcount = 1;
+  while ((gprim > 1) && (gcount < 9)) {
+    gcount = gcount + 1;
+    dtfraction = (double)(0.1f * (float)gcount);
+    dt0 = dt * dtfraction;
+    nr_vars(dt0, v, dvdx, dI, divD, dB, f0, f1, f2, f3);
+    gprim = nr_conv_g(f0, f1, f2);
+    if (gprim < gprimmin) {
+      gprimmin = gprim;
+      mindtfrac = dtfraction;
+    }
+  }
+  if (gprimmin < 1) dtnew = dt * mindtfrac;
+  if ((dtnew <= 0.0) && (fabs(v) > 0.0)) dtnew = fabs(dI / v);
+  return dtnew;
+}
+
+// NewtonRaphsonTimeStepExponentialAdvection (:2451-2554), at most 50 iterations
+__device__ double nr_time_step(double dt, double v, double dvdx, double dI, double divD, double dB) {
+  const double nrtol = (double)1e-6f;
+  const int maxIter = 50;
+  double nrerror = 1e6;
+  double dt0 = nr_initial_guess(dt, v, dvdx, dI, divD, dB);
+  if (dt0 == 0.0) return 0.0;
+  int countIter = 0;
+  while ((fabs(nrerror / dt0) > nrtol) && (countIter < maxIter)) {
+    countIter = countIter + 1;
+    const double f0 = adv_exponential(v, dvdx, dt0) + divD * dt0 + dB * sqrt(dt0) - dI;
+    const double f1 = v * exp(dvdx * dt0) + divD + 0.5 * dB / sqrt(dt0);
+    nrerror = -f0 / f1;
+    dt0 = dt0 + nrerror;
+    if (dt0 < 0.0) dt0 = -(double)0.9f * dt0;
+  }
+  if (dt0 > dt) return dt;
+  if ((countIter == maxIter) && (fabs(nrerror / dt0) > nrtol)) return 0.0;
+  return dt0;
+}
+
+// One axis of pr_DetectExitFaceAndUpdateTimeStepNewton (:1895-2079).
+// Returns true when the routine must return at once (exitFace, dt set).
+__device__ bool newton_axis(double npos, double pos, double d, double v, double dvdx, double divD, double dB,
+                            int faceLo, int faceHi, double dt, double &dtaxis, int &exitAxis, int &exitFace,
+                            double &dtout) {
+  double dI;
+  if (npos > 1.0) {
+    dI = d * (1.0 - pos);
+    exitAxis = faceHi;
+  } else {
+    dI = -d * pos;
+    exitAxis = faceLo;
+  }
+  if (dI == 0.0) {
+    exitFace = exitAxis;
+    dtout = 0.0;
+    return true;
+  }
+  dtaxis = nr_time_step(dt, v, dvdx, dI, divD, dB);
+  if (dtaxis > dt) dtaxis = 0.0;
+  return false;
+}
+
 template <typename R>
 struct Visit {
   R x, y, z;     // current local position (TrackSubCell x,y,z)
@@ -252,7 +445,7 @@ enum : int { PASS_CONTINUE = 0, PASS_MAXTIME = 1, PASS_EXIT = 2, PASS_UNDEFINED 
 // One pass of the `do while (continueTimeLoop)` body, TrackSubCell.F90:956-1368.
 // On PASS_MAXTIME / PASS_EXIT the final location is (ox,oy,oz,V.t); on
 // PASS_UNDEFINED the caller uses the last recorded point.
-template <typename R>
+template <typename R, bool EXP>
 __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double maxTime, int ndim, int d1, int d2,
                        uint64_t seed, uint64_t id, uint64_t &ctr, R &ox, R &oy, R &oz) {
   const R zero = R(0), one = R(1), half = R(0.5);
@@ -281,7 +474,27 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
   R ddz = divc(F, F_DIV + 14, x, y, z, xy, xz, yz);
   R bx, by, bz;
   random_displacement(F, ndim, d1, d2, x, y, z, seed, id, ctr, bx, by, bz);
-  R ax = vx * rdt, ay = vy * rdt, az = vz * rdt;
+  // advection displacement: EULERIAN v dt, EXPONENTIAL (FP64) v (e^{dv dt}-1)/dv
+  // with dv = (V2 - V1)/D of the cell (pr_AdvectionDisplacement*, :1487-1573)
+  double dvx = 0.0, dvy = 0.0, dvz = 0.0;
+  if constexpr (EXP) {
+    dvx = (double)F(F_DV + 0) / (double)dX;
+    dvy = (double)F(F_DV + 1) / (double)dY;
+    dvz = (double)F(F_DV + 2) / (double)dZ;
+  }
+  R ax, ay, az;
+  auto advect = [&]() {
+    if constexpr (EXP) {
+      ax = (R)adv_exponential((double)vx, dvx, dt);
+      ay = (R)adv_exponential((double)vy, dvy, dt);
+      az = (R)adv_exponential((double)vz, dvz, dt);
+    } else {
+      ax = vx * rdt;
+      ay = vy * rdt;
+      az = vz * rdt;
+    }
+  };
+  advect();
   R dxrw = ax + ddx * rdt + bx * sdt;
   R dyrw = ay + ddy * rdt + by * sdt;
   R dzrw = az + ddz * rdt + bz * sdt;
@@ -291,7 +504,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
     dt = dtRed * dt;
     rdt = (R)dt;
     sdt = sqrt(rdt);
-    ax = vx * rdt; ay = vy * rdt; az = vz * rdt;
+    advect();
     dxrw = ax + ddx * rdt + bx * sdt;
     dyrw = ay + ddy * rdt + by * sdt;
     dzrw = az + ddz * rdt + bz * sdt;
@@ -303,8 +516,34 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
   int intLoop = 0;
   while (MPRW_OUTSIDE(nx, ny, nz)) {
     ++intLoop;
-    R dtx = zero, dty = zero, dtz = zero;
-    {
+    if constexpr (EXP) {
+      // ExitFaceAndUpdateTimeStep (Newton, :1895-2079), FP64
+      double dtx = 0.0, dty = 0.0, dtz = 0.0;
+      int efx = 0, efy = 0, efz = 0;
+      bool ret = false;
+      V.t = V.t - dt;
+      if (!ret && ((nx > one) || (nx < zero)))
+        ret = newton_axis(nx, x, dX, vx, dvx, ddx, bx, 1, 2, dt, dtx, efx, V.exitFace, dt);
+      if (!ret && ((ny > one) || (ny < zero)))
+        ret = newton_axis(ny, y, dY, vy, dvy, ddy, by, 3, 4, dt, dty, efy, V.exitFace, dt);
+      if (!ret && ((nz > one) || (nz < zero)))
+        ret = newton_axis(nz, z, dZ, vz, dvz, ddz, bz, 5, 6, dt, dtz, efz, V.exitFace, dt);
+      if (!ret) {
+        if (dtx == 0.0 && dty == 0.0 && dtz == 0.0) {
+          V.t = V.t + dt;
+        } else {
+          int im = -1;
+          double best = 0.0;
+          if (dtx > 0.0) { im = 0; best = dtx; }
+          if (dty > 0.0 && (im < 0 || dty < best)) { im = 1; best = dty; }
+          if (dtz > 0.0 && (im < 0 || dtz < best)) { im = 2; best = dtz; }
+          dt = best;
+          V.exitFace = (im == 0) ? efx : (im == 1 ? efy : efz);
+          V.t = V.t + dt;
+        }
+      }
+    } else {
+      R dtx = zero, dty = zero, dtz = zero;
       // ExitFaceAndUpdateTimeStep (quadratic, :1576-1892)
       int efx = 0, efy = 0, efz = 0;
       bool ret = false;
@@ -342,7 +581,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
     }
     rdt = (R)dt;
     sdt = sqrt(rdt);
-    ax = vx * rdt; ay = vy * rdt; az = vz * rdt;
+    advect();
     V.reachedMax = false;
     int ef = V.exitFace;
     if (ef == 1 || ef == 2) {
@@ -399,7 +638,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
         V.reachedMax = true;
         rdt = (R)dt;
         sdt = sqrt(rdt);
-        ax = vx * rdt; ay = vy * rdt; az = vz * rdt;
+        advect();
         dxrw = ax + ddx * rdt + bx * sdt;
         dyrw = ay + ddy * rdt + by * sdt;
         dzrw = az + ddz * rdt + bz * sdt;
@@ -449,7 +688,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
 // structured and the loop head re-converges the warp, so the common pass body
 // runs with every tracking lane active; the loop ends when no lane of the warp
 // has work.
-template <typename R>
+template <typename R, bool EXP>
 __global__ void __launch_bounds__(kStepThreads) rwpt_advance_kernel(AdvanceArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw) + threadIdx.x;
@@ -577,7 +816,7 @@ __global__ void __launch_bounds__(kStepThreads) rwpt_advance_kernel(AdvanceArgs<
       if (++V.passes > kMaxStepsPerVisit) {
         r = PASS_UNDEFINED;
       } else {
-        r = rw_pass(V, F, massb, a.t_end, a.ndim, a.d1, a.d2, a.seed, id, ctr, ox, oy, oz);
+        r = rw_pass<R, EXP>(V, F, massb, a.t_end, a.ndim, a.d1, a.d2, a.seed, id, ctr, ox, oy, oz);
         ++my_passes;
       }
       if (r == PASS_MAXTIME) {
@@ -634,10 +873,10 @@ size_t advance_smem_bytes(int threads) {
 template <typename R>
 cudaError_t launch_advance(const AdvanceArgs<R> &a, int blocks, int threads, cudaStream_t s) {
   size_t smem = advance_smem_bytes<R>(threads);
-  cudaError_t e = cudaFuncSetAttribute(rwpt_advance_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+  auto kern = a.exp_adv ? rwpt_advance_kernel<R, true> : rwpt_advance_kernel<R, false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  rwpt_advance_kernel<R><<<blocks, threads, smem, s>>>(a);
+  kern<<<blocks, threads, smem, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -79,6 +79,47 @@ def uniform_flow(ncol=200, nrow=1, nlay=1, q=0.3, porosity=0.3, dx=1.0, dy=1.0, 
     return g, flow
 
 
+def graded_flow(ncol=40, q0=0.3, ratio=1.05, porosity=0.3):
+    """1-D column whose face flux grows geometrically, Q_i = q0 * ratio**i through
+    the left face of cell i (0-based), balanced by a source in every cell: the
+    velocity is linear inside each cell with v2 = ratio * v1, the field in which
+    exponential advection is exact.  No dispersion."""
+    g, f = uniform_flow(ncol=ncol, q=q0, porosity=porosity, alpha_l=0.0, alpha_t=0.0, dm=0.0)
+    n = g.ncell
+    Q = q0 * ratio ** np.arange(n + 1)
+    rows = np.repeat(np.arange(n), np.diff(f.ia))
+    m = f.ja - 1
+    flowja = np.zeros(f.ja.shape[0])
+    flowja[m == rows - 1] = Q[rows[m == rows - 1]]           # in through the left face
+    flowja[m == rows + 1] = -Q[rows[m == rows + 1] + 1]      # out through the right face
+    f.flowja = flowja
+    bflow = np.zeros(6 * n)
+    bflow[0] = Q[0]
+    bflow[6 * (n - 1) + 1] = -Q[n]
+    f.boundary_flows = bflow
+    f.source_flow = Q[1:] - Q[:-1]
+    return g, f, Q
+
+
+def graded_flow_exact(x0, t, Q, porosity=0.3, dx=1.0):
+    """Exact position at time t of a particle starting at x0 (m) in graded_flow:
+    within a cell v(p) = v1 + g p, p(t) = (v(p0)/g)(e^{g t} - 1) + p0, and the
+    travel time to the right face is ln(v2/v(p0))/g."""
+    x, rem = float(x0), float(t)
+    n = Q.shape[0] - 1
+    while True:
+        i = min(int(np.floor(x / dx)), n - 1)
+        p0 = x - i * dx
+        v1, v2 = Q[i] / (porosity * dx * dx), Q[i + 1] / (porosity * dx * dx)
+        gr = (v2 - v1) / dx
+        vp = v1 + gr * p0
+        tau = np.log(v2 / vp) / gr
+        if tau >= rem or i == n - 1:
+            return i * dx + p0 + (vp / gr) * np.expm1(gr * rem)
+        rem -= tau
+        x = (i + 1) * dx
+
+
 def lognormal_field(nlay, nrow, ncol, sigma2=1.0, kg=10.0, lh=10.0, lv=2.0, d=1.0, seed=0) -> np.ndarray:
     """ln K ~ N(ln kg, sigma2), exponential covariance; shape (nlay, nrow, ncol)."""
     rng = np.random.default_rng(seed)

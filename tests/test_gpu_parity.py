@@ -178,3 +178,52 @@ def test_mixed_precision_moments(gpu_lib):
         assert abs(m2 - m1) / abs(m1) < 0.005
         assert abs(v2 - v1) / v1 < 0.005 + 3 * np.sqrt(2.0 / p.n)
     assert (gm["status"] == ACTIVE).all()
+
+
+def _graded_particles(n, seed=11):
+    rng = np.random.default_rng(seed)
+    return Particles(cell=(1 + rng.integers(0, 5, n)).astype(np.int32), lx=rng.uniform(0, 1, n),
+                     ly=rng.uniform(0, 1, n), lz=rng.uniform(0, 1, n), t=np.zeros(n),
+                     status=np.full(n, ACTIVE, np.int32), mass=np.ones(n), id=np.arange(n, dtype=np.uint64),
+                     rng_ctr=np.zeros(n, np.uint64))
+
+
+def test_exponential_advection_graded_field(gpu_lib):
+    """EXPONENTIAL advection + Newton exit time on the GPU: the exact path of a
+    cell-wise linear field, and the oracle's trajectories to 1e-9."""
+    from mprw.model import EXPONENTIAL, Options
+    g, f, Q = W.graded_flow(ncol=40, q0=0.3, ratio=1.05)
+    p = _graded_particles(500)
+    opt = Options(time_step_kind=1, ts_param=(0.1, 0.1), advection_kind=EXPONENTIAL, precision=FP64)
+    iv = [(0.0, 6.0), (6.0, 15.0)]
+    gp, gs = run_gpu(g, f, opt, p, iv)
+    op, os_ = run_oracle(g, f, opt, p, iv)
+    assert gs == os_
+    np.testing.assert_array_equal(gp["cell"], op.cell)
+    np.testing.assert_array_equal(gp["status"], op.status)
+    np.testing.assert_allclose(gp["lx"], op.lx, rtol=0, atol=1e-9)
+    # particles whose exact path stays inside the column follow the closed
+    # form; the others reach the outlet face, which reflects (no IMP file:
+    # every domain face is a mass boundary) and hold them just inside it
+    x0 = (p.cell - 1) + p.lx
+    exact = np.array([W.graded_flow_exact(a, 15.0, Q) for a in x0])
+    act = exact < g.ncol
+    assert act.sum() > 100 and np.all(gp["status"] == ACTIVE)
+    assert np.all(gp["gx"][~act] > g.ncol - 0.1)
+    np.testing.assert_allclose(gp["gx"][act], exact[act], rtol=0, atol=1e-9)
+    # MIXED: FP32 positions, FP64 exponential displacement and exit times
+    opt.precision = MIXED
+    mp, _ = run_gpu(g, f, opt, p, iv)
+    np.testing.assert_array_equal(mp["status"], gp["status"])
+    np.testing.assert_allclose(mp["gx"][act], exact[act], rtol=0, atol=2e-5)
+
+
+def test_exponential_dispersion_heterogeneous(gpu_lib):
+    from mprw.model import EXPONENTIAL
+    g, f, p, opt, info = W.config2(n_particles=3000, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
+    opt.advection_kind = EXPONENTIAL
+    iv = [(0.0, 20.0), (20.0, 60.0)]
+    gp, gs = run_gpu(g, f, opt, p, iv)
+    op, os_ = run_oracle(g, f, opt, p, iv)
+    _compare_same_rng(gp, op, g, f, tol=1e-6, min_frac=0.99)
+    assert abs(gs - os_) <= 1e-3 * os_

@@ -98,3 +98,28 @@ def test_heterogeneous_weak_sink_stops():
     # particles that stopped at the outlet sit in the last column
     col = (q.cell[q.status == WEAK_SINK] - 1) % g.ncol
     assert np.all(col == g.ncol - 1)
+
+
+def test_exponential_advection_exact_in_linear_field():
+    """EXPONENTIAL advection (TrackSubCell.F90:1487-1538) with the Newton exit
+    time (:1895-2554) follows the exact path of a cell-wise linear velocity
+    field; EULERIAN advection does not."""
+    from mprw.model import EULERIAN, EXPONENTIAL, Options
+    g, f, Q = W.graded_flow(ncol=40, q0=0.3, ratio=1.05)
+    n = 5
+    x0 = np.array([0.0, 0.2, 0.45, 0.7, 0.95])
+    p = Particles(cell=np.ones(n, np.int32), lx=x0.copy(), ly=np.full(n, 0.5), lz=np.full(n, 0.5), t=np.zeros(n),
+                  status=np.full(n, ACTIVE, np.int32), mass=np.ones(n), id=np.arange(n, dtype=np.uint64),
+                  rng_ctr=np.zeros(n, np.uint64))
+    exact = np.array([W.graded_flow_exact(a, 15.0, Q) for a in x0])
+    err = {}
+    for kind in (EXPONENTIAL, EULERIAN):
+        opt = Options(time_step_kind=1, ts_param=(0.1, 0.1), advection_kind=kind, dim_mask=(1, 1, 1))
+        q, _ = O.advance(g, f, opt, p, 0.0, 15.0)
+        gx, _, _ = O.global_xyz(g, f, q)
+        assert np.all(q.status == ACTIVE)
+        err[kind] = np.abs(gx - exact).max()
+    # exact up to rounding: Newton's exit times converge far inside their
+    # relative 1e-6 tolerance here (NewtonRaphsonTimeStep..., :2451-2554)
+    assert err[EXPONENTIAL] < 1e-9
+    assert err[EULERIAN] > 1e-2
