@@ -23,8 +23,9 @@ Reported: ``value`` = particle-steps/s of the plain FP64 pipeline with the
 state resident in HBM; ``e2e`` = the same through the C ABI with pinned host
 buffers (particle state host->device, advance, state device->host, GPKDE
 density + histogram device->host, every step); ``mixed`` = the MIXED-precision
-pipeline on the same workload with its plume-moment errors against the FP64
-run; ``roofline`` of the step kernel (the dominant kernel); ``cpu_baseline`` =
+pipeline (FP32 positions and arithmetic, FP64 time; FP32 reconstruction with
+FP64 convergence sums) on the same workload with its plume-moment errors and
+density errors against the FP64 run; ``roofline`` of the step kernel (the dominant kernel); ``cpu_baseline`` =
 the C restatement of the reference's advance (OpenMP, all host threads) on a
 bounded sample -- without the GPKDE reconstruction, whose CPU restatement is
 numpy test code and not representative, so the CPU figure is an upper bound
@@ -183,6 +184,8 @@ def run_gpu_arm(args, rank, world, local):
     stream = torch.cuda.Stream()
 
     def timed_run(precision, steps, warmup):
+        # the MIXED pipeline reconstructs in FP32 too; FP64 is the reference's arithmetic
+        kde_prec = precision
         opt.precision = precision
         tr = mprw.Tracker(g, opt)
         tr.set_stream(stream.cuda_stream)   # launch on a stream the events below can see
@@ -191,7 +194,7 @@ def run_gpu_arm(args, rank, world, local):
         t = 0.0
         for _ in range(warmup):
             tr.advance(t, t + INTERVAL_D)
-            tr.gpkde(domain, bins, origin)
+            tr.gpkde(domain, bins, origin, precision=kde_prec)
             t += INTERVAL_D
         torch.cuda.synchronize()
         ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
@@ -204,7 +207,7 @@ def run_gpu_arm(args, rank, world, local):
             s = tr.advance(t, t + INTERVAL_D)
             tm = tr.timings()
             ev[k][1].record(stream)
-            _, _, nl = tr.gpkde(domain, bins, origin)
+            dens, _, nl = tr.gpkde(domain, bins, origin, precision=kde_prec)
             tk = tr.timings()
             ev[k][2].record(stream)
             torch.cuda.synchronize()
@@ -218,9 +221,15 @@ def run_gpu_arm(args, rank, world, local):
         ms = [a.elapsed_time(c) for a, _, c in ev]
         adv_ms = [a.elapsed_time(b) for a, b, _ in ev]
         out = tr.get_particles()
+        kde_err = None
+        if kde_prec != 0:
+            # the FP32 reconstruction against an FP64 one on the same particles (untimed)
+            d64, _, _ = tr.gpkde(domain, bins, origin)
+            kde_err = {"l2_rel": float(np.linalg.norm(dens - d64) / np.linalg.norm(d64)),
+                       "max_rel": float(np.abs(dens - d64).max() / d64.max())}
         tr.close()
         return dict(ms=ms, adv_ms=adv_ms, kern_ms=kern_ms, kde_ms=kde_ms, wall_ms=wall_ms, steps=steps_done,
-                    launches=launches, out=out, t_end=t, loops=loops)
+                    launches=launches, out=out, t_end=t, loops=loops, dens=dens, kde_err=kde_err)
 
     with ClockSampler(local) as clk:
         fp64 = timed_run(MIXED if args.precision == "mixed" else 0, args.steps, args.warmup)
@@ -381,7 +390,8 @@ def main():
                                           "speedup_vs_fp64": (mx["steps"] / adv32) / (fp["steps"] / adv64)},
                          "moment_error_vs_fp64": err, "active_fp64": n64,
                          "active_mixed": n32, "kernel_ms": float(np.mean(mx["kern_ms"])),
-                         "gpkde_ms": float(np.mean(mx["kde_ms"]))}
+                         "gpkde_ms": float(np.mean(mx["kde_ms"])), "gpkde_precision": "fp32",
+                         "gpkde_fp32_vs_fp64_same_particles": mx["kde_err"]}
     if not args.no_cpu:
         g, f, p, opt = res["geom"]
         line["cpu_baseline"] = cpu_baseline(g, f, p, opt, args.cpu_sample, args.warmup, min(args.steps, 5))

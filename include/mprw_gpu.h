@@ -166,6 +166,9 @@ typedef struct {
   int32_t skip_error_convergence;
   int32_t unit_volume;         /* ComputeDensity(unitVolume=.true.)            */
   double scaling_factor;       /* gpkdeScalingFactor, e.g. 1/binVolume         */
+  int32_t precision;           /* MPRW_FP64 (the reference's arithmetic) or    */
+                               /* MPRW_MIXED (FP32 smoothing passes and        */
+                               /* per-bin updates, FP64 convergence sums)      */
 } mprw_gpkde_options;
 
 /* GPKDE reconstruction of the ACTIVE particles (weights = particle masses).

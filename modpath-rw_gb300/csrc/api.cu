@@ -665,6 +665,9 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
     return fail(h, MPRW_E_INVAL, "mprw_gpkde: only 1-D and 3-D reconstruction grids are supported");
   if (!(o->min_hover_delta > 0.0) || !(o->max_hover_delta > o->min_hover_delta) || !(o->delta_hover_delta > 0.0))
     return fail(h, MPRW_E_INVAL, "mprw_gpkde: invalid kernel database parameters");
+  if (o->precision != MPRW_FP64 && o->precision != MPRW_MIXED)
+    return fail(h, MPRW_E_INVAL, "mprw_gpkde: precision");
+  const int fp32 = o->precision == MPRW_MIXED;
   if (n_bins_out)
     for (int d = 0; d < 3; ++d) n_bins_out[d] = nb[d];
   double binvol = 1.0;
@@ -798,7 +801,12 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
         meta.insert(meta.end(), sm[a].begin(), sm[a].end());
         meta.insert(meta.end(), sofs[a].begin(), sofs[a].end());
       }
+      std::vector<float> valf(val.begin(), val.end());
+      if (h->kde.d_valf) cudaFree(h->kde.d_valf);
+      h->kde.d_valf = nullptr;
+      CK(cudaMalloc(&h->kde.d_valf, sizeof(float) * valf.size()));
       CK(cudaMemcpyAsync(h->kde.d_val, val.data(), sizeof(double) * val.size(), cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(h->kde.d_valf, valf.data(), sizeof(float) * valf.size(), cudaMemcpyHostToDevice, s));
       CK(cudaMemcpyAsync(h->kde.d_meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, s));
       CK(cudaStreamSynchronize(s));  // the host vectors go out of scope
       h->kde_table_key = key;
@@ -808,7 +816,7 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
     for (int a = 0; a < 3; ++a)
       h->kde.sdtab[a] = KdeTable{h->kde.d_val, h->kde.d_meta + (2 + 2 * a) * L, h->kde.d_meta + (3 + 2 * a) * L};
     cudaError_t e = kde_run(h->kde, P, hs, npts, o->n_opt_loops, o->rel_err_convergence,
-                            o->skip_error_convergence != 0, s, &loops);
+                            o->skip_error_convergence != 0, fp32, s, &loops);
     if (e == cudaErrorInvalidValue) return fail(h, MPRW_E_INVAL, "mprw_gpkde: net roughness is zero everywhere");
     CK(e);
     // effective mass, unit volume, scaling (GridProjectedKDE.F90:4292-4306, 5080-5084)
@@ -816,10 +824,9 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
     double scale = 1.0;
     if (o->unit_volume) scale *= binvol;
     if (o->scaling_factor != 0.0) scale *= o->scaling_factor;
-    mul2_kernel<<<grid1d(ngrid), 256, 0, s>>>(h->kde.dens_grid, ngrid, f, scale);
-    CK(cudaGetLastError());
+    CK(kde_output(h->kde, P, fp32, f, scale, s));
   } else {
-    CK(cudaMemsetAsync(h->kde.dens_grid, 0, sizeof(double) * ngrid, s));
+    CK(cudaMemsetAsync(h->kde.dens_out, 0, sizeof(double) * ngrid, s));
   }
   // outputs through pinned staging (density, then histogram)
   const int64_t nout = histogram ? 2 * ngrid : ngrid;
@@ -831,7 +838,7 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
     CK(cudaMallocHost(&h->h_kout, sizeof(double) * nout));
     h->h_kout_cap = nout;
   }
-  CK(cudaMemcpyAsync(h->h_kout, h->kde.dens_grid, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(h->h_kout, h->kde.dens_out, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
   if (histogram) {
     mul2_kernel<<<grid1d(ngrid), 256, 0, s>>>(h->d_counts, ngrid, eff, 1.0);
     CK(cudaGetLastError());

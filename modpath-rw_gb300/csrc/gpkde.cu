@@ -10,19 +10,24 @@
 // factors (erf differences for W and the smoothing kernel, the Gaussian
 // derivative term for the second-derivative kernels,
 // KernelMultiGaussian.f90:720-1110), and the reflection at the grid edges
-// (209-390) folds each dimension independently.  So the database is a small
-// table of 1-D factors per dimension and h/delta index, each active bin is one
-// thread block that folds its three factors in shared memory and then
-//   * scatters count * fx fy fz into a grid (FP64 atomics), or
-//   * gathers grid * fx fy fz (block reduction),
-// and the per-bin smoothing updates are elementwise kernels.  Reductions over
-// bins are two-stage with a fixed order, so runs are repeatable; the host
-// takes the per-loop convergence decision from four scalars.
+// (209-390) folds each dimension independently.  So the database is a table
+// of 1-D factors per dimension and h/delta level:
+//   * the density scatter (anisotropic W kernel per bin) runs one warp per
+//     bin with FP64/FP32 atomics;
+//   * the smoothing-kernel gathers and the second-derivative scatters, whose
+//     kernels come from one scalar per bin, run as three 1-D passes per
+//     database level over the bounding box of that level's bins (no atomics);
+//   * per-bin updates are elementwise kernels; reductions over bins are
+//     two-stage with a fixed order, in FP64.
+// The host takes the per-loop convergence decision from a few scalars; one
+// loop is a captured CUDA graph.  The arithmetic type T is double (the
+// reference's arithmetic) or float (the mixed-precision pipeline).
 #include <cfloat>
 #include <algorithm>
 #include <climits>
 #include <cmath>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "gpkde.cuh"
@@ -35,9 +40,10 @@ constexpr int kThreads = 256;
 constexpr int kBinThreads = 64;   // per-bin elementwise kernels: spread few bins over all SMs
 constexpr int kPassBlocks = 64;   // blocks per key of a separable pass (grid-stride in the key's region)
 
-__device__ __forceinline__ int log_index(const KdeParams &P, double h, int d) {
-  if (h <= 0.0) return 1;
-  int i = (int)floor(log(h / P.bin[d] / P.min_hod) / P.dlog) + 1;
+template <typename T>
+__device__ __forceinline__ int log_index(const KdeParams &P, T h, int d) {
+  if (h <= T(0)) return 1;
+  int i = (int)floor(log(h / T(P.bin[d]) / T(P.min_hod)) / T(P.dlog)) + 1;
   if (i < 1) i = 1;
   if (i > P.ndelta) i = P.ndelta;
   return i;
@@ -47,13 +53,14 @@ __device__ __forceinline__ int log_index(const KdeParams &P, double h, int d) {
 // lanes of a warp splitting each loop: the part below cell 1 is added onto its
 // mirror image and cleared, then the part above cell nb likewise (targets and
 // sources of each step are disjoint).  m, gid and nb are warp-uniform.
-__device__ void fold_factor_warp(double *v, int m, int gid, int nb, int lane) {
+template <typename T>
+__device__ void fold_factor_warp(T *v, int m, int gid, int nb, int lane) {
   const int len = 2 * m + 1;
   if (gid - m < 1) {
     const int b = 1 - gid + m;
     for (int j = lane; j < b; j += 32) v[b + j] = v[b + j] + v[b - 1 - j];
     __syncwarp();
-    for (int j = lane; j < b; j += 32) v[j] = 0.0;
+    for (int j = lane; j < b; j += 32) v[j] = T(0);
     __syncwarp();
   }
   if (gid + m > nb) {
@@ -61,7 +68,7 @@ __device__ void fold_factor_warp(double *v, int m, int gid, int nb, int lane) {
     const int lenb = len - B + 1;
     for (int j = lane; j < lenb; j += 32) v[B - lenb - 1 + j] = v[B - lenb - 1 + j] + v[2 * m - j];
     __syncwarp();
-    for (int j = B - 1 + lane; j < len; j += 32) v[j] = 0.0;
+    for (int j = B - 1 + lane; j < len; j += 32) v[j] = T(0);
     __syncwarp();
   }
 }
@@ -73,24 +80,26 @@ struct Span {
 // ---- density scatter: one warp per bin --------------------------------------
 // The W kernel of a bin is anisotropic (one database level per dimension), so
 // bins share no kernel and each warp folds its bin's three factors in shared
-// memory and adds count * fy fz * fx over the span (FP64 atomics, one
-// multiply per cell with the row products cached).
+// memory and adds count * fy fz * fx over the span (atomics, one multiply per
+// cell with the row products cached).
 constexpr int kWarpsW = 4;
 constexpr int kRowCache = 256;
 
 // database level of every bin's W kernel per dimension (one thread per bin:
 // the logarithm and divisions run on full warps)
-__global__ void wlevel_kernel(KdeParams P, KdeBins B, int *wlev) {
+template <typename T>
+__global__ void wlevel_kernel(KdeParams P, KdeBinsT<T> B, int *wlev) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B.n) return;
-  for (int d = 0; d < 3; ++d) wlev[d * B.n + b] = P.mask[d] ? log_index(P, B.ks[d * B.n + b], d) : 1;
+  for (int d = 0; d < 3; ++d) wlev[d * B.n + b] = P.mask[d] ? log_index<T>(P, B.ks[d * B.n + b], d) : 1;
 }
 
-__global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, KdeBins B, KdeTable tab, int stride,
-                                                                const int *wlev, double *grid) {
-  __shared__ double sv_all[kWarpsW][3 * KDE_MAXLEN];
+template <typename T>
+__global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, KdeBinsT<T> B, KdeTableT<T> tab,
+                                                                int stride, const int *wlev, T *grid) {
+  __shared__ T sv_all[kWarpsW][3 * KDE_MAXLEN];
   __shared__ int sm_all[kWarpsW][3], sofs_all[kWarpsW][3];
-  __shared__ double crow_all[kWarpsW][kRowCache];
+  __shared__ T crow_all[kWarpsW][kRowCache];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int wi = blockIdx.x * kWarpsW + w;
   if (wi >= B.n) return;  // warp-uniform
@@ -98,7 +107,7 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
   // same cells at once; warp wi takes bin (wi * stride) mod n instead
   // (gcd(stride, n) = 1: a permutation), spreading the atomics over the grid
   const int b = (int)(((long long)wi * stride) % B.n);
-  double *sv = sv_all[w];
+  T *sv = sv_all[w];
   const int gid[3] = {B.gx[b], B.gy[b], B.gz[b]};
   if (lane < 3) {
     const int d = lane;
@@ -113,7 +122,7 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
   }
   __syncwarp();
   for (int d = 0; d < 3; ++d)
-    if (P.mask[d]) fold_factor_warp(sv + d * KDE_MAXLEN, sm_all[w][d], gid[d], P.nb[d], lane);
+    if (P.mask[d]) fold_factor_warp<T>(sv + d * KDE_MAXLEN, sm_all[w][d], gid[d], P.nb[d], lane);
   Span S;
   for (int d = 0; d < 3; ++d) {
     const int m = sm_all[w][d];
@@ -122,13 +131,13 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
     S.n[d] = g1 - g0 + 1;
     S.k0[d] = g0 - gid[d] + m;
   }
-  const double cnt = B.count[b];
+  const T cnt = (T)B.count[b];
   const int n0 = S.n[0], n1 = S.n[1], rows = S.n[1] * S.n[2];
-  const double *fx = sv + S.k0[0], *fy = sv + KDE_MAXLEN + S.k0[1], *fz = sv + 2 * KDE_MAXLEN + S.k0[2];
+  const T *fx = sv + S.k0[0], *fy = sv + KDE_MAXLEN + S.k0[1], *fz = sv + 2 * KDE_MAXLEN + S.k0[2];
   const int64_t sy = P.nb[0], sz = (int64_t)P.nb[0] * P.nb[1];
-  double *gbase = grid + (S.g0[0] - 1) + sy * (S.g0[1] - 1) + sz * (S.g0[2] - 1);
+  T *gbase = grid + (S.g0[0] - 1) + sy * (S.g0[1] - 1) + sz * (S.g0[2] - 1);
   // count * fy * fz per row (y fastest), cached when the span has few rows
-  double *crow = crow_all[w];
+  T *crow = crow_all[w];
   const bool cached = rows <= kRowCache;
   if (cached) {
     for (int r = lane; r < rows; r += 32) {
@@ -141,10 +150,10 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
     // 32 / n0 rows per pass, lane -> (row offset, x)
     const int rpi = 32 / n0, ix = lane % n0, r0 = lane / n0;
     if (r0 >= rpi) return;
-    const double fxv = fx[ix];
+    const T fxv = fx[ix];
     int iz = r0 / n1, iy = r0 - iz * n1;
     for (int r = r0; r < rows; r += rpi) {
-      const double c = cached ? crow[r] : cnt * (fy[iy] * fz[iz]);
+      const T c = cached ? crow[r] : cnt * (fy[iy] * fz[iz]);
       atomicAdd(gbase + ix + sy * iy + sz * iz, c * fxv);
       iy += rpi;
       while (iy >= n1) {
@@ -155,7 +164,7 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
   } else {
     for (int r = 0; r < rows; ++r) {
       const int iz = r / n1, iy = r - iz * n1;
-      const double c = cached ? crow[r] : cnt * (fy[iy] * fz[iz]);
+      const T c = cached ? crow[r] : cnt * (fy[iy] * fz[iz]);
       for (int ix = lane; ix < n0; ix += 32) atomicAdd(gbase + ix + sy * iy + sz * iz, c * fx[ix]);
     }
   }
@@ -163,19 +172,23 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
 
 // density grid = raw scatter / binVolume, and the density at every bin
 // (GridProjectedKDE.F90:4662-4667), both from the raw grid
-__global__ void scale_pick_kernel(KdeParams P, KdeBins B, const double *raw, double *grid, int64_t ngrid) {
+template <typename T>
+__global__ void scale_pick_kernel(KdeParams P, KdeBinsT<T> B, const T *raw, T *grid, int64_t ngrid) {
   const int64_t n = ngrid > B.n ? ngrid : (int64_t)B.n;
+  const T bv = T(P.binvol);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    if (i < ngrid) grid[i] = raw[i] / P.binvol;
+    if (i < ngrid) grid[i] = raw[i] / bv;
     if (i < B.n) {
       const int64_t g = (int64_t)(B.gx[i] - 1) + (int64_t)P.nb[0] * ((B.gy[i] - 1) + (int64_t)P.nb[1] * (B.gz[i] - 1));
-      B.dens[i] = raw[g] / P.binvol;
+      B.dens[i] = raw[g] / bv;
     }
   }
 }
 
-__device__ void support_update(const KdeParams &P, const KdeBins &B, int b, double ne1);
-__device__ void curvature_bandwidth(const KdeParams &P, const KdeBins &B, int b);
+template <typename T>
+__device__ void support_update(const KdeParams &P, const KdeBinsT<T> &B, int b, T ne1);
+template <typename T>
+__device__ void curvature_bandwidth(const KdeParams &P, const KdeBinsT<T> &B, int b);
 
 // ---- separable passes -------------------------------------------------------
 // The reference folds a kernel that crosses a grid edge back into the grid:
@@ -207,7 +220,8 @@ __global__ void key_init_kernel(KeyAcc *K) {
 // (GridProjectedKDE.F90:1723-1724; its 3-D path has no such test and no
 // defined kernel for NaN).  Boxes and counts are accumulated per
 // block in shared memory and merged into K once per block and key.
-__global__ void key_assign_kernel(KdeParams P, KdeBins B, int kind, int *bin_key, KeyAcc *K) {
+template <typename T>
+__global__ void key_assign_kernel(KdeParams P, KdeBinsT<T> B, int kind, int *bin_key, KeyAcc *K) {
   __shared__ int sb[KDE_KMAX][6];
   __shared__ int sl[KDE_KMAX][3];
   __shared__ int sc[KDE_KMAX];
@@ -228,19 +242,19 @@ __global__ void key_assign_kernel(KdeParams P, KdeBins B, int kind, int *bin_key
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
     const int g[3] = {B.gx[b], B.gy[b], B.gz[b]};
     if (kind == 1) {
-      const double s = B.support[b];
+      const T s = B.support[b];
       int lev[3] = {1, 1, 1};
       for (int d = 0; d < 3; ++d)
-        if (P.mask[d]) lev[d] = log_index(P, s, d);
+        if (P.mask[d]) lev[d] = log_index<T>(P, s, d);
       const int key = lev[0] + lev[1] + lev[2] - 3;
       bin_key[b] = key;
       record(key, lev, g);
     } else {
       for (int a = 0; a < 3; ++a) {
         int key = -1;
-        const double h = B.cb[a * B.n + b];
+        const T h = B.cb[a * B.n + b];
         if (P.mask[a] && h == h) {
-          const int n = log_index(P, h, a);
+          const int n = log_index<T>(P, h, a);
           const int lev[3] = {n, n, n};
           key = a * KDE_MAXDB + n - 1;
           record(key, lev, g);
@@ -287,8 +301,7 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, const K
     su[k][1] = su[k][3] = su[k][5] = INT_MIN;
   }
   const bool present = k < KDE_KMAX && K->cnt[k] > 0;
-  int m[3] = {0, 0, 0}, bx[6], r1[6], r2[6];
-  const double *f[3] = {nullptr, nullptr, nullptr};
+  int m[3] = {0, 0, 0}, fo[3] = {0, 0, 0}, bx[6], r1[6], r2[6];
   long long v1 = 0, v2 = 0;
   if (present) {
     const int axis = k / KDE_MAXDB;
@@ -296,7 +309,7 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, const K
     for (int d = 0; d < 3; ++d) {
       const int li = d * KDE_MAXDB + K->lev[k][d] - 1;
       m[d] = T.m[li];
-      f[d] = T.val + T.ofs[li];
+      fo[d] = T.ofs[li];
     }
     for (int i = 0; i < 6; ++i) bx[i] = r1[i] = r2[i] = K->box[k][i];
     if (!scatter) {
@@ -332,7 +345,7 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, const K
     const int j = sp[k] - 1;
     for (int d = 0; d < 3; ++d) {
       pl->m[j][d] = m[d];
-      pl->f[j][d] = f[d];
+      pl->fofs[j][d] = fo[d];
     }
     for (int i = 0; i < 6; ++i) {
       pl->box[j][i] = bx[i];
@@ -389,30 +402,31 @@ __device__ __forceinline__ long long region_loc(const int r[6], int x, int y, in
 // NC = 1: one field; NC = 6: the squared curvatures cx, cy, cz and their
 // pairwise products cx*cy, cx*cz, cy*cz (the roughness terms,
 // GridProjectedKDE.F90:2470-2600).
+template <typename T>
 struct Fields {
-  const double *f[6];
+  const T *f[6];
 };
 
-template <int NC>
-__global__ void gather_x_kernel(KdeParams P, const SepPlan *pl, Fields F, double *T1) {
+template <typename T, int NC>
+__global__ void gather_x_kernel(KdeParams P, const SepPlan *pl, const T *val, Fields<T> F, T *T1) {
   const int j = blockIdx.y;
   if (j >= pl->np) return;
   int r[6];
   for (int i = 0; i < 6; ++i) r[i] = pl->r1[j][i];
   const int m = pl->m[j][0], n = P.nb[0];
-  const double *f = pl->f[j][0];
-  double *out = T1 + pl->o1[j] * NC;
+  const T *f = val + pl->fofs[j][0];
+  T *out = T1 + pl->o1[j] * NC;
   const long long vol = region_vol(r);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
     int x, y, z;
     region_xyz(r, i, x, y, z);
     const long long row = (long long)P.nb[0] * ((y - 1) + (long long)P.nb[1] * (z - 1)) - 1;
-    double acc[NC];
-    for (int c = 0; c < NC; ++c) acc[c] = 0.0;
+    T acc[NC];
+    for (int c = 0; c < NC; ++c) acc[c] = T(0);
     for (int t = 0; t <= 2 * m; ++t) {
       const int p = reflect_pos(x - m + t, n);
       if (p < 1) continue;
-      const double w = f[t];
+      const T w = f[t];
       for (int c = 0; c < NC; ++c) acc[c] += w * F.f[c][row + p];
     }
     for (int c = 0; c < NC; ++c) out[i * NC + c] = acc[c];
@@ -420,10 +434,10 @@ __global__ void gather_x_kernel(KdeParams P, const SepPlan *pl, Fields F, double
 }
 
 // pairwise products of the squared curvatures (GridProjectedKDE.F90:2466-2468)
-__global__ void products_kernel(const double *cx, const double *cy, const double *cz, double *cxy, double *cxz,
-                                double *cyz, int64_t n) {
+template <typename T>
+__global__ void products_kernel(const T *cx, const T *cy, const T *cz, T *cxy, T *cxz, T *cyz, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double a = cx[i], b = cy[i], c = cz[i];
+    const T a = cx[i], b = cy[i], c = cz[i];
     cxy[i] = a * b;
     cxz[i] = a * c;
     cyz[i] = b * c;
@@ -431,8 +445,8 @@ __global__ void products_kernel(const double *cx, const double *cy, const double
 }
 
 // Gather pass 2: T2 = sum_t fy[t] T1(x, reflect(y - m + t), z) over region 2.
-template <int NC>
-__global__ void gather_y_kernel(KdeParams P, const SepPlan *pl, const double *T1, double *T2) {
+template <typename T, int NC>
+__global__ void gather_y_kernel(KdeParams P, const SepPlan *pl, const T *val, const T *T1, T *T2) {
   const int j = blockIdx.y;
   if (j >= pl->np) return;
   int r1[6], r2[6];
@@ -441,19 +455,19 @@ __global__ void gather_y_kernel(KdeParams P, const SepPlan *pl, const double *T1
     r2[i] = pl->r2[j][i];
   }
   const int m = pl->m[j][1], n = P.nb[1];
-  const double *f = pl->f[j][1];
-  const double *in = T1 + pl->o1[j] * NC;
-  double *out = T2 + pl->o2[j] * NC;
+  const T *f = val + pl->fofs[j][1];
+  const T *in = T1 + pl->o1[j] * NC;
+  T *out = T2 + pl->o2[j] * NC;
   const long long vol = region_vol(r2);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
     int x, y, z;
     region_xyz(r2, i, x, y, z);
-    double acc[NC];
-    for (int c = 0; c < NC; ++c) acc[c] = 0.0;
+    T acc[NC];
+    for (int c = 0; c < NC; ++c) acc[c] = T(0);
     for (int t = 0; t <= 2 * m; ++t) {
       const int p = reflect_pos(y - m + t, n);
       if (p < 1) continue;
-      const double w = f[t];
+      const T w = f[t];
       const long long l = region_loc(r1, x, p, z) * NC;
       for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
     }
@@ -468,45 +482,46 @@ __global__ void gather_y_kernel(KdeParams P, const SepPlan *pl, const double *T1
 // roughness (GridProjectedKDE.F90:2594-2600).
 enum { GZ_OUT = 0, GZ_SUPPORT = 1, GZ_NEST = 2 };
 
-template <int NC>
-__global__ void gather_z_kernel(KdeParams P, KdeBins B, const SepPlan *pl, const int *bin_key, const double *T2,
-                                int mode, double *out, double *out2) {
+template <typename T, int NC>
+__global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, const T *val, const int *bin_key,
+                                const T *T2, int mode, T *out, T *out2) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B.n || pl->np == 0) return;  // np == 0: the plan did not fit, the attempt is discarded
   const int j = pl->slot_of[bin_key[b]];
   const int m = pl->m[j][2], n = P.nb[2];
-  const double *f = pl->f[j][2];
+  const T *f = val + pl->fofs[j][2];
   const int *r2 = pl->r2[j];
-  const double *in = T2 + pl->o2[j] * NC;
+  const T *in = T2 + pl->o2[j] * NC;
   const int bx = B.gx[b], by = B.gy[b], bz = B.gz[b];
-  double acc[NC];
-  for (int c = 0; c < NC; ++c) acc[c] = 0.0;
+  T acc[NC];
+  for (int c = 0; c < NC; ++c) acc[c] = T(0);
   for (int t = 0; t <= 2 * m; ++t) {
     const int p = reflect_pos(bz - m + t, n);
     if (p < 1) continue;
-    const double w = f[t];
+    const T w = f[t];
     const long long l = region_loc(r2, bx, by, p) * NC;
     for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
   }
   if constexpr (NC == 1) {
     if (mode == GZ_SUPPORT) {
-      support_update(P, B, b, acc[0]);
+      support_update<T>(P, B, b, acc[0]);
     } else if (mode == GZ_NEST) {
       B.nest[b] = acc[0];
-      curvature_bandwidth(P, B, b);
+      curvature_bandwidth<T>(P, B, b);
     } else {
       out[b] = acc[0];
       if (out2) out2[b] = acc[0];
     }
   } else {
-    const double rxx = acc[0], ryy = acc[1], rzz = acc[2], rxy = acc[3], rxz = acc[4], ryz = acc[5];
+    const T rxx = acc[0], ryy = acc[1], rzz = acc[2], rxy = acc[3], rxz = acc[4], ryz = acc[5];
     B.rxx[b] = rxx;
     B.ryy[b] = ryy;
     B.rzz[b] = rzz;
-    double v = 3.0 * pow(rxx * ryy * rzz, 1.0 / 3.0);
-    if (ryz > 0.0) v = v + 2.0 * ryz * pow(rxx * rxx / ryy / rzz, 1.0 / 6.0);
-    if (rxz > 0.0) v = v + 2.0 * rxz * pow(ryy * ryy / rxx / rzz, 1.0 / 6.0);
-    if (rxy > 0.0) v = v + 2.0 * rxy * pow(rzz * rzz / rxx / ryy, 1.0 / 6.0);
+    const T third = T(1.0 / 3.0), sixth = T(1.0 / 6.0);
+    T v = T(3) * pow(rxx * ryy * rzz, third);
+    if (ryz > T(0)) v = v + T(2) * ryz * pow(rxx * rxx / ryy / rzz, sixth);
+    if (rxz > T(0)) v = v + T(2) * rxz * pow(ryy * ryy / rxx / rzz, sixth);
+    if (rxy > T(0)) v = v + T(2) * rxy * pow(rzz * rzz / rxx / ryy, sixth);
     B.net[b] = v;
   }
 }
@@ -516,22 +531,23 @@ __global__ void gather_z_kernel(KdeParams P, KdeBins B, const SepPlan *pl, const
 // lower face), x-2n (mirrored at the lower, then the upper face) and
 // 2n+1-x (mirrored at the upper face).  acc += f[t] * V(q + m - t) for each
 // such q, V read where it is non-zero: source positions in [lo, hi].
-__device__ __forceinline__ double scatter_taps(const double *f, int m, int x, int n, int lo, int hi,
-                                               const double *V, long long stride, long long base,
-                                               const int *cell_bin, const int *keys, int key, const double *cnt) {
+template <typename T>
+__device__ __forceinline__ T scatter_taps(const T *f, int m, int x, int n, int lo, int hi, const T *V,
+                                          long long stride, long long base, const int *cell_bin, const int *keys,
+                                          int key, const double *cnt) {
   const int q4[4] = {x, 1 - x, x - 2 * n, 2 * n + 1 - x};
-  double acc = 0.0;
+  T acc = T(0);
   for (int k = 0; k < 4; ++k) {
     const int q = q4[k];
     const int t0 = max(0, q + m - hi), t1 = min(2 * m, q + m - lo);
     for (int t = t0; t <= t1; ++t) {
       const int src = q + m - t;
       const long long l = base + (long long)src * stride;
-      double v;
+      T v;
       if (cell_bin) {
         const int cb = cell_bin[l];
         if (cb < 0 || keys[cb] != key) continue;
-        v = cnt[cb];
+        v = (T)cnt[cb];
       } else {
         v = V[l];
       }
@@ -542,8 +558,9 @@ __device__ __forceinline__ double scatter_taps(const double *f, int m, int x, in
 }
 
 // Scatter pass 1 (x) from the bins of each key (count per bin) over region 1.
-__global__ void scatter_x_kernel(KdeParams P, KdeBins B, const SepPlan *pl, const int *cell_bin, const int *bin_key,
-                                 double *V1) {
+template <typename T>
+__global__ void scatter_x_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, const T *val, const int *cell_bin,
+                                 const int *bin_key, T *V1) {
   const int j = blockIdx.y;
   if (j >= pl->np) return;
   int r[6], bx[6];
@@ -554,19 +571,20 @@ __global__ void scatter_x_kernel(KdeParams P, KdeBins B, const SepPlan *pl, cons
   const int key = pl->key[j], axis = key / KDE_MAXDB;
   const int *keys = bin_key + (long long)axis * B.n;
   const int m = pl->m[j][0], n = P.nb[0];
-  const double *f = pl->f[j][0];
-  double *out = V1 + pl->o1[j];
+  const T *f = val + pl->fofs[j][0];
+  T *out = V1 + pl->o1[j];
   const long long vol = region_vol(r);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
     int x, y, z;
     region_xyz(r, i, x, y, z);
     const long long row = (long long)P.nb[0] * ((y - 1) + (long long)P.nb[1] * (z - 1)) - 1;
-    out[i] = scatter_taps(f, m, x, n, bx[0], bx[1], nullptr, 1, row, cell_bin, keys, key, B.count);
+    out[i] = scatter_taps<T>(f, m, x, n, bx[0], bx[1], nullptr, 1, row, cell_bin, keys, key, B.count);
   }
 }
 
 // Scatter pass 2 (y) over region 2.
-__global__ void scatter_y_kernel(KdeParams P, const SepPlan *pl, const double *V1, double *V2) {
+template <typename T>
+__global__ void scatter_y_kernel(KdeParams P, const SepPlan *pl, const T *val, const T *V1, T *V2) {
   const int j = blockIdx.y;
   if (j >= pl->np) return;
   int r1[6], r2[6];
@@ -575,16 +593,16 @@ __global__ void scatter_y_kernel(KdeParams P, const SepPlan *pl, const double *V
     r2[i] = pl->r2[j][i];
   }
   const int m = pl->m[j][1], n = P.nb[1];
-  const double *f = pl->f[j][1];
-  const double *in = V1 + pl->o1[j];
-  double *out = V2 + pl->o2[j];
+  const T *f = val + pl->fofs[j][1];
+  const T *in = V1 + pl->o1[j];
+  T *out = V2 + pl->o2[j];
   const long long vol = region_vol(r2);
   const long long sy = r1[1] - r1[0] + 1;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
     int x, y, z;
     region_xyz(r2, i, x, y, z);
     const long long base = region_loc(r1, x, r1[2], z) - (long long)r1[2] * sy;
-    out[i] = scatter_taps(f, m, y, n, r1[2], r1[3], in, sy, base, nullptr, nullptr, 0, nullptr);
+    out[i] = scatter_taps<T>(f, m, y, n, r1[2], r1[3], in, sy, base, nullptr, nullptr, 0, nullptr);
   }
 }
 
@@ -592,12 +610,12 @@ __global__ void scatter_y_kernel(KdeParams P, const SepPlan *pl, const double *V
 // grid (zeroed before; only the union of the keys' output regions is
 // written), keys in increasing order, then the normalisation
 // ((c / binVolume) / binSize^2)^2 (GridProjectedKDE.F90:2366-2461).
-__global__ void scatter_z_kernel(KdeParams P, const SepPlan *pl, const double *V2, double *c0, double *c1,
-                                 double *c2) {
+template <typename T>
+__global__ void scatter_z_kernel(KdeParams P, const SepPlan *pl, const T *val, const T *V2, T *c0, T *c1, T *c2) {
   const int axis = blockIdx.y;
   if (!P.mask[axis]) return;
-  double *out = axis == 0 ? c0 : (axis == 1 ? c1 : c2);
-  const double bs2 = P.bin[axis] * P.bin[axis];
+  T *out = axis == 0 ? c0 : (axis == 1 ? c1 : c2);
+  const T bs2 = T(P.bin[axis] * P.bin[axis]), bv = T(P.binvol);
   int u[6];
   for (int i = 0; i < 6; ++i) u[i] = pl->ur[axis][i];
   if (u[0] > u[1]) return;  // no key on this axis: the grid stays zero
@@ -607,7 +625,7 @@ __global__ void scatter_z_kernel(KdeParams P, const SepPlan *pl, const double *V
     int x, y, z;
     region_xyz(u, i, x, y, z);
     const long long g = (long long)(x - 1) + (long long)P.nb[0] * ((y - 1) + (long long)P.nb[1] * (z - 1));
-    double acc = 0.0;
+    T acc = T(0);
     for (int j = 0; j < np; ++j) {
       if (pl->key[j] / KDE_MAXDB != axis) continue;
       const int *r2 = pl->r2[j];
@@ -616,87 +634,93 @@ __global__ void scatter_z_kernel(KdeParams P, const SepPlan *pl, const double *V
       if (z < r2[4] - m || z > r2[5] + m) continue;
       const long long sz = (long long)(r2[1] - r2[0] + 1) * (r2[3] - r2[2] + 1);
       const long long base = region_loc(r2, x, y, r2[4]) - (long long)r2[4] * sz;
-      acc += scatter_taps(pl->f[j][2], m, z, n, r2[4], r2[5], V2 + pl->o2[j], sz, base, nullptr, nullptr, 0,
-                          nullptr);
+      acc += scatter_taps<T>(val + pl->fofs[j][2], m, z, n, r2[4], r2[5], V2 + pl->o2[j], sz, base, nullptr,
+                             nullptr, 0, nullptr);
     }
-    double c = acc / P.binvol;
+    T c = acc / bv;
     c = c / bs2;
     out[g] = c * c;
   }
 }
 
-__device__ __forceinline__ double smoothing_scale(const KdeParams &P, const double ks[3]) {
-  double out = 1.0;
+template <typename T>
+__device__ __forceinline__ T smoothing_scale(const KdeParams &P, const T ks[3]) {
+  T out = T(1);
   int dimc = P.ndim;
   for (int d = 0; d < 3; ++d) {
     if (!P.mask[d]) continue;
-    if (ks[d] != 0.0) out = out * ks[d];
+    if (ks[d] != T(0)) out = out * ks[d];
     else dimc = dimc - 1;
   }
-  return (dimc != 0) ? pow(out, 1.0 / (double)P.ndim) : 0.0;
+  return (dimc != 0) ? pow(out, T(1.0 / (double)P.ndim)) : T(0);
 }
 
-__global__ void init_bins_kernel(KdeParams P, KdeBins B, double hs) {
+template <typename T>
+__global__ void init_bins_kernel(KdeParams P, KdeBinsT<T> B, double hs) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B.n) return;
-  double ks[3];
-  for (int d = 0; d < 3; ++d) ks[d] = P.mask[d] ? hs : 0.0;
-  const double sc = smoothing_scale(P, ks);
+  T ks[3];
+  for (int d = 0; d < 3; ++d) ks[d] = P.mask[d] ? T(hs) : T(0);
+  const T sc = smoothing_scale<T>(P, ks);
   B.scale[b] = sc;
-  B.support[b] = 2.0 * sc;
+  B.support[b] = T(2) * sc;
   for (int d = 0; d < 3; ++d) {
     B.ks[d * B.n + b] = ks[d];
-    B.shape[d * B.n + b] = (P.mask[d] && sc > 0.0) ? ks[d] / sc : 0.0;
+    B.shape[d * B.n + b] = (P.mask[d] && sc > T(0)) ? ks[d] / sc : T(0);
   }
-  B.nest[b] = 0.0;
-  B.net[b] = 0.0;
+  B.nest[b] = T(0);
+  B.net[b] = T(0);
 }
 
 // second-half of the sigma-support update (GridProjectedKDE.F90:4836-4860)
-__device__ void support_update(const KdeParams &P, const KdeBins &B, int b, double ne1) {
-  const double dn = B.dens[b];
+template <typename T>
+__device__ void support_update(const KdeParams &P, const KdeBinsT<T> &B, int b, T ne1) {
+  const T dn = B.dens[b];
   // nEstimate**0.5: the correctly rounded square root (as the C library's pow)
-  double ssc = sqrt(ne1) * pow(B.scale[b], P.one_plus_nd_q) / pow(4.0 * dn, 0.25) * P.support_c;
-  if (ssc > P.max_sigma_growth * B.support[b]) ssc = P.max_sigma_growth * B.support[b];
-  ssc = fmin(ssc, P.max_k[P.max_dim]);
-  if (ssc < P.min_k[P.min_dim]) ssc = P.min_k[P.min_dim];
+  T ssc = sqrt(ne1) * pow(B.scale[b], T(P.one_plus_nd_q)) / pow(T(4) * dn, T(0.25)) * T(P.support_c);
+  const T grow = T(P.max_sigma_growth) * B.support[b];
+  if (ssc > grow) ssc = grow;
+  ssc = fmin(ssc, T(P.max_k[P.max_dim]));
+  if (ssc < T(P.min_k[P.min_dim])) ssc = T(P.min_k[P.min_dim]);
   B.support[b] = ssc;
 }
 
 // prComputeCurvatureKernelBandwidth (GridProjectedKDE.F90:5207-5275);
 // nEstimate**fTWO is the product nEstimate*nEstimate, as Fortran compiles it
-__device__ void curvature_bandwidth(const KdeParams &P, const KdeBins &B, int b) {
-  double nvpb = 0.0;
-  const double dn = B.dens[b];
-  if (dn > 0.0) {
-    const double base = SQRT8PI_D * B.support[b];
-    double p = 1.0;
+template <typename T>
+__device__ void curvature_bandwidth(const KdeParams &P, const KdeBinsT<T> &B, int b) {
+  T nvpb = T(0);
+  const T dn = B.dens[b];
+  if (dn > T(0)) {
+    const T base = T(SQRT8PI_D) * B.support[b];
+    T p = T(1);
     for (int k = 0; k < P.ndim; ++k) p = (k == 0) ? base : p * base;  // integer power, left to right
     if (P.ndim == 3) p = base * (base * base);
-    const double ne = B.nest[b];
-    nvpb = pow(p * (ne * ne) / dn, P.beta_c);
+    const T ne = B.nest[b];
+    nvpb = pow(p * (ne * ne) / dn, T(P.beta_c));
   }
   for (int d = 0; d < 3; ++d) {
     if (!P.mask[d]) continue;
-    double tsum = 0.0;
+    T tsum = T(0);
     for (int k = 0; k < 3; ++k) {
       if (!P.mask[k]) continue;
-      const double sh = B.shape[k * B.n + b];
-      if (sh != 0.0) tsum = tsum + (k == d ? 5.0 : 1.0) / (sh * sh);
+      const T sh = B.shape[k * B.n + b];
+      if (sh != T(0)) tsum = tsum + (k == d ? T(5) : T(1)) / (sh * sh);
     }
-    const double shd = B.shape[d * B.n + b];
-    double term = 0.0;
-    if (shd != 0.0) term = pow((P.one_over_nd4 / pow(shd, 4.0)) * tsum, P.minus_one_over_nd6);
-    double c = P.alpha_c * nvpb * term * B.scale[b];
-    if (c > P.max_sd[d]) c = P.max_sd[d];
-    if (c < P.min_sd[d]) c = P.min_sd[d];
+    const T shd = B.shape[d * B.n + b];
+    T term = T(0);
+    if (shd != T(0)) term = pow((T(P.one_over_nd4) / pow(shd, T(4))) * tsum, T(P.minus_one_over_nd6));
+    T c = T(P.alpha_c) * nvpb * term * B.scale[b];
+    if (c > T(P.max_sd[d])) c = T(P.max_sd[d]);
+    if (c < T(P.min_sd[d])) c = T(P.min_sd[d]);
     B.cb[d * B.n + b] = c;
   }
 }
 
-// Per-bin reductions of the optimisation loop, in two stages with a fixed
-// order (per-block partials, then one warp), results in the device scalars
-// S so that the next kernels read them without a host round trip:
+// Per-bin reductions of the optimisation loop, in FP64 and in two stages
+// with a fixed order (per-block partials, then one warp), results in the
+// device scalars S so that the next kernels read them without a host round
+// trip:
 //   RED_NET:    S[0] = max(net roughness), S[2] = min(net roughness > 0)
 //   RED_MAX:    S[3] = max(density), S[4] = max(previous density),
 //               S[5] = -max(smoothing scale > 0), and S[9] as RED_ALMISE
@@ -723,7 +747,8 @@ __device__ __forceinline__ double warp_red(int op, double v) {
 }
 
 // npts2: nPoints**fTWO, which Fortran evaluates as the product nPoints*nPoints
-__global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBins B, int what, double npts2,
+template <typename T>
+__global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBinsT<T> B, int what, double npts2,
                                                               const double *S, double *partial) {
   __shared__ double red[kThreads / 32][4];
   int op[4];
@@ -733,33 +758,34 @@ __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBi
     a[k] = red_init(op[k]);
   }
   const double mx = (what == RED_ERR) ? S[3] : 0.0, mx_old = (what == RED_ERR) ? S[4] : 0.0;
-  const double nd = (double)P.ndim;
+  const T nd = T(P.ndim);
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
     if (what == RED_NET) {
-      const double r = B.net[b];
+      const double r = (double)B.net[b];
       a[0] = fmax(a[0], r);
       if (r > 0.0) a[2] = fmin(a[2], r);
     } else if (what == RED_ERR) {
-      const double dn = B.dens[b], dold = B.dens_old[b];
+      const double dn = (double)B.dens[b], dold = (double)B.dens_old[b];
       if (dold != 0.0) {
         const double e = fabs(dn / mx - dold / mx_old) / (dold / mx_old);
         a[0] += e * e;
       }
-      const double so = B.scale_old[b], sc = B.scale[b];
+      const double so = (double)B.scale_old[b], sc = (double)B.scale[b];
       if (so != 0.0) {
         const double e = fabs(sc - so) / so;
         a[1] += e * e;
       }
     } else {
-      const double sc = B.scale[b];
+      const T sc = B.scale[b];
       if (what == RED_MAX) {
-        a[0] = fmax(a[0], B.dens[b]);
-        a[1] = fmax(a[1], B.dens_old[b]);
-        if (sc > 0.0) a[2] = fmin(a[2], -sc);
+        a[0] = fmax(a[0], (double)B.dens[b]);
+        a[1] = fmax(a[1], (double)B.dens_old[b]);
+        if (sc > T(0)) a[2] = fmin(a[2], -(double)sc);
       }
-      if (sc != 0.0) {
-        const double e = (B.nest[b] / (pow(sc, nd) * P.four_pi_half_nd) + 0.25 * B.net[b] * pow(sc, 4.0)) / npts2;
-        a[3] += e * e;
+      if (sc != T(0)) {
+        const T e = (B.nest[b] / (pow(sc, nd) * T(P.four_pi_half_nd)) + T(0.25) * B.net[b] * pow(sc, T(4))) /
+                    T(npts2);
+        a[3] += (double)e * (double)e;
       }
     }
   }
@@ -808,43 +834,46 @@ __global__ void bin_reduce_final_kernel(int what, int nblk, const double *partia
 
 // prComputeOptimalSmoothingAndShape, per bin (GridProjectedKDE.F90:5404-5724).
 // phase 0: isotropy correction of the net roughness + scale where net > 0.
-__global__ void optimal_phase0_kernel(KdeParams P, KdeBins B, const double *S) {
+template <typename T>
+__global__ void optimal_phase0_kernel(KdeParams P, KdeBinsT<T> B, const double *S) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B.n) return;
-  const double min_pos_net = S[2];
-  const double nd = (double)P.ndim;
-  double net = B.net[b];
+  const T min_pos_net = T(S[2]);
+  const T nd = T(P.ndim), iso = T(P.iso_threshold);
+  T net = B.net[b];
   if (P.ndim == 3) {
-    double sm = B.rxx[b] + B.ryy[b] + B.rzz[b];
-    if (sm == 0.0) sm = min_pos_net;
-    if ((B.rxx[b] / sm > P.iso_threshold) || (B.ryy[b] / sm > P.iso_threshold) || (B.rzz[b] / sm > P.iso_threshold))
-      net = (1.0 - 0.5) * net + 0.5 * sm;
+    T sm = B.rxx[b] + B.ryy[b] + B.rzz[b];
+    if (sm == T(0)) sm = min_pos_net;
+    if ((B.rxx[b] / sm > iso) || (B.ryy[b] / sm > iso) || (B.rzz[b] / sm > iso))
+      net = (T(1) - T(0.5)) * net + T(0.5) * sm;
     B.net[b] = net;
   }
-  double sc = 0.0;
-  if (net > 0.0) sc = pow(nd * B.nest[b] / (P.four_pi_half_nd * net), P.one_over_nd4);
+  T sc = T(0);
+  if (net > T(0)) sc = pow(nd * B.nest[b] / (T(P.four_pi_half_nd) * net), T(P.one_over_nd4));
   B.scale[b] = sc;
 }
 
 // phase 1: scale for zero net roughness, shapes, bounded smoothing
-__global__ void optimal_phase1_kernel(KdeParams P, KdeBins B, const double *S, int *update_flag) {
+template <typename T>
+__global__ void optimal_phase1_kernel(KdeParams P, KdeBinsT<T> B, const double *S, int *update_flag) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B.n) return;
-  const double max_pos_scale = -S[5];
-  double sc = B.scale[b];
-  if (B.net[b] == 0.0) {
+  const T max_pos_scale = T(-S[5]);
+  T sc = B.scale[b];
+  if (B.net[b] == T(0)) {
     sc = max_pos_scale;
     B.scale[b] = sc;
   }
-  double sh[3] = {1.0, 1.0, 1.0};
+  T sh[3] = {T(1), T(1), T(1)};
   if (P.ndim == 3) {
-    const double rxx = B.rxx[b], ryy = B.ryy[b], rzz = B.rzz[b], net = B.net[b];
-    if (!(rxx == 0.0 || ryy == 0.0 || rzz == 0.0)) {
-      const double s1 = fmax(pow(net / rxx, 1.0 / 12.0), P.min_k[0] / sc);
-      const double s2 = fmax(pow(net / ryy, 1.0 / 12.0), P.min_k[1] / sc);
-      const double s3 = 1.0 / s1 / s2;
-      const double ns = pow(s1 * s2 * s3, (double)0.333f);
-      if (ns != 0.0) {
+    const T rxx = B.rxx[b], ryy = B.ryy[b], rzz = B.rzz[b], net = B.net[b];
+    if (!(rxx == T(0) || ryy == T(0) || rzz == T(0))) {
+      const T twelfth = T(1.0 / 12.0);
+      const T s1 = fmax(pow(net / rxx, twelfth), T(P.min_k[0]) / sc);
+      const T s2 = fmax(pow(net / ryy, twelfth), T(P.min_k[1]) / sc);
+      const T s3 = T(1) / s1 / s2;
+      const T ns = pow(s1 * s2 * s3, T(0.333f));
+      if (ns != T(0)) {
         sh[0] = s1 / ns;
         sh[1] = s2 / ns;
         sh[2] = s3 / ns;
@@ -855,16 +884,16 @@ __global__ void optimal_phase1_kernel(KdeParams P, KdeBins B, const double *S, i
   for (int d = 0; d < 3; ++d) {
     B.shape[d * B.n + b] = sh[d];
     if (!P.mask[d]) {
-      B.ks[d * B.n + b] = 0.0;
+      B.ks[d * B.n + b] = T(0);
       continue;
     }
-    double k = sh[d] * sc;
-    if (k > P.max_k[d]) {
-      k = P.max_k[d];
+    T k = sh[d] * sc;
+    if (k > T(P.max_k[d])) {
+      k = T(P.max_k[d]);
       upd = true;
     }
-    if (k < P.min_k[d]) {
-      k = P.min_k[d];
+    if (k < T(P.min_k[d])) {
+      k = T(P.min_k[d]);
       upd = true;
     }
     B.ks[d * B.n + b] = k;
@@ -873,16 +902,26 @@ __global__ void optimal_phase1_kernel(KdeParams P, KdeBins B, const double *S, i
 }
 
 // phase 2: smoothing scale from the bounded smoothing (all bins)
-__global__ void rescale_kernel(KdeParams P, KdeBins B, const int *update_flag) {
+template <typename T>
+__global__ void rescale_kernel(KdeParams P, KdeBinsT<T> B, const int *update_flag) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B.n || *update_flag == 0) return;
-  double ks[3] = {B.ks[b], B.ks[B.n + b], B.ks[2 * B.n + b]};
-  B.scale[b] = smoothing_scale(P, ks);
+  T ks[3] = {B.ks[b], B.ks[B.n + b], B.ks[2 * B.n + b]};
+  B.scale[b] = smoothing_scale<T>(P, ks);
 }
 
-__global__ void copy_kernel(double *dst, const double *src, int n) {
+template <typename T>
+__global__ void copy_kernel(T *dst, const T *src, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] = src[i];
+}
+
+// the exported density: grid * effective-mass factor * (binVolume, scaling
+// factor) in FP64 (GridProjectedKDE.F90:4292-4306)
+template <typename T>
+__global__ void output_kernel(const T *grid, double *out, int64_t n, double f, double scale) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = ((double)grid[i] * f) * scale;
 }
 
 // active-bin compaction (x fastest order, Histogram.F90:493-527): count
@@ -957,10 +996,14 @@ cudaError_t KdeState::ensure_bins(int n) {
     return cudaSuccess;
   }
   void *old[] = {bins.gx, bins.gy, bins.gz, bins.count, bins.ks, bins.scale, bins.shape, bins.support, bins.nest,
-                 bins.dens, bins.cb, bins.rxx, bins.ryy, bins.rzz, bins.net, bins.dens_old, bins.scale_old, tmp,
+                 bins.dens, bins.cb, bins.rxx, bins.ryy, bins.rzz, bins.net, bins.dens_old, bins.scale_old,
                  partial, bin_key, wlev};
   for (void *p : old)
     if (p) cudaFree(p);
+  bins = KdeBins{};
+  partial = nullptr;
+  bin_key = wlev = nullptr;
+  cap = 0;
   const size_t c = (size_t)n;
   cudaError_t e = cudaSuccess;
   auto I = [&](int **p, size_t k) {
@@ -972,7 +1015,7 @@ cudaError_t KdeState::ensure_bins(int n) {
   I(&bins.gx, c); I(&bins.gy, c); I(&bins.gz, c); I(&bin_key, 4 * c); I(&wlev, 3 * c);
   D(&bins.count, c); D(&bins.ks, 3 * c); D(&bins.scale, c); D(&bins.shape, 3 * c); D(&bins.support, c);
   D(&bins.nest, c); D(&bins.dens, c); D(&bins.cb, 3 * c); D(&bins.rxx, c); D(&bins.ryy, c); D(&bins.rzz, c);
-  D(&bins.net, c); D(&bins.dens_old, c); D(&bins.scale_old, c); D(&tmp, c);
+  D(&bins.net, c); D(&bins.dens_old, c); D(&bins.scale_old, c);
   D(&partial, 4 * 152 * 8 + 16);
   if (e != cudaSuccess) return e;
   cap = n;
@@ -985,7 +1028,6 @@ cudaError_t KdeState::ensure_grid(int64_t ngrid) {
     cudaError_t e = cudaMalloc((void **)&d_scalars, 16 * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&h_scalars, 16 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_flag, sizeof(int));
-    if (e == cudaSuccess) e = cudaMallocHost((void **)&h_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_keys, sizeof(KeyAcc));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_plan, 2 * sizeof(SepPlan));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_need, 4 * sizeof(long long));
@@ -993,19 +1035,19 @@ cudaError_t KdeState::ensure_grid(int64_t ngrid) {
     if (e != cudaSuccess) return e;
   }
   if (ngrid <= grid_cap) return cudaSuccess;
-  double *old[] = {dens_grid, dens_raw, cx, cy, cz, cxy, cxz, cyz};
-  for (double *p : old)
-    if (p) cudaFree(p);
+  double **grids[] = {&dens_grid, &dens_raw, &cx, &cy, &cz, &cxy, &cxz, &cyz, &dens_out};
+  for (double **p : grids) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+  }
   if (d_blockcnt) cudaFree(d_blockcnt);
   if (cell_bin) cudaFree(cell_bin);
-  cudaError_t e = cudaMalloc((void **)&dens_grid, sizeof(double) * ngrid);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&cell_bin, sizeof(int) * ngrid);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&dens_raw, sizeof(double) * ngrid);
-  for (double **p : {&cxy, &cxz, &cyz})
+  d_blockcnt = cell_bin = nullptr;
+  grid_cap = 0;
+  cudaError_t e = cudaSuccess;
+  for (double **p : grids)
     if (e == cudaSuccess) e = cudaMalloc((void **)p, sizeof(double) * ngrid);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&cx, sizeof(double) * ngrid);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&cy, sizeof(double) * ngrid);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&cz, sizeof(double) * ngrid);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&cell_bin, sizeof(int) * ngrid);
   if (e == cudaSuccess) e = cudaMalloc((void **)&d_blockcnt, sizeof(int) * ((ngrid + 4095) / 4096 + 1));
   if (e != cudaSuccess) return e;
   grid_cap = ngrid;
@@ -1036,16 +1078,16 @@ cudaError_t KdeState::ensure_pass(int64_t n1, int64_t n2) {
 
 void KdeState::release() {
   void *ptrs[] = {bins.gx, bins.gy, bins.gz, bins.count, bins.ks, bins.scale, bins.shape, bins.support, bins.nest,
-                  bins.dens, bins.cb, bins.rxx, bins.ryy, bins.rzz, bins.net, bins.dens_old, bins.scale_old, tmp,
-                  partial, dens_grid, cx, cy, cz, d_scalars, d_flag, d_blockcnt, d_val, d_meta, cell_bin, bin_key,
-                  d_keys, d_plan, t1, t2, dens_raw, d_need, wlev, cxy, cxz, cyz};
+                  bins.dens, bins.cb, bins.rxx, bins.ryy, bins.rzz, bins.net, bins.dens_old, bins.scale_old,
+                  partial, dens_grid, cx, cy, cz, d_scalars, d_flag, d_blockcnt, d_val, d_valf, d_meta, cell_bin,
+                  bin_key, d_keys, d_plan, t1, t2, dens_raw, d_need, wlev, cxy, cxz, cyz, dens_out};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_scalars) cudaFreeHost(h_scalars);
-  if (h_flag) cudaFreeHost(h_flag);
   if (h_need) cudaFreeHost(h_need);
   *this = KdeState();
 }
+
 static double erf_diff(double i, double hd) {
   const double s2 = std::sqrt(2.0);
   return std::erf((i + 0.5) / (hd * s2)) - std::erf((i - 0.5) / (hd * s2));
@@ -1146,11 +1188,12 @@ void kde_build_tables(const KdeParams &P, std::vector<double> &val, std::vector<
     if (e_ != cudaSuccess) return e_;     \
   } while (0)
 
-// One reconstruction attempt; *overflow is set when a plan found the pass
-// buffers too small (the sizes it needed are in st.h_need).
+// One reconstruction attempt in arithmetic type T; *overflow is set when a
+// plan found the pass buffers too small (the sizes it needed are in st.h_need).
+template <typename T>
 static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, double npts, int n_opt_loops,
                                double rel_err, bool skip_error, cudaStream_t s, int *loops_done, bool *overflow) {
-  KdeBins &B = st.bins;
+  const KdeBinsT<T> B = st.view<T>();
   const int nb = B.n;
   const int64_t ngrid = (int64_t)P.nb[0] * P.nb[1] * P.nb[2];
   const int bb = (nb + kBinThreads - 1) / kBinThreads;
@@ -1160,15 +1203,22 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   const int64_t npick = ngrid > nb ? ngrid : nb;
   double *S = st.d_scalars, *h = st.h_scalars;
   *overflow = false;
+  // typed views of the grids and pass buffers, the factor values
+  T *dens_grid = reinterpret_cast<T *>(st.dens_grid), *dens_raw = reinterpret_cast<T *>(st.dens_raw);
+  T *cx = reinterpret_cast<T *>(st.cx), *cy = reinterpret_cast<T *>(st.cy), *cz = reinterpret_cast<T *>(st.cz);
+  T *cxy = reinterpret_cast<T *>(st.cxy), *cxz = reinterpret_cast<T *>(st.cxz), *cyz = reinterpret_cast<T *>(st.cyz);
+  T *t1 = reinterpret_cast<T *>(st.t1), *t2 = reinterpret_cast<T *>(st.t2);
+  const T *val = std::is_same<T, double>::value ? reinterpret_cast<const T *>(st.d_val)
+                                                : reinterpret_cast<const T *>(st.d_valf);
+  const KdeTableT<T> wtab{val, st.wtab.m, st.wtab.ofs};
   // a stride near n/61 coprime with n (a permutation of the bins)
   int wstride = nb / 61 + 1;
   while (std::gcd(wstride, nb) != 1) ++wstride;
   auto density = [&](void) -> cudaError_t {
-    KCK(cudaMemsetAsync(st.dens_raw, 0, sizeof(double) * ngrid, s));
-    wlevel_kernel<<<bb, kBinThreads, 0, s>>>(P, B, st.wlev);
-    wscatter_kernel<<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, st.wtab, wstride, st.wlev,
-                                                                          st.dens_raw);
-    scale_pick_kernel<<<blocks_for(npick), kThreads, 0, s>>>(P, B, st.dens_raw, st.dens_grid, ngrid);
+    KCK(cudaMemsetAsync(dens_raw, 0, sizeof(T) * ngrid, s));
+    wlevel_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, st.wlev);
+    wscatter_kernel<T><<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, wtab, wstride, st.wlev, dens_raw);
+    scale_pick_kernel<T><<<blocks_for(npick), kThreads, 0, s>>>(P, B, dens_raw, dens_grid, ngrid);
     st.launches += 3;
     return cudaGetLastError();
   };
@@ -1178,7 +1228,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   const dim3 pgrid(kPassBlocks, KDE_KMAX);
   auto plan = [&](int kind, int nc) -> cudaError_t {
     key_init_kernel<<<1, kThreads, 0, s>>>(st.d_keys);
-    key_assign_kernel<<<kb, kThreads, 0, s>>>(P, B, kind, kind == 1 ? key1 : key2, st.d_keys);
+    key_assign_kernel<T><<<kb, kThreads, 0, s>>>(P, B, kind, kind == 1 ? key1 : key2, st.d_keys);
     if (kind == 1)
       plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.wtab, st.wtab, st.wtab, 0, plan1, nc, st.t1_cap,
                                              st.t2_cap, st.d_need);
@@ -1189,15 +1239,15 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     return cudaGetLastError();
   };
   // sum over every bin's smoothing kernel of `field`, at the bins
-  auto gather1 = [&](const double *field, int mode, double *out, double *out2) -> cudaError_t {
-    gather_x_kernel<1><<<pgrid, kThreads, 0, s>>>(P, plan1, Fields{{field}}, st.t1);
-    gather_y_kernel<1><<<pgrid, kThreads, 0, s>>>(P, plan1, st.t1, st.t2);
-    gather_z_kernel<1><<<bb, kBinThreads, 0, s>>>(P, B, plan1, key1, st.t2, mode, out, out2);
+  auto gather1 = [&](const T *field, int mode, T *out, T *out2) -> cudaError_t {
+    gather_x_kernel<T, 1><<<pgrid, kThreads, 0, s>>>(P, plan1, val, Fields<T>{{field}}, t1);
+    gather_y_kernel<T, 1><<<pgrid, kThreads, 0, s>>>(P, plan1, val, t1, t2);
+    gather_z_kernel<T, 1><<<bb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, mode, out, out2);
     st.launches += 3;
     return cudaGetLastError();
   };
   auto reduce = [&](int what) -> cudaError_t {
-    bin_reduce_kernel<<<rb, kThreads, 0, s>>>(P, B, what, npts * npts, S, st.partial);
+    bin_reduce_kernel<T><<<rb, kThreads, 0, s>>>(P, B, what, npts * npts, S, st.partial);
     bin_reduce_final_kernel<<<1, 32, 0, s>>>(what, rb, st.partial, S);
     st.launches += 2;
     return cudaGetLastError();
@@ -1218,45 +1268,43 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   // data-dependent choice inside is taken on the device, so one captured
   // graph replays every loop.
   auto body = [&](void) -> cudaError_t {
-    copy_kernel<<<bb, kBinThreads, 0, s>>>(B.dens_old, B.dens, nb);
-    copy_kernel<<<bb, kBinThreads, 0, s>>>(B.scale_old, B.scale, nb);
+    copy_kernel<T><<<bb, kBinThreads, 0, s>>>(B.dens_old, B.dens, nb);
+    copy_kernel<T><<<bb, kBinThreads, 0, s>>>(B.scale_old, B.scale, nb);
     st.launches += 2;
     // nEstimate with the current support, support update, nEstimate again
     // and the curvature bandwidths
     KCK(plan(1, 1));
-    KCK(gather1(st.dens_grid, GZ_SUPPORT, nullptr, nullptr));
+    KCK(gather1(dens_grid, GZ_SUPPORT, nullptr, nullptr));
     KCK(plan(1, P.ndim == 3 ? 6 : 1));
-    KCK(gather1(st.dens_grid, GZ_NEST, nullptr, nullptr));
+    KCK(gather1(dens_grid, GZ_NEST, nullptr, nullptr));
     // curvatures: second-derivative scatters of the counts, squared
     KCK(plan(2, 1));
-    for (double *c : {st.cx, st.cy, st.cz}) KCK(cudaMemsetAsync(c, 0, sizeof(double) * ngrid, s));
-    scatter_x_kernel<<<pgrid, kThreads, 0, s>>>(P, B, plan2, st.cell_bin, key2, st.t1);
-    scatter_y_kernel<<<pgrid, kThreads, 0, s>>>(P, plan2, st.t1, st.t2);
-    scatter_z_kernel<<<dim3(gb, 3), kThreads, 0, s>>>(P, plan2, st.t2, st.cx, st.cy, st.cz);
+    for (T *c : {cx, cy, cz}) KCK(cudaMemsetAsync(c, 0, sizeof(T) * ngrid, s));
+    scatter_x_kernel<T><<<pgrid, kThreads, 0, s>>>(P, B, plan2, val, st.cell_bin, key2, t1);
+    scatter_y_kernel<T><<<pgrid, kThreads, 0, s>>>(P, plan2, val, t1, t2);
+    scatter_z_kernel<T><<<dim3(gb, 3), kThreads, 0, s>>>(P, plan2, val, t2, cx, cy, cz);
     st.launches += 3;
     // net roughness: smoothing-kernel gathers of the squared curvatures
     if (P.ndim == 3) {
-      products_kernel<<<gb, kThreads, 0, s>>>(st.cx, st.cy, st.cz, st.cxy, st.cxz, st.cyz, ngrid);
-      gather_x_kernel<6><<<pgrid, kThreads, 0, s>>>(P, plan1, Fields{{st.cx, st.cy, st.cz, st.cxy, st.cxz, st.cyz}},
-                                                    st.t1);
-      st.launches += 1;
-      gather_y_kernel<6><<<pgrid, kThreads, 0, s>>>(P, plan1, st.t1, st.t2);
-      gather_z_kernel<6><<<bb, kBinThreads, 0, s>>>(P, B, plan1, key1, st.t2, GZ_OUT, nullptr, nullptr);
-      st.launches += 3;
+      products_kernel<T><<<gb, kThreads, 0, s>>>(cx, cy, cz, cxy, cxz, cyz, ngrid);
+      gather_x_kernel<T, 6><<<pgrid, kThreads, 0, s>>>(P, plan1, val, Fields<T>{{cx, cy, cz, cxy, cxz, cyz}}, t1);
+      gather_y_kernel<T, 6><<<pgrid, kThreads, 0, s>>>(P, plan1, val, t1, t2);
+      gather_z_kernel<T, 6><<<bb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, GZ_OUT, nullptr, nullptr);
+      st.launches += 4;
     } else {
       int a = 0;
       while (!P.mask[a]) ++a;
-      double *cg[3] = {st.cx, st.cy, st.cz};
-      double *r1 = (a == 0) ? B.rxx : (a == 1 ? B.ryy : B.rzz);
+      T *cg[3] = {cx, cy, cz};
+      T *r1 = (a == 0) ? B.rxx : (a == 1 ? B.ryy : B.rzz);
       KCK(gather1(cg[a], GZ_OUT, r1, B.net));
     }
     // optimal smoothing and shape; the extremes stay on the device
     KCK(reduce(RED_NET));
-    optimal_phase0_kernel<<<bb, kBinThreads, 0, s>>>(P, B, S);
+    optimal_phase0_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, S);
     KCK(reduce(RED_MAX));
     KCK(cudaMemsetAsync(st.d_flag, 0, sizeof(int), s));
-    optimal_phase1_kernel<<<bb, kBinThreads, 0, s>>>(P, B, S, st.d_flag);
-    rescale_kernel<<<bb, kBinThreads, 0, s>>>(P, B, st.d_flag);
+    optimal_phase1_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, S, st.d_flag);
+    rescale_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, st.d_flag);
     st.launches += 3;
     // density with the new smoothing, then the convergence measures
     KCK(density());
@@ -1265,7 +1313,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     return fetch_async();
   };
   KCK(cudaMemsetAsync(st.d_need, 0, 3 * sizeof(long long), s));
-  init_bins_kernel<<<bb, kBinThreads, 0, s>>>(P, B, hs);
+  init_bins_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, hs);
   st.launches += 1;
   KCK(density());
   KCK(reduce(RED_ALMISE));  // nEstimate and net roughness are zero: 0
@@ -1330,18 +1378,32 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
 // buffers the plans asked for (every attempt re-derives all per-bin state,
 // so the result does not depend on how many attempts ran).
 cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, int n_opt_loops, double rel_err,
-                    bool skip_error, cudaStream_t s, int *loops_done) {
+                    bool skip_error, int fp32, cudaStream_t s, int *loops_done) {
   const int64_t ngrid = (int64_t)P.nb[0] * P.nb[1] * P.nb[2];
   // eight grid volumes of the six roughness fields: enough for most plumes
   KCK(st.ensure_pass(48 * ngrid, 48 * ngrid));
   for (int attempt = 0; attempt < 8; ++attempt) {
     bool overflow = false;
-    KCK(kde_attempt(st, P, hs, npts, n_opt_loops, rel_err, skip_error, s, loops_done, &overflow));
+    if (fp32)
+      KCK(kde_attempt<float>(st, P, hs, npts, n_opt_loops, rel_err, skip_error, s, loops_done, &overflow));
+    else
+      KCK(kde_attempt<double>(st, P, hs, npts, n_opt_loops, rel_err, skip_error, s, loops_done, &overflow));
     if (!overflow) return cudaSuccess;
     // what a discarded attempt asked for is a lower bound: grow geometrically
     KCK(st.ensure_pass(std::max<int64_t>(st.h_need[0], 2 * st.t1_cap), std::max<int64_t>(st.h_need[1], 2 * st.t2_cap)));
   }
   return cudaErrorMemoryAllocation;
+}
+
+cudaError_t kde_output(KdeState &st, const KdeParams &P, int fp32, double f, double scale, cudaStream_t s) {
+  const int64_t ngrid = (int64_t)P.nb[0] * P.nb[1] * P.nb[2];
+  if (fp32)
+    output_kernel<float><<<blocks_for(ngrid), kThreads, 0, s>>>(reinterpret_cast<const float *>(st.dens_grid),
+                                                                 st.dens_out, ngrid, f, scale);
+  else
+    output_kernel<double><<<blocks_for(ngrid), kThreads, 0, s>>>(st.dens_grid, st.dens_out, ngrid, f, scale);
+  st.launches += 1;
+  return cudaGetLastError();
 }
 
 cudaError_t kde_collect_active(KdeState &st, const KdeParams &P, const double *counts, cudaStream_t s, int *nactive) {
@@ -1366,7 +1428,8 @@ cudaError_t kde_collect_active(KdeState &st, const KdeParams &P, const double *c
   KCK(cudaMemsetAsync(st.cell_bin, 0xff, sizeof(int) * ngrid, s));  // -1: no active bin
   active_write_kernel<<<nblk, kThreads, 0, s>>>(counts, ngrid, d_cnt, P, st.bins, st.cell_bin);
   st.launches += 2;
-  return cudaGetLastError();
+  KCK(cudaGetLastError());
+  return cudaStreamSynchronize(s);  // the offsets vector goes out of scope
 }
 
 }  // namespace mprw

@@ -29,11 +29,14 @@ struct KdeParams {
 
 // 1-D factor table: for dimension d and database index n (0-based),
 // m[d*KDE_MAXDB+n] is the half width and val[ofs[...] + k], k = 0..2m, the
-// full symmetric factor.
-struct KdeTable {
-  const double *val;
+// full symmetric factor.  Every table of a reconstruction indexes the same
+// value array (one copy per arithmetic type).
+template <typename T>
+struct KdeTableT {
+  const T *val;
   const int *m, *ofs;
 };
+using KdeTable = KdeTableT<double>;
 
 // Separable passes.  The smoothing (sigma) and second-derivative kernels of
 // a bin are chosen from the database by one scalar, so the bins fall into at
@@ -50,36 +53,43 @@ struct KeyAcc {
   int cnt[KDE_KMAX];
 };
 
-// The keys present, compacted: per key its half widths and factors per
-// dimension, the regions of the two intermediate passes and their offsets
-// (in elements) into the pass buffers.
+// The keys present, compacted: per key its half widths and the offsets of its
+// factors in the value array per dimension, the regions of the two
+// intermediate passes and their offsets (in elements) into the pass buffers.
 struct SepPlan {
   int np;
   int slot_of[KDE_KMAX];
   int key[KDE_KMAX];
   int m[KDE_KMAX][3];
-  const double *f[KDE_KMAX][3];
+  int fofs[KDE_KMAX][3];
   int box[KDE_KMAX][6], r1[KDE_KMAX][6], r2[KDE_KMAX][6];
   long long o1[KDE_KMAX], o2[KDE_KMAX];
   int ur[3][6];  // scatter: union of the output regions of each axis's keys
 };
 
-// Per active bin state (SoA).  3-vectors are stored dimension-major: v[d*n + b].
-struct KdeBins {
+// Per active bin state (SoA) in the reconstruction's arithmetic type T; the
+// histogram count stays FP64.  3-vectors are stored dimension-major: v[d*n + b].
+template <typename T>
+struct KdeBinsT {
   int n;
   int *gx, *gy, *gz;  // 1-based bin indexes
   double *count;
-  double *ks, *scale, *shape, *support, *nest, *dens, *cb, *rxx, *ryy, *rzz, *net, *dens_old, *scale_old;
+  T *ks, *scale, *shape, *support, *nest, *dens, *cb, *rxx, *ryy, *rzz, *net, *dens_old, *scale_old;
 };
+using KdeBins = KdeBinsT<double>;
 
+// Device state of the reconstructions of one handle.  Every array is
+// allocated with FP64 elements; an FP32 reconstruction uses the same memory
+// through float views (view<float>()).
 struct KdeState {
   KdeBins bins{};
   int cap = 0;
   double *dens_grid = nullptr, *dens_raw = nullptr, *cx = nullptr, *cy = nullptr, *cz = nullptr;
   double *cxy = nullptr, *cxz = nullptr, *cyz = nullptr;  // products of the squared curvatures
+  double *dens_out = nullptr;                             // FP64 output grid
   int64_t grid_cap = 0;
-  double *tmp = nullptr, *partial = nullptr, *d_scalars = nullptr, *h_scalars = nullptr;
-  int *d_flag = nullptr, *h_flag = nullptr, *d_blockcnt = nullptr;
+  double *partial = nullptr, *d_scalars = nullptr, *h_scalars = nullptr;
+  int *d_flag = nullptr, *d_blockcnt = nullptr;
   int *cell_bin = nullptr;          // per grid cell: active bin index or -1
   int *bin_key = nullptr;           // per bin: smoothing key (n) and SD keys per axis (3n)
   int *wlev = nullptr;              // per bin: W kernel database level per dimension (3n)
@@ -90,8 +100,25 @@ struct KdeState {
   long long *d_need = nullptr, *h_need = nullptr;  // pass-buffer sizes a plan needed, overflow flag
   KdeTable wtab{}, sdtab[3]{};
   double *d_val = nullptr;
-  int *d_meta = nullptr;  // wm, wofs, sm[3], sofs[3]
+  float *d_valf = nullptr;  // the factor values in FP32
+  int *d_meta = nullptr;    // wm, wofs, sm[3], sofs[3]
   int64_t launches = 0;
+
+  template <typename T>
+  KdeBinsT<T> view() const {
+    KdeBinsT<T> v;
+    v.n = bins.n;
+    v.gx = bins.gx;
+    v.gy = bins.gy;
+    v.gz = bins.gz;
+    v.count = bins.count;
+    double *const src[] = {bins.ks,  bins.scale, bins.shape, bins.support, bins.nest, bins.dens,     bins.cb,
+                           bins.rxx, bins.ryy,   bins.rzz,   bins.net,     bins.dens_old, bins.scale_old};
+    T **dst[] = {&v.ks,  &v.scale, &v.shape, &v.support, &v.nest, &v.dens,     &v.cb,
+                 &v.rxx, &v.ryy,   &v.rzz,   &v.net,     &v.dens_old, &v.scale_old};
+    for (int i = 0; i < 13; ++i) *dst[i] = reinterpret_cast<T *>(src[i]);
+    return v;
+  }
 
   cudaError_t ensure_bins(int n);
   cudaError_t ensure_pass(int64_t n1, int64_t n2);
@@ -103,7 +130,10 @@ void kde_build_tables(const KdeParams &P, std::vector<double> &val, std::vector<
                       std::vector<int> (&sm)[3], std::vector<int> (&sofs)[3]);
 cudaError_t kde_collect_active(KdeState &st, const KdeParams &P, const double *counts, cudaStream_t s,
                                int *nactive);
+// fp32 != 0: the reconstruction runs in FP32 (convergence sums in FP64)
 cudaError_t kde_run(KdeState &st, const KdeParams &P, double hs, double npts, int n_opt_loops, double rel_err,
-                    bool skip_error, cudaStream_t s, int *loops_done);
+                    bool skip_error, int fp32, cudaStream_t s, int *loops_done);
+// st.dens_out = density grid * f * scale (FP64), from the last reconstruction
+cudaError_t kde_output(KdeState &st, const KdeParams &P, int fp32, double f, double scale, cudaStream_t s);
 
 }  // namespace mprw

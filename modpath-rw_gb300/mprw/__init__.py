@@ -53,7 +53,8 @@ class GpkdeOptions(C.Structure):
     _fields_ = [("origin", C.c_double * 3), ("domain_size", C.c_double * 3), ("bin_size", C.c_double * 3),
                 ("n_opt_loops", C.c_int32), ("min_hover_delta", C.c_double), ("delta_hover_delta", C.c_double),
                 ("max_hover_delta", C.c_double), ("rel_err_convergence", C.c_double),
-                ("skip_error_convergence", C.c_int32), ("unit_volume", C.c_int32), ("scaling_factor", C.c_double)]
+                ("skip_error_convergence", C.c_int32), ("unit_volume", C.c_int32), ("scaling_factor", C.c_double),
+                ("precision", C.c_int32)]
 
 
 class FlowDesc(C.Structure):
@@ -227,8 +228,10 @@ class Tracker:
 
     @staticmethod
     def gpkde_options(domain_size, bin_size, origin=(0.0, 0.0, 0.0), n_opt_loops=10, kdb=(0.3, 0.3, 15.0),
-                      rel_err=0.02, skip_error=False, unit_volume=True, scaling_factor=1.0) -> "GpkdeOptions":
-        """The mprw_gpkde_options of a reconstruction grid (defaults: the reference's GPKDE input defaults)."""
+                      rel_err=0.02, skip_error=False, unit_volume=True, scaling_factor=1.0,
+                      precision=FP64) -> "GpkdeOptions":
+        """The mprw_gpkde_options of a reconstruction grid (defaults: the reference's GPKDE input
+        defaults, FP64 arithmetic)."""
         o = GpkdeOptions()
         for d in range(3):
             o.origin[d], o.domain_size[d], o.bin_size[d] = float(origin[d]), float(domain_size[d]), float(bin_size[d])
@@ -238,14 +241,15 @@ class Tracker:
         o.skip_error_convergence = int(skip_error)
         o.unit_volume = int(unit_volume)
         o.scaling_factor = float(scaling_factor)
+        o.precision = int(precision)
         return o
 
     def gpkde(self, domain_size, bin_size, origin=(0.0, 0.0, 0.0), n_opt_loops=10, kdb=(0.3, 0.3, 15.0),
-              rel_err=0.02, skip_error=False, unit_volume=True, scaling_factor=1.0):
+              rel_err=0.02, skip_error=False, unit_volume=True, scaling_factor=1.0, precision=FP64):
         """GPKDE reconstruction of the active particles.  Returns (density, histogram,
         loops) with the grids shaped (nz, ny, nx)."""
         o = self.gpkde_options(domain_size, bin_size, origin, n_opt_loops, kdb, rel_err, skip_error, unit_volume,
-                               scaling_factor)
+                               scaling_factor, precision)
         nb = [int(domain_size[d] / bin_size[d] + 0.5) if bin_size[d] != 0 else 1 for d in range(3)]
         dens = np.empty(int(np.prod(nb)))
         hist = np.empty(int(np.prod(nb)))

@@ -66,3 +66,30 @@ def test_gpkde_scaling_and_empty(gpu_lib):
     d3, h3, loops = tr.gpkde((10.0, 1.0, 1.0), (1.0, 1.0, 1.0), origin=(150.0, 0.0, 0.0))
     assert np.all(d3 == 0) and np.all(h3 == 0) and loops == 0
     tr.close()
+
+
+@pytest.mark.parametrize("case", ["1d", "3d"])
+def test_gpkde_fp32_against_fp64(gpu_lib, case):
+    """The mixed-precision reconstruction (FP32 passes and per-bin updates,
+    FP64 convergence sums) against the FP64 one on the same particles: the
+    same number of optimisation loops, the density within 1e-3 of its
+    maximum, the mass conserved to FP32 rounding."""
+    from mprw.model import MIXED
+    if case == "1d":
+        g, f, p, opt = W.config1(n_particles=20000)
+        t1, dom, lo = 50.0, (200.0, 1.0, 1.0), 10
+    else:
+        g, f, p, opt, info = W.config2(n_particles=20000, nlay=6, nrow=20, ncol=40, seed=1, use_torch=False)
+        t1, dom, lo = 30.0, (40.0, 20.0, 6.0), 10
+    tr = mprw.Tracker(g, opt)
+    tr.load_flow(f)
+    tr.set_particles(p)
+    tr.advance(0.0, t1)
+    n = _positions(tr).shape[0]
+    d64, h64, l64 = tr.gpkde(dom, (1.0, 1.0, 1.0), n_opt_loops=lo)
+    d32, h32, l32 = tr.gpkde(dom, (1.0, 1.0, 1.0), n_opt_loops=lo, precision=MIXED)
+    tr.close()
+    np.testing.assert_array_equal(h32, h64)
+    assert l32 == l64
+    assert np.abs(d32 - d64).max() <= 1e-3 * d64.max()
+    assert abs(d32.sum() - n) < 1e-4 * n
