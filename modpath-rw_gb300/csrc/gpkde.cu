@@ -49,6 +49,30 @@ __device__ __forceinline__ int log_index(const KdeParams &P, T h, int d) {
   return i;
 }
 
+// Device scalars of one reconstruction (S, FP64): slot meanings
+//   S_NETMAX  max net roughness           S_NETMINPOS  min positive net roughness
+//   S_DMAX    max density                 S_DMAXOLD    max previous density
+//   S_ERRD    sum of squared density changes   S_ERRS  ... smoothing changes
+//   S_ALMISE  sum of squared ALMISE terms S_SCMAX      max positive smoothing scale
+enum { S_NETMAX = 0, S_NETMINPOS = 2, S_DMAX = 3, S_DMAXOLD = 4, S_ERRD = 6, S_ERRS = 7, S_ALMISE = 9,
+       S_SCMAX = 11, S_COUNT = 12 };
+
+// Extremes of positive values by integer atomics on the IEEE bit patterns
+// (their order is the numeric order for positive doubles): order-independent,
+// so as repeatable as the fixed-order sums.  One atomic per warp.
+__device__ __forceinline__ void warp_max_pos(double *addr, double v) {
+  v = (v > 0.0) ? v : 0.0;
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0 && v > 0.0)
+    atomicMax(reinterpret_cast<unsigned long long *>(addr), (unsigned long long)__double_as_longlong(v));
+}
+__device__ __forceinline__ void warp_min_pos(double *addr, double v) {
+  v = (v > 0.0) ? v : DBL_MAX;
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0 && v < DBL_MAX)
+    atomicMin(reinterpret_cast<unsigned long long *>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
 // Fold one dimension's factor in place (prKernelReflection, one axis), the
 // lanes of a warp splitting each loop: the part below cell 1 is added onto its
 // mirror image and cleared, then the part above cell nb likewise (targets and
@@ -172,17 +196,22 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
 
 // density grid = raw scatter / binVolume, and the density at every bin
 // (GridProjectedKDE.F90:4662-4667), both from the raw grid
+// (and S[S_DMAX] = max density, zeroed before)
 template <typename T>
-__global__ void scale_pick_kernel(KdeParams P, KdeBinsT<T> B, const T *raw, T *grid, int64_t ngrid) {
+__global__ void scale_pick_kernel(KdeParams P, KdeBinsT<T> B, const T *raw, T *grid, int64_t ngrid, double *S) {
   const int64_t n = ngrid > B.n ? ngrid : (int64_t)B.n;
   const T bv = T(P.binvol);
+  double dmax = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     if (i < ngrid) grid[i] = raw[i] / bv;
     if (i < B.n) {
       const int64_t g = (int64_t)(B.gx[i] - 1) + (int64_t)P.nb[0] * ((B.gy[i] - 1) + (int64_t)P.nb[1] * (B.gz[i] - 1));
-      B.dens[i] = raw[g] / bv;
+      const T d = raw[g] / bv;
+      B.dens[i] = d;
+      dmax = fmax(dmax, (double)d);
     }
   }
+  warp_max_pos(S + S_DMAX, dmax);
 }
 
 template <typename T>
@@ -480,49 +509,61 @@ __global__ void gather_y_kernel(KdeParams P, const SepPlan *pl, const T *val, co
 // sigma-support update from this first nEstimate; GZ_NEST: nEstimate, then
 // the curvature bandwidths.  NC = 6: the roughness terms and the net
 // roughness (GridProjectedKDE.F90:2594-2600).
-enum { GZ_OUT = 0, GZ_SUPPORT = 1, GZ_NEST = 2 };
+enum { GZ_OUT = 0, GZ_SUPPORT = 1, GZ_NEST = 2, GZ_NET = 3 };
 
+// GZ_NET (1-D): out[b] = out2[b] = the roughness, which is the net roughness;
+// NC = 6 and GZ_NET also fold max(net) and min(net > 0) into S.
 template <typename T, int NC>
 __global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, const T *val, const int *bin_key,
-                                const T *T2, int mode, T *out, T *out2) {
+                                const T *T2, int mode, T *out, T *out2, double *S) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B.n || pl->np == 0) return;  // np == 0: the plan did not fit, the attempt is discarded
-  const int j = pl->slot_of[bin_key[b]];
-  const int m = pl->m[j][2], n = P.nb[2];
-  const T *f = val + pl->fofs[j][2];
-  const int *r2 = pl->r2[j];
-  const T *in = T2 + pl->o2[j] * NC;
-  const int bx = B.gx[b], by = B.gy[b], bz = B.gz[b];
-  T acc[NC];
-  for (int c = 0; c < NC; ++c) acc[c] = T(0);
-  for (int t = 0; t <= 2 * m; ++t) {
-    const int p = reflect_pos(bz - m + t, n);
-    if (p < 1) continue;
-    const T w = f[t];
-    const long long l = region_loc(r2, bx, by, p) * NC;
-    for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
-  }
-  if constexpr (NC == 1) {
-    if (mode == GZ_SUPPORT) {
-      support_update<T>(P, B, b, acc[0]);
-    } else if (mode == GZ_NEST) {
-      B.nest[b] = acc[0];
-      curvature_bandwidth<T>(P, B, b);
-    } else {
-      out[b] = acc[0];
-      if (out2) out2[b] = acc[0];
+  // np == 0: the plan did not fit, the attempt is discarded
+  const bool valid = b < B.n && pl->np != 0;
+  double net = 0.0;
+  if (valid) {
+    const int j = pl->slot_of[bin_key[b]];
+    const int m = pl->m[j][2], n = P.nb[2];
+    const T *f = val + pl->fofs[j][2];
+    const int *r2 = pl->r2[j];
+    const T *in = T2 + pl->o2[j] * NC;
+    const int bx = B.gx[b], by = B.gy[b], bz = B.gz[b];
+    T acc[NC];
+    for (int c = 0; c < NC; ++c) acc[c] = T(0);
+    for (int t = 0; t <= 2 * m; ++t) {
+      const int p = reflect_pos(bz - m + t, n);
+      if (p < 1) continue;
+      const T w = f[t];
+      const long long l = region_loc(r2, bx, by, p) * NC;
+      for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
     }
-  } else {
-    const T rxx = acc[0], ryy = acc[1], rzz = acc[2], rxy = acc[3], rxz = acc[4], ryz = acc[5];
-    B.rxx[b] = rxx;
-    B.ryy[b] = ryy;
-    B.rzz[b] = rzz;
-    const T third = T(1.0 / 3.0), sixth = T(1.0 / 6.0);
-    T v = T(3) * pow(rxx * ryy * rzz, third);
-    if (ryz > T(0)) v = v + T(2) * ryz * pow(rxx * rxx / ryy / rzz, sixth);
-    if (rxz > T(0)) v = v + T(2) * rxz * pow(ryy * ryy / rxx / rzz, sixth);
-    if (rxy > T(0)) v = v + T(2) * rxy * pow(rzz * rzz / rxx / ryy, sixth);
-    B.net[b] = v;
+    if constexpr (NC == 1) {
+      if (mode == GZ_SUPPORT) {
+        support_update<T>(P, B, b, acc[0]);
+      } else if (mode == GZ_NEST) {
+        B.nest[b] = acc[0];
+        curvature_bandwidth<T>(P, B, b);
+      } else {
+        out[b] = acc[0];
+        if (out2) out2[b] = acc[0];
+        net = (double)acc[0];
+      }
+    } else {
+      const T rxx = acc[0], ryy = acc[1], rzz = acc[2], rxy = acc[3], rxz = acc[4], ryz = acc[5];
+      B.rxx[b] = rxx;
+      B.ryy[b] = ryy;
+      B.rzz[b] = rzz;
+      const T third = T(1.0 / 3.0), sixth = T(1.0 / 6.0);
+      T v = T(3) * pow(rxx * ryy * rzz, third);
+      if (ryz > T(0)) v = v + T(2) * ryz * pow(rxx * rxx / ryy / rzz, sixth);
+      if (rxz > T(0)) v = v + T(2) * rxz * pow(ryy * ryy / rxx / rzz, sixth);
+      if (rxy > T(0)) v = v + T(2) * rxy * pow(rzz * rzz / rxx / ryy, sixth);
+      B.net[b] = v;
+      net = (double)v;
+    }
+  }
+  if (NC == 6 || mode == GZ_NET) {  // block-uniform: every lane takes part
+    warp_max_pos(S + S_NETMAX, net);
+    warp_min_pos(S + S_NETMINPOS, net);
   }
 }
 
@@ -656,8 +697,9 @@ __device__ __forceinline__ T smoothing_scale(const KdeParams &P, const T ks[3]) 
 }
 
 template <typename T>
-__global__ void init_bins_kernel(KdeParams P, KdeBinsT<T> B, double hs) {
+__global__ void init_bins_kernel(KdeParams P, KdeBinsT<T> B, double hs, double *S) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b == 0) S[S_DMAX] = 0.0;
   if (b >= B.n) return;
   T ks[3];
   for (int d = 0; d < 3; ++d) ks[d] = P.mask[d] ? T(hs) : T(0);
@@ -717,32 +759,19 @@ __device__ void curvature_bandwidth(const KdeParams &P, const KdeBinsT<T> &B, in
   }
 }
 
-// Per-bin reductions of the optimisation loop, in FP64 and in two stages
-// with a fixed order (per-block partials, then one warp), results in the
-// device scalars S so that the next kernels read them without a host round
-// trip:
-//   RED_NET:    S[0] = max(net roughness), S[2] = min(net roughness > 0)
-//   RED_MAX:    S[3] = max(density), S[4] = max(previous density),
-//               S[5] = -max(smoothing scale > 0), and S[9] as RED_ALMISE
-//   RED_ERR:    S[6], S[7] = sums of the squared relative density and
-//               smoothing changes (GridProjectedKDE.F90:4976-5000; uses
-//               S[3], S[4])
-//   RED_ALMISE: S[9] = sum of the squared ALMISE terms (4966-4972)
+// Per-bin sums of the optimisation loop, in FP64 and in two stages with a
+// fixed order (per-block partials, then one warp), results in the device
+// scalars S:
+//   RED_END:    S[S_ERRD], S[S_ERRS] = sums of the squared relative density
+//               and smoothing changes (GridProjectedKDE.F90:4976-5000, with
+//               S[S_DMAX], S[S_DMAXOLD]), and S[S_ALMISE]
+//   RED_ALMISE: S[S_ALMISE] = sum of the squared ALMISE terms (4966-4972)
+// (the maxima and minima are folded into the kernels that produce them)
 constexpr int kRedBlocks = 152;
-enum { RED_NET = 0, RED_ERR = 1, RED_MAX = 2, RED_ALMISE = 3 };
-enum { OP_SUM = 0, OP_MAX = 1, OP_MIN = 2 };
+enum { RED_END = 1, RED_ALMISE = 3 };
 
-__device__ __forceinline__ int red_op(int what, int slot) {
-  if (what == RED_NET) return slot == 0 ? OP_MAX : (slot == 2 ? OP_MIN : OP_SUM);
-  if (what == RED_MAX) return slot <= 1 ? OP_MAX : (slot == 2 ? OP_MIN : OP_SUM);
-  return OP_SUM;
-}
-__device__ __forceinline__ double red_init(int op) { return op == OP_MAX ? -DBL_MAX : (op == OP_MIN ? DBL_MAX : 0.0); }
-__device__ __forceinline__ double red_apply(int op, double a, double b) {
-  return op == OP_MAX ? fmax(a, b) : (op == OP_MIN ? fmin(a, b) : a + b);
-}
-__device__ __forceinline__ double warp_red(int op, double v) {
-  for (int o = 16; o > 0; o >>= 1) v = red_apply(op, v, __shfl_down_sync(0xffffffffu, v, o));
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
 }
 
@@ -750,21 +779,12 @@ __device__ __forceinline__ double warp_red(int op, double v) {
 template <typename T>
 __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBinsT<T> B, int what, double npts2,
                                                               const double *S, double *partial) {
-  __shared__ double red[kThreads / 32][4];
-  int op[4];
-  double a[4];
-  for (int k = 0; k < 4; ++k) {
-    op[k] = red_op(what, k);
-    a[k] = red_init(op[k]);
-  }
-  const double mx = (what == RED_ERR) ? S[3] : 0.0, mx_old = (what == RED_ERR) ? S[4] : 0.0;
+  __shared__ double red[kThreads / 32][3];
+  double a[3] = {0.0, 0.0, 0.0};
+  const double mx = S[S_DMAX], mx_old = S[S_DMAXOLD];
   const T nd = T(P.ndim);
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
-    if (what == RED_NET) {
-      const double r = (double)B.net[b];
-      a[0] = fmax(a[0], r);
-      if (r > 0.0) a[2] = fmin(a[2], r);
-    } else if (what == RED_ERR) {
+    if (what == RED_END) {
       const double dn = (double)B.dens[b], dold = (double)B.dens_old[b];
       if (dold != 0.0) {
         const double e = fabs(dn / mx - dold / mx_old) / (dold / mx_old);
@@ -775,30 +795,23 @@ __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBi
         const double e = fabs(sc - so) / so;
         a[1] += e * e;
       }
-    } else {
-      const T sc = B.scale[b];
-      if (what == RED_MAX) {
-        a[0] = fmax(a[0], (double)B.dens[b]);
-        a[1] = fmax(a[1], (double)B.dens_old[b]);
-        if (sc > T(0)) a[2] = fmin(a[2], -(double)sc);
-      }
-      if (sc != T(0)) {
-        const T e = (B.nest[b] / (pow(sc, nd) * T(P.four_pi_half_nd)) + T(0.25) * B.net[b] * pow(sc, T(4))) /
-                    T(npts2);
-        a[3] += (double)e * (double)e;
-      }
+    }
+    const T sc = B.scale[b];
+    if (sc != T(0)) {
+      const T e = (B.nest[b] / (pow(sc, nd) * T(P.four_pi_half_nd)) + T(0.25) * B.net[b] * pow(sc, T(4))) / T(npts2);
+      a[2] += (double)e * (double)e;
     }
   }
-  for (int k = 0; k < 4; ++k) a[k] = warp_red(op[k], a[k]);
+  for (int k = 0; k < 3; ++k) a[k] = warp_sum(a[k]);
   const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0)
-    for (int k = 0; k < 4; ++k) red[w][k] = a[k];
+    for (int k = 0; k < 3; ++k) red[w][k] = a[k];
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 3; ++k) {
       double v = red[0][k];
-      for (int i = 1; i < kThreads / 32; ++i) v = red_apply(op[k], v, red[i][k]);
-      partial[4 * blockIdx.x + k] = v;
+      for (int i = 1; i < kThreads / 32; ++i) v = v + red[i][k];
+      partial[3 * blockIdx.x + k] = v;
     }
   }
 }
@@ -806,51 +819,42 @@ __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBi
 // one warp: lane l folds partials l, l+32, ... then a shuffle tree
 __global__ void bin_reduce_final_kernel(int what, int nblk, const double *partial, double *S) {
   const int l = threadIdx.x;
-  double a[4];
-  int op[4];
-  for (int k = 0; k < 4; ++k) {
-    op[k] = red_op(what, k);
-    a[k] = red_init(op[k]);
-  }
+  double a[3] = {0.0, 0.0, 0.0};
   for (int i = l; i < nblk; i += 32)
-    for (int k = 0; k < 4; ++k) a[k] = red_apply(op[k], a[k], partial[4 * i + k]);
-  for (int k = 0; k < 4; ++k) a[k] = warp_red(op[k], a[k]);
+    for (int k = 0; k < 3; ++k) a[k] = a[k] + partial[3 * i + k];
+  for (int k = 0; k < 3; ++k) a[k] = warp_sum(a[k]);
   if (l != 0) return;
-  if (what == RED_NET) {
-    S[0] = a[0];
-    S[2] = a[2];
-  } else if (what == RED_MAX) {
-    S[3] = a[0];
-    S[4] = a[1];
-    S[5] = a[2];
-    S[9] = a[3];
-  } else if (what == RED_ERR) {
-    S[6] = a[0];
-    S[7] = a[1];
-  } else {
-    S[9] = a[3];
+  if (what == RED_END) {
+    S[S_ERRD] = a[0];
+    S[S_ERRS] = a[1];
   }
+  S[S_ALMISE] = a[2];
 }
 
 // prComputeOptimalSmoothingAndShape, per bin (GridProjectedKDE.F90:5404-5724).
 // phase 0: isotropy correction of the net roughness + scale where net > 0.
+// (and S[S_SCMAX] = max positive scale, for the bins with zero net roughness)
 template <typename T>
-__global__ void optimal_phase0_kernel(KdeParams P, KdeBinsT<T> B, const double *S) {
+__global__ void optimal_phase0_kernel(KdeParams P, KdeBinsT<T> B, double *S) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B.n) return;
-  const T min_pos_net = T(S[2]);
-  const T nd = T(P.ndim), iso = T(P.iso_threshold);
-  T net = B.net[b];
-  if (P.ndim == 3) {
-    T sm = B.rxx[b] + B.ryy[b] + B.rzz[b];
-    if (sm == T(0)) sm = min_pos_net;
-    if ((B.rxx[b] / sm > iso) || (B.ryy[b] / sm > iso) || (B.rzz[b] / sm > iso))
-      net = (T(1) - T(0.5)) * net + T(0.5) * sm;
-    B.net[b] = net;
+  double scv = 0.0;
+  if (b < B.n) {
+    const T min_pos_net = T(S[S_NETMINPOS]);
+    const T nd = T(P.ndim), iso = T(P.iso_threshold);
+    T net = B.net[b];
+    if (P.ndim == 3) {
+      T sm = B.rxx[b] + B.ryy[b] + B.rzz[b];
+      if (sm == T(0)) sm = min_pos_net;
+      if ((B.rxx[b] / sm > iso) || (B.ryy[b] / sm > iso) || (B.rzz[b] / sm > iso))
+        net = (T(1) - T(0.5)) * net + T(0.5) * sm;
+      B.net[b] = net;
+    }
+    T sc = T(0);
+    if (net > T(0)) sc = pow(nd * B.nest[b] / (T(P.four_pi_half_nd) * net), T(P.one_over_nd4));
+    B.scale[b] = sc;
+    scv = (double)sc;
   }
-  T sc = T(0);
-  if (net > T(0)) sc = pow(nd * B.nest[b] / (T(P.four_pi_half_nd) * net), T(P.one_over_nd4));
-  B.scale[b] = sc;
+  warp_max_pos(S + S_SCMAX, scv);
 }
 
 // phase 1: scale for zero net roughness, shapes, bounded smoothing
@@ -858,7 +862,7 @@ template <typename T>
 __global__ void optimal_phase1_kernel(KdeParams P, KdeBinsT<T> B, const double *S, int *update_flag) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B.n) return;
-  const T max_pos_scale = T(-S[5]);
+  const T max_pos_scale = T(S[S_SCMAX]);
   T sc = B.scale[b];
   if (B.net[b] == T(0)) {
     sc = max_pos_scale;
@@ -910,10 +914,22 @@ __global__ void rescale_kernel(KdeParams P, KdeBinsT<T> B, const int *update_fla
   B.scale[b] = smoothing_scale<T>(P, ks);
 }
 
+// start of an optimisation loop: previous density and smoothing scale, the
+// previous maximum density, and the extremes the loop accumulates reset
 template <typename T>
-__global__ void copy_kernel(T *dst, const T *src, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) dst[i] = src[i];
+__global__ void loop_init_kernel(KdeBinsT<T> B, double *S) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < B.n) {
+    B.dens_old[b] = B.dens[b];
+    B.scale_old[b] = B.scale[b];
+  }
+  if (b == 0) {
+    S[S_DMAXOLD] = S[S_DMAX];
+    S[S_DMAX] = 0.0;
+    S[S_NETMAX] = 0.0;
+    S[S_NETMINPOS] = DBL_MAX;
+    S[S_SCMAX] = 0.0;
+  }
 }
 
 // the exported density: grid * effective-mass factor * (binVolume, scaling
@@ -1016,7 +1032,7 @@ cudaError_t KdeState::ensure_bins(int n) {
   D(&bins.count, c); D(&bins.ks, 3 * c); D(&bins.scale, c); D(&bins.shape, 3 * c); D(&bins.support, c);
   D(&bins.nest, c); D(&bins.dens, c); D(&bins.cb, 3 * c); D(&bins.rxx, c); D(&bins.ryy, c); D(&bins.rzz, c);
   D(&bins.net, c); D(&bins.dens_old, c); D(&bins.scale_old, c);
-  D(&partial, 4 * 152 * 8 + 16);
+  D(&partial, 3 * 152 * 8 + 16);
   if (e != cudaSuccess) return e;
   cap = n;
   bins.n = n;
@@ -1218,7 +1234,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     KCK(cudaMemsetAsync(dens_raw, 0, sizeof(T) * ngrid, s));
     wlevel_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, st.wlev);
     wscatter_kernel<T><<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, wtab, wstride, st.wlev, dens_raw);
-    scale_pick_kernel<T><<<blocks_for(npick), kThreads, 0, s>>>(P, B, dens_raw, dens_grid, ngrid);
+    scale_pick_kernel<T><<<blocks_for(npick), kThreads, 0, s>>>(P, B, dens_raw, dens_grid, ngrid, S);
     st.launches += 3;
     return cudaGetLastError();
   };
@@ -1242,7 +1258,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   auto gather1 = [&](const T *field, int mode, T *out, T *out2) -> cudaError_t {
     gather_x_kernel<T, 1><<<pgrid, kThreads, 0, s>>>(P, plan1, val, Fields<T>{{field}}, t1);
     gather_y_kernel<T, 1><<<pgrid, kThreads, 0, s>>>(P, plan1, val, t1, t2);
-    gather_z_kernel<T, 1><<<bb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, mode, out, out2);
+    gather_z_kernel<T, 1><<<bb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, mode, out, out2, S);
     st.launches += 3;
     return cudaGetLastError();
   };
@@ -1253,7 +1269,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     return cudaGetLastError();
   };
   auto fetch_async = [&](void) -> cudaError_t {
-    KCK(cudaMemcpyAsync(h, S, 10 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    KCK(cudaMemcpyAsync(h, S, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
     return cudaMemcpyAsync(st.h_need, st.d_need, 3 * sizeof(long long), cudaMemcpyDeviceToHost, s);
   };
   auto fetch_wait = [&](void) -> cudaError_t {
@@ -1268,9 +1284,8 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   // data-dependent choice inside is taken on the device, so one captured
   // graph replays every loop.
   auto body = [&](void) -> cudaError_t {
-    copy_kernel<T><<<bb, kBinThreads, 0, s>>>(B.dens_old, B.dens, nb);
-    copy_kernel<T><<<bb, kBinThreads, 0, s>>>(B.scale_old, B.scale, nb);
-    st.launches += 2;
+    loop_init_kernel<T><<<bb, kBinThreads, 0, s>>>(B, S);
+    st.launches += 1;
     // nEstimate with the current support, support update, nEstimate again
     // and the curvature bandwidths
     KCK(plan(1, 1));
@@ -1289,37 +1304,34 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
       products_kernel<T><<<gb, kThreads, 0, s>>>(cx, cy, cz, cxy, cxz, cyz, ngrid);
       gather_x_kernel<T, 6><<<pgrid, kThreads, 0, s>>>(P, plan1, val, Fields<T>{{cx, cy, cz, cxy, cxz, cyz}}, t1);
       gather_y_kernel<T, 6><<<pgrid, kThreads, 0, s>>>(P, plan1, val, t1, t2);
-      gather_z_kernel<T, 6><<<bb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, GZ_OUT, nullptr, nullptr);
+      gather_z_kernel<T, 6><<<bb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, GZ_OUT, nullptr, nullptr, S);
       st.launches += 4;
     } else {
       int a = 0;
       while (!P.mask[a]) ++a;
       T *cg[3] = {cx, cy, cz};
       T *r1 = (a == 0) ? B.rxx : (a == 1 ? B.ryy : B.rzz);
-      KCK(gather1(cg[a], GZ_OUT, r1, B.net));
+      KCK(gather1(cg[a], GZ_NET, r1, B.net));
     }
     // optimal smoothing and shape; the extremes stay on the device
-    KCK(reduce(RED_NET));
     optimal_phase0_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, S);
-    KCK(reduce(RED_MAX));
     KCK(cudaMemsetAsync(st.d_flag, 0, sizeof(int), s));
     optimal_phase1_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, S, st.d_flag);
     rescale_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, st.d_flag);
     st.launches += 3;
     // density with the new smoothing, then the convergence measures
     KCK(density());
-    KCK(reduce(RED_MAX));  // with the ALMISE sum
-    KCK(reduce(RED_ERR));
+    KCK(reduce(RED_END));
     return fetch_async();
   };
   KCK(cudaMemsetAsync(st.d_need, 0, 3 * sizeof(long long), s));
-  init_bins_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, hs);
+  init_bins_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, hs, S);
   st.launches += 1;
   KCK(density());
   KCK(reduce(RED_ALMISE));  // nEstimate and net roughness are zero: 0
   KCK(fetch_async());
   KCK(fetch_wait());
-  double alm = std::sqrt(h[9] / nb);
+  double alm = std::sqrt(h[S_ALMISE] / nb);
   double alm_old = alm, cum = alm, cum_old = alm;
   // capture the loop body once; a stream that cannot be captured (the legacy
   // default stream) runs it directly
@@ -1355,9 +1367,9 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     KCK(fetch_wait());
     if (*overflow) return cudaSuccess;
     // maxval(netRoughness) == 0: the reference stops (GridProjectedKDE.F90:5443-5446)
-    if (h[0] == 0.0) return cudaErrorInvalidValue;
-    const double err_dens = std::sqrt(h[6] / nb), err_smooth = std::sqrt(h[7] / nb);
-    alm = std::sqrt(h[9] / nb);
+    if (h[S_NETMAX] == 0.0) return cudaErrorInvalidValue;
+    const double err_dens = std::sqrt(h[S_ERRD] / nb), err_smooth = std::sqrt(h[S_ERRS] / nb);
+    alm = std::sqrt(h[S_ALMISE] / nb);
     cum = cum + alm;
     if (!skip_error) {
       if (alm_old > 0.0 && std::fabs(alm - alm_old) / alm_old < rel_err) break;
