@@ -442,7 +442,8 @@ int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_do
     a.d2 = h->d2;
     a.seed = h->opt.rng_seed;
     a.exp_adv = h->opt.advection_kind == 1;
-    int blocks = h->sms * 2;
+    // EULERIAN MIXED is compiled for 3 resident blocks per SM (80 registers)
+    int blocks = h->sms * (a.exp_adv ? 1 : 3);
     int64_t need = (h->n + threads - 1) / threads;
     if (need < blocks) blocks = (int)need;
     CK(launch_advance<float>(a, blocks, threads, s));
