@@ -452,11 +452,31 @@ __global__ void gather_x_kernel(KdeParams P, const SepPlan *pl, const T *val, Fi
     const long long row = (long long)P.nb[0] * ((y - 1) + (long long)P.nb[1] * (z - 1)) - 1;
     T acc[NC];
     for (int c = 0; c < NC; ++c) acc[c] = T(0);
-    for (int t = 0; t <= 2 * m; ++t) {
-      const int p = reflect_pos(x - m + t, n);
-      if (p < 1) continue;
-      const T w = f[t];
-      for (int c = 0; c < NC; ++c) acc[c] += w * F.f[c][row + p];
+    if (x - m >= 1 && x + m <= n) {
+      // the window misses both edges: a straight loop, two partial sums per
+      // field so that the loads run ahead of the multiply-adds
+      T acc2[NC];
+      for (int c = 0; c < NC; ++c) acc2[c] = T(0);
+      const long long base = row + x - m;
+      int t = 0;
+#pragma unroll 2
+      for (; t + 1 <= 2 * m; t += 2) {
+        const T w0 = f[t], w1 = f[t + 1];
+        for (int c = 0; c < NC; ++c) {
+          acc[c] += w0 * F.f[c][base + t];
+          acc2[c] += w1 * F.f[c][base + t + 1];
+        }
+      }
+      if (t <= 2 * m)
+        for (int c = 0; c < NC; ++c) acc[c] += f[t] * F.f[c][base + t];
+      for (int c = 0; c < NC; ++c) acc[c] += acc2[c];
+    } else {
+      for (int t = 0; t <= 2 * m; ++t) {
+        const int p = reflect_pos(x - m + t, n);
+        if (p < 1) continue;
+        const T w = f[t];
+        for (int c = 0; c < NC; ++c) acc[c] += w * F.f[c][row + p];
+      }
     }
     for (int c = 0; c < NC; ++c) out[i * NC + c] = acc[c];
   }
@@ -493,12 +513,32 @@ __global__ void gather_y_kernel(KdeParams P, const SepPlan *pl, const T *val, co
     region_xyz(r2, i, x, y, z);
     T acc[NC];
     for (int c = 0; c < NC; ++c) acc[c] = T(0);
-    for (int t = 0; t <= 2 * m; ++t) {
-      const int p = reflect_pos(y - m + t, n);
-      if (p < 1) continue;
-      const T w = f[t];
-      const long long l = region_loc(r1, x, p, z) * NC;
-      for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
+    if (y - m >= 1 && y + m <= n) {
+      // interior window (inside region 1 by construction): straight loop
+      T acc2[NC];
+      for (int c = 0; c < NC; ++c) acc2[c] = T(0);
+      const T *src = in + region_loc(r1, x, y - m, z) * NC;
+      const long long st = (long long)(r1[1] - r1[0] + 1) * NC;
+      int t = 0;
+#pragma unroll 2
+      for (; t + 1 <= 2 * m; t += 2) {
+        const T w0 = f[t], w1 = f[t + 1];
+        for (int c = 0; c < NC; ++c) {
+          acc[c] += w0 * src[t * st + c];
+          acc2[c] += w1 * src[(t + 1) * st + c];
+        }
+      }
+      if (t <= 2 * m)
+        for (int c = 0; c < NC; ++c) acc[c] += f[t] * src[t * st + c];
+      for (int c = 0; c < NC; ++c) acc[c] += acc2[c];
+    } else {
+      for (int t = 0; t <= 2 * m; ++t) {
+        const int p = reflect_pos(y - m + t, n);
+        if (p < 1) continue;
+        const T w = f[t];
+        const long long l = region_loc(r1, x, p, z) * NC;
+        for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
+      }
     }
     for (int c = 0; c < NC; ++c) out[i * NC + c] = acc[c];
   }
