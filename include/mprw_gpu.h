@@ -183,6 +183,27 @@ typedef struct {
 int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *opt, double *density, double *histogram,
                int32_t n_bins_out[3], int32_t *loops_done);
 
+/* Observation cells (TrackingOptions%isObservation / idObservation;
+ * Observation.f90:7-60).  cells[i] (1-based) belongs to observation obs[i]
+ * (0-based, < nobs); style[k] of observation k is 1 (resident) or 2 (sink).
+ * A cell belongs to at most one observation.  Replaces the observation
+ * bookkeeping of the particle loop, MPathRW.F90:1337-1392 and 1460-1535. */
+int mprw_set_observations(mprw_handle *h, int32_t ncells, const int32_t *cells, const int32_t *obs,
+                          int32_t nobs, const int32_t *style);
+
+/* Resident observations at the current time (MPathRW.F90:1460-1535): for
+ * every style-1 observation k, count[k] ACTIVE particles lie in its cells
+ * with total mass mass[k] (nobs entries each). */
+int mprw_observe_resident(mprw_handle *h, int64_t *count, double *mass);
+
+/* Sink observations of the last mprw_advance (MPathRW.F90:1337-1392): the
+ * particles that stopped at a weak sink or weak source (status 3 or 4)
+ * during that interval in a cell of a style-2 observation, as records
+ * (observation, particle id, stop time, mass) in particle order.  At most
+ * capacity records are copied; n_records receives how many there are. */
+int mprw_observe_sinks(mprw_handle *h, int64_t capacity, int32_t *obs, uint64_t *id, double *time,
+                       double *mass, int64_t *n_records);
+
 /* Allocation-free unit-mass histogram.  No counterpart in the reference: it
  * exists for callers that cannot allocate device memory when they bin -- a
  * host code that owns a fixed device-memory budget and hands the library only

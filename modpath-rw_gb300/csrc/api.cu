@@ -56,6 +56,13 @@ struct mprw_handle {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   double step_ms = 0, prep_ms = 0, hist_ms = 0, kde_ms = 0;
   KdeState kde;
+  // observation cells
+  int32_t *d_obs_of_cell = nullptr, *d_obs_style = nullptr;
+  int32_t nobs = 0;
+  unsigned long long *d_obs_count = nullptr;
+  double *d_obs_mass = nullptr;
+  double last_t_begin = 0.0, last_t_end = 0.0;
+  bool advanced = false;
   double *d_kpart = nullptr;          // coordinate-statistics partials
   double *h_kout = nullptr;           // pinned staging of the density / histogram grids
   int64_t h_kout_cap = 0;
@@ -110,6 +117,8 @@ void free_all(mprw_handle *h) {
   if (h->h_counters) cudaFreeHost(h->h_counters);
   if (h->d_counts) cudaFree(h->d_counts);
   if (h->d_kpart) cudaFree(h->d_kpart);
+  for (void *p : {(void *)h->d_obs_of_cell, (void *)h->d_obs_style, (void *)h->d_obs_count, (void *)h->d_obs_mass})
+    if (p) cudaFree(p);
   if (h->h_kout) cudaFreeHost(h->h_kout);
   h->kde.release();
   if (h->hscratch) cudaFreeHost(h->hscratch);
@@ -405,6 +414,9 @@ int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_do
   if (!h->flow_loaded) return fail(h, MPRW_E_STATE, "mprw_advance before mprw_load_flow");
   if (!(t_end >= t_begin)) return fail(h, MPRW_E_INVAL, "t_end < t_begin");
   h->launches = 0;
+  h->last_t_begin = t_begin;
+  h->last_t_end = t_end;
+  h->advanced = true;
   if (h->n == 0) {
     if (steps_done) *steps_done = 0;
     return MPRW_OK;
@@ -854,6 +866,104 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
   h->kde_ms = ms;
   h->launches += h->kde.launches + 2;
   if (loops_done) *loops_done = loops;
+  return MPRW_OK;
+}
+
+// ---- observation cells (Observation.f90; MPathRW.F90:1337-1392, 1460-1535) ----
+static ObsArgs obs_args(const mprw_handle *h) {
+  ObsArgs a{};
+  a.n = h->n;
+  a.cell = h->d_cell;
+  a.status = h->d_status;
+  a.t = h->d_t;
+  a.mass = h->unit_mass ? nullptr : h->d_mass;
+  a.id = h->has_id ? h->d_id : nullptr;
+  a.obs_of_cell = h->d_obs_of_cell;
+  a.obs_style = h->d_obs_style;
+  a.t_begin = h->last_t_begin;
+  a.t_end = h->last_t_end;
+  return a;
+}
+
+int mprw_set_observations(mprw_handle *h, int32_t ncells, const int32_t *cells, const int32_t *obs, int32_t nobs,
+                          const int32_t *style) {
+  if (!h) return MPRW_E_INVAL;
+  if (ncells < 0 || nobs < 0 || (ncells > 0 && (!cells || !obs)) || (nobs > 0 && !style))
+    return fail(h, MPRW_E_INVAL, "mprw_set_observations: null argument or negative size");
+  const int32_t ncell = h->g.ncell;
+  std::vector<int32_t> of(ncell, -1);
+  for (int32_t i = 0; i < ncells; ++i) {
+    if (cells[i] < 1 || cells[i] > ncell) return fail(h, MPRW_E_INVAL, "mprw_set_observations: cell out of range");
+    if (obs[i] < 0 || obs[i] >= nobs) return fail(h, MPRW_E_INVAL, "mprw_set_observations: observation index");
+    int32_t &o = of[cells[i] - 1];
+    if (o >= 0 && o != obs[i]) return fail(h, MPRW_E_INVAL, "mprw_set_observations: cell in two observations");
+    o = obs[i];
+  }
+  for (int32_t k = 0; k < nobs; ++k)
+    if (style[k] != 1 && style[k] != 2) return fail(h, MPRW_E_INVAL, "mprw_set_observations: style (1 or 2)");
+  cudaStream_t s = h->stream;
+  CK(cudaStreamSynchronize(s));
+  for (void *p : {(void *)h->d_obs_of_cell, (void *)h->d_obs_style, (void *)h->d_obs_count, (void *)h->d_obs_mass})
+    if (p) cudaFree(p);
+  h->d_obs_of_cell = h->d_obs_style = nullptr;
+  h->d_obs_count = nullptr;
+  h->d_obs_mass = nullptr;
+  h->nobs = 0;
+  const size_t k = nobs > 0 ? (size_t)nobs : 1;
+  CK(cudaMalloc(&h->d_obs_of_cell, sizeof(int32_t) * ncell));
+  CK(cudaMalloc(&h->d_obs_style, sizeof(int32_t) * k));
+  CK(cudaMalloc(&h->d_obs_count, sizeof(unsigned long long) * k));
+  CK(cudaMalloc(&h->d_obs_mass, sizeof(double) * k));
+  CK(cudaMemcpyAsync(h->d_obs_of_cell, of.data(), sizeof(int32_t) * ncell, cudaMemcpyHostToDevice, s));
+  if (nobs > 0) CK(cudaMemcpyAsync(h->d_obs_style, style, sizeof(int32_t) * nobs, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  h->nobs = nobs;
+  return MPRW_OK;
+}
+
+int mprw_observe_resident(mprw_handle *h, int64_t *count, double *mass) {
+  if (!h) return MPRW_E_INVAL;
+  if (!h->d_obs_of_cell) return fail(h, MPRW_E_STATE, "mprw_observe_resident before mprw_set_observations");
+  if (h->nobs > 0 && (!count || !mass)) return fail(h, MPRW_E_INVAL, "mprw_observe_resident: null argument");
+  if (h->nobs == 0) return MPRW_OK;
+  cudaStream_t s = h->stream;
+  CK(cudaMemsetAsync(h->d_obs_count, 0, sizeof(unsigned long long) * h->nobs, s));
+  CK(cudaMemsetAsync(h->d_obs_mass, 0, sizeof(double) * h->nobs, s));
+  CK(launch_resident(obs_args(h), h->d_obs_count, h->d_obs_mass, s));
+  std::vector<unsigned long long> c(h->nobs);
+  CK(cudaMemcpyAsync(c.data(), h->d_obs_count, sizeof(unsigned long long) * h->nobs, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(mass, h->d_obs_mass, sizeof(double) * h->nobs, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int32_t k = 0; k < h->nobs; ++k) count[k] = (int64_t)c[k];
+  h->launches = 1;
+  return MPRW_OK;
+}
+
+int mprw_observe_sinks(mprw_handle *h, int64_t capacity, int32_t *obs, uint64_t *id, double *time, double *mass,
+                       int64_t *n_records) {
+  if (!h) return MPRW_E_INVAL;
+  if (!h->d_obs_of_cell) return fail(h, MPRW_E_STATE, "mprw_observe_sinks before mprw_set_observations");
+  if (!n_records || capacity < 0 || (capacity > 0 && (!obs || !id || !time || !mass)))
+    return fail(h, MPRW_E_INVAL, "mprw_observe_sinks: null argument or negative capacity");
+  *n_records = 0;
+  if (!h->advanced || h->n == 0 || h->nobs == 0) return MPRW_OK;
+  cudaStream_t s = h->stream;
+  int64_t m = 0;
+  CK(collect_sink_records(obs_args(h), &h->scratch, &h->scratch_bytes, &m, s));
+  *n_records = m;
+  const int64_t w = m < capacity ? m : capacity;
+  if (w > 0) {
+    int32_t *d_obs;
+    uint64_t *d_id;
+    double *d_t, *d_m;
+    CK(sink_record_arrays(h->scratch, h->n, &d_obs, &d_id, &d_t, &d_m));
+    CK(cudaMemcpyAsync(obs, d_obs, sizeof(int32_t) * w, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(id, d_id, sizeof(uint64_t) * w, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(time, d_t, sizeof(double) * w, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(mass, d_m, sizeof(double) * w, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  h->launches = 3;
   return MPRW_OK;
 }
 

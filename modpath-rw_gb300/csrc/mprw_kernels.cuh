@@ -89,6 +89,26 @@ cudaError_t launch_coord_sums(const Geometry &geo, int64_t n, const int32_t *cel
                               const void *x, const void *y, const void *z, int mixed, int pass, const double mean[3],
                               double *partial, int *nblocks, cudaStream_t s);
 
+// ---- observation cells (obs.cu) -------------------------------------------
+struct ObsArgs {
+  int64_t n;
+  const int32_t *cell, *status;  // cell 0-based
+  const double *t, *mass;        // mass may be null (unit mass)
+  const uint64_t *id;            // may be null: id = index
+  const int32_t *obs_of_cell;    // per cell: observation index or -1
+  const int32_t *obs_style;      // per observation: 1 resident, 2 sink
+  double t_begin, t_end;         // interval of the last advance
+};
+
+// Sink records of the last advance into the scratch buffer; *n_records = how many.
+cudaError_t collect_sink_records(const ObsArgs &a, void **scratch, size_t *scratch_bytes, int64_t *n_records,
+                                 cudaStream_t s);
+// Device addresses of the record arrays collect_sink_records left in scratch (same n).
+cudaError_t sink_record_arrays(void *scratch, int64_t n, int32_t **obs, uint64_t **id, double **time,
+                               double **mass);
+// count[k] += 1, msum[k] += mass for every ACTIVE particle in a style-1 observation cell.
+cudaError_t launch_resident(const ObsArgs &a, unsigned long long *count, double *msum, cudaStream_t s);
+
 // Ordered (order-preserving) weighted sums: sort.cu
 cudaError_t ordered_bin_sums(const int64_t *bin_of, const double *mass, const int32_t *status, int64_t n,
                              int64_t nbins, double *counts, double *total_mass, double *sum_w2,

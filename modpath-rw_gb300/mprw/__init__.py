@@ -85,6 +85,9 @@ def load_library() -> C.CDLL:
         "mprw_get_particles": (C.c_int, [H, _ip, _dp, _dp, _dp, _dp, _ip, _up, _dp, _dp, _dp]),
         "mprw_histogram": (C.c_int, [H, _dp, _dp, _ip, _dp, C.POINTER(C.c_int64), _dp]),
         "mprw_gpkde": (C.c_int, [H, C.POINTER(GpkdeOptions), _dp, _dp, _ip, _ip]),
+        "mprw_set_observations": (C.c_int, [H, C.c_int32, _ip, _ip, C.c_int32, _ip]),
+        "mprw_observe_resident": (C.c_int, [H, C.POINTER(C.c_int64), _dp]),
+        "mprw_observe_sinks": (C.c_int, [H, C.c_int64, _ip, _up, _dp, _dp, C.POINTER(C.c_int64)]),
         "mprw_set_stream": (C.c_int, [H, C.c_void_p]),
         "mprw_last_timings": (C.c_int, [H, _dp, _dp, _dp, _dp, C.POINTER(C.c_int64)]),
         "mprw_destroy": (C.c_int, [H]),
@@ -259,6 +262,35 @@ class Tracker:
                                         C.byref(loops)), "mprw_gpkde")
         shp = (nb[2], nb[1], nb[0])
         return dens.reshape(shp), hist.reshape(shp), loops.value
+
+    def set_observations(self, cells, obs, style):
+        """Observation cells: cells (1-based) belong to observations obs (0-based);
+        style[k] = 1 resident, 2 sink."""
+        c, o, st = _i32(cells), _i32(obs), _i32(style)
+        self._obs = (c, o, st)
+        self.nobs = int(st.shape[0])
+        self._check(self.lib.mprw_set_observations(self.h, int(c.shape[0]), _p(c, _ip), _p(o, _ip), self.nobs,
+                                                   _p(st, _ip)), "mprw_set_observations")
+
+    def observe_resident(self):
+        """(count, mass) of the ACTIVE particles in each resident observation."""
+        cnt = np.zeros(self.nobs, np.int64)
+        mass = np.zeros(self.nobs)
+        self._check(self.lib.mprw_observe_resident(self.h, cnt.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                   _p(mass, _dp)), "mprw_observe_resident")
+        return cnt, mass
+
+    def observe_sinks(self):
+        """Sink-observation records of the last advance: dict of obs, id, time, mass."""
+        nrec = C.c_int64(0)
+        cap = int(self.n)
+        out = dict(obs=np.empty(cap, np.int32), id=np.empty(cap, np.uint64), time=np.empty(cap),
+                   mass=np.empty(cap))
+        self._check(self.lib.mprw_observe_sinks(self.h, cap, _p(out["obs"], _ip), _p(out["id"], _up),
+                                                _p(out["time"], _dp), _p(out["mass"], _dp), C.byref(nrec)),
+                    "mprw_observe_sinks")
+        m = nrec.value
+        return {k: v[:m] for k, v in out.items()}
 
     def set_stream(self, stream_ptr: int):
         self._check(self.lib.mprw_set_stream(self.h, C.c_void_p(stream_ptr)), "mprw_set_stream")
