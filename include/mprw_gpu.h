@@ -75,7 +75,7 @@ typedef struct {
   double ts_param[2];         /* timeStepParameters(1:2)                     */
   int32_t advection_kind;     /* 1 EXPONENTIAL (Newton exit time), 2 EULERIAN */
   int32_t dim_mask[3];        /* random-walk dimension mask                  */
-  int32_t dispersion_model;   /* 0 linear isotropic                          */
+  int32_t dispersion_model;   /* 0 linear isotropic, 1 linear axisymmetric   */
   int32_t stop_weak_sinks;
   int32_t stop_weak_sources;
   int32_t backward;
@@ -107,6 +107,9 @@ typedef struct {
   const double *dm_eff;
   int32_t uniform_dispersion;
   int32_t steady_state;
+  const double *alpha_lv;     /* axisymmetric model: vertical longitudinal and */
+  const double *alpha_tv;     /* transverse dispersivities (layout of alpha_l), */
+                              /* or NULL: equal to alpha_l / alpha_t           */
 } mprw_flow_desc;
 
 /* Create a handle on the current CUDA device.

@@ -32,6 +32,7 @@ struct mprw_handle {
   int64_t nja_cap = 0;
   double *d_flowja = nullptr, *d_bflow = nullptr, *d_por = nullptr, *d_ret = nullptr, *d_heads = nullptr;
   double *d_src = nullptr, *d_snk = nullptr, *d_aL = nullptr, *d_aT = nullptr, *d_dm = nullptr;
+  double *d_aLV = nullptr, *d_aTV = nullptr;
   int32_t *d_ibts = nullptr, *d_icb = nullptr, *d_ctype = nullptr, *d_zones = nullptr;
   CellBase base{};
   uint8_t *d_massb = nullptr;
@@ -108,7 +109,7 @@ cudaError_t upload(mprw_handle *h, T **p, const T *src, size_t count) {
 void free_all(mprw_handle *h) {
   void *ptrs[] = {h->d_delr, h->d_delc, h->d_top, h->d_botm, h->d_colL, h->d_colR, h->d_rowF, h->d_rowB,
                   h->d_sattop, h->d_ia, h->d_ja, h->d_flowja, h->d_bflow, h->d_por, h->d_ret, h->d_heads,
-                  h->d_src, h->d_snk, h->d_aL, h->d_aT, h->d_dm, h->d_ibts, h->d_icb, h->d_ctype,
+                  h->d_src, h->d_snk, h->d_aL, h->d_aT, h->d_dm, h->d_aLV, h->d_aTV, h->d_ibts, h->d_icb, h->d_ctype,
                   h->d_zones, h->base.q, h->base.dz, h->base.conn, h->base.flags, h->d_massb, h->d_rec64,
                   h->d_rec32, h->d_cell, h->d_status, h->d_x, h->d_y, h->d_z, h->d_t, h->d_mass,
                   h->d_stage, h->d_ctr, h->d_id, h->d_perm, h->d_counters, h->scratch};
@@ -192,7 +193,8 @@ int mprw_create(mprw_handle **out, const mprw_grid_desc *gd, const mprw_options 
   *out = h;
   if (o->advection_kind != 1 && o->advection_kind != 2)
     return fail(h, MPRW_E_INVAL, "advection_kind: 1 (EXPONENTIAL) or 2 (EULERIAN)");
-  if (o->dispersion_model != 0) return fail(h, MPRW_E_INVAL, "dispersion_model: only linear isotropic (0)");
+  if (o->dispersion_model != 0 && o->dispersion_model != 1)
+    return fail(h, MPRW_E_INVAL, "dispersion_model: 0 (linear isotropic) or 1 (linear axisymmetric)");
   if (o->time_step_kind < 1 || o->time_step_kind > 4) return fail(h, MPRW_E_INVAL, "time_step_kind");
   if (o->precision != MPRW_FP64 && o->precision != MPRW_MIXED) return fail(h, MPRW_E_INVAL, "precision");
   h->opt = *o;
@@ -285,6 +287,8 @@ int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *f) {
   CK(upload(h, &h->d_aL, f->alpha_l, nd));
   CK(upload(h, &h->d_aT, f->alpha_t, nd));
   CK(upload(h, &h->d_dm, f->dm_eff, nd));
+  if (f->alpha_lv) CK(upload(h, &h->d_aLV, f->alpha_lv, nd));
+  if (f->alpha_tv) CK(upload(h, &h->d_aTV, f->alpha_tv, nd));
   // SaturatedTop (FlowModelData.f90:258-279) for ConvertToModelXYZ
   std::vector<double> sat(h->h_top_cell);
   {
@@ -329,6 +333,9 @@ int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *f) {
   in.alpha_l = h->d_aL;
   in.alpha_t = h->d_aT;
   in.dm_eff = h->d_dm;
+  in.alpha_lv = f->alpha_lv ? h->d_aLV : nullptr;
+  in.alpha_tv = f->alpha_tv ? h->d_aTV : nullptr;
+  in.dispersion_model = h->opt.dispersion_model;
   in.uniform_dispersion = f->uniform_dispersion;
   in.steady_state = f->steady_state;
   in.time_step_kind = h->opt.time_step_kind;
@@ -454,6 +461,7 @@ int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_do
     a.d2 = h->d2;
     a.seed = h->opt.rng_seed;
     a.exp_adv = h->opt.advection_kind == 1;
+    a.axi = h->opt.dispersion_model == 1;
     // EULERIAN MIXED is compiled for 3 resident blocks per SM (80 registers)
     int blocks = h->sms * (a.exp_adv ? 1 : 3);
     int64_t need = (h->n + threads - 1) / threads;
@@ -483,6 +491,7 @@ int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_do
     a.d2 = h->d2;
     a.seed = h->opt.rng_seed;
     a.exp_adv = h->opt.advection_kind == 1;
+    a.axi = h->opt.dispersion_model == 1;
     int blocks = h->sms * 1;
     int64_t need = (h->n + threads - 1) / threads;
     if (need < blocks) blocks = (int)need;

@@ -33,6 +33,7 @@ struct __align__(16) CellRec {
   R vb[3][8];    // corner velocity q_c/phi_c, trilinear monomials
   R aL, aT, dm, two_over_r;
   R v2[3];       // VX2, VY2, VZ2 (exit-face solver needs face values)
+  R aLV, aTV;    // vertical dispersivities (axisymmetric model; = aL, aT otherwise)
   double dtcell; // ComputeRandomWalkTimeStep (TrackSubCell.F90:1376-1458)
   double sqrt_dtcell;
   int32_t conn[6];     // 0-based neighbour, -1 = boundary face or inactive neighbour

@@ -25,6 +25,7 @@ struct AdvanceArgs {
   int ndim, d1, d2;
   uint64_t seed;
   int exp_adv;  // EXPONENTIAL advection with the Newton exit time (else EULERIAN)
+  int axi;      // linear axisymmetric dispersion (else linear isotropic)
 };
 
 template <typename R>
@@ -46,7 +47,9 @@ struct PrepInputs {
   const double *source_flow, *sink_flow;
   const int32_t *zones;
   const double *alpha_l, *alpha_t, *dm_eff;
+  const double *alpha_lv, *alpha_tv;  // axisymmetric model (null: = alpha_l, alpha_t)
   int32_t uniform_dispersion, steady_state;
+  int32_t dispersion_model;           // 0 linear isotropic, 1 linear axisymmetric
   // options
   int32_t time_step_kind;
   double ts_param0, ts_param1;

@@ -169,8 +169,9 @@ __constant__ int8_t kSub[6][2] = {{2, 3}, {2, 3}, {4, 5}, {4, 5}, {0, 1}, {0, 1}
 
 template <typename R>
 __device__ void store_record(CellRec<R> *dst, const double v1[3], const double v2[3], const double d[3],
-                             const double div[3][7], const double vb[3][8], double aL, double aT, double dm,
-                             double tr, double dtcell, const int32_t conn[6], int32_t es, uint32_t mb) {
+                             const double div[3][7], const double vb[3][8], double aL, double aT, double aLV,
+                             double aTV, double dm, double tr, double dtcell, const int32_t conn[6], int32_t es,
+                             uint32_t mb) {
   CellRec<R> r;
   for (int m = 0; m < 3; ++m) {
     r.v1[m] = (R)v1[m];
@@ -183,6 +184,8 @@ __device__ void store_record(CellRec<R> *dst, const double v1[3], const double v
   }
   r.aL = (R)aL;
   r.aT = (R)aT;
+  r.aLV = (R)aLV;
+  r.aTV = (R)aTV;
   r.dm = (R)dm;
   r.two_over_r = (R)tr;
   r.dtcell = dtcell;
@@ -217,6 +220,7 @@ __global__ void prep_rec_kernel(PrepInputs in, CellBase base, const uint8_t *mas
   v[5] = sign * Q[5] / DX / DY / phi / R;
   int di = in.uniform_dispersion ? 0 : n;
   double aL = in.alpha_l[di], aT = in.alpha_t[di], dm = in.dm_eff[di];
+  double aLV = in.alpha_lv ? in.alpha_lv[di] : aL, aTV = in.alpha_tv ? in.alpha_tv[di] : aT;
   // ComputeRandomWalkTimeStep
   double mx = fmax(fabs(v[0]), fabs(v[1])), my = fmax(fabs(v[2]), fabs(v[3])), mz = fmax(fabs(v[4]), fabs(v[5]));
   double dtcell = 0.0;
@@ -317,6 +321,28 @@ __global__ void prep_rec_kernel(PrepInputs in, CellBase base, const uint8_t *mas
       qp[6] = qp[0] + qp[3];
       for (int m = 0; m < 7; ++m) qp[m] = qp[m] / qc[c][3];
     }
+    if (in.dispersion_model == 1) {
+      // pr_CornerDispersionAxisymmetric (TrackSubCell.F90:3117-3303): per
+      // corner alphaL/alphaT blended with cosinesq = qz**2/|q| (as written),
+      // Dxyx from the xx product (as written)
+      if (qc[c][3] > 0.0 && qp[6] > 0.0) qp[7] = (qc[c][2] * qc[c][2]) / (qc[c][0] * qc[c][0] + qc[c][1] * qc[c][1]);
+      const double pD = phic[c] * dm;
+      double cosinesq = 0.0;
+      if (qc[c][3] > 0.0) cosinesq = qc[c][2] * qc[c][2] / qc[c][3];
+      const double aLc = aL + cosinesq * (aLV - aL);
+      const double aTc = aTV + cosinesq * (aT - aTV);
+      const double aLmTc = aLc - aTc;
+      D[0][c] = pD + (aLc + aTc * qp[7]) * qp[0] + aT * qp[3] * (1.0 + qp[7]);
+      D[1][c] = pD + aT * qp[0] * (1.0 + qp[7]) + qp[3] * (aLc + aTc * qp[7]);
+      D[3][c] = (aLc - aT * (1.0 + qp[7]) + aTc * qp[7]) * qp[0];
+      D[5][c] = D[3][c];
+      D[2][c] = pD + aTc * qp[6] + aLc * qp[5];
+      D[4][c] = aLmTc * qp[2];
+      D[6][c] = aLmTc * qp[4];
+      D[7][c] = D[4][c];
+      D[8][c] = D[6][c];
+      continue;
+    }
     double qn = (c == 0) ? qc[0][3] : qc[1][3];
     double aTQ = aT * qn + phic[c] * dm;
     D[0][c] = aTQ + aLmT * qp[0];
@@ -380,8 +406,10 @@ __global__ void prep_rec_kernel(PrepInputs in, CellBase base, const uint8_t *mas
   }
   double v1[3] = {v[0], v[2], v[4]}, v2[3] = {v[1], v[3], v[5]}, d[3] = {DX, DY, DZ};
   double tr = 2.0 / R;
-  if (rec64) store_record<double>(rec64 + n, v1, v2, d, div, vb, aL, aT, dm, tr, dtcell, conn, es, massb[n]);
-  if (rec32) store_record<float>(rec32 + n, v1, v2, d, div, vb, aL, aT, dm, tr, dtcell, conn, es, massb[n]);
+  if (rec64)
+    store_record<double>(rec64 + n, v1, v2, d, div, vb, aL, aT, aLV, aTV, dm, tr, dtcell, conn, es, massb[n]);
+  if (rec32)
+    store_record<float>(rec32 + n, v1, v2, d, div, vb, aL, aT, aLV, aTV, dm, tr, dtcell, conn, es, massb[n]);
 }
 
 cudaError_t launch_prep(const PrepInputs &in, CellBase base, uint8_t *massb, CellRec<double> *rec64,

@@ -25,7 +25,7 @@ namespace mprw {
 // conflict-free for a warp reading the same field.
 enum : int {
   F_V1 = 0, F_DV = 3, F_D = 6, F_INVD = 9, F_DIV = 12, F_VB = 33,
-  F_AL = 57, F_AT = 58, F_DM = 59, F_2R = 60, F_V2 = 61, NFIELDS = 64
+  F_AL = 57, F_AT = 58, F_DM = 59, F_2R = 60, F_V2 = 61, F_ALV = 64, F_ATV = 65, NFIELDS = 66
 };
 
 template <typename R>
@@ -94,14 +94,27 @@ struct Normals<float> {
   }
 };
 
-// pr_DisplacementRandomDischarge (3-D :2821-2928, 2-D :2931-3028, 1-D :3031-3113)
-template <typename R>
+// pr_DisplacementRandomDischarge (3-D :2821-2928, 2-D :2931-3028, 1-D :3031-3113).
+// AXI (linear axisymmetric model): alphaL, alphaT are blended with the
+// particle's velocity (vpx, vpy, vpz) as pr_RWPTDisplacementsAxisymmetric
+// does (:750-806, cosinesq = vz**2/|v| as written), and the horizontal
+// transverse terms use alphaTH (pr_DisplacementRandomDischargeAxisymmetric
+// {,2D,1D}, :3306-3604).
+template <typename R, bool AXI>
 __device__ __forceinline__ void random_displacement(const Lane<R> &F, int ndim, int d1, int d2, R x, R y,
-                                                    R z, uint64_t seed, uint64_t id, uint64_t &ctr, R &bx,
-                                                    R &by, R &bz) {
+                                                    R z, R vpx, R vpy, R vpz, uint64_t seed, uint64_t id,
+                                                    uint64_t &ctr, R &bx, R &by, R &bz) {
   const R zero = R(0);
   R xy = x * y, xz = x * z, yz = y * z, xyz = xy * z;
   R aL = F(F_AL), aT = F(F_AT), dm = F(F_DM), tr = F(F_2R);
+  R aTH = aT;
+  if constexpr (AXI) {
+    const R vnorm = sqrt(vpx * vpx + vpy * vpy + vpz * vpz);
+    R cosinesq = zero;
+    if (vnorm > zero) cosinesq = vpz * vpz / vnorm;
+    aL = aL + cosinesq * (F(F_ALV) - aL);
+    aT = F(F_ATV) + cosinesq * (aTH - F(F_ATV));
+  }
   if (ndim == 3) {
     R vx = tril(F, F_VB + 0, x, y, z, xy, xz, yz, xyz);
     R vy = tril(F, F_VB + 8, x, y, z, xy, xz, yz, xyz);
@@ -114,6 +127,7 @@ __device__ __forceinline__ void random_displacement(const Lane<R> &F, int ndim, 
       R nrm = n2 * inv;
       R sL = sqrt(tr * fma(aL, nrm, dm));
       R sT = sqrt(tr * fma(aT, nrm, dm));
+      R sTH = AXI ? sqrt(tr * fma(aTH, nrm, dm)) : sT;
       R sLi = sL * inv;
       B11 = vx * sLi;
       B21 = vy * sLi;
@@ -126,7 +140,7 @@ __device__ __forceinline__ void random_displacement(const Lane<R> &F, int ndim, 
         R sTixy = sTi * invxy;
         B12 = -(vx * vz) * sTixy;
         B22 = -(vy * vz) * sTixy;
-        R sTxy = sT * invxy;
+        R sTxy = sTH * invxy;
         B13 = -vy * sTxy;
         B23 = vx * sTxy;
       }
@@ -145,7 +159,7 @@ __device__ __forceinline__ void random_displacement(const Lane<R> &F, int ndim, 
       R inv = rsqrt(n2);
       R nrm = n2 * inv;
       R sLi = sqrt(tr * fma(aL, nrm, dm)) * inv;
-      R sTi = sqrt(tr * fma(aT, nrm, dm)) * inv;
+      R sTi = sqrt(tr * fma(aTH, nrm, dm)) * inv;
       B11 = v1 * sLi;
       B21 = v2 * sLi;
       B12 = -v2 * sTi;
@@ -445,7 +459,7 @@ enum : int { PASS_CONTINUE = 0, PASS_MAXTIME = 1, PASS_EXIT = 2, PASS_UNDEFINED 
 // One pass of the `do while (continueTimeLoop)` body, TrackSubCell.F90:956-1368.
 // On PASS_MAXTIME / PASS_EXIT the final location is (ox,oy,oz,V.t); on
 // PASS_UNDEFINED the caller uses the last recorded point.
-template <typename R, bool EXP>
+template <typename R, bool EXP, bool AXI>
 __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double maxTime, int ndim, int d1, int d2,
                        uint64_t seed, uint64_t id, uint64_t &ctr, R &ox, R &oy, R &oz) {
   const R zero = R(0), one = R(1), half = R(0.5);
@@ -473,7 +487,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
   R ddy = divc(F, F_DIV + 7, x, y, z, xy, xz, yz);
   R ddz = divc(F, F_DIV + 14, x, y, z, xy, xz, yz);
   R bx, by, bz;
-  random_displacement(F, ndim, d1, d2, x, y, z, seed, id, ctr, bx, by, bz);
+  random_displacement<R, AXI>(F, ndim, d1, d2, x, y, z, vx, vy, vz, seed, id, ctr, bx, by, bz);
   // advection displacement: EULERIAN v dt, EXPONENTIAL (FP64) v (e^{dv dt}-1)/dv
   // with dv = (V2 - V1)/D of the cell (pr_AdvectionDisplacement*, :1487-1573)
   double dvx = 0.0, dvy = 0.0, dvz = 0.0;
@@ -688,7 +702,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
 // structured and the loop head re-converges the warp, so the common pass body
 // runs with every tracking lane active; the loop ends when no lane of the warp
 // has work.
-template <typename R, bool EXP>
+template <typename R, bool EXP, bool AXI>
 __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1) rwpt_advance_kernel(AdvanceArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw) + threadIdx.x;
@@ -816,7 +830,7 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
       if (++V.passes > kMaxStepsPerVisit) {
         r = PASS_UNDEFINED;
       } else {
-        r = rw_pass<R, EXP>(V, F, massb, a.t_end, a.ndim, a.d1, a.d2, a.seed, id, ctr, ox, oy, oz);
+        r = rw_pass<R, EXP, AXI>(V, F, massb, a.t_end, a.ndim, a.d1, a.d2, a.seed, id, ctr, ox, oy, oz);
         ++my_passes;
       }
       if (r == PASS_MAXTIME) {
@@ -873,7 +887,8 @@ size_t advance_smem_bytes(int threads) {
 template <typename R>
 cudaError_t launch_advance(const AdvanceArgs<R> &a, int blocks, int threads, cudaStream_t s) {
   size_t smem = advance_smem_bytes<R>(threads);
-  auto kern = a.exp_adv ? rwpt_advance_kernel<R, true> : rwpt_advance_kernel<R, false>;
+  auto kern = a.exp_adv ? (a.axi ? rwpt_advance_kernel<R, true, true> : rwpt_advance_kernel<R, true, false>)
+                        : (a.axi ? rwpt_advance_kernel<R, false, true> : rwpt_advance_kernel<R, false, false>);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   kern<<<blocks, threads, smem, s>>>(a);

@@ -62,7 +62,8 @@ class FlowDesc(C.Structure):
                 ("porosity", _dp), ("retardation", _dp), ("iboundts", _ip), ("icboundts", _ip),
                 ("default_icbound", C.c_int32), ("heads", _dp), ("celltype", _ip), ("source_flow", _dp),
                 ("sink_flow", _dp), ("zones", _ip), ("alpha_l", _dp), ("alpha_t", _dp), ("dm_eff", _dp),
-                ("uniform_dispersion", C.c_int32), ("steady_state", C.c_int32)]
+                ("uniform_dispersion", C.c_int32), ("steady_state", C.c_int32), ("alpha_lv", _dp),
+                ("alpha_tv", _dp)]
 
 
 _lib = None
@@ -162,7 +163,7 @@ class Tracker:
                     dm=_f64(f.dm_eff))
         opt = dict(icb=(f.icboundts, _i32, _ip), bf=(f.boundary_flows, _f64, _dp), hd=(f.heads, _f64, _dp),
                    ct=(f.celltype, _i32, _ip), src=(f.source_flow, _f64, _dp), snk=(f.sink_flow, _f64, _dp),
-                   zn=(f.zones, _i32, _ip))
+                   zn=(f.zones, _i32, _ip), aLV=(f.alpha_lv, _f64, _dp), aTV=(f.alpha_tv, _f64, _dp))
         ptrs = {}
         for k, (arr, conv, pt) in opt.items():
             keep[k] = None if arr is None else conv(arr)
@@ -188,6 +189,8 @@ class Tracker:
         fd.dm_eff = _p(keep["dm"], _dp)
         fd.uniform_dispersion = int(f.uniform_dispersion)
         fd.steady_state = int(f.steady_state)
+        fd.alpha_lv = ptrs["aLV"]
+        fd.alpha_tv = ptrs["aTV"]
         self._check(self.lib.mprw_load_flow(self.h, C.byref(fd)), "mprw_load_flow")
 
     def set_particles(self, p: Particles):

@@ -66,6 +66,8 @@ class Flow:
     source_flow: Optional[np.ndarray] = None
     sink_flow: Optional[np.ndarray] = None
     zones: Optional[np.ndarray] = None
+    alpha_lv: Optional[np.ndarray] = None   # axisymmetric model: vertical dispersivities
+    alpha_tv: Optional[np.ndarray] = None   # (None: equal to alpha_l / alpha_t)
 
 
 @dataclass

@@ -240,7 +240,7 @@ typedef struct {
   double Porosity, Retardation, SourceFlow, SinkFlow;
   double Q[6];
   int SubFaceConn[6], MassBoundary[6];
-  double alphaLH, alphaTH, dMEff;
+  double alphaLH, alphaTH, alphaLV, alphaTV, dMEff;
   int dry, partiallyDry;
 } cdata;
 
@@ -300,6 +300,8 @@ static void fill_cell(const grid_t *g, int n, cdata *c) {
   int di = f->uniform_dispersion ? 0 : n0;
   c->alphaLH = f->alpha_l[di];
   c->alphaTH = f->alpha_t[di];
+  c->alphaLV = f->alpha_lv ? f->alpha_lv[di] : c->alphaLH;
+  c->alphaTV = f->alpha_tv ? f->alpha_tv[di] : c->alphaTH;
   c->dMEff = f->dm_eff[di];
 }
 
@@ -351,7 +353,7 @@ typedef struct {
   double DX, DY, DZ;
   double VX1, VX2, VY1, VY2, VZ1, VZ2;
   int Connection[6], MassBoundary[6];
-  double Porosity, Retardation, alphaLH, alphaTH, dMEff;
+  double Porosity, Retardation, alphaLH, alphaTH, alphaLV, alphaTV, dMEff;
   int dry, partiallyDry;
   double qC[8][4];   /* qCorner000..111 (qx,qy,qz,|q|) */
   double phiC[8];    /* porosity000..111 */
@@ -382,6 +384,8 @@ static void fill_subcell(cdata *c, int backward, subcell_t *s) {
   s->Retardation = c->Retardation;
   s->alphaLH = c->alphaLH;
   s->alphaTH = c->alphaTH;
+  s->alphaLV = c->alphaLV;
+  s->alphaTV = c->alphaTV;
   s->dMEff = c->dMEff;
 }
 
@@ -423,7 +427,8 @@ static const int CPI[8][6] = {{1, 2, 7, 8, 13, 14}, {4, 5, 7, 8, 13, 15}, {1, 3,
                               {1, 3, 10, 12, 16, 17}, {4, 6, 10, 11, 13, 15}};
 
 /* pr_ComputeCornerVariables, TrackSubCell.F90:3667-3850 */
-static void corner_variables(const grid_t *g, int n, cdata *center, subcell_t *s, int uniform_porosity) {
+static void corner_variables(const grid_t *g, int n, cdata *center, subcell_t *s, int uniform_porosity,
+                             int dispersion_model) {
   cdata nb[18];
   fill_neighbours(g, n, nb);
   double nflow[18][6], narea[18][3], nvol[18], nphi[18];
@@ -505,6 +510,31 @@ static void corner_variables(const grid_t *g, int n, cdata *center, subcell_t *s
       for (int m = 0; m < 7; ++m) qp[m] = qp[m] / q[3];
     }
   }
+  if (dispersion_model == 1) {
+    /* pr_CornerDispersionAxisymmetric, :3117-3303: per corner, alphaL/alphaT
+     * blended with cosinesq = qz**2/|q| (as written: over |q|, not |q|**2);
+     * Dxyx uses the xx product (as written) */
+    const double aLH = s->alphaLH, aLV = s->alphaLV, aTH = s->alphaTH, aTV = s->alphaTV, dm = s->dMEff;
+    for (int corner = 0; corner < 8; ++corner) {
+      const double *q = s->qC[corner], *qp = qprod[corner];
+      const double pD = s->phiC[corner] * dm;
+      double cosinesq = 0.0;
+      if (q[3] > 0.0) cosinesq = q[2] * q[2] / q[3];
+      const double aL = aLH + cosinesq * (aLV - aLH);
+      const double aT = aTV + cosinesq * (aTH - aTV);
+      const double aLmT = aL - aT;
+      s->D[0][corner] = pD + (aL + aT * qp[7]) * qp[0] + aTH * qp[3] * (1.0 + qp[7]);
+      s->D[1][corner] = pD + aTH * qp[0] * (1.0 + qp[7]) + qp[3] * (aL + aT * qp[7]);
+      s->D[3][corner] = (aL - aTH * (1.0 + qp[7]) + aT * qp[7]) * qp[0];
+      s->D[5][corner] = s->D[3][corner];
+      s->D[2][corner] = pD + aT * qp[6] + aL * qp[5];
+      s->D[4][corner] = aLmT * qp[2];
+      s->D[6][corner] = aLmT * qp[4];
+      s->D[7][corner] = s->D[4][corner];
+      s->D[8][corner] = s->D[6][corner];
+    }
+    return;
+  }
   /* pr_CornerDispersionLinearIsotropic, :2557-2691 (quirk: corners 3..8 use
    * qCorner100(4)) */
   double dMEff = s->dMEff, aL = s->alphaLH, aT = s->alphaTH;
@@ -580,11 +610,24 @@ static void divergence(const subcell_t *s, double x, double y, double z, double 
   *dz = (dDxzdx + dDyzdy + dDzzdz) / s->Porosity / s->Retardation;
 }
 
-/* pr_DisplacementRandomDischarge{,2D,1D}, :2821-3113 */
+/* pr_DisplacementRandomDischarge{,2D,1D}, :2821-3113; axisymmetric model:
+ * pr_RWPTDisplacementsAxisymmetric :750-806 blends alphaL/alphaT with the
+ * particle's velocity (cosinesq = vz**2/|v|, as written) and
+ * pr_DisplacementRandomDischargeAxisymmetric{,2D,1D} :3306-3604 use alphaTH
+ * for the horizontal transverse terms */
 static void random_displacement(const subcell_t *s, const orc_options *o, const int *dims, int ndim,
-                                double x, double y, double z, rng_t *rng,
+                                double x, double y, double z, double vx, double vy, double vz, rng_t *rng,
                                 double *dBx, double *dBy, double *dBz) {
   double aL = s->alphaLH, aT = s->alphaTH, dm = s->dMEff, R = s->Retardation;
+  double aTH = aT;  /* horizontal transverse term of the axisymmetric model */
+  if (o->dispersion_model == 1) {
+    const double vnorm = sqrt(pow(vx, 2.0) + pow(vy, 2.0) + pow(vz, 2.0));
+    double cosinesq = 0.0;
+    if (vnorm > 0.0) cosinesq = pow(vz, 2.0) / vnorm;
+    aL = s->alphaLH + cosinesq * (s->alphaLV - s->alphaLH);
+    aT = s->alphaTV + cosinesq * (s->alphaTH - s->alphaTV);
+    aTH = s->alphaTH;
+  }
   double vc[3][8];
   for (int c = 0; c < 8; ++c)
     for (int m = 0; m < 3; ++m) vc[m][c] = s->qC[c][m] / s->phiC[c];
@@ -603,9 +646,9 @@ static void random_displacement(const subcell_t *s, const orc_options *o, const 
       B32 = vBnormxy * sqrt(2 * (aT * vBnorm + dm) / R) / vBnorm;
       if (vBnormxy > 0.0) {
         B12 = -(vBx * vBz * sqrt(2 * (aT * vBnorm + dm) / R) / vBnorm / vBnormxy);
-        B13 = -(vBy * sqrt(2 * (aT * vBnorm + dm) / R) / vBnormxy);
+        B13 = -(vBy * sqrt(2 * (aTH * vBnorm + dm) / R) / vBnormxy);
         B22 = -(vBy * vBz * sqrt(2 * (aT * vBnorm + dm) / R) / vBnorm / vBnormxy);
-        B23 = vBx * sqrt(2 * (aT * vBnorm + dm) / R) / vBnormxy;
+        B23 = vBx * sqrt(2 * (aTH * vBnorm + dm) / R) / vBnormxy;
       }
     }
     double rx = rng_normal(rng), ry = rng_normal(rng), rz = rng_normal(rng);
@@ -621,8 +664,8 @@ static void random_displacement(const subcell_t *s, const orc_options *o, const 
     if (vBnorm > 0.0) {
       B11 = vB1 * sqrt(2 * (aL * vBnorm + dm) / R) / vBnorm;
       B21 = vB2 * sqrt(2 * (aL * vBnorm + dm) / R) / vBnorm;
-      B12 = -(vB2 * sqrt(2 * (aT * vBnorm + dm) / R) / vBnorm);
-      B22 = vB1 * sqrt(2 * (aT * vBnorm + dm) / R) / vBnorm;
+      B12 = -(vB2 * sqrt(2 * (aTH * vBnorm + dm) / R) / vBnorm);
+      B22 = vB1 * sqrt(2 * (aTH * vBnorm + dm) / R) / vBnorm;
     }
     double r1 = rng_normal(rng), r2 = rng_normal(rng);
     double dB[3] = {0, 0, 0};
@@ -1039,7 +1082,7 @@ static void track_subcell(const subcell_t *s, const orc_options *o, const int *d
     vy = (1.0 - y) * s->VY1 + y * s->VY2;
     vz = (1.0 - z) * s->VZ1 + z * s->VZ2;
     divergence(s, x, y, z, &ddx, &ddy, &ddz);
-    random_displacement(s, o, dims, ndim, x, y, z, rng, &bx, &by, &bz);
+    random_displacement(s, o, dims, ndim, x, y, z, vx, vy, vz, rng, &bx, &by, &bz);
     advection(s, kind, dt, vx, vy, vz, &ax, &ay, &az);
     dxrw = ax + ddx * dt + bx * sqrt(dt);
     dyrw = ay + ddy * dt + by * sqrt(dt);
@@ -1256,7 +1299,7 @@ static int track_path(const grid_t *g, const orc_options *o, const int *dims, in
     }
     subcell_t s;
     fill_subcell(&c, o->backward, &s);
-    corner_variables(g, n, &c, &s, o->uniform_porosity);
+    corner_variables(g, n, &c, &s, o->uniform_porosity, o->dispersion_model);
     scres_t r;
     track_subcell(&s, o, dims, ndim, stopIfNoSubCellExit, loc.x, loc.y, loc.z, loc.t, maximumTime, rng, &r, steps);
     switch (r.status) {
@@ -1397,7 +1440,7 @@ int orc_cell_record(const orc_flow *f, const orc_options *o, int cell, double *v
   subcell_t s;
   fill_cell(&g, cell, &c);
   fill_subcell(&c, o->backward, &s);
-  corner_variables(&g, cell, &c, &s, o->uniform_porosity);
+  corner_variables(&g, cell, &c, &s, o->uniform_porosity, o->dispersion_model);
   double v[6] = {s.VX1, s.VX2, s.VY1, s.VY2, s.VZ1, s.VZ2};
   for (int q = 0; q < 6; ++q) {
     vface6[q] = v[q];

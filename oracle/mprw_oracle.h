@@ -50,6 +50,8 @@ typedef struct {
   const double *dm_eff;
   int           uniform_dispersion;
   int           steady_state;
+  const double *alpha_lv;    /* vertical dispersivities of the axisymmetric  */
+  const double *alpha_tv;    /* model (layout of alpha_l), or NULL: = alpha_l / alpha_t */
 } orc_flow;
 
 typedef struct {
@@ -63,6 +65,7 @@ typedef struct {
                                 1 = Philox4x32-10 per-particle counters + Irwin-Hall(12) */
   uint64_t seed;             /* Philox key (rng_kind 1)                 */
   int    nthreads;           /* >1: OpenMP particle loop (rng_kind 0 uses one stream per thread) */
+  int    dispersion_model;   /* 0 linear isotropic, 1 linear axisymmetric  */
 } orc_options;
 
 /* Particle status codes of the driver (MPathRW.F90:1337-1403). */

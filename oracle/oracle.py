@@ -32,14 +32,15 @@ class OrcFlow(C.Structure):
                 ("bflow", _dp), ("porosity", _dp), ("retardation", _dp), ("ibound", _ip), ("iboundts", _ip),
                 ("icboundts", _ip), ("default_icbound", C.c_int), ("heads", _dp), ("celltype", _ip),
                 ("source_flow", _dp), ("sink_flow", _dp), ("zones", _ip), ("alpha_l", _dp), ("alpha_t", _dp),
-                ("dm_eff", _dp), ("uniform_dispersion", C.c_int), ("steady_state", C.c_int)]
+                ("dm_eff", _dp), ("uniform_dispersion", C.c_int), ("steady_state", C.c_int),
+                ("alpha_lv", _dp), ("alpha_tv", _dp)]
 
 
 class OrcOptions(C.Structure):
     _fields_ = [("time_step_kind", C.c_int), ("ts_param", C.c_double * 2), ("advection_kind", C.c_int),
                 ("dim_mask", C.c_int * 3), ("stop_weak_sinks", C.c_int), ("stop_weak_sources", C.c_int),
                 ("backward", C.c_int), ("stop_zone", C.c_int), ("uniform_porosity", C.c_int),
-                ("rng_kind", C.c_int), ("seed", C.c_uint64), ("nthreads", C.c_int)]
+                ("rng_kind", C.c_int), ("seed", C.c_uint64), ("nthreads", C.c_int), ("dispersion_model", C.c_int)]
 
 
 _lib = None
@@ -96,7 +97,8 @@ class _Inputs:
                       por=f64(flow.porosity), ret=f64(flow.retardation), ibts=i32(flow.iboundts),
                       icb=i32(flow.icboundts), heads=f64(flow.heads), ct=i32(flow.celltype),
                       src=f64(flow.source_flow), snk=f64(flow.sink_flow), zn=i32(flow.zones),
-                      aL=f64(flow.alpha_l), aT=f64(flow.alpha_t), dm=f64(flow.dm_eff))
+                      aL=f64(flow.alpha_l), aT=f64(flow.alpha_t), dm=f64(flow.dm_eff),
+                      aLV=f64(getattr(flow, "alpha_lv", None)), aTV=f64(getattr(flow, "alpha_tv", None)))
         k = self.k
         self.f = OrcFlow(grid.nlay, grid.nrow, grid.ncol, _p(k["delr"], _dp), _p(k["delc"], _dp),
                          _p(k["top"], _dp), _p(k["botm"], _dp), _p(k["ia"], _ip), _p(k["ja"], _ip),
@@ -104,7 +106,8 @@ class _Inputs:
                          _p(k["ret"], _dp), _p(k["ibts"], _ip), _p(k["ibts"], _ip), _p(k["icb"], _ip),
                          int(flow.default_icbound), _p(k["heads"], _dp), _p(k["ct"], _ip), _p(k["src"], _dp),
                          _p(k["snk"], _dp), _p(k["zn"], _ip), _p(k["aL"], _dp), _p(k["aT"], _dp),
-                         _p(k["dm"], _dp), int(flow.uniform_dispersion), int(flow.steady_state))
+                         _p(k["dm"], _dp), int(flow.uniform_dispersion), int(flow.steady_state),
+                         _p(k["aLV"], _dp), _p(k["aTV"], _dp))
         o = OrcOptions()
         o.time_step_kind = opt.time_step_kind
         o.ts_param[0], o.ts_param[1] = float(opt.ts_param[0]), float(opt.ts_param[1])
@@ -119,6 +122,7 @@ class _Inputs:
         o.rng_kind = rng_kind
         o.seed = int(opt.rng_seed) & 0xFFFFFFFFFFFFFFFF
         o.nthreads = nthreads
+        o.dispersion_model = int(getattr(opt, "dispersion_model", 0))
         self.o = o
 
 

@@ -227,3 +227,22 @@ def test_exponential_dispersion_heterogeneous(gpu_lib):
     op, os_ = run_oracle(g, f, opt, p, iv)
     _compare_same_rng(gp, op, g, f, tol=1e-6, min_frac=0.99)
     assert abs(gs - os_) <= 1e-3 * os_
+
+
+@pytest.mark.parametrize("advection", ["eulerian", "exponential"])
+def test_axisymmetric_dispersion_heterogeneous(gpu_lib, advection):
+    """Linear axisymmetric dispersion (dispersion model 1: four dispersivities,
+    TrackSubCell.F90:3117-3303, 750-806, 3306-3604) against the oracle on the
+    shared random stream."""
+    from mprw.model import EXPONENTIAL
+    g, f, p, opt, info = W.config2(n_particles=3000, nlay=4, nrow=12, ncol=30, seed=1, use_torch=False)
+    f.alpha_lv = np.array([0.2])
+    f.alpha_tv = np.array([0.01])
+    opt.dispersion_model = 1
+    if advection == "exponential":
+        opt.advection_kind = EXPONENTIAL
+    iv = [(0.0, 10.0), (10.0, 25.0)]
+    gp, gs = run_gpu(g, f, opt, p, iv)
+    op, os_ = run_oracle(g, f, opt, p, iv)
+    _compare_same_rng(gp, op, g, f, tol=1e-6, min_frac=0.99)
+    assert abs(gs - os_) <= 1e-3 * os_

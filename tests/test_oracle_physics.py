@@ -123,3 +123,31 @@ def test_exponential_advection_exact_in_linear_field():
     # relative 1e-6 tolerance here (NewtonRaphsonTimeStep..., :2451-2554)
     assert err[EXPONENTIAL] < 1e-9
     assert err[EULERIAN] > 1e-2
+
+
+def test_axisymmetric_dispersion_uniform_flow():
+    """Linear axisymmetric dispersion (pr_CornerDispersionAxisymmetric,
+    TrackSubCell.F90:3117-3303; displacements :750-806, :3306-3604) in uniform
+    flow along x: the plume spreads with alphaLH along x, alphaTH across in y
+    and alphaTV across in z (the isotropic model uses alphaT for both)."""
+    from mprw.model import ADV, Options
+    g, f = W.uniform_flow(ncol=60, nrow=21, nlay=21, q=0.3, porosity=0.3, alpha_l=0.1, alpha_t=0.02, dm=0.0)
+    f.alpha_lv = np.array([0.05])
+    f.alpha_tv = np.array([0.004])
+    n, t = 12000, 20.0
+    node = g.node(10, 10, 10)
+    p = Particles(cell=np.full(n, node, np.int32), lx=np.zeros(n), ly=np.full(n, 0.5), lz=np.full(n, 0.5),
+                  t=np.zeros(n), status=np.full(n, ACTIVE, np.int32), mass=np.ones(n),
+                  id=np.arange(n, dtype=np.uint64), rng_ctr=np.zeros(n, np.uint64))
+    k = {}
+    for model in (0, 1):
+        opt = Options(time_step_kind=ADV, ts_param=(0.1, 0.1), dispersion_model=model)
+        q, _ = O.advance(g, f, opt, p, 0.0, t, rng_kind=O.RNG_PHILOX, nthreads=8)
+        assert np.all(q.status == ACTIVE)
+        gx, gy, gz = O.global_xyz(g, f, q)
+        k[model] = (gx.var() / (2 * t), gy.var() / (2 * t), gz.var() / (2 * t))
+    # longitudinal: alphaLH (the interface-forcing scheme biases it low by < 12 %)
+    assert abs(k[1][0] - 0.1) < 0.012 and abs(k[0][0] - 0.1) < 0.012
+    assert abs(k[1][1] - 0.02) < 0.02 * 0.06        # alphaTH
+    assert abs(k[1][2] - 0.004) < 0.004 * 0.06      # alphaTV
+    assert abs(k[0][2] - 0.02) < 0.02 * 0.06        # isotropic: alphaT
