@@ -150,8 +150,13 @@ class ClockSampler:
 
 
 def build_workload(n_particles, rank=0, use_torch=True):
+    import tempfile
     from mprw import workloads as W
-    g, f, p, opt, info = W.config2(n_particles=n_particles, seed=0, use_torch=use_torch)
+    # the flow reaches the tracker the way a MODFLOW 6 run delivers it: written as
+    # .grb/.hds/.bud and read back through the binary readers
+    with tempfile.TemporaryDirectory() as d:
+        g, f, p, opt, info = W.config2(n_particles=n_particles, seed=0, use_torch=use_torch, mf6_dir=d)
+        info = dict(info, mf6_bytes=sum(os.path.getsize(x) for x in info["mf6_files"]))
     if rank:
         # weak scaling: every rank tracks its own particle set on the same field
         q = W.release_in_box(g, n_particles, 0.0, 10.0, 0.0, 100.0, float(g.botm[-1]), float(g.top[0]),
@@ -359,7 +364,9 @@ def main():
                                f"{args.particles} particles from the inlet slab, step = one 10-day interval "
                                "(advance + GPKDE reconstruction on the 1 m grid, density and histogram to host)",
                    "particles_per_gpu": args.particles, "interval_days": INTERVAL_D,
-                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"particles x{world}"},
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"particles x{world}",
+                   "flow_input": f"MODFLOW 6 binary .grb/.hds/.bud ({info['mf6_bytes']} B: FLOW-JA-FACE imeth 1, "
+                                 "CHD imeth 6) written from the CG solve and read back by mprw.mf6io"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": f"{peak_kind} hbm_gbs",
                      "traffic": None if tr_ps is None else tr_ps * steps_per_launch,

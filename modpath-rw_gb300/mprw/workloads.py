@@ -273,10 +273,24 @@ def config1(n_particles=100_000, pure_advection=False, precision=FP64):
     return g, f, p, opt
 
 
-def config2(n_particles=1_000_000, nlay=20, nrow=100, ncol=200, seed=0, precision=FP64, use_torch=None):
-    """200x100x20 lognormal K (sigma2 1, 10 m / 2 m), 1e6 particles in the 10 m inlet slab."""
+def config2(n_particles=1_000_000, nlay=20, nrow=100, ncol=200, seed=0, precision=FP64, use_torch=None,
+            mf6_dir=None):
+    """200x100x20 lognormal K (sigma2 1, 10 m / 2 m), 1e6 particles in the 10 m inlet slab.
+
+    With ``mf6_dir`` the solved flow is written there as MODFLOW 6 binary files
+    (``config2.grb/.hds/.bud``: FLOW-JA-FACE and a CHD list) and the flow
+    returned is the one read back from them, as a MODFLOW 6 run would feed
+    the tracker; ``info["mf6_files"]`` names the files."""
     g, f, info = heterogeneous_flow(nlay, nrow, ncol, sigma2=1.0, kg=10.0, lh=10.0, lv=2.0, porosity=0.25,
                                     alpha_l=0.5, alpha_t=0.05, dm=1e-4, seed=seed, use_torch=use_torch)
+    if mf6_dir is not None:
+        import os
+        from . import mf6io
+        files = mf6io.write_flow_files(os.path.join(os.fspath(mf6_dir), "config2"), g, f, spdis=False)
+        f = mf6io.flow_from_mf6(mf6io.read_grb(files[0]), mf6io.read_heads(files[1]), mf6io.read_budget(files[2]),
+                                1, 1, porosity=f.porosity, retardation=f.retardation, alpha_l=f.alpha_l,
+                                alpha_t=f.alpha_t, dm_eff=f.dm_eff, uniform_dispersion=f.uniform_dispersion)
+        info = dict(info, mf6_files=files)
     p = release_in_box(g, n_particles, 0.0, min(10.0, ncol), 0.0, float(nrow), float(g.botm[-1]),
                        float(g.top[0]), seed=1000 + seed)
     opt = Options(time_step_kind=MIN_ADV_DISP, ts_param=(0.1, 0.1), advection_kind=EULERIAN, dim_mask=(1, 1, 1),

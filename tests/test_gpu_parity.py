@@ -124,6 +124,20 @@ def test_dispersion_shared_rng_heterogeneous(gpu_lib, seed):
         assert abs(int(a) - int(b)) <= max(2, 0.005 * p.n)
 
 
+def test_heterogeneous_flow_read_from_mf6_files(gpu_lib, tmp_path):
+    """The lognormal-field flow written as MODFLOW 6 .grb/.hds/.bud and read
+    back (all-zero boundary faces and ICELLTYPE arrays instead of absent ones)
+    tracks on the GPU like the oracle does on the solver's own arrays."""
+    g, f, p, opt, info = W.config2(n_particles=3000, nlay=4, nrow=12, ncol=30, seed=2, use_torch=False)
+    _, f6, _, _, info6 = W.config2(n_particles=10, nlay=4, nrow=12, ncol=30, seed=2, use_torch=False,
+                                   mf6_dir=tmp_path)
+    assert f6.boundary_flows is not None and f6.celltype is not None
+    iv = [(0.0, 20.0), (20.0, 60.0)]
+    gp, gs = run_gpu(g, f6, opt, p, iv)
+    op, os_ = run_oracle(g, f, opt, p, iv)
+    _compare_same_rng(gp, op, g, f, tol=1e-6, min_frac=0.995)
+
+
 def test_histogram_bit_exact(gpu_lib):
     g, f, p, opt = W.config1(n_particles=20000)
     tr = mprw.Tracker(g, opt)
