@@ -70,6 +70,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--realizations", type=int, default=16,
+                    help="ensemble size of the batched leg (realizations 0..R-1 of the 64-member ensemble)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="precision of the headline run (mixed: for profiling the MIXED kernel alone)")
     return ap.parse_args()
@@ -244,7 +247,105 @@ def run_gpu_arm(args, rank, world, local):
     if not args.no_e2e:
         res["e2e"] = e2e_run(args, g, f, p, opt, origin, bins, domain, flush)
     res["geom"] = (g, f, p, opt)
+    if not args.no_batched and rank == 0:
+        res["batched"] = batched_run(args, flush)
     return res
+
+
+def batched_run(args, flush):
+    """The ensemble (mprw.workloads.config3, the first R realizations) as ONE
+    batch: each step advances every realization's particles in one persistent
+    launch and reconstructs every realization with GPKDE.  Timed in MIXED
+    precision (FP32 advance + FP32 reconstruction) and, on the same particles
+    and random streams, in FP64; the plume moments of the two are compared
+    per realization."""
+    import torch
+    import mprw
+    from mprw import workloads as W
+    from mprw.model import MIXED
+    t_setup = time.perf_counter()
+    prm = W.config3_params(64)[: args.realizations]
+    ens, opt, _ = W.config3(members=prm, use_torch=True)
+    t_setup = time.perf_counter() - t_setup
+    stream = torch.cuda.Stream()
+    bins = (1.0, 1.0, 1.0)
+    doms = [(float(g.ncol), float(g.nrow), float(g.top[0] - g.botm[-1])) for g, _, _ in ens]
+
+    def run(precision):
+        opt.precision = precision
+        b = mprw.Batch([e[0] for e in ens], opt)
+        b.set_stream(stream.cuda_stream)
+        for k, (g, f, p) in enumerate(ens):
+            b.load_flow(k, f)
+        b.set_particles([e[2] for e in ens])
+        t = 0.0
+
+        def one_step(t):
+            s = b.advance(t, t + INTERVAL_D)
+            nl = b.timings()["launches"]
+            for k, m in enumerate(b.members):
+                m.gpkde(doms[k], bins, precision=precision)
+                nl += m.timings()["launches"]
+            return s, nl
+        for _ in range(args.warmup):
+            one_step(t)
+            t += INTERVAL_D
+        torch.cuda.synchronize()
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        steps, launches, adv_kern = 0, 0, []
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ev[k][0].record(stream)
+            s = b.advance(t, t + INTERVAL_D)
+            adv_kern.append(b.timings()["step_ms"])
+            launches += b.timings()["launches"]
+            ev[k][1].record(stream)
+            for j, m in enumerate(b.members):
+                m.gpkde(doms[j], bins, precision=precision)
+                launches += m.timings()["launches"]
+            ev[k][2].record(stream)
+            torch.cuda.synchronize()
+            steps += s
+            t += INTERVAL_D
+        ms = sum(a.elapsed_time(c) for a, _, c in ev)
+        adv = sum(a.elapsed_time(bb) for a, bb, _ in ev)
+        outs = b.get_particles()
+        b.close()
+        return dict(steps=steps, ms=ms, adv_ms=adv, kern_ms=float(np.sum(adv_kern)), launches=launches, outs=outs,
+                    t_end=t)
+
+    mx = run(MIXED)
+    fp = run(0)
+    errs = []
+    for k, (g, f, p) in enumerate(ens):
+        m32, n32 = moments(mx["outs"][k])
+        m64, n64 = moments(fp["outs"][k])
+        x0 = 5.0  # centre of the 10 m inlet slab: first moments are taken as displacement from it
+        e = {"mean_disp_x_rel": abs(m32["gx"][0] - m64["gx"][0]) / max(abs(m64["gx"][0] - x0), 1e-30)}
+        for ax in ("gx", "gy", "gz"):
+            e[f"var_{ax[1]}_rel"] = abs(m32[ax][1] - m64[ax][1]) / max(m64[ax][1], 1e-30)
+        # Monte-Carlo standard error of a variance estimate, relative: sqrt(2 / n)
+        e["mc_var_rel_se"] = float(np.sqrt(2.0 / max(n64, 1)))
+        e["active"] = [n32, n64]
+        errs.append(e)
+    worst = {key: max(e[key] for e in errs) for key in ("mean_disp_x_rel", "var_x_rel", "var_y_rel", "var_z_rel")}
+    v32 = mx["steps"] / (mx["ms"] / 1e3)
+    v64 = fp["steps"] / (fp["ms"] / 1e3)
+    return {"workload": f"realizations 0..{len(ens) - 1} of the 64-member ensemble (config-2 generator; grids "
+                        "U[100..400]x[50..200]x[10..20], sigma2 lnK U[0.5,2], alphaL U[0.1,1], alphaT = alphaL/10, "
+                        "particles log-U[1e5,4e6]), one batch: one advance launch for all realizations + one "
+                        "GPKDE per realization per 10-day step",
+            "realizations": len(ens), "particles": int(sum(p.n for _, _, p in ens)),
+            "cells": int(sum(g.ncell for g, _, _ in ens)), "setup_s": t_setup,
+            "value": v32, "unit": UNIT, "ms_per_step": mx["ms"] / args.steps,
+            "advance_ms_per_step": mx["adv_ms"] / args.steps, "advance_kernel_ms_per_step": mx["kern_ms"] / args.steps,
+            "gpkde_ms_per_step": (mx["ms"] - mx["adv_ms"]) / args.steps, "gpu_launches": mx["launches"],
+            "fp64": {"value": v64, "ms_per_step": fp["ms"] / args.steps,
+                     "advance_ms_per_step": fp["adv_ms"] / args.steps},
+            "speedup_vs_fp64_same_ensemble": v32 / v64,
+            "moment_error_vs_fp64": {"worst_over_realizations": worst, "per_realization": errs},
+            "t_end_days": mx["t_end"]}
 
 
 def e2e_run(args, g, f, p, opt, origin, bins, domain, flush):
@@ -399,6 +500,9 @@ def main():
                          "active_mixed": n32, "kernel_ms": float(np.mean(mx["kern_ms"])),
                          "gpkde_ms": float(np.mean(mx["kde_ms"])), "gpkde_precision": "fp32",
                          "gpkde_fp32_vs_fp64_same_particles": mx["kde_err"]}
+    if "batched" in res:
+        line["batched"] = res["batched"]
+        line["batched"]["speedup_vs_plain_fp64"] = res["batched"]["value"] / value_rank
     if not args.no_cpu:
         g, f, p, opt = res["geom"]
         line["cpu_baseline"] = cpu_baseline(g, f, p, opt, args.cpu_sample, args.warmup, min(args.steps, 5))

@@ -234,6 +234,41 @@ int mprw_histogram_noalloc(const double *gx, const double *gy, const double *gz,
                            int64_t n, const double origin[3], const double bin_size[3],
                            const int32_t n_bins[3], double *counts, int64_t *n_binned, void *stream);
 
+/* Batched realizations.  No counterpart in the reference, which tracks one
+ * realization per run (one mpathrw process per flow model): a batch holds
+ * nmembers grids of any sizes that share the tracking options, one flow time
+ * step and one particle set per member, and mprw_advance on the batch tracks
+ * every member's particles in ONE persistent launch over the concatenated
+ * cell records and particle arrays (each member's cells link only to its own
+ * cells).
+ *   mprw_create_batch      grids[nmembers]; the batch is destroyed with
+ *                          mprw_destroy, which also ends its member views
+ *   mprw_batch_member      a view handle of member k: mprw_load_flow,
+ *                          mprw_get_particles (its particles, its cell
+ *                          numbers), mprw_histogram, mprw_gpkde and the
+ *                          observation calls work on it as on a single
+ *                          handle; mprw_set_particles on it overwrites its
+ *                          particles but cannot change their count;
+ *                          mprw_advance, mprw_set_stream and mprw_destroy on
+ *                          it return MPRW_E_STATE
+ *   mprw_set_particles_batch  counts[nmembers] particles per member, the
+ *                          arrays concatenated in member order, cell numbers
+ *                          1-based within each member's grid
+ * On the batch handle itself, mprw_advance advances every member (all member
+ * flows loaded first); mprw_get_particles returns every member's particles
+ * in batch order with member cell numbers; mprw_load_flow, mprw_histogram,
+ * mprw_gpkde and the observation calls return MPRW_E_STATE.  Particle ids
+ * select the random streams: without ids the id is the particle's index in
+ * the batch, so members draw independent streams; a member reproduces a
+ * separate single-handle run when both use the same ids. */
+int mprw_create_batch(mprw_handle **batch, int32_t nmembers, const mprw_grid_desc *grids,
+                      const mprw_options *opt);
+int mprw_batch_member(mprw_handle *batch, int32_t member, mprw_handle **view);
+int mprw_set_particles_batch(mprw_handle *batch, const int64_t *counts, const int32_t *cell,
+                             const double *lx, const double *ly, const double *lz, const double *t,
+                             const int32_t *status, const double *mass, const uint64_t *id,
+                             const uint64_t *rng_ctr);
+
 /* Optional: launch on a caller-provided cudaStream_t (NULL = the handle's). */
 int mprw_set_stream(mprw_handle *h, void *stream);
 

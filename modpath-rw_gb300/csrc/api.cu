@@ -3,6 +3,16 @@
 // The handle owns the device copy of the grid, one flow time step (raw
 // arrays + per-cell records), the particle state and a CUDA stream.  All
 // work is issued on that stream; calls that return data synchronise it.
+//
+// A batch handle (mprw_create_batch) concatenates the cell records,
+// IBOUNDTS, cell flags and particle arrays of several realizations: member m
+// owns cells [cell0, cell0 + ncell_m) and particles [p0, p0 + n_m) of the
+// batch, its records link only to its own cells (connections offset by
+// cell0), so one persistent advance launch over the batch tracks every
+// realization at once.  Member views (mprw_batch_member) are ordinary
+// handles whose record, IBOUNDTS, flag and particle pointers alias their
+// slices of the batch; per-realization calls (load_flow, get_particles,
+// histogram, gpkde, observations) go through them.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -67,13 +77,19 @@ struct mprw_handle {
   double *d_kpart = nullptr;          // coordinate-statistics partials
   double *h_kout = nullptr;           // pinned staging of the density / histogram grids
   int64_t h_kout_cap = 0;
-  std::vector<double> kde_table_key;  // database parameters of the uploaded factor tables
+  std::vector<double> kde_table_key;  // database parameters of the uploaded factor tables (of *kdep)
   double *d_counts = nullptr;
   int64_t counts_cap = 0;
   int64_t launches = 0;
   int sms = 152;
   int sort_enabled = 1;
   std::string err;
+  // batched realizations
+  mprw_handle *parent = nullptr;        // member view: the batch it belongs to
+  std::vector<mprw_handle *> members;   // batch: member views, in cell / particle order
+  int32_t cell0 = 0;                    // member: first cell in the batch's cell numbering
+  int64_t p0 = 0;                       // member: first particle in the batch's particle arrays
+  KdeState *kdep = &kde;                // GPKDE state (a member uses the batch's)
 };
 
 namespace {
@@ -107,6 +123,23 @@ cudaError_t upload(mprw_handle *h, T **p, const T *src, size_t count) {
 }
 
 void free_all(mprw_handle *h) {
+  if (h->parent) {
+    // slices of the batch's arrays
+    h->d_rec64 = nullptr;
+    h->d_rec32 = nullptr;
+    h->d_ibts = nullptr;
+    h->base.flags = nullptr;
+    h->d_cell = h->d_status = nullptr;
+    h->d_x = h->d_y = h->d_z = nullptr;
+    h->d_t = h->d_mass = h->d_stage = nullptr;
+    h->d_ctr = h->d_id = nullptr;
+    h->d_perm = nullptr;
+  }
+  for (mprw_handle *m : h->members) {
+    free_all(m);
+    delete m;
+  }
+  h->members.clear();
   void *ptrs[] = {h->d_delr, h->d_delc, h->d_top, h->d_botm, h->d_colL, h->d_colR, h->d_rowF, h->d_rowB,
                   h->d_sattop, h->d_ia, h->d_ja, h->d_flowja, h->d_bflow, h->d_por, h->d_ret, h->d_heads,
                   h->d_src, h->d_snk, h->d_aL, h->d_aT, h->d_dm, h->d_aLV, h->d_aTV, h->d_ibts, h->d_icb, h->d_ctype,
@@ -121,7 +154,7 @@ void free_all(mprw_handle *h) {
   for (void *p : {(void *)h->d_obs_of_cell, (void *)h->d_obs_style, (void *)h->d_obs_count, (void *)h->d_obs_mass})
     if (p) cudaFree(p);
   if (h->h_kout) cudaFreeHost(h->h_kout);
-  h->kde.release();
+  h->kde.release();  // (a member view's own state is empty)
   if (h->hscratch) cudaFreeHost(h->hscratch);
   cudaEvent_t evs[] = {h->ev0, h->ev1, h->ev2, h->ev3};
   for (auto e : evs)
@@ -165,32 +198,18 @@ Geometry geometry(mprw_handle *h) {
   geo.botm = h->d_botm;
   geo.sattop = h->d_sattop;
   geo.g = h->g;
+  geo.cell0 = h->cell0;
   return geo;
 }
 
-cudaError_t ensure_host(mprw_handle *h, size_t bytes) {
-  if (h->hscratch_bytes >= bytes) return cudaSuccess;
-  if (h->hscratch) cudaFreeHost(h->hscratch);
-  h->hscratch = nullptr;
-  h->hscratch_bytes = 0;
-  cudaError_t e = cudaMallocHost(&h->hscratch, bytes);
-  if (e == cudaSuccess) h->hscratch_bytes = bytes;
-  return e;
+bool grid_ok(const mprw_grid_desc *gd) {
+  if (gd->nlay <= 0 || gd->nrow <= 0 || gd->ncol <= 0 || !gd->delr || !gd->delc || !gd->top || !gd->botm)
+    return false;
+  return (int64_t)gd->nlay * gd->nrow * gd->ncol < ((int64_t)1 << 31);
 }
 
-}  // namespace
-
-extern "C" {
-
-int mprw_create(mprw_handle **out, const mprw_grid_desc *gd, const mprw_options *o) {
-  if (!out || !gd || !o) return MPRW_E_INVAL;
-  *out = nullptr;
-  if (gd->nlay <= 0 || gd->nrow <= 0 || gd->ncol <= 0 || !gd->delr || !gd->delc || !gd->top || !gd->botm)
-    return MPRW_E_INVAL;
-  int64_t ncell = (int64_t)gd->nlay * gd->nrow * gd->ncol;
-  if (ncell >= (int64_t)1 << 31) return MPRW_E_INVAL;
-  mprw_handle *h = new mprw_handle();
-  *out = h;
+// Options, device attributes, events and counters of a handle.
+int init_common(mprw_handle *h, const mprw_options *o) {
   if (o->advection_kind != 1 && o->advection_kind != 2)
     return fail(h, MPRW_E_INVAL, "advection_kind: 1 (EXPONENTIAL) or 2 (EULERIAN)");
   if (o->dispersion_model != 0 && o->dispersion_model != 1)
@@ -205,23 +224,27 @@ int mprw_create(mprw_handle **out, const mprw_grid_desc *gd, const mprw_options 
   h->ndim = nd;
   h->d1 = dims[0];
   h->d2 = nd > 1 ? dims[1] : 0;
-  h->g.nlay = gd->nlay;
-  h->g.nrow = gd->nrow;
-  h->g.ncol = gd->ncol;
-  h->g.ncpl = gd->nrow * gd->ncol;
-  h->g.ncell = (int32_t)ncell;
-  while (((int64_t)1 << h->ncell_bits) < ncell) ++h->ncell_bits;
   CK(cudaGetDevice(&h->device));
   CK(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device));
-  CK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
-  h->stream = h->own_stream;
   CK(cudaEventCreate(&h->ev0));
   CK(cudaEventCreate(&h->ev1));
   CK(cudaEventCreate(&h->ev2));
   CK(cudaEventCreate(&h->ev3));
   CK(cudaMallocHost(&h->h_counters, 4 * sizeof(unsigned long long)));
   CK(dalloc(&h->d_counters, 4));
-  // geometry as the binary-grid reader builds it (RectangularGridDisMf6.f90:301-340)
+  return MPRW_OK;
+}
+
+// Grid dimensions and the geometry arrays, built as the binary-grid reader
+// builds them (RectangularGridDisMf6.f90:301-340).
+int init_grid(mprw_handle *h, const mprw_grid_desc *gd) {
+  const int64_t ncell = (int64_t)gd->nlay * gd->nrow * gd->ncol;
+  h->g.nlay = gd->nlay;
+  h->g.nrow = gd->nrow;
+  h->g.ncol = gd->ncol;
+  h->g.ncpl = gd->nrow * gd->ncol;
+  h->g.ncell = (int32_t)ncell;
+  while (((int64_t)1 << h->ncell_bits) < ncell) ++h->ncell_bits;
   const int ncol = gd->ncol, nrow = gd->nrow, ncpl = h->g.ncpl;
   std::vector<double> colL(ncol), colR(ncol), rowF(nrow), rowB(nrow);
   double X = 0.0;
@@ -256,8 +279,102 @@ int mprw_create(mprw_handle **out, const mprw_grid_desc *gd, const mprw_options 
   return MPRW_OK;
 }
 
+// Member records link to member-local cells; in the batch's numbering the
+// connections move by cell0.
+template <typename R>
+__global__ void offset_conn_kernel(CellRec<R> *rec, int64_t n, int32_t cell0) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int f = 0; f < 6; ++f)
+      if (rec[i].conn[f] >= 0) rec[i].conn[f] += cell0;
+}
+
+cudaError_t ensure_host(mprw_handle *h, size_t bytes) {
+  if (h->hscratch_bytes >= bytes) return cudaSuccess;
+  if (h->hscratch) cudaFreeHost(h->hscratch);
+  h->hscratch = nullptr;
+  h->hscratch_bytes = 0;
+  cudaError_t e = cudaMallocHost(&h->hscratch, bytes);
+  if (e == cudaSuccess) h->hscratch_bytes = bytes;
+  return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mprw_create(mprw_handle **out, const mprw_grid_desc *gd, const mprw_options *o) {
+  if (!out || !gd || !o) return MPRW_E_INVAL;
+  *out = nullptr;
+  if (!grid_ok(gd)) return MPRW_E_INVAL;
+  mprw_handle *h = new mprw_handle();
+  *out = h;
+  int rc = init_common(h, o);
+  if (rc != MPRW_OK) return rc;
+  CK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
+  h->stream = h->own_stream;
+  return init_grid(h, gd);
+}
+
+int mprw_create_batch(mprw_handle **out, int32_t nmembers, const mprw_grid_desc *grids, const mprw_options *o) {
+  if (!out || !grids || !o || nmembers < 1) return MPRW_E_INVAL;
+  *out = nullptr;
+  int64_t total = 0;
+  for (int32_t m = 0; m < nmembers; ++m) {
+    if (!grid_ok(&grids[m])) return MPRW_E_INVAL;
+    total += (int64_t)grids[m].nlay * grids[m].nrow * grids[m].ncol;
+  }
+  if (total >= (int64_t)1 << 31) return MPRW_E_INVAL;
+  mprw_handle *h = new mprw_handle();
+  *out = h;
+  int rc = init_common(h, o);
+  if (rc != MPRW_OK) return rc;
+  CK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
+  h->stream = h->own_stream;
+  h->g.ncell = (int32_t)total;
+  while (((int64_t)1 << h->ncell_bits) < total) ++h->ncell_bits;
+  // the concatenated arrays the advance kernel reads
+  if (h->opt.precision == MPRW_FP64) CK(dalloc(&h->d_rec64, total));
+  else CK(dalloc(&h->d_rec32, total));
+  CK(dalloc(&h->d_ibts, total));
+  CK(dalloc(&h->base.flags, total));
+  CK(cudaMemsetAsync(h->d_ibts, 0, sizeof(int32_t) * total, h->stream));
+  CK(cudaMemsetAsync(h->base.flags, 0, total, h->stream));
+  int64_t cell0 = 0;
+  for (int32_t k = 0; k < nmembers; ++k) {
+    mprw_handle *m = new mprw_handle();
+    h->members.push_back(m);
+    m->parent = h;
+    m->kdep = &h->kde;
+    m->cell0 = (int32_t)cell0;
+    rc = init_common(m, o);
+    if (rc != MPRW_OK) return fail(h, rc, "member " + std::to_string(k) + ": " + m->err);
+    m->stream = h->stream;
+    rc = init_grid(m, &grids[k]);
+    if (rc != MPRW_OK) return fail(h, rc, "member " + std::to_string(k) + ": " + m->err);
+    if (h->d_rec64) m->d_rec64 = h->d_rec64 + cell0;
+    if (h->d_rec32) m->d_rec32 = h->d_rec32 + cell0;
+    m->d_ibts = h->d_ibts + cell0;
+    m->base.flags = h->base.flags + cell0;
+    cell0 += m->g.ncell;
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  return MPRW_OK;
+}
+
+int mprw_batch_member(mprw_handle *h, int32_t member, mprw_handle **view) {
+  if (!h || !view) return MPRW_E_INVAL;
+  *view = nullptr;
+  if (h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_batch_member: not a batch handle");
+  if (member < 0 || member >= (int32_t)h->members.size())
+    return fail(h, MPRW_E_INVAL, "mprw_batch_member: member index out of range");
+  *view = h->members[member];
+  return MPRW_OK;
+}
+
 int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *f) {
   if (!h) return MPRW_E_INVAL;
+  if (!h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_load_flow on a batch: load each member's flow");
   if (!f || !f->ia || !f->ja || !f->flowja || !f->porosity || !f->retardation || !f->iboundts || !f->alpha_l ||
       !f->alpha_t || !f->dm_eff)
     return fail(h, MPRW_E_INVAL, "mprw_load_flow: missing required array");
@@ -277,7 +394,10 @@ int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *f) {
   if (f->boundary_flows) CK(upload(h, &h->d_bflow, f->boundary_flows, 6 * nc));
   CK(upload(h, &h->d_por, f->porosity, nc));
   CK(upload(h, &h->d_ret, f->retardation, nc));
-  CK(upload(h, &h->d_ibts, f->iboundts, nc));
+  if (h->parent)
+    CK(cudaMemcpyAsync(h->d_ibts, f->iboundts, sizeof(int32_t) * nc, cudaMemcpyHostToDevice, h->stream));
+  else
+    CK(upload(h, &h->d_ibts, f->iboundts, nc));
   if (f->icboundts) CK(upload(h, &h->d_icb, f->icboundts, nc));
   if (f->heads) CK(upload(h, &h->d_heads, f->heads, nc));
   if (f->celltype) CK(upload(h, &h->d_ctype, f->celltype, nc));
@@ -305,10 +425,12 @@ int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *f) {
     CK(dalloc(&h->base.q, 6 * nc));
     CK(dalloc(&h->base.dz, nc));
     CK(dalloc(&h->base.conn, 6 * nc));
-    CK(dalloc(&h->base.flags, nc));
     CK(dalloc(&h->d_massb, nc));
-    if (h->opt.precision == MPRW_FP64) CK(dalloc(&h->d_rec64, nc));
-    else CK(dalloc(&h->d_rec32, nc));
+    if (!h->parent) {  // a member's flags and records are slices of the batch's
+      CK(dalloc(&h->base.flags, nc));
+      if (h->opt.precision == MPRW_FP64) CK(dalloc(&h->d_rec64, nc));
+      else CK(dalloc(&h->d_rec32, nc));
+    }
   }
   PrepInputs in{};
   in.g = h->g;
@@ -348,6 +470,11 @@ int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *f) {
   in.uniform_porosity = h->opt.uniform_porosity;
   CK(cudaEventRecord(h->ev2, h->stream));
   CK(launch_prep(in, h->base, h->d_massb, h->d_rec64, h->d_rec32, h->stream));
+  if (h->cell0 != 0) {
+    if (h->d_rec64) offset_conn_kernel<double><<<grid1d(nc), 256, 0, h->stream>>>(h->d_rec64, nc, h->cell0);
+    else offset_conn_kernel<float><<<grid1d(nc), 256, 0, h->stream>>>(h->d_rec32, nc, h->cell0);
+    CK(cudaGetLastError());
+  }
   CK(cudaEventRecord(h->ev3, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   float ms = 0;
@@ -357,18 +484,19 @@ int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *f) {
   return MPRW_OK;
 }
 
-int mprw_set_particles(mprw_handle *h, int64_t n, const int32_t *cell, const double *lx, const double *ly,
-                       const double *lz, const double *t, const int32_t *status, const double *mass,
-                       const uint64_t *id, const uint64_t *rng_ctr) {
-  if (!h) return MPRW_E_INVAL;
-  if (n < 0 || n >= ((int64_t)1 << 32)) return fail(h, MPRW_E_INVAL, "particle count out of range");
-  if (n > 0 && (!cell || !lx || !ly || !lz || !t || !status))
-    return fail(h, MPRW_E_INVAL, "mprw_set_particles: missing required array");
-  for (int64_t p = 0; p < n; ++p)
-    if (cell[p] < 1 || cell[p] > h->g.ncell) return fail(h, MPRW_E_INVAL, "particle cell number out of range");
+}  // extern "C"
+
+namespace {
+
+// Copies n particles into h's arrays (allocating them when h owns them and
+// they are too small).  Cells arrive 1-based and are stored 0-based + shift.
+int upload_particles(mprw_handle *h, int64_t n, const int32_t *cell, const double *lx, const double *ly,
+                     const double *lz, const double *t, const int32_t *status, const double *mass,
+                     const uint64_t *id, const uint64_t *rng_ctr, int32_t shift) {
   const bool mixed = h->opt.precision == MPRW_MIXED;
   const size_t rs = mixed ? sizeof(float) : sizeof(double);
   if (n > h->cap) {
+    if (h->parent) return fail(h, MPRW_E_STATE, "batch member particle slice too small");
     size_t c = (size_t)n;
     CK(dalloc(&h->d_cell, c));
     CK(dalloc(&h->d_status, c));
@@ -387,7 +515,7 @@ int mprw_set_particles(mprw_handle *h, int64_t n, const int32_t *cell, const dou
   if (n == 0) return MPRW_OK;
   cudaStream_t s = h->stream;
   CK(cudaMemcpyAsync(h->d_cell, cell, 4 * n, cudaMemcpyHostToDevice, s));
-  cell_shift_kernel<<<grid1d(n), 256, 0, s>>>(h->d_cell, n, -1);
+  cell_shift_kernel<<<grid1d(n), 256, 0, s>>>(h->d_cell, n, shift);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(h->d_status, status, 4 * n, cudaMemcpyHostToDevice, s));
   const double *src[3] = {lx, ly, lz};
@@ -416,14 +544,106 @@ int mprw_set_particles(mprw_handle *h, int64_t n, const int32_t *cell, const dou
   return MPRW_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int mprw_set_particles(mprw_handle *h, int64_t n, const int32_t *cell, const double *lx, const double *ly,
+                       const double *lz, const double *t, const int32_t *status, const double *mass,
+                       const uint64_t *id, const uint64_t *rng_ctr) {
+  if (!h) return MPRW_E_INVAL;
+  if (!h->members.empty())
+    return fail(h, MPRW_E_STATE, "mprw_set_particles on a batch: use mprw_set_particles_batch");
+  if (n < 0 || n >= ((int64_t)1 << 32)) return fail(h, MPRW_E_INVAL, "particle count out of range");
+  if (n > 0 && (!cell || !lx || !ly || !lz || !t || !status))
+    return fail(h, MPRW_E_INVAL, "mprw_set_particles: missing required array");
+  if (h->parent) {
+    if (n != h->n) return fail(h, MPRW_E_STATE, "a batch member's particle count is set by mprw_set_particles_batch");
+    if ((id != nullptr) != h->parent->has_id)
+      return fail(h, MPRW_E_INVAL, "a batch member's particles carry ids exactly when the batch's do");
+  }
+  for (int64_t p = 0; p < n; ++p)
+    if (cell[p] < 1 || cell[p] > h->g.ncell) return fail(h, MPRW_E_INVAL, "particle cell number out of range");
+  return upload_particles(h, n, cell, lx, ly, lz, t, status, mass, id, rng_ctr, h->cell0 - 1);
+}
+
+int mprw_set_particles_batch(mprw_handle *h, const int64_t *counts, const int32_t *cell, const double *lx,
+                             const double *ly, const double *lz, const double *t, const int32_t *status,
+                             const double *mass, const uint64_t *id, const uint64_t *rng_ctr) {
+  if (!h) return MPRW_E_INVAL;
+  if (h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_set_particles_batch: not a batch handle");
+  if (!counts) return fail(h, MPRW_E_INVAL, "mprw_set_particles_batch: null counts");
+  const int32_t nm = (int32_t)h->members.size();
+  int64_t n = 0;
+  for (int32_t k = 0; k < nm; ++k) {
+    if (counts[k] < 0) return fail(h, MPRW_E_INVAL, "mprw_set_particles_batch: negative count");
+    n += counts[k];
+    if (n >= ((int64_t)1 << 32)) return fail(h, MPRW_E_INVAL, "particle count out of range");
+  }
+  if (n > 0 && (!cell || !lx || !ly || !lz || !t || !status))
+    return fail(h, MPRW_E_INVAL, "mprw_set_particles_batch: missing required array");
+  {
+    int64_t p = 0;
+    for (int32_t k = 0; k < nm; ++k)
+      for (int64_t e = p + counts[k]; p < e; ++p)
+        if (cell[p] < 1 || cell[p] > h->members[k]->g.ncell)
+          return fail(h, MPRW_E_INVAL, "member " + std::to_string(k) + ": particle cell number out of range");
+  }
+  int rc = upload_particles(h, n, cell, lx, ly, lz, t, status, mass, id, rng_ctr, -1);
+  if (rc != MPRW_OK) return rc;
+  const size_t rs = h->opt.precision == MPRW_MIXED ? sizeof(float) : sizeof(double);
+  int64_t p0 = 0;
+  for (int32_t k = 0; k < nm; ++k) {
+    mprw_handle *m = h->members[k];
+    const int64_t nk = counts[k];
+    m->p0 = p0;
+    m->n = m->cap = nk;
+    m->d_cell = h->d_cell + p0;
+    m->d_status = h->d_status + p0;
+    m->d_x = (char *)h->d_x + rs * p0;
+    m->d_y = (char *)h->d_y + rs * p0;
+    m->d_z = (char *)h->d_z + rs * p0;
+    m->d_t = h->d_t + p0;
+    m->d_mass = h->d_mass + p0;
+    m->d_ctr = h->d_ctr + p0;
+    m->d_id = h->d_id + p0;
+    m->d_stage = h->d_stage ? h->d_stage + p0 : nullptr;
+    m->d_perm = nullptr;
+    m->has_id = h->has_id;
+    m->unit_mass = true;
+    if (mass)
+      for (int64_t q = p0; q < p0 + nk && m->unit_mass; ++q) m->unit_mass = (mass[q] == 1.0);
+    m->advanced = false;
+    if (nk > 0 && m->cell0 != 0) {
+      cell_shift_kernel<<<grid1d(nk), 256, 0, h->stream>>>(m->d_cell, nk, m->cell0);
+      CK(cudaGetLastError());
+    }
+    p0 += nk;
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  return MPRW_OK;
+}
+
 int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_done) {
   if (!h) return MPRW_E_INVAL;
+  if (h->parent) return fail(h, MPRW_E_STATE, "mprw_advance on a batch member: advance the batch");
+  if (!h->members.empty()) {
+    h->flow_loaded = true;
+    for (size_t k = 0; k < h->members.size(); ++k)
+      if (!h->members[k]->flow_loaded)
+        return fail(h, MPRW_E_STATE, "mprw_advance before member " + std::to_string(k) + "'s mprw_load_flow");
+  }
   if (!h->flow_loaded) return fail(h, MPRW_E_STATE, "mprw_advance before mprw_load_flow");
   if (!(t_end >= t_begin)) return fail(h, MPRW_E_INVAL, "t_end < t_begin");
   h->launches = 0;
   h->last_t_begin = t_begin;
   h->last_t_end = t_end;
   h->advanced = true;
+  for (mprw_handle *m : h->members) {
+    m->last_t_begin = t_begin;
+    m->last_t_end = t_end;
+    m->advanced = true;
+  }
   if (h->n == 0) {
     if (steps_done) *steps_done = 0;
     return MPRW_OK;
@@ -511,6 +731,18 @@ int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_do
 int mprw_get_particles(mprw_handle *h, int32_t *cell, double *lx, double *ly, double *lz, double *t,
                        int32_t *status, uint64_t *rng_ctr, double *gx, double *gy, double *gz) {
   if (!h) return MPRW_E_INVAL;
+  if (!h->members.empty()) {
+    // a batch: every member's particles in batch order, member-local cells
+    for (mprw_handle *m : h->members) {
+      const int64_t o = m->p0;
+      int rc = mprw_get_particles(m, cell ? cell + o : nullptr, lx ? lx + o : nullptr, ly ? ly + o : nullptr,
+                                  lz ? lz + o : nullptr, t ? t + o : nullptr, status ? status + o : nullptr,
+                                  rng_ctr ? rng_ctr + o : nullptr, gx ? gx + o : nullptr, gy ? gy + o : nullptr,
+                                  gz ? gz + o : nullptr);
+      if (rc != MPRW_OK) return fail(h, rc, m->err);
+    }
+    return MPRW_OK;
+  }
   const int64_t n = h->n;
   if (n == 0) return MPRW_OK;
   cudaStream_t s = h->stream;
@@ -559,7 +791,7 @@ int mprw_get_particles(mprw_handle *h, int32_t *cell, double *lx, double *ly, do
   }
   CK(cudaStreamSynchronize(s));
   if (cell)
-    for (int64_t p = 0; p < n; ++p) cell[p] += 1;
+    for (int64_t p = 0; p < n; ++p) cell[p] += 1 - h->cell0;
   return MPRW_OK;
 }
 
@@ -651,6 +883,7 @@ extern "C" {
 int mprw_histogram(mprw_handle *h, const double origin[3], const double bin_size[3], const int32_t n_bins[3],
                    double *counts, int64_t *n_binned, double *eff_mass) {
   if (!h) return MPRW_E_INVAL;
+  if (!h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_histogram on a batch: use a member view");
   if (!origin || !bin_size || !n_bins || !counts) return fail(h, MPRW_E_INVAL, "mprw_histogram: null argument");
   h->launches = 0;
   cudaStream_t s = h->stream;
@@ -670,6 +903,7 @@ int mprw_histogram(mprw_handle *h, const double origin[3], const double bin_size
 int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, double *histogram,
                int32_t n_bins_out[3], int32_t *loops_done) {
   if (!h) return MPRW_E_INVAL;
+  if (!h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_gpkde on a batch: use a member view");
   if (!o || !density) return fail(h, MPRW_E_INVAL, "mprw_gpkde: null argument");
   // prInitialize (GridProjectedKDE.F90:354-998)
   KdeParams P{};
@@ -748,8 +982,9 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
   P.min_dim = mind;
 
   cudaStream_t s = h->stream;
+  mprw_handle *rt = h->parent ? h->parent : h;  // owner of the GPKDE state and the pinned staging
   h->launches = 0;
-  h->kde.launches = 0;
+  h->kdep->launches = 0;
   CK(cudaEventRecord(h->ev2, s));
   // histogram (counts / effective mass)
   int64_t nbinned = 0;
@@ -758,7 +993,7 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
   if (rc != MPRW_OK) return rc;
   const int64_t ngrid = (int64_t)nb[0] * nb[1] * nb[2];
   // statistics of the active particles' coordinates (GridProjectedKDE.F90:4023-4030)
-  CK(h->kde.ensure_grid(ngrid));
+  CK(h->kdep->ensure_grid(ngrid));
   double mean[3] = {0, 0, 0}, sd[3] = {0, 0, 0}, npts = 0.0;
   {
     std::vector<double> part;
@@ -790,7 +1025,7 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
   }
   // active bins
   int nactive = 0;
-  CK(kde_collect_active(h->kde, P, h->d_counts, s, &nactive));
+  CK(kde_collect_active(*h->kdep, P, h->d_counts, s, &nactive));
   int loops = 0;
   if (nactive > 0) {
     // initial smoothing (initialSmoothingSelection 0: Silverman-type scale)
@@ -804,18 +1039,18 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
     std::vector<double> key = {(double)P.ndim, (double)P.ndelta, P.bin[0], P.bin[1], P.bin[2],
                                (double)P.mask[0], (double)P.mask[1], (double)P.mask[2]};
     key.insert(key.end(), P.hod, P.hod + P.ndelta);
-    if (!h->kde.d_val || key != h->kde_table_key) {
+    if (!h->kdep->d_val || key != rt->kde_table_key) {
       std::vector<double> val;
       std::vector<int> wm, wofs, sm[3], sofs[3];
       kde_build_tables(P, val, wm, wofs, sm, sofs);
       CK(cudaStreamSynchronize(s));
-      if (h->kde.d_val) cudaFree(h->kde.d_val);
-      if (h->kde.d_meta) cudaFree(h->kde.d_meta);
-      h->kde.d_val = nullptr;
-      h->kde.d_meta = nullptr;
-      h->kde_table_key.clear();
-      CK(cudaMalloc(&h->kde.d_val, sizeof(double) * val.size()));
-      CK(cudaMalloc(&h->kde.d_meta, sizeof(int) * 8 * 3 * KDE_MAXDB));
+      if (h->kdep->d_val) cudaFree(h->kdep->d_val);
+      if (h->kdep->d_meta) cudaFree(h->kdep->d_meta);
+      h->kdep->d_val = nullptr;
+      h->kdep->d_meta = nullptr;
+      rt->kde_table_key.clear();
+      CK(cudaMalloc(&h->kdep->d_val, sizeof(double) * val.size()));
+      CK(cudaMalloc(&h->kdep->d_meta, sizeof(int) * 8 * 3 * KDE_MAXDB));
       std::vector<int> meta;
       meta.insert(meta.end(), wm.begin(), wm.end());
       meta.insert(meta.end(), wofs.begin(), wofs.end());
@@ -824,20 +1059,20 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
         meta.insert(meta.end(), sofs[a].begin(), sofs[a].end());
       }
       std::vector<float> valf(val.begin(), val.end());
-      if (h->kde.d_valf) cudaFree(h->kde.d_valf);
-      h->kde.d_valf = nullptr;
-      CK(cudaMalloc(&h->kde.d_valf, sizeof(float) * valf.size()));
-      CK(cudaMemcpyAsync(h->kde.d_val, val.data(), sizeof(double) * val.size(), cudaMemcpyHostToDevice, s));
-      CK(cudaMemcpyAsync(h->kde.d_valf, valf.data(), sizeof(float) * valf.size(), cudaMemcpyHostToDevice, s));
-      CK(cudaMemcpyAsync(h->kde.d_meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, s));
+      if (h->kdep->d_valf) cudaFree(h->kdep->d_valf);
+      h->kdep->d_valf = nullptr;
+      CK(cudaMalloc(&h->kdep->d_valf, sizeof(float) * valf.size()));
+      CK(cudaMemcpyAsync(h->kdep->d_val, val.data(), sizeof(double) * val.size(), cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(h->kdep->d_valf, valf.data(), sizeof(float) * valf.size(), cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(h->kdep->d_meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, s));
       CK(cudaStreamSynchronize(s));  // the host vectors go out of scope
-      h->kde_table_key = key;
+      rt->kde_table_key = key;
     }
     const int L = 3 * KDE_MAXDB;
-    h->kde.wtab = KdeTable{h->kde.d_val, h->kde.d_meta, h->kde.d_meta + L};
+    h->kdep->wtab = KdeTable{h->kdep->d_val, h->kdep->d_meta, h->kdep->d_meta + L};
     for (int a = 0; a < 3; ++a)
-      h->kde.sdtab[a] = KdeTable{h->kde.d_val, h->kde.d_meta + (2 + 2 * a) * L, h->kde.d_meta + (3 + 2 * a) * L};
-    cudaError_t e = kde_run(h->kde, P, hs, npts, o->n_opt_loops, o->rel_err_convergence,
+      h->kdep->sdtab[a] = KdeTable{h->kdep->d_val, h->kdep->d_meta + (2 + 2 * a) * L, h->kdep->d_meta + (3 + 2 * a) * L};
+    cudaError_t e = kde_run(*h->kdep, P, hs, npts, o->n_opt_loops, o->rel_err_convergence,
                             o->skip_error_convergence != 0, fp32, s, &loops);
     if (e == cudaErrorInvalidValue) return fail(h, MPRW_E_INVAL, "mprw_gpkde: net roughness is zero everywhere");
     CK(e);
@@ -846,34 +1081,34 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
     double scale = 1.0;
     if (o->unit_volume) scale *= binvol;
     if (o->scaling_factor != 0.0) scale *= o->scaling_factor;
-    CK(kde_output(h->kde, P, fp32, f, scale, s));
+    CK(kde_output(*h->kdep, P, fp32, f, scale, s));
   } else {
-    CK(cudaMemsetAsync(h->kde.dens_out, 0, sizeof(double) * ngrid, s));
+    CK(cudaMemsetAsync(h->kdep->dens_out, 0, sizeof(double) * ngrid, s));
   }
   // outputs through pinned staging (density, then histogram)
   const int64_t nout = histogram ? 2 * ngrid : ngrid;
-  if (nout > h->h_kout_cap) {
+  if (nout > rt->h_kout_cap) {
     CK(cudaStreamSynchronize(s));
-    if (h->h_kout) cudaFreeHost(h->h_kout);
-    h->h_kout = nullptr;
-    h->h_kout_cap = 0;
-    CK(cudaMallocHost(&h->h_kout, sizeof(double) * nout));
-    h->h_kout_cap = nout;
+    if (rt->h_kout) cudaFreeHost(rt->h_kout);
+    rt->h_kout = nullptr;
+    rt->h_kout_cap = 0;
+    CK(cudaMallocHost(&rt->h_kout, sizeof(double) * nout));
+    rt->h_kout_cap = nout;
   }
-  CK(cudaMemcpyAsync(h->h_kout, h->kde.dens_out, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(rt->h_kout, h->kdep->dens_out, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
   if (histogram) {
     mul2_kernel<<<grid1d(ngrid), 256, 0, s>>>(h->d_counts, ngrid, eff, 1.0);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(h->h_kout + ngrid, h->d_counts, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(rt->h_kout + ngrid, h->d_counts, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
   }
   CK(cudaEventRecord(h->ev3, s));
   CK(cudaStreamSynchronize(s));
-  std::memcpy(density, h->h_kout, sizeof(double) * ngrid);
-  if (histogram) std::memcpy(histogram, h->h_kout + ngrid, sizeof(double) * ngrid);
+  std::memcpy(density, rt->h_kout, sizeof(double) * ngrid);
+  if (histogram) std::memcpy(histogram, rt->h_kout + ngrid, sizeof(double) * ngrid);
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, h->ev2, h->ev3));
   h->kde_ms = ms;
-  h->launches += h->kde.launches + 2;
+  h->launches += h->kdep->launches + 2;
   if (loops_done) *loops_done = loops;
   return MPRW_OK;
 }
@@ -891,12 +1126,14 @@ static ObsArgs obs_args(const mprw_handle *h) {
   a.obs_style = h->d_obs_style;
   a.t_begin = h->last_t_begin;
   a.t_end = h->last_t_end;
+  a.cell0 = h->cell0;
   return a;
 }
 
 int mprw_set_observations(mprw_handle *h, int32_t ncells, const int32_t *cells, const int32_t *obs, int32_t nobs,
                           const int32_t *style) {
   if (!h) return MPRW_E_INVAL;
+  if (!h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_set_observations on a batch: use a member view");
   if (ncells < 0 || nobs < 0 || (ncells > 0 && (!cells || !obs)) || (nobs > 0 && !style))
     return fail(h, MPRW_E_INVAL, "mprw_set_observations: null argument or negative size");
   const int32_t ncell = h->g.ncell;
@@ -978,7 +1215,9 @@ int mprw_observe_sinks(mprw_handle *h, int64_t capacity, int32_t *obs, uint64_t 
 
 int mprw_set_stream(mprw_handle *h, void *stream) {
   if (!h) return MPRW_E_INVAL;
+  if (h->parent) return fail(h, MPRW_E_STATE, "mprw_set_stream on a batch member: set the batch's stream");
   h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  for (mprw_handle *m : h->members) m->stream = h->stream;
   return MPRW_OK;
 }
 
@@ -995,6 +1234,7 @@ int mprw_last_timings(mprw_handle *h, double *step_ms, double *prep_ms, double *
 
 int mprw_destroy(mprw_handle *h) {
   if (!h) return MPRW_OK;
+  if (h->parent) return MPRW_E_STATE;  // member views go with their batch
   if (h->stream) cudaStreamSynchronize(h->stream);
   free_all(h);
   delete h;

@@ -16,6 +16,7 @@ template <typename R>
 __device__ __forceinline__ void model_xyz(const Geometry &geo, int32_t c, R lx, R ly, R lz, double &X,
                                           double &Y, double &Z) {
   const GridDims g = geo.g;
+  c -= geo.cell0;
   int k = c / g.ncpl;
   int r = c - k * g.ncpl;
   int i = r / g.ncol;

@@ -65,6 +65,7 @@ struct Geometry {
   const double *row_front, *row_back;   // nrow  (GetFront / GetBack)
   const double *botm, *sattop;          // ncell
   GridDims g;
+  int32_t cell0;                        // particle cells are numbered from cell0 (batch member)
 };
 
 template <typename R>
@@ -101,6 +102,7 @@ struct ObsArgs {
   const int32_t *obs_of_cell;    // per cell: observation index or -1
   const int32_t *obs_style;      // per observation: 1 resident, 2 sink
   double t_begin, t_end;         // interval of the last advance
+  int32_t cell0;                 // particle cells are numbered from cell0 (batch member)
 };
 
 // Sink records of the last advance into the scratch buffer; *n_records = how many.

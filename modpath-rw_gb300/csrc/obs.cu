@@ -42,7 +42,7 @@ __global__ void sink_flags_kernel(ObsArgs a, uint8_t *flag) {
     const int32_t st = a.status[i];
     bool f = false;
     if ((st == ST_WEAK_SINK || st == ST_WEAK_SOURCE) && a.t[i] > a.t_begin && a.t[i] <= a.t_end) {
-      const int32_t k = a.obs_of_cell[a.cell[i]];
+      const int32_t k = a.obs_of_cell[a.cell[i] - a.cell0];
       f = k >= 0 && a.obs_style[k] == 2;
     }
     flag[i] = f ? 1 : 0;
@@ -54,7 +54,7 @@ __global__ void sink_records_kernel(ObsArgs a, const int64_t *sel, const int64_t
   const int64_t m = *nsel;
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = sel[r];
-    obs[r] = a.obs_of_cell[a.cell[i]];
+    obs[r] = a.obs_of_cell[a.cell[i] - a.cell0];
     id[r] = a.id ? a.id[i] : (uint64_t)i;
     time[r] = a.t[i];
     mass[r] = a.mass ? a.mass[i] : 1.0;
@@ -64,7 +64,7 @@ __global__ void sink_records_kernel(ObsArgs a, const int64_t *sel, const int64_t
 __global__ void resident_kernel(ObsArgs a, unsigned long long *count, double *msum) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
     if (a.status[i] != ST_ACTIVE) continue;
-    const int32_t k = a.obs_of_cell[a.cell[i]];
+    const int32_t k = a.obs_of_cell[a.cell[i] - a.cell0];
     if (k < 0 || a.obs_style[k] != 1) continue;
     atomicAdd(&count[k], 1ull);
     atomicAdd(&msum[k], a.mass ? a.mass[i] : 1.0);

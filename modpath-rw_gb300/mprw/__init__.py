@@ -92,6 +92,10 @@ def load_library() -> C.CDLL:
         "mprw_set_stream": (C.c_int, [H, C.c_void_p]),
         "mprw_last_timings": (C.c_int, [H, _dp, _dp, _dp, _dp, C.POINTER(C.c_int64)]),
         "mprw_destroy": (C.c_int, [H]),
+        "mprw_create_batch": (C.c_int, [C.POINTER(H), C.c_int32, C.POINTER(GridDesc), C.POINTER(OptionsDesc)]),
+        "mprw_batch_member": (C.c_int, [H, C.c_int32, C.POINTER(H)]),
+        "mprw_set_particles_batch": (C.c_int, [H, C.POINTER(C.c_int64), _ip, _dp, _dp, _dp, _dp, _ip, _dp, _up,
+                                               _up]),
         "mprw_last_error": (C.c_char_p, [H]),
     }
     for name, (res, args) in sig.items():
@@ -118,6 +122,31 @@ def _p(a, ptype):
     return None if a is None else a.ctypes.data_as(ptype)
 
 
+def _grid_desc(grid: Grid, keep: list) -> GridDesc:
+    g = dict(delr=_f64(grid.delr), delc=_f64(grid.delc), top=_f64(grid.top), botm=_f64(grid.botm))
+    keep.append(g)
+    return GridDesc(grid.nlay, grid.nrow, grid.ncol, _p(g["delr"], _dp), _p(g["delc"], _dp), _p(g["top"], _dp),
+                    _p(g["botm"], _dp))
+
+
+def _options_desc(opt: Options) -> OptionsDesc:
+    od = OptionsDesc()
+    od.time_step_kind = opt.time_step_kind
+    od.ts_param[0], od.ts_param[1] = float(opt.ts_param[0]), float(opt.ts_param[1])
+    od.advection_kind = opt.advection_kind
+    for d in range(3):
+        od.dim_mask[d] = int(opt.dim_mask[d])
+    od.dispersion_model = opt.dispersion_model
+    od.stop_weak_sinks = int(opt.stop_weak_sinks)
+    od.stop_weak_sources = int(opt.stop_weak_sources)
+    od.backward = int(opt.backward)
+    od.stop_zone = int(opt.stop_zone)
+    od.uniform_porosity = int(opt.uniform_porosity)
+    od.rng_seed = int(opt.rng_seed) & 0xFFFFFFFFFFFFFFFF
+    od.precision = int(opt.precision)
+    return od
+
+
 class Tracker:
     """One device-resident tracking engine (one C-ABI handle)."""
 
@@ -126,23 +155,8 @@ class Tracker:
         self.grid = grid
         self.opt = opt
         self._keep = []
-        self._g = dict(delr=_f64(grid.delr), delc=_f64(grid.delc), top=_f64(grid.top), botm=_f64(grid.botm))
-        gd = GridDesc(grid.nlay, grid.nrow, grid.ncol, _p(self._g["delr"], _dp), _p(self._g["delc"], _dp),
-                      _p(self._g["top"], _dp), _p(self._g["botm"], _dp))
-        od = OptionsDesc()
-        od.time_step_kind = opt.time_step_kind
-        od.ts_param[0], od.ts_param[1] = float(opt.ts_param[0]), float(opt.ts_param[1])
-        od.advection_kind = opt.advection_kind
-        for d in range(3):
-            od.dim_mask[d] = int(opt.dim_mask[d])
-        od.dispersion_model = opt.dispersion_model
-        od.stop_weak_sinks = int(opt.stop_weak_sinks)
-        od.stop_weak_sources = int(opt.stop_weak_sources)
-        od.backward = int(opt.backward)
-        od.stop_zone = int(opt.stop_zone)
-        od.uniform_porosity = int(opt.uniform_porosity)
-        od.rng_seed = int(opt.rng_seed) & 0xFFFFFFFFFFFFFFFF
-        od.precision = int(opt.precision)
+        gd = _grid_desc(grid, self._keep)
+        od = _options_desc(opt)
         self.h = C.c_void_p()
         rc = self.lib.mprw_create(C.byref(self.h), C.byref(gd), C.byref(od))
         if rc != 0:
@@ -306,6 +320,131 @@ class Tracker:
         return dict(step_ms=s.value, prep_ms=p.value, hist_ms=h.value, gpkde_ms=k.value, launches=n.value)
 
     def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.mprw_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class _MemberView(Tracker):
+    """Tracker interface on one member of a Batch (mprw_batch_member): its
+    flow, particles, histogram, GPKDE and observations.  The batch owns the
+    handle; advancing is done on the batch."""
+
+    def __init__(self, batch: "Batch", k: int, grid: Grid):
+        self.lib = batch.lib
+        self.grid = grid
+        self.opt = batch.opt
+        self._keep = []
+        self._batch = batch
+        self.h = C.c_void_p()
+        rc = self.lib.mprw_batch_member(batch.h, int(k), C.byref(self.h))
+        if rc != 0:
+            raise MprwError(f"mprw_batch_member: rc={rc}: {self.lib.mprw_last_error(batch.h).decode()}")
+        self.n = 0
+
+    def advance(self, t_begin, t_end):
+        raise MprwError("a batch member is advanced by its batch")
+
+    def close(self):
+        self.h = C.c_void_p()
+
+
+class Batch:
+    """Several realizations (grids of any sizes, shared options) tracked in one
+    persistent launch per advance (mprw_create_batch).  ``member(k)`` is the
+    Tracker interface of realization k."""
+
+    def __init__(self, grids, opt: Options):
+        self.lib = load_library()
+        self.grids = list(grids)
+        self.opt = opt
+        self._keep = []
+        arr = (GridDesc * len(self.grids))(*[_grid_desc(g, self._keep) for g in self.grids])
+        od = _options_desc(opt)
+        self.h = C.c_void_p()
+        rc = self.lib.mprw_create_batch(C.byref(self.h), len(self.grids), arr, C.byref(od))
+        if rc != 0:
+            msg = self.lib.mprw_last_error(self.h).decode() if self.h.value else "mprw_create_batch failed"
+            if self.h.value:
+                self.lib.mprw_destroy(self.h)
+                self.h = C.c_void_p()
+            raise MprwError(f"mprw_create_batch: rc={rc}: {msg}")
+        self.members = [_MemberView(self, k, g) for k, g in enumerate(self.grids)]
+        self.counts = np.zeros(len(self.grids), np.int64)
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise MprwError(f"{what}: rc={rc}: {self.lib.mprw_last_error(self.h).decode()}")
+
+    def member(self, k: int) -> Tracker:
+        return self.members[k]
+
+    def load_flow(self, k: int, f: Flow):
+        self.members[k].load_flow(f)
+
+    def set_particles(self, parts):
+        """One Particles per member (cells 1-based in the member's grid)."""
+        parts = list(parts)
+        if len(parts) != len(self.members):
+            raise MprwError("set_particles: one particle set per member")
+        counts = np.array([p.n for p in parts], np.int64)
+
+        def cat(name, conv):
+            vals = [getattr(p, name) for p in parts]
+            if any(v is None for v in vals):
+                if all(v is None for v in vals):
+                    return None
+                if name == "mass":
+                    vals = [np.ones(p.n) if v is None else v for p, v in zip(parts, vals)]
+                else:
+                    raise MprwError(f"set_particles: {name} given for some members only")
+            return conv(np.concatenate([np.asarray(v) for v in vals]))
+
+        a = dict(cell=cat("cell", _i32), lx=cat("lx", _f64), ly=cat("ly", _f64), lz=cat("lz", _f64),
+                 t=cat("t", _f64), st=cat("status", _i32), m=cat("mass", _f64), id=cat("id", _u64),
+                 rc=cat("rng_ctr", _u64))
+        self._check(self.lib.mprw_set_particles_batch(
+            self.h, counts.ctypes.data_as(C.POINTER(C.c_int64)), _p(a["cell"], _ip), _p(a["lx"], _dp),
+            _p(a["ly"], _dp), _p(a["lz"], _dp), _p(a["t"], _dp), _p(a["st"], _ip), _p(a["m"], _dp),
+            _p(a["id"], _up), _p(a["rc"], _up)), "mprw_set_particles_batch")
+        self.counts = counts
+        for m, c in zip(self.members, counts):
+            m.n = int(c)
+
+    def advance(self, t_begin: float, t_end: float) -> int:
+        """Advance every member's particles in one launch; returns the total particle-steps."""
+        steps = C.c_int64(0)
+        self._check(self.lib.mprw_advance(self.h, float(t_begin), float(t_end), C.byref(steps)), "mprw_advance")
+        return steps.value
+
+    def get_particles(self, global_xyz: bool = True) -> list:
+        return [m.get_particles(global_xyz) for m in self.members]
+
+    def set_stream(self, stream_ptr: int):
+        self._check(self.lib.mprw_set_stream(self.h, C.c_void_p(stream_ptr)), "mprw_set_stream")
+
+    def timings(self) -> dict:
+        s, p, h, k = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        n = C.c_int64()
+        self._check(self.lib.mprw_last_timings(self.h, C.byref(s), C.byref(p), C.byref(h), C.byref(k), C.byref(n)),
+                    "mprw_last_timings")
+        return dict(step_ms=s.value, launches=n.value)
+
+    def close(self):
+        for m in getattr(self, "members", []):
+            m.close()
         if getattr(self, "h", None) is not None and self.h.value:
             self.lib.mprw_destroy(self.h)
             self.h = C.c_void_p()

@@ -19,7 +19,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .model import ADV, EULERIAN, FP64, MIN_ADV_DISP, PENDING, Flow, Grid, Options, Particles
+from .model import ADV, EULERIAN, FP64, MIN_ADV_DISP, MIXED, PENDING, Flow, Grid, Options, Particles
 
 
 def structured_grid(nlay, nrow, ncol, dx=1.0, dy=1.0, dz=1.0, top=None) -> Grid:
@@ -296,3 +296,42 @@ def config2(n_particles=1_000_000, nlay=20, nrow=100, ncol=200, seed=0, precisio
     opt = Options(time_step_kind=MIN_ADV_DISP, ts_param=(0.1, 0.1), advection_kind=EULERIAN, dim_mask=(1, 1, 1),
                   stop_weak_sinks=True, precision=precision)
     return g, f, p, opt, info
+
+
+def config3_params(n_real=64, scale=1.0):
+    """Per-realization draws of the ensemble: realization r draws, from
+    numpy's default_rng(r), the grid (ncol in [100, 400], nrow in [50, 200],
+    nlay in [10, 20], each uniform), sigma2 lnK in U[0.5, 2], alphaL in
+    U[0.1, 1] m (alphaT = alphaL / 10) and a particle count log-uniform in
+    [1e5, 4e6] (times ``scale``)."""
+    out = []
+    for r in range(n_real):
+        rng = np.random.default_rng(r)
+        ncol, nrow, nlay = int(rng.integers(100, 401)), int(rng.integers(50, 201)), int(rng.integers(10, 21))
+        sigma2 = float(rng.uniform(0.5, 2.0))
+        aL = float(rng.uniform(0.1, 1.0))
+        n = int(round(np.exp(rng.uniform(np.log(1e5), np.log(4e6))) * scale))
+        out.append(dict(r=r, ncol=ncol, nrow=nrow, nlay=nlay, sigma2=sigma2, alpha_l=aL, alpha_t=aL / 10.0,
+                        n_particles=max(n, 1)))
+    return out
+
+
+def config3(n_real=64, scale=1.0, precision=MIXED, use_torch=None, members=None):
+    """Ensemble of config-2-generator realizations (config3_params): per member
+    (grid, flow, particles); field seed r, placement seed 1000 + r; particle
+    ids (r << 40) + index, so every member has its own random streams and a
+    separate run of the member with the same ids draws the same ones.
+    ``members`` overrides the parameter list (for smaller ensembles)."""
+    params = config3_params(n_real, scale) if members is None else members
+    ens = []
+    for prm in params:
+        g, f, info = heterogeneous_flow(prm["nlay"], prm["nrow"], prm["ncol"], sigma2=prm["sigma2"], kg=10.0, lh=10.0,
+                                        lv=2.0, porosity=0.25, alpha_l=prm["alpha_l"], alpha_t=prm["alpha_t"],
+                                        dm=1e-4, seed=prm["r"], use_torch=use_torch)
+        p = release_in_box(g, prm["n_particles"], 0.0, min(10.0, float(prm["ncol"])), 0.0, float(prm["nrow"]),
+                           float(g.botm[-1]), float(g.top[0]), seed=1000 + prm["r"])
+        p.id = (np.uint64(prm["r"]) << np.uint64(40)) + np.arange(p.n, dtype=np.uint64)
+        ens.append((g, f, p))
+    opt = Options(time_step_kind=MIN_ADV_DISP, ts_param=(0.1, 0.1), advection_kind=EULERIAN, dim_mask=(1, 1, 1),
+                  stop_weak_sinks=True, precision=precision)
+    return ens, opt, params
