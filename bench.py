@@ -73,6 +73,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--realizations", type=int, default=16,
                     help="ensemble size of the batched leg (realizations 0..R-1 of the 64-member ensemble)")
+    ap.add_argument("--kde-streams", type=int, default=4,
+                    help="batched leg: reconstructions run concurrently (mprw_gpkde_batch concurrency)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="precision of the headline run (mixed: for profiling the MIXED kernel alone)")
     return ap.parse_args()
@@ -247,6 +249,7 @@ def run_gpu_arm(args, rank, world, local):
     if not args.no_e2e:
         res["e2e"] = e2e_run(args, g, f, p, opt, origin, bins, domain, flush)
     res["geom"] = (g, f, p, opt)
+    res["mf6_bytes"] = info["mf6_bytes"]
     if not args.no_batched and rank == 0:
         res["batched"] = batched_run(args, flush)
     return res
@@ -282,11 +285,8 @@ def batched_run(args, flush):
 
         def one_step(t):
             s = b.advance(t, t + INTERVAL_D)
-            nl = b.timings()["launches"]
-            for k, m in enumerate(b.members):
-                m.gpkde(doms[k], bins, precision=precision)
-                nl += m.timings()["launches"]
-            return s, nl
+            b.gpkde(doms, bins, precision=precision, concurrency=args.kde_streams)
+            return s
         for _ in range(args.warmup):
             one_step(t)
             t += INTERVAL_D
@@ -301,9 +301,8 @@ def batched_run(args, flush):
             adv_kern.append(b.timings()["step_ms"])
             launches += b.timings()["launches"]
             ev[k][1].record(stream)
-            for j, m in enumerate(b.members):
-                m.gpkde(doms[j], bins, precision=precision)
-                launches += m.timings()["launches"]
+            b.gpkde(doms, bins, precision=precision, concurrency=args.kde_streams)
+            launches += b.timings()["launches"]
             ev[k][2].record(stream)
             torch.cuda.synchronize()
             steps += s
@@ -335,7 +334,7 @@ def batched_run(args, flush):
     return {"workload": f"realizations 0..{len(ens) - 1} of the 64-member ensemble (config-2 generator; grids "
                         "U[100..400]x[50..200]x[10..20], sigma2 lnK U[0.5,2], alphaL U[0.1,1], alphaT = alphaL/10, "
                         "particles log-U[1e5,4e6]), one batch: one advance launch for all realizations + one "
-                        "GPKDE per realization per 10-day step",
+                        f"GPKDE per realization per 10-day step ({args.kde_streams} reconstructions at a time)",
             "realizations": len(ens), "particles": int(sum(p.n for _, _, p in ens)),
             "cells": int(sum(g.ncell for g, _, _ in ens)), "setup_s": t_setup,
             "value": v32, "unit": UNIT, "ms_per_step": mx["ms"] / args.steps,
@@ -466,7 +465,7 @@ def main():
                                "(advance + GPKDE reconstruction on the 1 m grid, density and histogram to host)",
                    "particles_per_gpu": args.particles, "interval_days": INTERVAL_D,
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"particles x{world}",
-                   "flow_input": f"MODFLOW 6 binary .grb/.hds/.bud ({info['mf6_bytes']} B: FLOW-JA-FACE imeth 1, "
+                   "flow_input": f"MODFLOW 6 binary .grb/.hds/.bud ({res['mf6_bytes']} B: FLOW-JA-FACE imeth 1, "
                                  "CHD imeth 6) written from the CG solve and read back by mprw.mf6io"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": f"{peak_kind} hbm_gbs",

@@ -269,6 +269,18 @@ int mprw_set_particles_batch(mprw_handle *batch, const int64_t *counts, const in
                              const int32_t *status, const double *mass, const uint64_t *id,
                              const uint64_t *rng_ctr);
 
+/* GPKDE of every member of a batch (as mprw_gpkde on each member view), up to
+ * `concurrency` members at a time (<= 0: 4; at most 16), each on its own
+ * non-blocking stream driven by its own host thread, so that one member's
+ * host round trips and small launches overlap another's kernels.  opts,
+ * density and loops_done (may be NULL) have one entry per member; histogram
+ * may be NULL or hold one pointer (NULL allowed) per member.  The
+ * reconstructions see the particles after the batch's last advance.  Each
+ * concurrency slot keeps its own reconstruction state (pass buffers sized
+ * for the largest grid it has reconstructed). */
+int mprw_gpkde_batch(mprw_handle *batch, const mprw_gpkde_options *opts, double *const *density,
+                     double *const *histogram, int32_t *loops_done, int32_t concurrency);
+
 /* Optional: launch on a caller-provided cudaStream_t (NULL = the handle's). */
 int mprw_set_stream(mprw_handle *h, void *stream);
 

@@ -13,10 +13,13 @@
 // handles whose record, IBOUNDTS, flag and particle pointers alias their
 // slices of the batch; per-realization calls (load_flow, get_particles,
 // histogram, gpkde, observations) go through them.
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/mprw_gpu.h"
@@ -24,6 +27,13 @@
 #include "mprw_kernels.cuh"
 
 using namespace mprw;
+
+// One concurrent reconstruction slot of a batch (mprw_gpkde_batch): a
+// non-blocking stream and the GPKDE state that reconstructions on it use.
+struct KdeWorker {
+  cudaStream_t stream = nullptr;
+  KdeState kde;
+};
 
 struct mprw_handle {
   int device = 0;
@@ -75,9 +85,6 @@ struct mprw_handle {
   double last_t_begin = 0.0, last_t_end = 0.0;
   bool advanced = false;
   double *d_kpart = nullptr;          // coordinate-statistics partials
-  double *h_kout = nullptr;           // pinned staging of the density / histogram grids
-  int64_t h_kout_cap = 0;
-  std::vector<double> kde_table_key;  // database parameters of the uploaded factor tables (of *kdep)
   double *d_counts = nullptr;
   int64_t counts_cap = 0;
   int64_t launches = 0;
@@ -90,6 +97,7 @@ struct mprw_handle {
   int32_t cell0 = 0;                    // member: first cell in the batch's cell numbering
   int64_t p0 = 0;                       // member: first particle in the batch's particle arrays
   KdeState *kdep = &kde;                // GPKDE state (a member uses the batch's)
+  std::vector<KdeWorker *> kde_workers; // batch: concurrent reconstruction slots
 };
 
 namespace {
@@ -140,6 +148,12 @@ void free_all(mprw_handle *h) {
     delete m;
   }
   h->members.clear();
+  for (KdeWorker *w : h->kde_workers) {
+    w->kde.release();
+    if (w->stream) cudaStreamDestroy(w->stream);
+    delete w;
+  }
+  h->kde_workers.clear();
   void *ptrs[] = {h->d_delr, h->d_delc, h->d_top, h->d_botm, h->d_colL, h->d_colR, h->d_rowF, h->d_rowB,
                   h->d_sattop, h->d_ia, h->d_ja, h->d_flowja, h->d_bflow, h->d_por, h->d_ret, h->d_heads,
                   h->d_src, h->d_snk, h->d_aL, h->d_aT, h->d_dm, h->d_aLV, h->d_aTV, h->d_ibts, h->d_icb, h->d_ctype,
@@ -153,7 +167,6 @@ void free_all(mprw_handle *h) {
   if (h->d_kpart) cudaFree(h->d_kpart);
   for (void *p : {(void *)h->d_obs_of_cell, (void *)h->d_obs_style, (void *)h->d_obs_count, (void *)h->d_obs_mass})
     if (p) cudaFree(p);
-  if (h->h_kout) cudaFreeHost(h->h_kout);
   h->kde.release();  // (a member view's own state is empty)
   if (h->hscratch) cudaFreeHost(h->hscratch);
   cudaEvent_t evs[] = {h->ev0, h->ev1, h->ev2, h->ev3};
@@ -982,7 +995,6 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
   P.min_dim = mind;
 
   cudaStream_t s = h->stream;
-  mprw_handle *rt = h->parent ? h->parent : h;  // owner of the GPKDE state and the pinned staging
   h->launches = 0;
   h->kdep->launches = 0;
   CK(cudaEventRecord(h->ev2, s));
@@ -1039,7 +1051,7 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
     std::vector<double> key = {(double)P.ndim, (double)P.ndelta, P.bin[0], P.bin[1], P.bin[2],
                                (double)P.mask[0], (double)P.mask[1], (double)P.mask[2]};
     key.insert(key.end(), P.hod, P.hod + P.ndelta);
-    if (!h->kdep->d_val || key != rt->kde_table_key) {
+    if (!h->kdep->d_val || key != h->kdep->table_key) {
       std::vector<double> val;
       std::vector<int> wm, wofs, sm[3], sofs[3];
       kde_build_tables(P, val, wm, wofs, sm, sofs);
@@ -1048,7 +1060,7 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
       if (h->kdep->d_meta) cudaFree(h->kdep->d_meta);
       h->kdep->d_val = nullptr;
       h->kdep->d_meta = nullptr;
-      rt->kde_table_key.clear();
+      h->kdep->table_key.clear();
       CK(cudaMalloc(&h->kdep->d_val, sizeof(double) * val.size()));
       CK(cudaMalloc(&h->kdep->d_meta, sizeof(int) * 8 * 3 * KDE_MAXDB));
       std::vector<int> meta;
@@ -1066,7 +1078,7 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
       CK(cudaMemcpyAsync(h->kdep->d_valf, valf.data(), sizeof(float) * valf.size(), cudaMemcpyHostToDevice, s));
       CK(cudaMemcpyAsync(h->kdep->d_meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, s));
       CK(cudaStreamSynchronize(s));  // the host vectors go out of scope
-      rt->kde_table_key = key;
+      h->kdep->table_key = key;
     }
     const int L = 3 * KDE_MAXDB;
     h->kdep->wtab = KdeTable{h->kdep->d_val, h->kdep->d_meta, h->kdep->d_meta + L};
@@ -1087,29 +1099,88 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
   }
   // outputs through pinned staging (density, then histogram)
   const int64_t nout = histogram ? 2 * ngrid : ngrid;
-  if (nout > rt->h_kout_cap) {
+  if (nout > h->kdep->h_out_cap) {
     CK(cudaStreamSynchronize(s));
-    if (rt->h_kout) cudaFreeHost(rt->h_kout);
-    rt->h_kout = nullptr;
-    rt->h_kout_cap = 0;
-    CK(cudaMallocHost(&rt->h_kout, sizeof(double) * nout));
-    rt->h_kout_cap = nout;
+    if (h->kdep->h_out) cudaFreeHost(h->kdep->h_out);
+    h->kdep->h_out = nullptr;
+    h->kdep->h_out_cap = 0;
+    CK(cudaMallocHost(&h->kdep->h_out, sizeof(double) * nout));
+    h->kdep->h_out_cap = nout;
   }
-  CK(cudaMemcpyAsync(rt->h_kout, h->kdep->dens_out, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(h->kdep->h_out, h->kdep->dens_out, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
   if (histogram) {
     mul2_kernel<<<grid1d(ngrid), 256, 0, s>>>(h->d_counts, ngrid, eff, 1.0);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(rt->h_kout + ngrid, h->d_counts, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h->kdep->h_out + ngrid, h->d_counts, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
   }
   CK(cudaEventRecord(h->ev3, s));
   CK(cudaStreamSynchronize(s));
-  std::memcpy(density, rt->h_kout, sizeof(double) * ngrid);
-  if (histogram) std::memcpy(histogram, rt->h_kout + ngrid, sizeof(double) * ngrid);
+  std::memcpy(density, h->kdep->h_out, sizeof(double) * ngrid);
+  if (histogram) std::memcpy(histogram, h->kdep->h_out + ngrid, sizeof(double) * ngrid);
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, h->ev2, h->ev3));
   h->kde_ms = ms;
   h->launches += h->kdep->launches + 2;
   if (loops_done) *loops_done = loops;
+  return MPRW_OK;
+}
+
+int mprw_gpkde_batch(mprw_handle *h, const mprw_gpkde_options *opts, double *const *density,
+                     double *const *histogram, int32_t *loops_done, int32_t concurrency) {
+  if (!h) return MPRW_E_INVAL;
+  if (h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_gpkde_batch: not a batch handle");
+  if (!opts || !density) return fail(h, MPRW_E_INVAL, "mprw_gpkde_batch: null argument");
+  const int nm = (int)h->members.size();
+  for (int k = 0; k < nm; ++k)
+    if (!density[k]) return fail(h, MPRW_E_INVAL, "mprw_gpkde_batch: null density for member " + std::to_string(k));
+  int nw = concurrency > 0 ? concurrency : 4;
+  if (nw > 16) nw = 16;
+  if (nw > nm) nw = nm;
+  while ((int)h->kde_workers.size() < nw) {
+    KdeWorker *w = new KdeWorker();
+    h->kde_workers.push_back(w);
+    CK(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  // the reconstructions read what the batch's stream last wrote
+  CK(cudaEventRecord(h->ev2, h->stream));
+  for (int i = 0; i < nw; ++i) CK(cudaStreamWaitEvent(h->kde_workers[i]->stream, h->ev2, 0));
+  std::atomic<int> next{0};
+  std::vector<int> rcs(nw, MPRW_OK);
+  std::vector<std::string> errs(nw);
+  std::vector<int64_t> launches(nw, 0);
+  auto work = [&](int i) {
+    KdeWorker *w = h->kde_workers[i];
+    for (;;) {
+      const int k = next.fetch_add(1);
+      if (k >= nm) break;
+      mprw_handle *m = h->members[k];
+      cudaStream_t s0 = m->stream;
+      KdeState *k0 = m->kdep;
+      m->stream = w->stream;
+      m->kdep = &w->kde;
+      const int rc = mprw_gpkde(m, &opts[k], density[k], histogram ? histogram[k] : nullptr, nullptr,
+                                loops_done ? &loops_done[k] : nullptr);
+      m->stream = s0;
+      m->kdep = k0;
+      launches[i] += m->launches;
+      if (rc != MPRW_OK) {
+        rcs[i] = rc;
+        errs[i] = "member " + std::to_string(k) + ": " + m->err;
+        next.store(nm);
+        break;
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int i = 1; i < nw; ++i) pool.emplace_back(work, i);
+  work(0);
+  for (auto &t : pool) t.join();
+  for (int i = 0; i < nw; ++i)
+    if (rcs[i] != MPRW_OK) return fail(h, rcs[i], errs[i]);
+  h->launches = 0;
+  for (int i = 0; i < nw; ++i) h->launches += launches[i];
+  h->kde_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return MPRW_OK;
 }
 

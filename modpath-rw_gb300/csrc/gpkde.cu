@@ -1141,6 +1141,7 @@ void KdeState::release() {
     if (p) cudaFree(p);
   if (h_scalars) cudaFreeHost(h_scalars);
   if (h_need) cudaFreeHost(h_need);
+  if (h_out) cudaFreeHost(h_out);
   *this = KdeState();
 }
 

@@ -102,6 +102,9 @@ struct KdeState {
   double *d_val = nullptr;
   float *d_valf = nullptr;  // the factor values in FP32
   int *d_meta = nullptr;    // wm, wofs, sm[3], sofs[3]
+  std::vector<double> table_key;  // database parameters of the uploaded factor tables
+  double *h_out = nullptr;  // pinned staging of the density / histogram grids
+  int64_t h_out_cap = 0;
   int64_t launches = 0;
 
   template <typename T>

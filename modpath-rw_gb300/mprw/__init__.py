@@ -96,6 +96,8 @@ def load_library() -> C.CDLL:
         "mprw_batch_member": (C.c_int, [H, C.c_int32, C.POINTER(H)]),
         "mprw_set_particles_batch": (C.c_int, [H, C.POINTER(C.c_int64), _ip, _dp, _dp, _dp, _dp, _ip, _dp, _up,
                                                _up]),
+        "mprw_gpkde_batch": (C.c_int, [H, C.POINTER(GpkdeOptions), C.POINTER(_dp), C.POINTER(_dp), _ip,
+                                       C.c_int32]),
         "mprw_last_error": (C.c_char_p, [H]),
     }
     for name, (res, args) in sig.items():
@@ -432,6 +434,33 @@ class Batch:
     def get_particles(self, global_xyz: bool = True) -> list:
         return [m.get_particles(global_xyz) for m in self.members]
 
+    def gpkde(self, domains, bin_size, origin=(0.0, 0.0, 0.0), n_opt_loops=10, kdb=(0.3, 0.3, 15.0), rel_err=0.02,
+              skip_error=False, unit_volume=True, scaling_factor=1.0, precision=FP64, concurrency=4,
+              histograms=False):
+        """GPKDE of every member (mprw_gpkde_batch), ``domains[k]`` the domain
+        size of member k's reconstruction grid.  Returns a list of densities
+        (and histograms) shaped (nz, ny, nx), and the loops run per member."""
+        nm = len(self.members)
+        opts = (GpkdeOptions * nm)()
+        dens, hists, shapes = [], [], []
+        for k in range(nm):
+            o = Tracker.gpkde_options(domains[k], bin_size, origin, n_opt_loops, kdb, rel_err, skip_error,
+                                      unit_volume, scaling_factor, precision)
+            C.memmove(C.byref(opts, k * C.sizeof(GpkdeOptions)), C.byref(o), C.sizeof(GpkdeOptions))
+            nb = [int(domains[k][d] / bin_size[d] + 0.5) if bin_size[d] != 0 else 1 for d in range(3)]
+            shapes.append((nb[2], nb[1], nb[0]))
+            dens.append(np.empty(int(np.prod(nb))))
+            hists.append(np.empty(int(np.prod(nb))) if histograms else None)
+        dp = (_dp * nm)(*[_p(d, _dp) for d in dens])
+        hp = (_dp * nm)(*[_p(h, _dp) for h in hists]) if histograms else None
+        loops = np.zeros(nm, np.int32)
+        self._check(self.lib.mprw_gpkde_batch(self.h, opts, dp, hp, _p(loops, _ip), int(concurrency)),
+                    "mprw_gpkde_batch")
+        dens = [d.reshape(s) for d, s in zip(dens, shapes)]
+        if histograms:
+            return dens, [h.reshape(s) for h, s in zip(hists, shapes)], loops
+        return dens, loops
+
     def set_stream(self, stream_ptr: int):
         self._check(self.lib.mprw_set_stream(self.h, C.c_void_p(stream_ptr)), "mprw_set_stream")
 
@@ -440,7 +469,7 @@ class Batch:
         n = C.c_int64()
         self._check(self.lib.mprw_last_timings(self.h, C.byref(s), C.byref(p), C.byref(h), C.byref(k), C.byref(n)),
                     "mprw_last_timings")
-        return dict(step_ms=s.value, launches=n.value)
+        return dict(step_ms=s.value, gpkde_ms=k.value, launches=n.value)
 
     def close(self):
         for m in getattr(self, "members", []):

@@ -48,9 +48,14 @@ def test_batch_members_equal_separate_runs(gpu_lib, precision):
     b.set_particles([m[2] for m in mem])
     steps = sum(b.advance(t0, t1) for t0, t1 in iv)
     outs = b.get_particles()
+    doms = [(float(g.ncol), float(g.nrow), float(g.top[0] - g.botm[-1])) for g, _, _ in mem]
+    # every member at once, three reconstructions in flight
+    dens_all, loops = b.gpkde(doms, (1.0, 1.0, 1.0), concurrency=3)
+    assert (loops >= 1).all()
     total = 0
     for k, (g, f, p) in enumerate(mem):
         ref, s, hist, dens = _separate(g, f, p, opt, iv)
+        assert np.linalg.norm(dens_all[k] - dens) <= 1e-9 * np.linalg.norm(dens)
         total += s
         for key in ("cell", "status", "lx", "ly", "lz", "t", "rng_ctr", "gx", "gy", "gz"):
             np.testing.assert_array_equal(outs[k][key], ref[key], err_msg=f"member {k}: {key}")
