@@ -106,34 +106,25 @@ __device__ __forceinline__ double normal_ih12(uint64_t seed, uint64_t id, uint64
   return d - 1048582.0;  // 2^20 + 6
 }
 
-// MIXED-precision normals: the same Irwin-Hall(12) distribution on 8-bit
-// uniforms.  One 32-bit word holds four bytes b_i; a normal sums the 12 bytes
-// of three words with dp4a: xi = (sum + 6)/256 - 6, i.e. sum_i (b_i+0.5)/256 - 6,
-// exactly representable in FP32.  Three normals use 9 words of 3 Philox
-// blocks (ctr advances by ceil(3*ndim/4)).
-__device__ __forceinline__ void normals_ih12_u8(int ndim, uint64_t seed, uint64_t id, uint64_t &ctr,
-                                                float out[3]) {
-  uint32_t w[12];
-  const int nblk = (3 * ndim + 3) / 4;
+// MIXED-precision normals: the same three Philox blocks (twelve 32-bit
+// words) as normal_ih12, so both precisions draw the same normal from the
+// same counter (common random numbers); only the final value is rounded to
+// FP32.  With S = hi*2^32 + lo the normal is (hi - 6) + lo*2^-32: hi - 6 is an
+// exact small integer, lo*2^-32 < 1 carries one FP32 rounding, and the FMA
+// adds a second, so the result is within 2^-23 of the FP64 normal.
+__device__ __forceinline__ float normal_ih12_f32(uint64_t seed, uint64_t id, uint64_t &ctr) {
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  uint32_t i0 = (uint32_t)id, i1 = (uint32_t)(id >> 32);
+  uint64_t sum = 0;
 #pragma unroll
   for (int b = 0; b < 3; ++b) {
-    if (b < nblk) {
-      uint64_t n = ctr++;
-      philox4x32_10((uint32_t)n, (uint32_t)(n >> 32), (uint32_t)id, (uint32_t)(id >> 32), (uint32_t)seed,
-                    (uint32_t)(seed >> 32), &w[4 * b]);
-    }
+    uint64_t n = ctr++;
+    uint32_t o[4];
+    philox4x32_10((uint32_t)n, (uint32_t)(n >> 32), i0, i1, k0, k1, o);
+    sum += (uint64_t)o[0] + o[1] + o[2] + o[3];
   }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    if (k < ndim) {
-      unsigned s = __dp4a(w[3 * k], 0x01010101u, 0u);  // unsigned bytes
-      s = __dp4a(w[3 * k + 1], 0x01010101u, s);
-      s = __dp4a(w[3 * k + 2], 0x01010101u, s);
-      out[k] = fmaf((float)s, 0.00390625f, -5.9765625f);  // (s + 6)/256 - 6
-    } else {
-      out[k] = 0.0f;
-    }
-  }
+  const int hi = (int)(sum >> 32);
+  return fmaf(__uint2float_rn((uint32_t)sum), 2.3283064365386963e-10f, (float)(hi - 6));  // 2^-32
 }
 
 // Driver status codes (MPathRW.F90:1337-1403).

@@ -69,8 +69,8 @@ __device__ __forceinline__ R divc(const Lane<R> &F, int base, R x, R y, R z, R x
 }
 
 // The step's standard normals, the reference's Irwin-Hall(12) distribution
-// in both paths: FP64 -- exact 32-bit uniforms (3 Philox blocks per normal);
-// MIXED -- 8-bit uniforms summed with dp4a (3 blocks per 3-D step).
+// in both paths, from the same 3 Philox blocks per normal: FP64 exact, MIXED
+// rounded to FP32 (the two precisions share their random numbers).
 template <typename R>
 struct Normals;
 template <>
@@ -86,11 +86,9 @@ template <>
 struct Normals<float> {
   __device__ __forceinline__ static void draw(int ndim, uint64_t seed, uint64_t id, uint64_t &ctr, float &r0,
                                               float &r1, float &r2) {
-    float v[3];
-    normals_ih12_u8(ndim, seed, id, ctr, v);
-    r0 = v[0];
-    r1 = v[1];
-    r2 = v[2];
+    r0 = normal_ih12_f32(seed, id, ctr);
+    r1 = (ndim > 1) ? normal_ih12_f32(seed, id, ctr) : 0.0f;
+    r2 = (ndim > 2) ? normal_ih12_f32(seed, id, ctr) : 0.0f;
   }
 };
 

@@ -10,7 +10,8 @@
 * heterogeneous lognormal field with weak-sink stops: same statuses and
   positions;
 * GPKDE histogram: bit-identical counts for identical particle positions;
-* MIXED precision: plume moments within 0.5 % of the FP64 path.
+* MIXED precision: the same normals as the FP64 path (common random
+  numbers), plume moments within 0.1 % (mean) and 0.5 % (variance).
 """
 import numpy as np
 import pytest
@@ -186,12 +187,16 @@ def test_mixed_precision_moments(gpu_lib):
     gp, _ = run_gpu(g, f, opt, p, iv)
     opt.precision = MIXED
     gm, _ = run_gpu(g, f, opt, p, iv)
-    for k in ("gx",):
+    # both precisions draw the same normals from the same counters (common
+    # random numbers), so the plumes differ by rounding, not by sampling noise
+    for k in ("gx", "gy", "gz"):
         m1, m2 = gp[k].mean(), gm[k].mean()
         v1, v2 = gp[k].var(), gm[k].var()
-        assert abs(m2 - m1) / abs(m1) < 0.005
-        assert abs(v2 - v1) / v1 < 0.005 + 3 * np.sqrt(2.0 / p.n)
+        assert abs(m2 - m1) / abs(m1) < 1e-3
+        assert abs(v2 - v1) / v1 < 5e-3
     assert (gm["status"] == ACTIVE).all()
+    assert (gm["rng_ctr"] == gp["rng_ctr"]).mean() > 0.95
+    assert np.median(np.abs(gm["gx"] - gp["gx"])) < 1e-3
 
 
 def _graded_particles(n, seed=11):
