@@ -281,6 +281,31 @@ int mprw_set_particles_batch(mprw_handle *batch, const int64_t *counts, const in
 int mprw_gpkde_batch(mprw_handle *batch, const mprw_gpkde_options *opts, double *const *density,
                      double *const *histogram, int32_t *loops_done, int32_t concurrency);
 
+/* Launch tuning of mprw_advance.  No counterpart in the reference (its loop
+ * is `!$omp parallel do schedule(dynamic,1)`).  blocks_per_sm: resident
+ * blocks per SM of the persistent step kernel (0 = the variant's default: 3
+ * for EULERIAN MIXED, else 1; at most what its registers allow, which
+ * mprw_get_tuning reports as max_blocks); sort_interval: the particles are
+ * sorted by cell before every k-th advance and processed in that order
+ * until the next sort (1 = every advance, the default; 0 = never).  Results
+ * do not depend on the tuning: each particle's steps use only its own state
+ * and its own counter-based random numbers.
+ *
+ * mprw_autotune picks both on the handle's real work: from the current
+ * particle state it runs one advance over [t_begin, t_end] per candidate
+ * (sorted first, with 1 .. min(max_blocks, 4) blocks per SM, then the best
+ * block count unsorted), restoring the state before each trial and at the
+ * end, so the particles are unchanged on return.  The fastest block count
+ * (particle-steps per ms, sort included) is kept; sorting is kept every
+ * advance if it pays, every 4th if unsorted is within 3 %, never if unsorted
+ * is more than 5 % faster.  rates (may be NULL; room for 5 doubles) receives
+ * the particle-steps per ms of each trial in that order.  Costs one extra
+ * copy of the particle state on the device. */
+int mprw_set_tuning(mprw_handle *h, int32_t blocks_per_sm, int32_t sort_interval);
+int mprw_get_tuning(mprw_handle *h, int32_t *blocks_per_sm, int32_t *sort_interval, int32_t *max_blocks);
+int mprw_autotune(mprw_handle *h, double t_begin, double t_end, int32_t *blocks_per_sm, int32_t *sort_interval,
+                  double *rates);
+
 /* Optional: launch on a caller-provided cudaStream_t (NULL = the handle's). */
 int mprw_set_stream(mprw_handle *h, void *stream);
 

@@ -13,6 +13,7 @@
 // handles whose record, IBOUNDTS, flag and particle pointers alias their
 // slices of the batch; per-realization calls (load_flow, get_particles,
 // histogram, gpkde, observations) go through them.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -89,7 +90,11 @@ struct mprw_handle {
   int64_t counts_cap = 0;
   int64_t launches = 0;
   int sms = 152;
-  int sort_enabled = 1;
+  // launch tuning (mprw_set_tuning / mprw_autotune)
+  int blocks_per_sm = 0;     // 0: the variant's default
+  int sort_interval = 1;     // sort by cell every k-th advance (0 never)
+  int64_t advance_count = 0;
+  bool perm_valid = false;   // d_perm holds a permutation of the current n particles
   std::string err;
   // batched realizations
   mprw_handle *parent = nullptr;        // member view: the batch it belongs to
@@ -525,6 +530,8 @@ int upload_particles(mprw_handle *h, int64_t n, const int32_t *cell, const doubl
     h->cap = n;
   }
   h->n = n;
+  h->perm_valid = false;
+  h->advance_count = 0;
   if (n == 0) return MPRW_OK;
   cudaStream_t s = h->stream;
   CK(cudaMemcpyAsync(h->d_cell, cell, 4 * n, cudaMemcpyHostToDevice, s));
@@ -637,6 +644,110 @@ int mprw_set_particles_batch(mprw_handle *h, const int64_t *counts, const int32_
   return MPRW_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Resident blocks per SM of the step kernel variant a handle launches: the
+// tuned value, capped by what the variant's registers and shared memory allow.
+int max_blocks_per_sm(mprw_handle *h) {
+  const bool mixed = h->opt.precision == MPRW_MIXED;
+  const bool exp_adv = h->opt.advection_kind == 1, axi = h->opt.dispersion_model == 1;
+  int nb = 0;
+  cudaError_t e = mixed ? advance_occupancy<float>(exp_adv, axi, kStepThreads, &nb)
+                        : advance_occupancy<double>(exp_adv, axi, kStepThreads, &nb);
+  if (e != cudaSuccess || nb < 1) nb = 1;
+  return nb;
+}
+
+int default_blocks_per_sm(mprw_handle *h) {
+  // EULERIAN MIXED is compiled for 3 resident blocks per SM (80 registers)
+  return (h->opt.precision == MPRW_MIXED && h->opt.advection_kind != 1) ? 3 : 1;
+}
+
+// One launch of the persistent step kernel over every particle, processing
+// them in the order of d_perm when use_perm; *ms the event-timed duration.
+int launch_step(mprw_handle *h, double t_begin, double t_end, int bps, bool use_perm, float *ms, int64_t *steps) {
+  cudaStream_t s = h->stream;
+  CK(cudaMemsetAsync(h->d_counters, 0, 4 * sizeof(unsigned long long), s));
+  const int threads = kStepThreads;
+  int64_t need = (h->n + threads - 1) / threads;
+  int64_t blocks = (int64_t)h->sms * bps;
+  if (need < blocks) blocks = need;
+  CK(cudaEventRecord(h->ev0, s));
+  if (h->opt.precision == MPRW_MIXED) {
+    AdvanceArgs<float> a{};
+    a.recs = h->d_rec32;
+    a.iboundts = h->d_ibts;
+    a.cellflags = h->base.flags;
+    a.cell = h->d_cell;
+    a.status = h->d_status;
+    a.x = (float *)h->d_x;
+    a.y = (float *)h->d_y;
+    a.z = (float *)h->d_z;
+    a.t = h->d_t;
+    a.ctr = h->d_ctr;
+    a.id = h->has_id ? h->d_id : nullptr;
+    a.perm = use_perm ? h->d_perm : nullptr;
+    a.queue = h->d_counters;
+    a.steps = h->d_counters + 1;
+    a.n = h->n;
+    a.t_begin = t_begin;
+    a.t_end = t_end;
+    a.ndim = h->ndim;
+    a.d1 = h->d1;
+    a.d2 = h->d2;
+    a.seed = h->opt.rng_seed;
+    a.exp_adv = h->opt.advection_kind == 1;
+    a.axi = h->opt.dispersion_model == 1;
+    CK(launch_advance<float>(a, (int)blocks, threads, s));
+  } else {
+    AdvanceArgs<double> a{};
+    a.recs = h->d_rec64;
+    a.iboundts = h->d_ibts;
+    a.cellflags = h->base.flags;
+    a.cell = h->d_cell;
+    a.status = h->d_status;
+    a.x = (double *)h->d_x;
+    a.y = (double *)h->d_y;
+    a.z = (double *)h->d_z;
+    a.t = h->d_t;
+    a.ctr = h->d_ctr;
+    a.id = h->has_id ? h->d_id : nullptr;
+    a.perm = use_perm ? h->d_perm : nullptr;
+    a.queue = h->d_counters;
+    a.steps = h->d_counters + 1;
+    a.n = h->n;
+    a.t_begin = t_begin;
+    a.t_end = t_end;
+    a.ndim = h->ndim;
+    a.d1 = h->d1;
+    a.d2 = h->d2;
+    a.seed = h->opt.rng_seed;
+    a.exp_adv = h->opt.advection_kind == 1;
+    a.axi = h->opt.dispersion_model == 1;
+    CK(launch_advance<double>(a, (int)blocks, threads, s));
+  }
+  h->launches += 1;
+  CK(cudaEventRecord(h->ev1, s));
+  CK(cudaMemcpyAsync(h->h_counters, h->d_counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaEventElapsedTime(ms, h->ev0, h->ev1));
+  *steps = (int64_t)h->h_counters[1];
+  return MPRW_OK;
+}
+
+int sort_particles(mprw_handle *h) {
+  CK(sort_cells(h->d_cell, h->d_perm, h->n, h->ncell_bits, &h->scratch, &h->scratch_bytes, h->stream));
+  h->launches += 2;
+  h->perm_valid = true;
+  return MPRW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_done) {
   if (!h) return MPRW_E_INVAL;
   if (h->parent) return fail(h, MPRW_E_STATE, "mprw_advance on a batch member: advance the batch");
@@ -661,83 +772,128 @@ int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_do
     if (steps_done) *steps_done = 0;
     return MPRW_OK;
   }
-  cudaStream_t s = h->stream;
-  if (h->sort_enabled) {
-    CK(sort_cells(h->d_cell, h->d_perm, h->n, h->ncell_bits, &h->scratch, &h->scratch_bytes, s));
-    h->launches += 2;
+  // sort the particles by cell every sort_interval-th advance; in between the
+  // last order is reused (the permutation stays valid while n is unchanged)
+  if (h->sort_interval > 0 && (h->advance_count % h->sort_interval == 0 || !h->perm_valid)) {
+    int rc = sort_particles(h);
+    if (rc != MPRW_OK) return rc;
   }
-  CK(cudaMemsetAsync(h->d_counters, 0, 4 * sizeof(unsigned long long), s));
-  const bool mixed = h->opt.precision == MPRW_MIXED;
-  const int threads = kStepThreads;
-  CK(cudaEventRecord(h->ev0, s));
-  if (mixed) {
-    AdvanceArgs<float> a{};
-    a.recs = h->d_rec32;
-    a.iboundts = h->d_ibts;
-    a.cellflags = h->base.flags;
-    a.cell = h->d_cell;
-    a.status = h->d_status;
-    a.x = (float *)h->d_x;
-    a.y = (float *)h->d_y;
-    a.z = (float *)h->d_z;
-    a.t = h->d_t;
-    a.ctr = h->d_ctr;
-    a.id = h->has_id ? h->d_id : nullptr;
-    a.perm = h->sort_enabled ? h->d_perm : nullptr;
-    a.queue = h->d_counters;
-    a.steps = h->d_counters + 1;
-    a.n = h->n;
-    a.t_begin = t_begin;
-    a.t_end = t_end;
-    a.ndim = h->ndim;
-    a.d1 = h->d1;
-    a.d2 = h->d2;
-    a.seed = h->opt.rng_seed;
-    a.exp_adv = h->opt.advection_kind == 1;
-    a.axi = h->opt.dispersion_model == 1;
-    // EULERIAN MIXED is compiled for 3 resident blocks per SM (80 registers)
-    int blocks = h->sms * (a.exp_adv ? 1 : 3);
-    int64_t need = (h->n + threads - 1) / threads;
-    if (need < blocks) blocks = (int)need;
-    CK(launch_advance<float>(a, blocks, threads, s));
-  } else {
-    AdvanceArgs<double> a{};
-    a.recs = h->d_rec64;
-    a.iboundts = h->d_ibts;
-    a.cellflags = h->base.flags;
-    a.cell = h->d_cell;
-    a.status = h->d_status;
-    a.x = (double *)h->d_x;
-    a.y = (double *)h->d_y;
-    a.z = (double *)h->d_z;
-    a.t = h->d_t;
-    a.ctr = h->d_ctr;
-    a.id = h->has_id ? h->d_id : nullptr;
-    a.perm = h->sort_enabled ? h->d_perm : nullptr;
-    a.queue = h->d_counters;
-    a.steps = h->d_counters + 1;
-    a.n = h->n;
-    a.t_begin = t_begin;
-    a.t_end = t_end;
-    a.ndim = h->ndim;
-    a.d1 = h->d1;
-    a.d2 = h->d2;
-    a.seed = h->opt.rng_seed;
-    a.exp_adv = h->opt.advection_kind == 1;
-    a.axi = h->opt.dispersion_model == 1;
-    int blocks = h->sms * 1;
-    int64_t need = (h->n + threads - 1) / threads;
-    if (need < blocks) blocks = (int)need;
-    CK(launch_advance<double>(a, blocks, threads, s));
-  }
-  h->launches += 1;
-  CK(cudaEventRecord(h->ev1, s));
-  CK(cudaMemcpyAsync(h->h_counters, h->d_counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
+  ++h->advance_count;
+  const int bps = h->blocks_per_sm > 0 ? h->blocks_per_sm : default_blocks_per_sm(h);
   float ms = 0;
-  CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  int64_t steps = 0;
+  int rc = launch_step(h, t_begin, t_end, bps, h->sort_interval > 0 && h->perm_valid, &ms, &steps);
+  if (rc != MPRW_OK) return rc;
   h->step_ms = ms;
-  if (steps_done) *steps_done = (int64_t)h->h_counters[1];
+  if (steps_done) *steps_done = steps;
+  return MPRW_OK;
+}
+
+int mprw_set_tuning(mprw_handle *h, int32_t blocks_per_sm, int32_t sort_interval) {
+  if (!h) return MPRW_E_INVAL;
+  if (h->parent) return fail(h, MPRW_E_STATE, "mprw_set_tuning on a batch member: tune the batch");
+  if (blocks_per_sm < 0 || sort_interval < 0) return fail(h, MPRW_E_INVAL, "mprw_set_tuning: negative value");
+  if (blocks_per_sm > max_blocks_per_sm(h))
+    return fail(h, MPRW_E_INVAL, "mprw_set_tuning: more blocks per SM than the step kernel can keep resident");
+  h->blocks_per_sm = blocks_per_sm;
+  h->sort_interval = sort_interval;
+  h->advance_count = 0;
+  return MPRW_OK;
+}
+
+int mprw_get_tuning(mprw_handle *h, int32_t *blocks_per_sm, int32_t *sort_interval, int32_t *max_blocks) {
+  if (!h) return MPRW_E_INVAL;
+  if (blocks_per_sm) *blocks_per_sm = h->blocks_per_sm > 0 ? h->blocks_per_sm : default_blocks_per_sm(h);
+  if (sort_interval) *sort_interval = h->sort_interval;
+  if (max_blocks) *max_blocks = max_blocks_per_sm(h);
+  return MPRW_OK;
+}
+
+int mprw_autotune(mprw_handle *h, double t_begin, double t_end, int32_t *blocks_per_sm, int32_t *sort_interval,
+                  double *rates) {
+  if (!h) return MPRW_E_INVAL;
+  if (h->parent) return fail(h, MPRW_E_STATE, "mprw_autotune on a batch member: tune the batch");
+  if (!h->members.empty()) {
+    h->flow_loaded = true;
+    for (size_t k = 0; k < h->members.size(); ++k)
+      if (!h->members[k]->flow_loaded) return fail(h, MPRW_E_STATE, "mprw_autotune before every member's flow");
+  }
+  if (!h->flow_loaded) return fail(h, MPRW_E_STATE, "mprw_autotune before mprw_load_flow");
+  if (!(t_end > t_begin)) return fail(h, MPRW_E_INVAL, "mprw_autotune: t_end <= t_begin");
+  if (h->n == 0) return fail(h, MPRW_E_STATE, "mprw_autotune without particles");
+  cudaStream_t s = h->stream;
+  const int64_t n = h->n;
+  const size_t rs = h->opt.precision == MPRW_MIXED ? sizeof(float) : sizeof(double);
+  // the trials run on the real arrays from a saved copy of the state they change
+  struct Field {
+    void *p;
+    size_t bytes;
+  } fields[] = {{h->d_cell, 4 * (size_t)n}, {h->d_status, 4 * (size_t)n}, {h->d_x, rs * n}, {h->d_y, rs * n},
+                {h->d_z, rs * n},         {h->d_t, 8 * (size_t)n},      {h->d_ctr, 8 * (size_t)n}};
+  size_t total = 0;
+  for (const Field &f : fields) total += (f.bytes + 255) / 256 * 256;
+  char *save = nullptr;
+  CK(cudaMalloc(&save, total));
+  struct Free {
+    char *p;
+    ~Free() { cudaFree(p); }
+  } guard{save};
+  auto snapshot = [&](bool restore) -> cudaError_t {
+    size_t o = 0;
+    for (const Field &f : fields) {
+      cudaError_t e = restore ? cudaMemcpyAsync(f.p, save + o, f.bytes, cudaMemcpyDeviceToDevice, s)
+                              : cudaMemcpyAsync(save + o, f.p, f.bytes, cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return e;
+      o += (f.bytes + 255) / 256 * 256;
+    }
+    return cudaSuccess;
+  };
+  CK(snapshot(false));
+  const int maxb = std::min(max_blocks_per_sm(h), 4);
+  double best_rate = -1.0, rate_sorted = 0.0;
+  int best_b = default_blocks_per_sm(h);
+  int k = 0;
+  // blocks per SM: every resident count, each from the same state, sorted first
+  for (int b = 1; b <= maxb; ++b) {
+    CK(snapshot(true));
+    CK(cudaEventRecord(h->ev2, s));
+    int rc = sort_particles(h);
+    if (rc != MPRW_OK) return rc;
+    float ms = 0, sort_ms = 0;
+    int64_t st = 0;
+    CK(cudaEventRecord(h->ev3, s));
+    rc = launch_step(h, t_begin, t_end, b, true, &ms, &st);
+    if (rc != MPRW_OK) return rc;
+    CK(cudaEventElapsedTime(&sort_ms, h->ev2, h->ev3));
+    const double r = st / (double)(ms + sort_ms);
+    if (rates) rates[k++] = r;
+    if (r > best_rate) {
+      best_rate = r;
+      best_b = b;
+      rate_sorted = r;
+    }
+  }
+  // the same without sorting: the particles in the order the caller gave
+  CK(snapshot(true));
+  float ms_u = 0;
+  int64_t st_u = 0;
+  int rc = launch_step(h, t_begin, t_end, best_b, false, &ms_u, &st_u);
+  if (rc != MPRW_OK) return rc;
+  const double rate_unsorted = st_u / (double)ms_u;
+  if (rates) rates[k++] = rate_unsorted;
+  // sorting pays when a sorted advance (sort included) is faster; when it is
+  // close, sort every 4th advance to keep most of the locality for less
+  int si = 1;
+  if (rate_unsorted > rate_sorted * 1.05) si = 0;
+  else if (rate_unsorted > rate_sorted * 0.97) si = 4;
+  CK(snapshot(true));
+  CK(cudaStreamSynchronize(s));
+  h->perm_valid = false;
+  h->blocks_per_sm = best_b;
+  h->sort_interval = si;
+  h->advance_count = 0;
+  if (blocks_per_sm) *blocks_per_sm = best_b;
+  if (sort_interval) *sort_interval = si;
   return MPRW_OK;
 }
 

@@ -32,6 +32,9 @@ template <typename R>
 cudaError_t launch_advance(const AdvanceArgs<R> &a, int blocks, int threads, cudaStream_t s);
 template <typename R>
 size_t advance_smem_bytes(int threads);
+// resident blocks per SM of the step kernel variant (cudaOccupancyMaxActiveBlocksPerMultiprocessor)
+template <typename R>
+cudaError_t advance_occupancy(int exp_adv, int axi, int threads, int *blocks_per_sm);
 
 // ---- prep (prep.cu) -------------------------------------------------------
 struct PrepInputs {

@@ -893,7 +893,19 @@ cudaError_t launch_advance(const AdvanceArgs<R> &a, int blocks, int threads, cud
   return cudaGetLastError();
 }
 
+template <typename R>
+cudaError_t advance_occupancy(int exp_adv, int axi, int threads, int *blocks_per_sm) {
+  size_t smem = advance_smem_bytes<R>(threads);
+  auto kern = exp_adv ? (axi ? rwpt_advance_kernel<R, true, true> : rwpt_advance_kernel<R, true, false>)
+                      : (axi ? rwpt_advance_kernel<R, false, true> : rwpt_advance_kernel<R, false, false>);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kern, threads, smem);
+}
+
 template cudaError_t launch_advance<double>(const AdvanceArgs<double> &, int, int, cudaStream_t);
+template cudaError_t advance_occupancy<double>(int, int, int, int *);
+template cudaError_t advance_occupancy<float>(int, int, int, int *);
 template cudaError_t launch_advance<float>(const AdvanceArgs<float> &, int, int, cudaStream_t);
 template size_t advance_smem_bytes<double>(int);
 template size_t advance_smem_bytes<float>(int);

@@ -98,6 +98,9 @@ def load_library() -> C.CDLL:
                                                _up]),
         "mprw_gpkde_batch": (C.c_int, [H, C.POINTER(GpkdeOptions), C.POINTER(_dp), C.POINTER(_dp), _ip,
                                        C.c_int32]),
+        "mprw_set_tuning": (C.c_int, [H, C.c_int32, C.c_int32]),
+        "mprw_get_tuning": (C.c_int, [H, _ip, _ip, _ip]),
+        "mprw_autotune": (C.c_int, [H, C.c_double, C.c_double, _ip, _ip, _dp]),
         "mprw_last_error": (C.c_char_p, [H]),
     }
     for name, (res, args) in sig.items():
@@ -314,6 +317,23 @@ class Tracker:
     def set_stream(self, stream_ptr: int):
         self._check(self.lib.mprw_set_stream(self.h, C.c_void_p(stream_ptr)), "mprw_set_stream")
 
+    def set_tuning(self, blocks_per_sm: int = 0, sort_interval: int = 1):
+        self._check(self.lib.mprw_set_tuning(self.h, int(blocks_per_sm), int(sort_interval)), "mprw_set_tuning")
+
+    def tuning(self) -> dict:
+        b, si, mx = C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(self.lib.mprw_get_tuning(self.h, C.byref(b), C.byref(si), C.byref(mx)), "mprw_get_tuning")
+        return dict(blocks_per_sm=b.value, sort_interval=si.value, max_blocks_per_sm=mx.value)
+
+    def autotune(self, t_begin: float, t_end: float) -> dict:
+        """Pick blocks per SM and the sort interval by timing trial advances
+        over [t_begin, t_end] from the current state (left unchanged)."""
+        b, si = C.c_int32(), C.c_int32()
+        rates = np.zeros(5)
+        self._check(self.lib.mprw_autotune(self.h, float(t_begin), float(t_end), C.byref(b), C.byref(si),
+                                           _p(rates, _dp)), "mprw_autotune")
+        return dict(blocks_per_sm=b.value, sort_interval=si.value, trial_rates_per_ms=rates.tolist())
+
     def timings(self) -> dict:
         s, p, h, k = C.c_double(), C.c_double(), C.c_double(), C.c_double()
         n = C.c_int64()
@@ -463,6 +483,10 @@ class Batch:
 
     def set_stream(self, stream_ptr: int):
         self._check(self.lib.mprw_set_stream(self.h, C.c_void_p(stream_ptr)), "mprw_set_stream")
+
+    set_tuning = Tracker.set_tuning
+    tuning = Tracker.tuning
+    autotune = Tracker.autotune
 
     def timings(self) -> dict:
         s, p, h, k = C.c_double(), C.c_double(), C.c_double(), C.c_double()
