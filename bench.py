@@ -73,6 +73,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--realizations", type=int, default=16,
                     help="ensemble size of the batched leg (realizations 0..R-1 of the 64-member ensemble)")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the default launch tuning instead of mprw_autotune before the warm-up")
     ap.add_argument("--kde-streams", type=int, default=4,
                     help="batched leg: reconstructions run concurrently (mprw_gpkde_batch concurrency)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
@@ -201,6 +203,7 @@ def run_gpu_arm(args, rank, world, local):
         tr.set_stream(stream.cuda_stream)   # launch on a stream the events below can see
         tr.load_flow(f)
         tr.set_particles(p)
+        tuning = tr.autotune(0.0, INTERVAL_D) if args.autotune else tr.tuning()
         t = 0.0
         for _ in range(warmup):
             tr.advance(t, t + INTERVAL_D)
@@ -239,7 +242,7 @@ def run_gpu_arm(args, rank, world, local):
                        "max_rel": float(np.abs(dens - d64).max() / d64.max())}
         tr.close()
         return dict(ms=ms, adv_ms=adv_ms, kern_ms=kern_ms, kde_ms=kde_ms, wall_ms=wall_ms, steps=steps_done,
-                    launches=launches, out=out, t_end=t, loops=loops, dens=dens, kde_err=kde_err)
+                    launches=launches, out=out, t_end=t, loops=loops, dens=dens, kde_err=kde_err, tuning=tuning)
 
     with ClockSampler(local) as clk:
         fp64 = timed_run(MIXED if args.precision == "mixed" else 0, args.steps, args.warmup)
@@ -281,6 +284,7 @@ def batched_run(args, flush):
         for k, (g, f, p) in enumerate(ens):
             b.load_flow(k, f)
         b.set_particles([e[2] for e in ens])
+        tuning = b.autotune(0.0, INTERVAL_D) if args.autotune else b.tuning()
         t = 0.0
 
         def one_step(t):
@@ -312,7 +316,7 @@ def batched_run(args, flush):
         outs = b.get_particles()
         b.close()
         return dict(steps=steps, ms=ms, adv_ms=adv, kern_ms=float(np.sum(adv_kern)), launches=launches, outs=outs,
-                    t_end=t)
+                    t_end=t, tuning=tuning)
 
     mx = run(MIXED)
     fp = run(0)
@@ -341,7 +345,8 @@ def batched_run(args, flush):
             "advance_ms_per_step": mx["adv_ms"] / args.steps, "advance_kernel_ms_per_step": mx["kern_ms"] / args.steps,
             "gpkde_ms_per_step": (mx["ms"] - mx["adv_ms"]) / args.steps, "gpu_launches": mx["launches"],
             "fp64": {"value": v64, "ms_per_step": fp["ms"] / args.steps,
-                     "advance_ms_per_step": fp["adv_ms"] / args.steps},
+                     "advance_ms_per_step": fp["adv_ms"] / args.steps, "tuning": fp["tuning"]},
+            "tuning": mx["tuning"],
             "speedup_vs_fp64_same_ensemble": v32 / v64,
             "moment_error_vs_fp64": {"worst_over_realizations": worst, "per_realization": errs},
             "t_end_days": mx["t_end"]}
@@ -474,6 +479,7 @@ def main():
                      "bytes_model": "1008 B per particle-step (state 96 B + cell record 912 B)"},
         "clocks": res["clocks"],
         "gpu_launches": int(fp["launches"]),
+        "tuning": fp["tuning"],
         "kernel_time_share": {"advance_kernel_ms": float(np.sum(fp["kern_ms"])),
                               "advance_event_ms": float(np.sum(fp["adv_ms"])),
                               "gpkde_ms": float(np.sum(fp["kde_ms"])), "step_event_ms": float(np.sum(fp["ms"])),
@@ -497,7 +503,7 @@ def main():
                                           "speedup_vs_fp64": (mx["steps"] / adv32) / (fp["steps"] / adv64)},
                          "moment_error_vs_fp64": err, "active_fp64": n64,
                          "active_mixed": n32, "kernel_ms": float(np.mean(mx["kern_ms"])),
-                         "gpkde_ms": float(np.mean(mx["kde_ms"])), "gpkde_precision": "fp32",
+                         "gpkde_ms": float(np.mean(mx["kde_ms"])), "gpkde_precision": "fp32", "tuning": mx["tuning"],
                          "gpkde_fp32_vs_fp64_same_particles": mx["kde_err"]}
     if "batched" in res:
         line["batched"] = res["batched"]
