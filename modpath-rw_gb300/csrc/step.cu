@@ -184,10 +184,10 @@ __device__ __forceinline__ void random_displacement(const Lane<R> &F, int ndim, 
 
 // One axis of pr_DetectExitFaceAndUpdateTimeStepQuadratic (:1622-1710).
 // Returns true when the routine must return at once (exitFace, dt set).
-template <typename R, typename DT>
+template <typename R>
 __device__ __forceinline__ bool quad_axis(R npos, R pos, R d, R v, R divD, R dB, int faceLo, int faceHi,
-                                          DT dt, R &dtaxis, int &exitAxis, int &exitFace,
-                                          DT &dtout) {
+                                          double dt, R &dtaxis, int &exitAxis, int &exitFace,
+                                          double &dtout) {
   const R zero = R(0), one = R(1);
   R dI;
   if (npos > one) {
@@ -199,7 +199,7 @@ __device__ __forceinline__ bool quad_axis(R npos, R pos, R d, R v, R divD, R dB,
   }
   if (dI == zero) {
     exitFace = exitAxis;
-    dtout = DT(0);
+    dtout = 0.0;
     return true;
   }
   R A = v + divD, B = dB;
@@ -222,12 +222,12 @@ __device__ __forceinline__ bool quad_axis(R npos, R pos, R d, R v, R divD, R dB,
       dtaxis = zm * zm;
       if (dtaxis == zero) {
         exitFace = exitAxis;
-        dtout = DT(0);
+        dtout = 0.0;
         return true;
       }
     } else if (z1 == zero || z2 == zero) {
       exitFace = exitAxis;
-      dtout = DT(0);
+      dtout = 0.0;
       return true;
     }
   } else if (A == zero) {
@@ -236,12 +236,12 @@ __device__ __forceinline__ bool quad_axis(R npos, R pos, R d, R v, R divD, R dB,
       dtaxis = q * q;
       if (dtaxis == zero) {
         exitFace = exitAxis;
-        dtout = DT(0);
+        dtout = 0.0;
         return true;
       }
     }
   }
-  if ((DT)dtaxis > dt) dtaxis = zero;
+  if ((double)dtaxis > dt) dtaxis = zero;
   return false;
 }
 
@@ -438,57 +438,11 @@ __device__ bool newton_axis(double npos, double pos, double d, double v, double 
   return false;
 }
 
-// Simulation time within a cell visit.  FP64 and EXPONENTIAL paths: one
-// double, as the reference.  EULERIAN MIXED: the time at the start of the
-// visit (or of the last restart) in FP64 plus the FP32 sum of the steps taken
-// since, compared with the FP32 time left to maxTime, so a step's time
-// bookkeeping is FP32 work; the FP64 time is formed only where a location is
-// recorded.  The FP32 sum covers one visit (tens of steps), so its rounding
-// stays within ~1e-7 of the visit's duration.
-template <bool FAST>
-struct Clock;
-template <>
-struct Clock<false> {
-  using dt_t = double;
-  double t;
-  __device__ __forceinline__ void reset(double t0, double) { t = t0; }
-  __device__ __forceinline__ void add(double dt) { t = t + dt; }
-  __device__ __forceinline__ void sub(double dt) { t = t - dt; }
-  __device__ __forceinline__ bool past(double tmax) const { return tmax < t; }
-  __device__ __forceinline__ double remaining(double tmax) const { return fmax(tmax - t, 0.0); }
-  __device__ __forceinline__ void to_max(double tmax) { t = tmax; }
-  __device__ __forceinline__ double value() const { return t; }
-};
-template <>
-struct Clock<true> {
-  using dt_t = float;
-  double base;
-  float acc, rem;
-  __device__ __forceinline__ void reset(double t0, double tmax) {
-    base = t0;
-    acc = 0.0f;
-    rem = (float)(tmax - t0);
-  }
-  __device__ __forceinline__ void add(float dt) { acc = acc + dt; }
-  __device__ __forceinline__ void sub(float dt) { acc = acc - dt; }
-  __device__ __forceinline__ bool past(double) const { return rem < acc; }
-  __device__ __forceinline__ float remaining(double) const { return fmaxf(rem - acc, 0.0f); }
-  __device__ __forceinline__ void to_max(double tmax) {
-    base = tmax;
-    acc = 0.0f;
-    rem = 0.0f;
-  }
-  __device__ __forceinline__ double value() const { return base + (double)acc; }
-};
-
-template <typename R, bool EXP>
+template <typename R>
 struct Visit {
-  static constexpr bool kFast = sizeof(R) == 4 && !EXP;
-  using DT = typename Clock<kFast>::dt_t;
   R x, y, z;     // current local position (TrackSubCell x,y,z)
   R ix, iy, iz;  // cell-entry location (initialLocation)
-  Clock<kFast> clk;
-  double tinit, dtcell;
+  double t, tinit, dtcell;
   R sqrt_dtcell, rdt_cell;
   int exitFace, posRestart;
   bool reachedMax;
@@ -504,18 +458,17 @@ enum : int { PASS_CONTINUE = 0, PASS_MAXTIME = 1, PASS_EXIT = 2, PASS_UNDEFINED 
 // On PASS_MAXTIME / PASS_EXIT the final location is (ox,oy,oz,V.t); on
 // PASS_UNDEFINED the caller uses the last recorded point.
 template <typename R, bool EXP, bool AXI>
-__device__ int rw_pass(Visit<R, EXP> &V, const Lane<R> &F, uint32_t massb, double maxTime, int ndim, int d1,
-                       int d2, uint64_t seed, uint64_t id, uint64_t &ctr, R &ox, R &oy, R &oz) {
-  using DT = typename Visit<R, EXP>::DT;
+__device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double maxTime, int ndim, int d1, int d2,
+                       uint64_t seed, uint64_t id, uint64_t &ctr, R &ox, R &oy, R &oz) {
   const R zero = R(0), one = R(1), half = R(0.5);
-  const DT dtRed = (DT)0.1f;  // dtReductionFactor, a single-precision literal (:850)
-  DT dt = Visit<R, EXP>::kFast ? (DT)V.rdt_cell : (DT)V.dtcell;
+  const double dtRed = (double)0.1f;  // dtReductionFactor, a single-precision literal (:850)
+  double dt = V.dtcell;
   R rdt = V.rdt_cell, sdt = V.sqrt_dtcell;  // FP32 copies: no conversion on the common pass
-  V.clk.add(dt);
-  if (V.clk.past(maxTime)) {
-    V.clk.sub(dt);
-    dt = V.clk.remaining(maxTime);
-    V.clk.to_max(maxTime);
+  V.t = V.t + dt;
+  if (maxTime < V.t) {
+    V.t = V.t - dt;
+    dt = fmax(maxTime - V.t, 0.0);
+    V.t = maxTime;
     V.reachedMax = true;
     rdt = (R)dt;
     sdt = sqrt(rdt);
@@ -559,7 +512,7 @@ __device__ int rw_pass(Visit<R, EXP> &V, const Lane<R> &F, uint32_t massb, doubl
   R dzrw = az + ddz * rdt + bz * sdt;
   // jump limiter (:989-1013)
   while ((fabs(dxrw * iX) > half) || (fabs(dyrw * iY) > half) || (fabs(dzrw * iZ) > half)) {
-    V.clk.sub(dt);
+    V.t = V.t - dt;
     dt = dtRed * dt;
     rdt = (R)dt;
     sdt = sqrt(rdt);
@@ -567,7 +520,7 @@ __device__ int rw_pass(Visit<R, EXP> &V, const Lane<R> &F, uint32_t massb, doubl
     dxrw = ax + ddx * rdt + bx * sdt;
     dyrw = ay + ddy * rdt + by * sdt;
     dzrw = az + ddz * rdt + bz * sdt;
-    V.clk.add(dt);
+    V.t = V.t + dt;
     V.reachedMax = false;
   }
   R nx = x + dxrw * iX, ny = y + dyrw * iY, nz = z + dzrw * iZ;
@@ -580,7 +533,7 @@ __device__ int rw_pass(Visit<R, EXP> &V, const Lane<R> &F, uint32_t massb, doubl
       double dtx = 0.0, dty = 0.0, dtz = 0.0;
       int efx = 0, efy = 0, efz = 0;
       bool ret = false;
-      V.clk.sub(dt);
+      V.t = V.t - dt;
       if (!ret && ((nx > one) || (nx < zero)))
         ret = newton_axis(nx, x, dX, vx, dvx, ddx, bx, 1, 2, dt, dtx, efx, V.exitFace, dt);
       if (!ret && ((ny > one) || (ny < zero)))
@@ -589,7 +542,7 @@ __device__ int rw_pass(Visit<R, EXP> &V, const Lane<R> &F, uint32_t massb, doubl
         ret = newton_axis(nz, z, dZ, vz, dvz, ddz, bz, 5, 6, dt, dtz, efz, V.exitFace, dt);
       if (!ret) {
         if (dtx == 0.0 && dty == 0.0 && dtz == 0.0) {
-          V.clk.add(dt);
+          V.t = V.t + dt;
         } else {
           int im = -1;
           double best = 0.0;
@@ -598,7 +551,7 @@ __device__ int rw_pass(Visit<R, EXP> &V, const Lane<R> &F, uint32_t massb, doubl
           if (dtz > 0.0 && (im < 0 || dtz < best)) { im = 2; best = dtz; }
           dt = best;
           V.exitFace = (im == 0) ? efx : (im == 1 ? efy : efz);
-          V.clk.add(dt);
+          V.t = V.t + dt;
         }
       }
     } else {
@@ -606,7 +559,7 @@ __device__ int rw_pass(Visit<R, EXP> &V, const Lane<R> &F, uint32_t massb, doubl
       // ExitFaceAndUpdateTimeStep (quadratic, :1576-1892)
       int efx = 0, efy = 0, efz = 0;
       bool ret = false;
-      V.clk.sub(dt);
+      V.t = V.t - dt;
       if (!ret && ((nx > one) || (nx < zero)))
         ret = quad_axis(nx, x, dX, vx, ddx, bx, 1, 2, dt, dtx, efx, V.exitFace, dt);
       if (!ret && ((ny > one) || (ny < zero)))
@@ -615,23 +568,23 @@ __device__ int rw_pass(Visit<R, EXP> &V, const Lane<R> &F, uint32_t massb, doubl
         ret = quad_axis(nz, z, dZ, vz, ddz, bz, 5, 6, dt, dtz, efz, V.exitFace, dt);
       if (!ret) {
         if (dtx == zero && dty == zero && dtz == zero) {
-          V.clk.add(dt);
+          V.t = V.t + dt;
         } else {
           int im = -1;
           R best = zero;
           if (dtx > zero) { im = 0; best = dtx; }
           if (dty > zero && (im < 0 || dty < best)) { im = 1; best = dty; }
           if (dtz > zero && (im < 0 || dtz < best)) { im = 2; best = dtz; }
-          dt = (DT)best;
+          dt = (double)best;
           V.exitFace = (im == 0) ? efx : (im == 1 ? efy : efz);
-          V.clk.add(dt);
+          V.t = V.t + dt;
         }
       }
     }
     if (intLoop > 5) {
       nx = V.ix; ny = V.iy; nz = V.iz;
-      V.clk.reset(V.tinit, maxTime);
-      dt = Visit<R, EXP>::kFast ? (DT)V.rdt_cell : (DT)V.dtcell;
+      V.t = V.tinit;
+      dt = V.dtcell;
       if (++V.posRestart > 10) {
         V.x = x; V.y = y; V.z = z;
         return PASS_UNDEFINED;
@@ -663,8 +616,8 @@ __device__ int rw_pass(Visit<R, EXP> &V, const Lane<R> &F, uint32_t massb, doubl
       nz = (ef == 5) ? zero : one;
     } else {
       nx = V.ix; ny = V.iy; nz = V.iz;
-      V.clk.reset(V.tinit, maxTime);
-      dt = Visit<R, EXP>::kFast ? (DT)V.rdt_cell : (DT)V.dtcell;
+      V.t = V.tinit;
+      dt = V.dtcell;
       if (++V.posRestart > 10) {
         V.x = x; V.y = y; V.z = z;
         return PASS_UNDEFINED;
@@ -681,19 +634,19 @@ __device__ int rw_pass(Visit<R, EXP> &V, const Lane<R> &F, uint32_t massb, doubl
         return PASS_UNDEFINED;
       }
       R xi = nx, yi = ny, zi = nz;
-      if (dt == DT(0)) {
+      if (dt == 0.0) {
         nx = V.ix; ny = V.iy; nz = V.iz;
-        V.clk.sub(dt);
-        dt = Visit<R, EXP>::kFast ? (DT)V.rdt_cell : (DT)V.dtcell;
+        V.t = V.t - dt;
+        dt = V.dtcell;
         V.exitFace = 0;
         ++V.posRestart;
         break;
       }
-      V.clk.add(dt);
-      if (V.clk.past(maxTime)) {
-        V.clk.sub(dt);
-        dt = V.clk.remaining(maxTime);
-        V.clk.to_max(maxTime);
+      V.t = V.t + dt;
+      if (maxTime < V.t) {
+        V.t = V.t - dt;
+        dt = fmax(maxTime - V.t, 0.0);
+        V.t = maxTime;
         V.reachedMax = true;
         rdt = (R)dt;
         sdt = sqrt(rdt);
@@ -717,7 +670,7 @@ __device__ int rw_pass(Visit<R, EXP> &V, const Lane<R> &F, uint32_t massb, doubl
         else { vz = -vz; ddz = -ddz; bz = -bz; }
         V.exitFace = 0;
       } else {
-        dt = Visit<R, EXP>::kFast ? (DT)V.rdt_cell : (DT)V.dtcell;
+        dt = V.dtcell;
         V.exitFace = 0;
         if (nx == zero) V.exitFace = 1;
         if (nx == one) V.exitFace = 2;
@@ -770,10 +723,9 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
   // location at cell entry
   R ex = zero, ey = zero, ez = zero;
   double et = 0.0;
-  Visit<R, EXP> V;
+  Visit<R> V;
   V.x = V.y = V.z = V.ix = V.iy = V.iz = zero;
-  V.clk.reset(0.0, 0.0);
-  V.tinit = V.dtcell = 0.0;
+  V.t = V.tinit = V.dtcell = 0.0;
   V.sqrt_dtcell = zero;
   V.rdt_cell = zero;
   V.exitFace = V.posRestart = 0;
@@ -847,8 +799,7 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
           for (int f = 0; f < 6; ++f) conn6[f] = rec->conn[f];
           V.x = ex; V.y = ey; V.z = ez;
           V.ix = ex; V.iy = ey; V.iz = ez;
-          V.clk.reset(et, a.t_end);
-          V.tinit = et;
+          V.t = et; V.tinit = et;
           V.dtcell = rec->dtcell;
           V.sqrt_dtcell = (R)rec->sqrt_dtcell;
           V.rdt_cell = (R)rec->dtcell;
@@ -881,7 +832,7 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
         ++my_passes;
       }
       if (r == PASS_MAXTIME) {
-        a.cell[p] = c; a.x[p] = ox; a.y[p] = oy; a.z[p] = oz; a.t[p] = V.clk.value();
+        a.cell[p] = c; a.x[p] = ox; a.y[p] = oy; a.z[p] = oz; a.t[p] = V.t;
         a.status[p] = ST_ACTIVE;
         a.ctr[p] = ctr;
         p = -1;
@@ -893,7 +844,7 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
       } else if (r == PASS_EXIT) {
         // the exit point becomes the last pathline point
         const int face = V.exitFace;
-        lc = c; lx = ox; ly = oy; lz = oz; lt = V.clk.value();
+        lc = c; lx = ox; ly = oy; lz = oz; lt = V.t;
         const int32_t nc = conn6[face - 1];
         // ConvertFromNeighbor: the exit coordinate must sit exactly on the face
         const bool bad = (face == 2 && ox != one) || (face == 1 && ox != zero) || (face == 4 && oy != one) ||
@@ -904,7 +855,7 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
           a.ctr[p] = ctr;
           p = -1;
         } else {
-          ex = ox; ey = oy; ez = oz; et = V.clk.value();
+          ex = ox; ey = oy; ez = oz; et = V.t;
           if (face == 2) ex = zero;
           if (face == 1) ex = one;
           if (face == 4) ey = zero;
