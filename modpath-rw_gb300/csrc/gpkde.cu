@@ -38,7 +38,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kBinThreads = 64;   // per-bin elementwise kernels: spread few bins over all SMs
-constexpr int kPassBlocks = 64;   // blocks per key of a separable pass (grid-stride in the key's region)
+constexpr int kPassBlocks = 1216; // blocks of a separable pass: 8 per SM, grid-stride over all keys' regions
 
 template <typename T>
 __device__ __forceinline__ int log_index(const KdeParams &P, T h, int d) {
@@ -403,6 +403,8 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, const K
     for (int i = 0; i < 6; ++i) pl->ur[k][i] = fits ? su[k][i] : (i & 1 ? INT_MIN : INT_MAX);
   if (k == 0) {
     pl->np = fits ? np : 0;
+    pl->tot1 = fits ? tot1 : 0;
+    pl->tot2 = fits ? tot2 : 0;
     if (!fits) {
       atomicMax(&need[0], tot1 * nc);
       atomicMax(&need[1], tot2 * nc);
@@ -427,6 +429,29 @@ __device__ __forceinline__ long long region_loc(const int r[6], int x, int y, in
   return (long long)(x - r[0]) + (long long)(r[1] - r[0] + 1) * ((y - r[2]) + (long long)(r[3] - r[2] + 1) * (z - r[4]));
 }
 
+// The separable passes index every key's region of one pass buffer with one
+// flat index g (the buffer's element): the regions are consecutive in key
+// order, region j starting at o[j].  A block copies the offsets to shared
+// memory once; each element finds its key by binary search.  All keys share
+// the grid, so a key with a large region gets the whole GPU, not a fixed
+// number of blocks.
+__device__ __forceinline__ int load_offsets(const SepPlan *pl, const long long *o, long long *so) {
+  const int np = pl->np;
+  for (int j = threadIdx.x; j < np; j += blockDim.x) so[j] = o[j];
+  __syncthreads();
+  return np;
+}
+
+__device__ __forceinline__ int flat_slot(const long long *so, int np, long long g) {
+  int lo = 0, hi = np - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (so[mid] <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 // Gather pass 1: T1 = sum_t fx[t] F(reflect(x - m + t), y, z) over region 1.
 // NC = 1: one field; NC = 6: the squared curvatures cx, cy, cz and their
 // pairwise products cx*cy, cx*cz, cy*cz (the roughness terms,
@@ -438,15 +463,17 @@ struct Fields {
 
 template <typename T, int NC>
 __global__ void gather_x_kernel(KdeParams P, const SepPlan *pl, const T *val, Fields<T> F, T *T1) {
-  const int j = blockIdx.y;
-  if (j >= pl->np) return;
-  int r[6];
-  for (int i = 0; i < 6; ++i) r[i] = pl->r1[j][i];
-  const int m = pl->m[j][0], n = P.nb[0];
-  const T *f = val + pl->fofs[j][0];
-  T *out = T1 + pl->o1[j] * NC;
-  const long long vol = region_vol(r);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
+  __shared__ long long so[KDE_KMAX];
+  const int np = load_offsets(pl, pl->o1, so);
+  const long long tot = pl->tot1;
+  const int n = P.nb[0];
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < tot; g += (long long)gridDim.x * blockDim.x) {
+    const int j = flat_slot(so, np, g);
+    const long long i = g - so[j];
+    const int *r = pl->r1[j];
+    const int m = pl->m[j][0];
+    const T *f = val + pl->fofs[j][0];
+    T *out = T1 + so[j] * NC;
     int x, y, z;
     region_xyz(r, i, x, y, z);
     const long long row = (long long)P.nb[0] * ((y - 1) + (long long)P.nb[1] * (z - 1)) - 1;
@@ -496,19 +523,18 @@ __global__ void products_kernel(const T *cx, const T *cy, const T *cz, T *cxy, T
 // Gather pass 2: T2 = sum_t fy[t] T1(x, reflect(y - m + t), z) over region 2.
 template <typename T, int NC>
 __global__ void gather_y_kernel(KdeParams P, const SepPlan *pl, const T *val, const T *T1, T *T2) {
-  const int j = blockIdx.y;
-  if (j >= pl->np) return;
-  int r1[6], r2[6];
-  for (int i = 0; i < 6; ++i) {
-    r1[i] = pl->r1[j][i];
-    r2[i] = pl->r2[j][i];
-  }
-  const int m = pl->m[j][1], n = P.nb[1];
-  const T *f = val + pl->fofs[j][1];
-  const T *in = T1 + pl->o1[j] * NC;
-  T *out = T2 + pl->o2[j] * NC;
-  const long long vol = region_vol(r2);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
+  __shared__ long long so[KDE_KMAX];
+  const int np = load_offsets(pl, pl->o2, so);
+  const long long tot = pl->tot2;
+  const int n = P.nb[1];
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < tot; g += (long long)gridDim.x * blockDim.x) {
+    const int j = flat_slot(so, np, g);
+    const long long i = g - so[j];
+    const int *r1 = pl->r1[j], *r2 = pl->r2[j];
+    const int m = pl->m[j][1];
+    const T *f = val + pl->fofs[j][1];
+    const T *in = T1 + pl->o1[j] * NC;
+    T *out = T2 + so[j] * NC;
     int x, y, z;
     region_xyz(r2, i, x, y, z);
     T acc[NC];
@@ -642,48 +668,44 @@ __device__ __forceinline__ T scatter_taps(const T *f, int m, int x, int n, int l
 template <typename T>
 __global__ void scatter_x_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, const T *val, const int *cell_bin,
                                  const int *bin_key, T *V1) {
-  const int j = blockIdx.y;
-  if (j >= pl->np) return;
-  int r[6], bx[6];
-  for (int i = 0; i < 6; ++i) {
-    r[i] = pl->r1[j][i];
-    bx[i] = pl->box[j][i];
-  }
-  const int key = pl->key[j], axis = key / KDE_MAXDB;
-  const int *keys = bin_key + (long long)axis * B.n;
-  const int m = pl->m[j][0], n = P.nb[0];
-  const T *f = val + pl->fofs[j][0];
-  T *out = V1 + pl->o1[j];
-  const long long vol = region_vol(r);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
+  __shared__ long long so[KDE_KMAX];
+  const int np = load_offsets(pl, pl->o1, so);
+  const long long tot = pl->tot1;
+  const int n = P.nb[0];
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < tot; g += (long long)gridDim.x * blockDim.x) {
+    const int j = flat_slot(so, np, g);
+    const long long i = g - so[j];
+    const int *r = pl->r1[j], *bx = pl->box[j];
+    const int key = pl->key[j], axis = key / KDE_MAXDB;
+    const int *keys = bin_key + (long long)axis * B.n;
+    const int m = pl->m[j][0];
+    const T *f = val + pl->fofs[j][0];
     int x, y, z;
     region_xyz(r, i, x, y, z);
     const long long row = (long long)P.nb[0] * ((y - 1) + (long long)P.nb[1] * (z - 1)) - 1;
-    out[i] = scatter_taps<T>(f, m, x, n, bx[0], bx[1], nullptr, 1, row, cell_bin, keys, key, B.count);
+    V1[g] = scatter_taps<T>(f, m, x, n, bx[0], bx[1], nullptr, 1, row, cell_bin, keys, key, B.count);
   }
 }
 
 // Scatter pass 2 (y) over region 2.
 template <typename T>
 __global__ void scatter_y_kernel(KdeParams P, const SepPlan *pl, const T *val, const T *V1, T *V2) {
-  const int j = blockIdx.y;
-  if (j >= pl->np) return;
-  int r1[6], r2[6];
-  for (int i = 0; i < 6; ++i) {
-    r1[i] = pl->r1[j][i];
-    r2[i] = pl->r2[j][i];
-  }
-  const int m = pl->m[j][1], n = P.nb[1];
-  const T *f = val + pl->fofs[j][1];
-  const T *in = V1 + pl->o1[j];
-  T *out = V2 + pl->o2[j];
-  const long long vol = region_vol(r2);
-  const long long sy = r1[1] - r1[0] + 1;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
+  __shared__ long long so[KDE_KMAX];
+  const int np = load_offsets(pl, pl->o2, so);
+  const long long tot = pl->tot2;
+  const int n = P.nb[1];
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < tot; g += (long long)gridDim.x * blockDim.x) {
+    const int j = flat_slot(so, np, g);
+    const long long i = g - so[j];
+    const int *r1 = pl->r1[j], *r2 = pl->r2[j];
+    const int m = pl->m[j][1];
+    const T *f = val + pl->fofs[j][1];
+    const T *in = V1 + pl->o1[j];
+    const long long sy = r1[1] - r1[0] + 1;
     int x, y, z;
     region_xyz(r2, i, x, y, z);
     const long long base = region_loc(r1, x, r1[2], z) - (long long)r1[2] * sy;
-    out[i] = scatter_taps<T>(f, m, y, n, r1[2], r1[3], in, sy, base, nullptr, nullptr, 0, nullptr);
+    V2[g] = scatter_taps<T>(f, m, y, n, r1[2], r1[3], in, sy, base, nullptr, nullptr, 0, nullptr);
   }
 }
 
@@ -1282,7 +1304,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   // plans: [0] smoothing kernels (kind 1), [1] second-derivative kernels (kind 2)
   SepPlan *plan1 = st.d_plan, *plan2 = st.d_plan + 1;
   int *key1 = st.bin_key, *key2 = st.bin_key + nb;
-  const dim3 pgrid(kPassBlocks, KDE_KMAX);
+  const dim3 pgrid(kPassBlocks);
   auto plan = [&](int kind, int nc) -> cudaError_t {
     key_init_kernel<<<1, kThreads, 0, s>>>(st.d_keys);
     key_assign_kernel<T><<<kb, kThreads, 0, s>>>(P, B, kind, kind == 1 ? key1 : key2, st.d_keys);

@@ -58,6 +58,7 @@ struct KeyAcc {
 // intermediate passes and their offsets (in elements) into the pass buffers.
 struct SepPlan {
   int np;
+  long long tot1, tot2;  // elements (region cells) of the two pass buffers, all keys
   int slot_of[KDE_KMAX];
   int key[KDE_KMAX];
   int m[KDE_KMAX][3];
