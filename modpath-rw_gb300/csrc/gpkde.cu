@@ -318,7 +318,7 @@ static_assert(kPlanThreads >= KDE_KMAX, "one plan thread per key");
 // more than cap1 / cap2 elements (nc per region cell) records the sizes it
 // needs in need[0..1], sets need[2] and presents no key, so the passes do
 // nothing and the host reruns the reconstruction with larger buffers.
-__global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, const KeyAcc *K, KdeTable t0, KdeTable t1,
+__global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, KeyAcc *K, KdeTable t0, KdeTable t1,
                                                             KdeTable t2, int scatter, SepPlan *pl, int nc,
                                                             long long cap1, long long cap2, long long *need) {
   __shared__ long long sv1[kPlanThreads], sv2[kPlanThreads];
@@ -393,6 +393,13 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, const K
       atomicMin(&su[axis][4], max(1, bx[4] - m[2]));
       atomicMax(&su[axis][5], min(P.nb[2], bx[5] + m[2]));
     }
+  }
+  // the accumulators of key k were read by thread k only: reset them for the
+  // next key_assign (key_init runs once per reconstruction attempt)
+  if (k < KDE_KMAX) {
+    K->box[k][0] = K->box[k][2] = K->box[k][4] = INT_MAX;
+    K->box[k][1] = K->box[k][3] = K->box[k][5] = INT_MIN;
+    K->cnt[k] = 0;
   }
   // totals: the inclusive scans end at the last key
   const int np = sp[kPlanThreads - 1];
@@ -716,18 +723,22 @@ __global__ void scatter_y_kernel(KdeParams P, const SepPlan *pl, const T *val, c
 template <typename T>
 __global__ void scatter_z_kernel(KdeParams P, const SepPlan *pl, const T *val, const T *V2, T *c0, T *c1, T *c2) {
   const int axis = blockIdx.y;
-  if (!P.mask[axis]) return;
   T *out = axis == 0 ? c0 : (axis == 1 ? c1 : c2);
   const T bs2 = T(P.bin[axis] * P.bin[axis]), bv = T(P.binvol);
   int u[6];
   for (int i = 0; i < 6; ++i) u[i] = pl->ur[axis][i];
-  if (u[0] > u[1]) return;  // no key on this axis: the grid stays zero
-  const long long vol = region_vol(u);
+  // an inactive axis, or one without keys, keeps a zero grid
+  const bool any = P.mask[axis] && u[0] <= u[1];
+  const long long ngrid = (long long)P.nb[0] * P.nb[1] * P.nb[2];
   const int np = pl->np, n = P.nb[2];
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol; i += (long long)gridDim.x * blockDim.x) {
-    int x, y, z;
-    region_xyz(u, i, x, y, z);
-    const long long g = (long long)(x - 1) + (long long)P.nb[0] * ((y - 1) + (long long)P.nb[1] * (z - 1));
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ngrid; g += (long long)gridDim.x * blockDim.x) {
+    const int x = 1 + (int)(g % P.nb[0]);
+    const long long q = g / P.nb[0];
+    const int y = 1 + (int)(q % P.nb[1]), z = 1 + (int)(q / P.nb[1]);
+    if (!any || x < u[0] || x > u[1] || y < u[2] || y > u[3] || z < u[4] || z > u[5]) {
+      out[g] = T(0);
+      continue;
+    }
     T acc = T(0);
     for (int j = 0; j < np; ++j) {
       if (pl->key[j] / KDE_MAXDB != axis) continue;
@@ -897,8 +908,9 @@ __global__ void bin_reduce_final_kernel(int what, int nblk, const double *partia
 // phase 0: isotropy correction of the net roughness + scale where net > 0.
 // (and S[S_SCMAX] = max positive scale, for the bins with zero net roughness)
 template <typename T>
-__global__ void optimal_phase0_kernel(KdeParams P, KdeBinsT<T> B, double *S) {
+__global__ void optimal_phase0_kernel(KdeParams P, KdeBinsT<T> B, double *S, int *flag) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b == 0) *flag = 0;  // read by optimal_phase1 / rescale, which run after this kernel
   double scv = 0.0;
   if (b < B.n) {
     const T min_pos_net = T(S[S_NETMINPOS]);
@@ -1306,7 +1318,6 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   int *key1 = st.bin_key, *key2 = st.bin_key + nb;
   const dim3 pgrid(kPassBlocks);
   auto plan = [&](int kind, int nc) -> cudaError_t {
-    key_init_kernel<<<1, kThreads, 0, s>>>(st.d_keys);
     key_assign_kernel<T><<<kb, kThreads, 0, s>>>(P, B, kind, kind == 1 ? key1 : key2, st.d_keys);
     if (kind == 1)
       plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.wtab, st.wtab, st.wtab, 0, plan1, nc, st.t1_cap,
@@ -1314,7 +1325,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     else
       plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.sdtab[0], st.sdtab[1], st.sdtab[2], 1, plan2, nc,
                                              st.t1_cap, st.t2_cap, st.d_need);
-    st.launches += 3;
+    st.launches += 2;
     return cudaGetLastError();
   };
   // sum over every bin's smoothing kernel of `field`, at the bins
@@ -1355,9 +1366,9 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     KCK(gather1(dens_grid, GZ_SUPPORT, nullptr, nullptr));
     KCK(plan(1, P.ndim == 3 ? 6 : 1));
     KCK(gather1(dens_grid, GZ_NEST, nullptr, nullptr));
-    // curvatures: second-derivative scatters of the counts, squared
+    // curvatures: second-derivative scatters of the counts, squared (every
+    // cell of the three grids is written, zero outside the keys' regions)
     KCK(plan(2, 1));
-    for (T *c : {cx, cy, cz}) KCK(cudaMemsetAsync(c, 0, sizeof(T) * ngrid, s));
     scatter_x_kernel<T><<<pgrid, kThreads, 0, s>>>(P, B, plan2, val, st.cell_bin, key2, t1);
     scatter_y_kernel<T><<<pgrid, kThreads, 0, s>>>(P, plan2, val, t1, t2);
     scatter_z_kernel<T><<<dim3(gb, 3), kThreads, 0, s>>>(P, plan2, val, t2, cx, cy, cz);
@@ -1377,8 +1388,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
       KCK(gather1(cg[a], GZ_NET, r1, B.net));
     }
     // optimal smoothing and shape; the extremes stay on the device
-    optimal_phase0_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, S);
-    KCK(cudaMemsetAsync(st.d_flag, 0, sizeof(int), s));
+    optimal_phase0_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, S, st.d_flag);
     optimal_phase1_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, S, st.d_flag);
     rescale_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, st.d_flag);
     st.launches += 3;
@@ -1388,8 +1398,9 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     return fetch_async();
   };
   KCK(cudaMemsetAsync(st.d_need, 0, 3 * sizeof(long long), s));
+  key_init_kernel<<<1, kThreads, 0, s>>>(st.d_keys);
   init_bins_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, hs, S);
-  st.launches += 1;
+  st.launches += 2;
   KCK(density());
   KCK(reduce(RED_ALMISE));  // nEstimate and net roughness are zero: 0
   KCK(fetch_async());
