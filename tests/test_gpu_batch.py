@@ -132,3 +132,39 @@ def test_batch_state_errors(gpu_lib):
         b.member(1).set_particles(W.release_in_box(g, 10, 0.5, 1.5, 0.5, 1.5, 0.5, 1.5))
     b.advance(0.0, 5.0)
     b.close()
+
+
+def test_batch_member_observations_and_empty_member(gpu_lib):
+    """Observation records of a member that does not start at cell 0 equal a
+    separate handle's; a member without particles is carried along."""
+    g, f, p, opt, info = W.config2(n_particles=4000, nlay=4, nrow=12, ncol=30, seed=7, use_torch=False)
+    u, fu = W.uniform_flow(ncol=20, q=0.3)
+    empty = W.release_in_box(u, 0, 1.0, 2.0, 0.0, 1.0, 0.0, 1.0)
+    k, i, j = np.meshgrid(np.arange(g.nlay), np.arange(g.nrow), np.arange(g.ncol), indexing="ij")
+    node = (k * g.nrow * g.ncol + i * g.ncol + j + 1).ravel()
+    col = j.ravel()
+    cells = np.concatenate([node[col == g.ncol - 1], node[col == g.ncol // 2]]).astype(np.int32)
+    obs = np.concatenate([np.zeros((col == g.ncol - 1).sum()), np.ones((col == g.ncol // 2).sum())]).astype(np.int32)
+    style = np.array([2, 1], np.int32)
+    ref = mprw.Tracker(g, opt)
+    ref.load_flow(f)
+    ref.set_particles(p)
+    ref.set_observations(cells, obs, style)
+    b = mprw.Batch([u, g], opt)         # the field is member 1: its cells start after the column's 20
+    b.load_flow(0, fu)
+    b.load_flow(1, f)
+    b.set_particles([empty, p])
+    m = b.member(1)
+    m.set_observations(cells, obs, style)
+    for t0, t1 in ((0.0, 40.0), (40.0, 120.0)):
+        assert b.advance(t0, t1) == ref.advance(t0, t1)
+        r1, r2 = m.observe_sinks(), ref.observe_sinks()
+        for key in ("obs", "id", "time", "mass"):
+            np.testing.assert_array_equal(r1[key], r2[key])
+        c1, m1 = m.observe_resident()
+        c2, m2 = ref.observe_resident()
+        np.testing.assert_array_equal(c1, c2)
+        np.testing.assert_array_equal(m1, m2)
+    assert b.member(0).get_particles()["cell"].shape == (0,)
+    ref.close()
+    b.close()
