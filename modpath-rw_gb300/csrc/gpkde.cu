@@ -587,60 +587,42 @@ enum { GZ_OUT = 0, GZ_SUPPORT = 1, GZ_NEST = 2, GZ_NET = 3 };
 // GZ_NET (1-D): out[b] = out2[b] = the roughness, which is the net roughness;
 // NC = 6 and GZ_NET also fold max(net) and min(net > 0) into S.
 // A group of kZLanes<NC> consecutive lanes shares one bin: each lane sums
-// every kZLanes-th tap and the group adds its partial sums (a shuffle tree)
-// into shared memory.  The bin's epilogue (support update, curvature
-// bandwidth, net roughness: FP64 pow chains when T = double) then runs one
-// bin per thread on the block's first kZBins threads, so its warps are full
-// (a GB300 FP64 warp instruction costs the same with 1 or 32 lanes active).
-// Launch with kThreads-thread blocks, kZBins<NC> bins per block.
+// every kZLanes-th tap, then the group adds its partial sums (a shuffle tree),
+// and the group's first lane finishes the bin.  Launch with
+// kZLanes<NC> * nbins threads.
 template <int NC>
 constexpr int kZLanes = NC == 1 ? 8 : 4;
-template <int NC>
-constexpr int kZBins = kThreads / kZLanes<NC>;
 
 template <typename T, int NC>
-__global__ void __launch_bounds__(kThreads) gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl,
-                                                            const T *val, const int *bin_key, const T *T2, int mode,
-                                                            T *out, T *out2, double *S) {
-  constexpr int G = kZLanes<NC>, NB = kZBins<NC>;
-  __shared__ T red[NB][NC];
-  const int b0 = blockIdx.x * NB;
-  const int local = threadIdx.x / G, sub = threadIdx.x % G;
+__global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, const T *val, const int *bin_key,
+                                const T *T2, int mode, T *out, T *out2, double *S) {
+  constexpr int G = kZLanes<NC>;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = tid / G, sub = tid % G;
   // np == 0: the plan did not fit, the attempt is discarded
-  const bool planned = pl->np != 0;
-  {
-    const int b = b0 + local;
-    T acc[NC];
-    for (int c = 0; c < NC; ++c) acc[c] = T(0);
-    if (planned && b < B.n) {
-      const int j = pl->slot_of[bin_key[b]];
-      const int m = pl->m[j][2], n = P.nb[2];
-      const T *f = val + pl->fofs[j][2];
-      const int *r2 = pl->r2[j];
-      const T *in = T2 + pl->o2[j] * NC;
-      const int bx = B.gx[b], by = B.gy[b], bz = B.gz[b];
-      for (int t = sub; t <= 2 * m; t += G) {
-        const int p = reflect_pos(bz - m + t, n);
-        if (p < 1) continue;
-        const T w = f[t];
-        const long long l = region_loc(r2, bx, by, p) * NC;
-        for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
-      }
-    }
-    // every lane takes part (groups never straddle a warp)
-    for (int o = G / 2; o > 0; o >>= 1)
-      for (int c = 0; c < NC; ++c) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], o, G);
-    if (sub == 0)
-      for (int c = 0; c < NC; ++c) red[local][c] = acc[c];
-  }
-  __syncthreads();
-  if (threadIdx.x >= NB) return;  // whole warps: NB is a multiple of 32
-  const int b = b0 + threadIdx.x;
-  const bool valid = planned && b < B.n;
-  double net = 0.0;
+  const bool valid = b < B.n && pl->np != 0;
+  T acc[NC];
+  for (int c = 0; c < NC; ++c) acc[c] = T(0);
   if (valid) {
-    T acc[NC];
-    for (int c = 0; c < NC; ++c) acc[c] = red[threadIdx.x][c];
+    const int j = pl->slot_of[bin_key[b]];
+    const int m = pl->m[j][2], n = P.nb[2];
+    const T *f = val + pl->fofs[j][2];
+    const int *r2 = pl->r2[j];
+    const T *in = T2 + pl->o2[j] * NC;
+    const int bx = B.gx[b], by = B.gy[b], bz = B.gz[b];
+    for (int t = sub; t <= 2 * m; t += G) {
+      const int p = reflect_pos(bz - m + t, n);
+      if (p < 1) continue;
+      const T w = f[t];
+      const long long l = region_loc(r2, bx, by, p) * NC;
+      for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
+    }
+  }
+  // every lane of the warp takes part (groups never straddle a warp)
+  for (int o = G / 2; o > 0; o >>= 1)
+    for (int c = 0; c < NC; ++c) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], o, G);
+  double net = 0.0;
+  if (valid && sub == 0) {
     if constexpr (NC == 1) {
       if (mode == GZ_SUPPORT) {
         support_update<T>(P, B, b, acc[0]);
@@ -1320,9 +1302,9 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   const int nb = B.n;
   const int64_t ngrid = (int64_t)P.nb[0] * P.nb[1] * P.nb[2];
   const int bb = (nb + kBinThreads - 1) / kBinThreads;
-  // z passes: kZBins bins per block of kThreads
-  const int zb1 = (nb + kZBins<1> - 1) / kZBins<1>;
-  const int zb6 = (nb + kZBins<6> - 1) / kZBins<6>;
+  // z passes: kZLanes threads per bin
+  const int zb1 = (int)(((long long)nb * kZLanes<1> + kThreads - 1) / kThreads);
+  const int zb6 = (int)(((long long)nb * kZLanes<6> + kThreads - 1) / kThreads);
   const int gb = blocks_for(ngrid);
   const int rb = std::min(blocks_for(nb), kRedBlocks);
   const int kb = std::min((nb + kThreads - 1) / kThreads, 2 * kRedBlocks);
