@@ -586,23 +586,13 @@ enum { GZ_OUT = 0, GZ_SUPPORT = 1, GZ_NEST = 2, GZ_NET = 3 };
 
 // GZ_NET (1-D): out[b] = out2[b] = the roughness, which is the net roughness;
 // NC = 6 and GZ_NET also fold max(net) and min(net > 0) into S.
-// A group of kZLanes<NC> consecutive lanes shares one bin: each lane sums
-// every kZLanes-th tap, then the group adds its partial sums (a shuffle tree),
-// and the group's first lane finishes the bin.  Launch with
-// kZLanes<NC> * nbins threads.
-template <int NC>
-constexpr int kZLanes = NC == 1 ? 8 : 4;
-
 template <typename T, int NC>
 __global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, const T *val, const int *bin_key,
                                 const T *T2, int mode, T *out, T *out2, double *S) {
-  constexpr int G = kZLanes<NC>;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int b = tid / G, sub = tid % G;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
   // np == 0: the plan did not fit, the attempt is discarded
   const bool valid = b < B.n && pl->np != 0;
-  T acc[NC];
-  for (int c = 0; c < NC; ++c) acc[c] = T(0);
+  double net = 0.0;
   if (valid) {
     const int j = pl->slot_of[bin_key[b]];
     const int m = pl->m[j][2], n = P.nb[2];
@@ -610,19 +600,15 @@ __global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, c
     const int *r2 = pl->r2[j];
     const T *in = T2 + pl->o2[j] * NC;
     const int bx = B.gx[b], by = B.gy[b], bz = B.gz[b];
-    for (int t = sub; t <= 2 * m; t += G) {
+    T acc[NC];
+    for (int c = 0; c < NC; ++c) acc[c] = T(0);
+    for (int t = 0; t <= 2 * m; ++t) {
       const int p = reflect_pos(bz - m + t, n);
       if (p < 1) continue;
       const T w = f[t];
       const long long l = region_loc(r2, bx, by, p) * NC;
       for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
     }
-  }
-  // every lane of the warp takes part (groups never straddle a warp)
-  for (int o = G / 2; o > 0; o >>= 1)
-    for (int c = 0; c < NC; ++c) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], o, G);
-  double net = 0.0;
-  if (valid && sub == 0) {
     if constexpr (NC == 1) {
       if (mode == GZ_SUPPORT) {
         support_update<T>(P, B, b, acc[0]);
@@ -1302,9 +1288,6 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   const int nb = B.n;
   const int64_t ngrid = (int64_t)P.nb[0] * P.nb[1] * P.nb[2];
   const int bb = (nb + kBinThreads - 1) / kBinThreads;
-  // z passes: kZLanes threads per bin
-  const int zb1 = (int)(((long long)nb * kZLanes<1> + kThreads - 1) / kThreads);
-  const int zb6 = (int)(((long long)nb * kZLanes<6> + kThreads - 1) / kThreads);
   const int gb = blocks_for(ngrid);
   const int rb = std::min(blocks_for(nb), kRedBlocks);
   const int kb = std::min((nb + kThreads - 1) / kThreads, 2 * kRedBlocks);
@@ -1349,7 +1332,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   auto gather1 = [&](const T *field, int mode, T *out, T *out2) -> cudaError_t {
     gather_x_kernel<T, 1><<<pgrid, kThreads, 0, s>>>(P, plan1, val, Fields<T>{{field}}, t1);
     gather_y_kernel<T, 1><<<pgrid, kThreads, 0, s>>>(P, plan1, val, t1, t2);
-    gather_z_kernel<T, 1><<<zb1, kThreads, 0, s>>>(P, B, plan1, val, key1, t2, mode, out, out2, S);
+    gather_z_kernel<T, 1><<<bb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, mode, out, out2, S);
     st.launches += 3;
     return cudaGetLastError();
   };
@@ -1395,7 +1378,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
       products_kernel<T><<<gb, kThreads, 0, s>>>(cx, cy, cz, cxy, cxz, cyz, ngrid);
       gather_x_kernel<T, 6><<<pgrid, kThreads, 0, s>>>(P, plan1, val, Fields<T>{{cx, cy, cz, cxy, cxz, cyz}}, t1);
       gather_y_kernel<T, 6><<<pgrid, kThreads, 0, s>>>(P, plan1, val, t1, t2);
-      gather_z_kernel<T, 6><<<zb6, kThreads, 0, s>>>(P, B, plan1, val, key1, t2, GZ_OUT, nullptr, nullptr, S);
+      gather_z_kernel<T, 6><<<bb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, GZ_OUT, nullptr, nullptr, S);
       st.launches += 4;
     } else {
       int a = 0;
