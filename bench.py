@@ -75,7 +75,7 @@ def parse():
                     help="ensemble size of the batched leg (realizations 0..R-1 of the 64-member ensemble)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default launch tuning instead of mprw_autotune before the warm-up")
-    ap.add_argument("--kde-streams", type=int, default=8,
+    ap.add_argument("--kde-streams", type=int, default=4,
                     help="batched leg: reconstructions run concurrently (mprw_gpkde_batch concurrency)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="precision of the headline run (mixed: for profiling the MIXED kernel alone)")

@@ -270,7 +270,7 @@ int mprw_set_particles_batch(mprw_handle *batch, const int64_t *counts, const in
                              const uint64_t *rng_ctr);
 
 /* GPKDE of every member of a batch (as mprw_gpkde on each member view), up to
- * `concurrency` members at a time (<= 0: 8; at most 16), each on its own
+ * `concurrency` members at a time (<= 0: 4; at most 16), each on its own
  * non-blocking stream driven by its own host thread, so that one member's
  * host round trips and small launches overlap another's kernels.  opts,
  * density and loops_done (may be NULL) have one entry per member; histogram

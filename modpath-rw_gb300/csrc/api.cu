@@ -1289,7 +1289,7 @@ int mprw_gpkde_batch(mprw_handle *h, const mprw_gpkde_options *opts, double *con
   const int nm = (int)h->members.size();
   for (int k = 0; k < nm; ++k)
     if (!density[k]) return fail(h, MPRW_E_INVAL, "mprw_gpkde_batch: null density for member " + std::to_string(k));
-  int nw = concurrency > 0 ? concurrency : 8;
+  int nw = concurrency > 0 ? concurrency : 4;
   if (nw > 16) nw = 16;
   if (nw > nm) nw = nm;
   while ((int)h->kde_workers.size() < nw) {

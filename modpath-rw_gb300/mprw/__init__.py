@@ -455,7 +455,7 @@ class Batch:
         return [m.get_particles(global_xyz) for m in self.members]
 
     def gpkde(self, domains, bin_size, origin=(0.0, 0.0, 0.0), n_opt_loops=10, kdb=(0.3, 0.3, 15.0), rel_err=0.02,
-              skip_error=False, unit_volume=True, scaling_factor=1.0, precision=FP64, concurrency=8,
+              skip_error=False, unit_volume=True, scaling_factor=1.0, precision=FP64, concurrency=4,
               histograms=False):
         """GPKDE of every member (mprw_gpkde_batch), ``domains[k]`` the domain
         size of member k's reconstruction grid.  Returns a list of densities
