@@ -306,6 +306,22 @@ int mprw_get_tuning(mprw_handle *h, int32_t *blocks_per_sm, int32_t *sort_interv
 int mprw_autotune(mprw_handle *h, double t_begin, double t_end, int32_t *blocks_per_sm, int32_t *sort_interval,
                   double *rates);
 
+/* Cancellation of mprw_advance (the reference has none: its loops end by
+ * their own caps).  The step kernel reads a cancel flag in mapped host memory
+ * every few hundred iterations of each warp.  mprw_set_timeout: an advance
+ * that is still running after timeout_ms (0 = no limit, the default) raises
+ * the flag.  mprw_cancel raises it from any host thread and stops the advance
+ * that is running, or else the next one.  A cancelled advance returns
+ * MPRW_E_ABORTED after the kernel has returned (the context stays usable):
+ * every particle then holds a valid location -- its last completed step, or
+ * the start of the cell it was entering -- with status ACTIVE and its random
+ * counter; particles not reached keep their previous state.  The next
+ * mprw_advance continues from there (it starts new cell visits, so the
+ * result is a valid trajectory but not bit-identical to an uninterrupted
+ * one).  On a batch member both apply to the batch. */
+int mprw_set_timeout(mprw_handle *h, double timeout_ms);
+int mprw_cancel(mprw_handle *h);
+
 /* Optional: launch on a caller-provided cudaStream_t (NULL = the handle's). */
 int mprw_set_stream(mprw_handle *h, void *stream);
 

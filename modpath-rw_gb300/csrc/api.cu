@@ -95,6 +95,10 @@ struct mprw_handle {
   int sort_interval = 1;     // sort by cell every k-th advance (0 never)
   int64_t advance_count = 0;
   bool perm_valid = false;   // d_perm holds a permutation of the current n particles
+  // cancel flag of the step kernel: pinned, mapped host memory
+  volatile int *h_abort = nullptr;
+  int *d_abort = nullptr;
+  double timeout_ms = 0.0;   // mprw_set_timeout: 0 = wait as long as the advance takes
   std::string err;
   // batched realizations
   mprw_handle *parent = nullptr;        // member view: the batch it belongs to
@@ -168,6 +172,7 @@ void free_all(mprw_handle *h) {
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->h_counters) cudaFreeHost(h->h_counters);
+  if (h->h_abort) cudaFreeHost((void *)h->h_abort);
   if (h->d_counts) cudaFree(h->d_counts);
   if (h->d_kpart) cudaFree(h->d_kpart);
   for (void *p : {(void *)h->d_obs_of_cell, (void *)h->d_obs_style, (void *)h->d_obs_count, (void *)h->d_obs_mass})
@@ -250,6 +255,11 @@ int init_common(mprw_handle *h, const mprw_options *o) {
   CK(cudaEventCreate(&h->ev3));
   CK(cudaMallocHost(&h->h_counters, 4 * sizeof(unsigned long long)));
   CK(dalloc(&h->d_counters, 4));
+  void *ab = nullptr;
+  CK(cudaHostAlloc(&ab, sizeof(int), cudaHostAllocMapped));
+  h->h_abort = (volatile int *)ab;
+  *h->h_abort = 0;
+  CK(cudaHostGetDevicePointer((void **)&h->d_abort, ab, 0));
   return MPRW_OK;
 }
 
@@ -691,6 +701,7 @@ int launch_step(mprw_handle *h, double t_begin, double t_end, int bps, bool use_
     a.perm = use_perm ? h->d_perm : nullptr;
     a.queue = h->d_counters;
     a.steps = h->d_counters + 1;
+    a.abort = h->d_abort;
     a.n = h->n;
     a.t_begin = t_begin;
     a.t_end = t_end;
@@ -717,6 +728,7 @@ int launch_step(mprw_handle *h, double t_begin, double t_end, int bps, bool use_
     a.perm = use_perm ? h->d_perm : nullptr;
     a.queue = h->d_counters;
     a.steps = h->d_counters + 1;
+    a.abort = h->d_abort;
     a.n = h->n;
     a.t_begin = t_begin;
     a.t_end = t_end;
@@ -731,9 +743,32 @@ int launch_step(mprw_handle *h, double t_begin, double t_end, int bps, bool use_
   h->launches += 1;
   CK(cudaEventRecord(h->ev1, s));
   CK(cudaMemcpyAsync(h->h_counters, h->d_counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  // wait; past the timeout, raise the cancel flag (the kernel reads it every
+  // kAbortPoll iterations of each warp and returns)
+  bool timed_out = false;
+  if (h->timeout_ms > 0.0) {
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+      const cudaError_t q = cudaEventQuery(h->ev1);
+      if (q == cudaSuccess) break;
+      if (q != cudaErrorNotReady) CK(q);
+      if (std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count() > h->timeout_ms) {
+        *h->h_abort = 1;
+        timed_out = true;
+        break;
+      }
+      std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+  }
   CK(cudaStreamSynchronize(s));
+  const bool cancelled = *h->h_abort != 0;
+  *h->h_abort = 0;
   CK(cudaEventElapsedTime(ms, h->ev0, h->ev1));
   *steps = (int64_t)h->h_counters[1];
+  if (cancelled)
+    return fail(h, MPRW_E_ABORTED,
+                timed_out ? "advance stopped at its timeout; the particles hold their last completed pass"
+                          : "advance cancelled; the particles hold their last completed pass");
   return MPRW_OK;
 }
 
@@ -786,6 +821,21 @@ int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_do
   if (rc != MPRW_OK) return rc;
   h->step_ms = ms;
   if (steps_done) *steps_done = steps;
+  return MPRW_OK;
+}
+
+int mprw_set_timeout(mprw_handle *h, double timeout_ms) {
+  if (!h) return MPRW_E_INVAL;
+  if (h->parent) return fail(h, MPRW_E_STATE, "mprw_set_timeout on a batch member: set the batch's");
+  if (!(timeout_ms >= 0.0)) return fail(h, MPRW_E_INVAL, "mprw_set_timeout: negative or NaN timeout");
+  h->timeout_ms = timeout_ms;
+  return MPRW_OK;
+}
+
+int mprw_cancel(mprw_handle *h) {
+  if (!h) return MPRW_E_INVAL;
+  mprw_handle *t = h->parent ? h->parent : h;
+  if (t->h_abort) *t->h_abort = 1;
   return MPRW_OK;
 }
 

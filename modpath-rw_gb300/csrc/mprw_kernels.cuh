@@ -5,6 +5,7 @@
 namespace mprw {
 
 constexpr int kStepThreads = 256;
+constexpr int kAbortPoll = 256;  // main-loop iterations between two reads of the cancel flag
 
 template <typename R>
 struct AdvanceArgs {
@@ -20,6 +21,7 @@ struct AdvanceArgs {
   const uint32_t *perm;      // processing order (cell-sorted) or null
   unsigned long long *queue; // work counter, zeroed before launch
   unsigned long long *steps; // particle-step counter
+  const volatile int *abort; // host-mapped cancel flag (may be null): polled every kAbortPoll iterations
   int64_t n;
   double t_begin, t_end;
   int ndim, d1, d2;

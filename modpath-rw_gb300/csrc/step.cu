@@ -734,8 +734,30 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
   uint32_t massb = 0;
   int32_t conn6[6] = {-1, -1, -1, -1, -1, -1};
 
+  unsigned iter = 0;
   for (;;) {
     __syncwarp(FULL);
+    // cancel: the host set the flag (timeout or mprw_cancel).  Each lane keeps
+    // its particle where it is -- the start of the cell it is entering, or the
+    // last completed pass of its visit -- as ACTIVE, and the queue is not
+    // drained further, so every particle holds a valid location.
+    if (a.abort && (++iter % kAbortPoll) == 0) {
+      int ab = (lane == 0) ? *a.abort : 0;
+      ab = __shfl_sync(FULL, ab, 0);
+      if (ab) {
+        if (p >= 0) {
+          a.cell[p] = c;
+          if (need_cell) {
+            a.x[p] = ex; a.y[p] = ey; a.z[p] = ez; a.t[p] = et;
+          } else {
+            a.x[p] = V.x; a.y[p] = V.y; a.z[p] = V.z; a.t[p] = V.t;
+          }
+          a.status[p] = ST_ACTIVE;
+          a.ctr[p] = ctr;
+        }
+        break;
+      }
+    }
     // (a) refill
     const bool want = (p < 0) && open;
     const unsigned m = __ballot_sync(FULL, want);

@@ -37,6 +37,10 @@ class MprwError(RuntimeError):
     pass
 
 
+class MprwAborted(MprwError):
+    """An advance stopped by its timeout or by cancel() (MPRW_E_ABORTED)."""
+
+
 class GridDesc(C.Structure):
     _fields_ = [("nlay", C.c_int32), ("nrow", C.c_int32), ("ncol", C.c_int32),
                 ("delr", _dp), ("delc", _dp), ("top", _dp), ("botm", _dp)]
@@ -99,6 +103,8 @@ def load_library() -> C.CDLL:
         "mprw_gpkde_batch": (C.c_int, [H, C.POINTER(GpkdeOptions), C.POINTER(_dp), C.POINTER(_dp), _ip,
                                        C.c_int32]),
         "mprw_set_tuning": (C.c_int, [H, C.c_int32, C.c_int32]),
+        "mprw_set_timeout": (C.c_int, [H, C.c_double]),
+        "mprw_cancel": (C.c_int, [H]),
         "mprw_get_tuning": (C.c_int, [H, _ip, _ip, _ip]),
         "mprw_autotune": (C.c_int, [H, C.c_double, C.c_double, _ip, _ip, _dp]),
         "mprw_last_error": (C.c_char_p, [H]),
@@ -174,7 +180,8 @@ class Tracker:
 
     def _check(self, rc, what):
         if rc != 0:
-            raise MprwError(f"{what}: rc={rc}: {self.lib.mprw_last_error(self.h).decode()}")
+            cls = MprwAborted if rc == -5 else MprwError
+            raise cls(f"{what}: rc={rc}: {self.lib.mprw_last_error(self.h).decode()}")
 
     def load_flow(self, f: Flow):
         keep = dict(ia=_i32(f.ia), ja=_i32(f.ja), flowja=_f64(f.flowja), por=_f64(f.porosity),
@@ -317,6 +324,15 @@ class Tracker:
     def set_stream(self, stream_ptr: int):
         self._check(self.lib.mprw_set_stream(self.h, C.c_void_p(stream_ptr)), "mprw_set_stream")
 
+    def set_timeout(self, timeout_ms: float):
+        """Stop an advance still running after timeout_ms (0: no limit); it then
+        raises MprwAborted with every particle at a valid location."""
+        self._check(self.lib.mprw_set_timeout(self.h, float(timeout_ms)), "mprw_set_timeout")
+
+    def cancel(self):
+        """Stop the running (or else the next) advance; safe from another thread."""
+        self.lib.mprw_cancel(self.h)
+
     def set_tuning(self, blocks_per_sm: int = 0, sort_interval: int = 1):
         self._check(self.lib.mprw_set_tuning(self.h, int(blocks_per_sm), int(sort_interval)), "mprw_set_tuning")
 
@@ -406,9 +422,9 @@ class Batch:
         self.members = [_MemberView(self, k, g) for k, g in enumerate(self.grids)]
         self.counts = np.zeros(len(self.grids), np.int64)
 
-    def _check(self, rc, what):
-        if rc != 0:
-            raise MprwError(f"{what}: rc={rc}: {self.lib.mprw_last_error(self.h).decode()}")
+    _check = Tracker._check
+    set_timeout = Tracker.set_timeout
+    cancel = Tracker.cancel
 
     def member(self, k: int) -> Tracker:
         return self.members[k]
