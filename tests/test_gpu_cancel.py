@@ -73,7 +73,7 @@ def test_cancel_from_another_thread(gpu_lib):
 
     th = threading.Thread(target=run)
     th.start()
-    time.sleep(0.2)
+    time.sleep(0.005)     # the cancel stops the running advance, or the one about to start
     tr.cancel()
     th.join(timeout=60.0)
     assert not th.is_alive() and len(err) == 1
