@@ -18,10 +18,13 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/mprw_gpu.h"
 #include "gpkde.cuh"
@@ -110,6 +113,23 @@ struct mprw_handle {
 };
 
 namespace {
+
+// NVTX ranges around the library's calls, for a profiler's timeline, when
+// the environment sets MPRW_NVTX (NVTX is header-only: without a tool
+// attached a range costs a branch).
+bool nvtx_on() {
+  static const bool on = std::getenv("MPRW_NVTX") != nullptr;
+  return on;
+}
+struct NvtxRange {
+  bool on;
+  explicit NvtxRange(const char *name) : on(nvtx_on()) {
+    if (on) nvtxRangePushA(name);
+  }
+  ~NvtxRange() {
+    if (on) nvtxRangePop();
+  }
+};
 
 int fail(mprw_handle *h, int code, const std::string &msg) {
   if (h) h->err = msg;
@@ -401,6 +421,7 @@ int mprw_batch_member(mprw_handle *h, int32_t member, mprw_handle **view) {
 }
 
 int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *f) {
+  NvtxRange nvtx_("mprw_load_flow");
   if (!h) return MPRW_E_INVAL;
   if (!h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_load_flow on a batch: load each member's flow");
   if (!f || !f->ia || !f->ja || !f->flowja || !f->porosity || !f->retardation || !f->iboundts || !f->alpha_l ||
@@ -784,6 +805,7 @@ int sort_particles(mprw_handle *h) {
 extern "C" {
 
 int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_done) {
+  NvtxRange nvtx_("mprw_advance");
   if (!h) return MPRW_E_INVAL;
   if (h->parent) return fail(h, MPRW_E_STATE, "mprw_advance on a batch member: advance the batch");
   if (!h->members.empty()) {
@@ -861,6 +883,7 @@ int mprw_get_tuning(mprw_handle *h, int32_t *blocks_per_sm, int32_t *sort_interv
 
 int mprw_autotune(mprw_handle *h, double t_begin, double t_end, int32_t *blocks_per_sm, int32_t *sort_interval,
                   double *rates) {
+  NvtxRange nvtx_("mprw_autotune");
   if (!h) return MPRW_E_INVAL;
   if (h->parent) return fail(h, MPRW_E_STATE, "mprw_autotune on a batch member: tune the batch");
   if (!h->members.empty()) {
@@ -1101,6 +1124,7 @@ extern "C" {
 
 int mprw_histogram(mprw_handle *h, const double origin[3], const double bin_size[3], const int32_t n_bins[3],
                    double *counts, int64_t *n_binned, double *eff_mass) {
+  NvtxRange nvtx_("mprw_histogram");
   if (!h) return MPRW_E_INVAL;
   if (!h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_histogram on a batch: use a member view");
   if (!origin || !bin_size || !n_bins || !counts) return fail(h, MPRW_E_INVAL, "mprw_histogram: null argument");
@@ -1121,6 +1145,7 @@ int mprw_histogram(mprw_handle *h, const double origin[3], const double bin_size
 
 int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, double *histogram,
                int32_t n_bins_out[3], int32_t *loops_done) {
+  NvtxRange nvtx_("mprw_gpkde");
   if (!h) return MPRW_E_INVAL;
   if (!h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_gpkde on a batch: use a member view");
   if (!o || !density) return fail(h, MPRW_E_INVAL, "mprw_gpkde: null argument");
@@ -1333,6 +1358,7 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
 
 int mprw_gpkde_batch(mprw_handle *h, const mprw_gpkde_options *opts, double *const *density,
                      double *const *histogram, int32_t *loops_done, int32_t concurrency) {
+  NvtxRange nvtx_("mprw_gpkde_batch");
   if (!h) return MPRW_E_INVAL;
   if (h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_gpkde_batch: not a batch handle");
   if (!opts || !density) return fail(h, MPRW_E_INVAL, "mprw_gpkde_batch: null argument");

@@ -228,6 +228,25 @@ class Tracker:
             _p(arrs["t"], _dp), _p(arrs["st"], _ip), _p(arrs["m"], _dp), _p(arrs["id"], _up),
             _p(arrs["rc"], _up)), "mprw_set_particles")
         self.n = p.n
+        self._ids, self._mass = arrs["id"], arrs["m"]   # host copies for checkpoints
+
+    def checkpoint(self, path):
+        """Write the particle state (cell, local x/y/z, time, status, random
+        counter, id, mass) to ``path`` (.npz).  With counter-based random
+        numbers, restore() + the remaining advances reproduce an
+        uninterrupted run bit for bit."""
+        o = self.get_particles(global_xyz=False)
+        n = self.n
+        np.savez(path, cell=o["cell"], lx=o["lx"], ly=o["ly"], lz=o["lz"], t=o["t"], status=o["status"],
+                 rng_ctr=o["rng_ctr"], id=np.arange(n, dtype=np.uint64) if self._ids is None else self._ids,
+                 mass=np.ones(n) if self._mass is None else self._mass, has_id=self._ids is not None)
+
+    def restore(self, path):
+        """Set the particles from a checkpoint() file."""
+        d = np.load(path)
+        self.set_particles(Particles(cell=d["cell"], lx=d["lx"], ly=d["ly"], lz=d["lz"], t=d["t"],
+                                     status=d["status"], mass=d["mass"],
+                                     id=d["id"] if bool(d["has_id"]) else None, rng_ctr=d["rng_ctr"]))
 
     def advance(self, t_begin: float, t_end: float) -> int:
         steps = C.c_int64(0)
