@@ -335,3 +335,21 @@ def config3(n_real=64, scale=1.0, precision=MIXED, use_torch=None, members=None)
     opt = Options(time_step_kind=MIN_ADV_DISP, ts_param=(0.1, 0.1), advection_kind=EULERIAN, dim_mask=(1, 1, 1),
                   stop_weak_sinks=True, precision=precision)
     return ens, opt, params
+
+
+def config5(n_particles=100_000_000, nlay=50, nrow=500, ncol=500, seed=5, precision=FP64, use_torch=None,
+            source=((10.0, 30.0), (240.0, 260.0), (20.0, 30.0)), release_days=50.0):
+    """Large single run with continuous injection: 500x500x50 cells of 1 m,
+    ln K as config 2 with sigma2 2 and correlation lengths 20 m / 2 m, heads
+    1 m / 0 m at the x ends; n_particles released at a constant rate over
+    release_days (pending particles with uniform release times) from a
+    20x20x10 m source (x, y, z ranges of ``source``, model coordinates)."""
+    g, f, info = heterogeneous_flow(nlay, nrow, ncol, sigma2=2.0, kg=10.0, lh=20.0, lv=2.0, porosity=0.25,
+                                    alpha_l=0.5, alpha_t=0.05, dm=1e-4, seed=seed, use_torch=use_torch)
+    (x0, x1), (y0, y1), (z0, z1) = source
+    p = release_in_box(g, n_particles, x0, x1, y0, y1, z0, z1, seed=1000 + seed)
+    rng = np.random.default_rng(2000 + seed)
+    p.t = rng.uniform(0.0, release_days, n_particles)
+    opt = Options(time_step_kind=MIN_ADV_DISP, ts_param=(0.1, 0.1), advection_kind=EULERIAN, dim_mask=(1, 1, 1),
+                  stop_weak_sinks=True, precision=precision)
+    return g, f, p, opt, info
