@@ -1,6 +1,6 @@
 """Benchmark of the random-walk particle-tracking hot path on one GB300.
 
-Workload (BASELINE config 2): 200x100x20 cells of 1 m, lognormal K
+Workload (the lognormal slab): 200x100x20 cells of 1 m, lognormal K
 (sigma2 lnK = 1, geometric mean 10 m/d, exponential covariance 10 m / 2 m,
 seeded FFT field), FP64 steady heads by CG to 1e-12, porosity 0.25,
 alphaL 0.5 m, alphaT 0.05 m, Dm 1e-4 m2/d, 1,000,000 unit-mass particles
@@ -75,10 +75,10 @@ def parse():
                     help="ensemble size of the batched leg (realizations 0..R-1 of the 64-member ensemble)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default launch tuning instead of mprw_autotune before the warm-up")
-    ap.add_argument("--workload", default="config2", choices=["config2", "config5"],
-                    help="config5: the large continuous-injection run, whole (20 x 25 days), FP64 then MIXED; "
+    ap.add_argument("--workload", default="lognormal_slab", choices=["lognormal_slab", "lognormal_injection"],
+                    help="lognormal_injection: the large continuous-injection run, whole (20 x 25 days), FP64 then MIXED; "
                          "prints its own line")
-    ap.add_argument("--config5-particles", type=int, default=100_000_000)
+    ap.add_argument("--injection-particles", type=int, default=100_000_000)
     ap.add_argument("--kde-streams", type=int, default=4,
                     help="batched leg: reconstructions run concurrently (mprw_gpkde_batch concurrency)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
@@ -103,7 +103,7 @@ def peaks():
 
 def ncu_figure(key):
     """A figure of the step kernel's committed ncu summary (per particle-step or percent)."""
-    f = ROOT / "profiles" / "rwpt_advance_kernel_config2.md"
+    f = ROOT / "profiles" / "rwpt_advance_kernel_lognormal_slab.md"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
@@ -166,7 +166,7 @@ def build_workload(n_particles, rank=0, use_torch=True):
     # the flow reaches the tracker the way a MODFLOW 6 run delivers it: written as
     # .grb/.hds/.bud and read back through the binary readers
     with tempfile.TemporaryDirectory() as d:
-        g, f, p, opt, info = W.config2(n_particles=n_particles, seed=0, use_torch=use_torch, mf6_dir=d)
+        g, f, p, opt, info = W.lognormal_slab(n_particles=n_particles, seed=0, use_torch=use_torch, mf6_dir=d)
         info = dict(info, mf6_bytes=sum(os.path.getsize(x) for x in info["mf6_files"]))
     if rank:
         # weak scaling: every rank tracks its own particle set on the same field
@@ -263,7 +263,7 @@ def run_gpu_arm(args, rank, world, local):
 
 
 def batched_run(args, flush):
-    """The ensemble (mprw.workloads.config3, the first R realizations) as ONE
+    """The ensemble (mprw.workloads.lognormal_ensemble, the first R realizations) as ONE
     batch: each step advances every realization's particles in one persistent
     launch and reconstructs every realization with GPKDE.  Timed in MIXED
     precision (FP32 advance + FP32 reconstruction) and, on the same particles
@@ -274,8 +274,8 @@ def batched_run(args, flush):
     from mprw import workloads as W
     from mprw.model import MIXED
     t_setup = time.perf_counter()
-    prm = W.config3_params(64)[: args.realizations]
-    ens, opt, _ = W.config3(members=prm, use_torch=True)
+    prm = W.ensemble_params(64)[: args.realizations]
+    ens, opt, _ = W.lognormal_ensemble(members=prm, use_torch=True)
     t_setup = time.perf_counter() - t_setup
     stream = torch.cuda.Stream()
     bins = (1.0, 1.0, 1.0)
@@ -339,7 +339,7 @@ def batched_run(args, flush):
     worst = {key: max(e[key] for e in errs) for key in ("mean_disp_x_rel", "var_x_rel", "var_y_rel", "var_z_rel")}
     v32 = mx["steps"] / (mx["ms"] / 1e3)
     v64 = fp["steps"] / (fp["ms"] / 1e3)
-    return {"workload": f"realizations 0..{len(ens) - 1} of the 64-member ensemble (config-2 generator; grids "
+    return {"workload": f"realizations 0..{len(ens) - 1} of the 64-member ensemble (the lognormal-slab generator; grids "
                         "U[100..400]x[50..200]x[10..20], sigma2 lnK U[0.5,2], alphaL U[0.1,1], alphaT = alphaL/10, "
                         "particles log-U[1e5,4e6]), one batch: one advance launch for all realizations + one "
                         f"GPKDE per realization per 10-day step ({args.kde_streams} reconstructions at a time)",
@@ -442,8 +442,8 @@ def main():
         dist.init_process_group("gloo")
     if args.impl == "reference":
         return main_reference(args, rank, world)
-    if args.workload == "config5":
-        return main_config5(args)
+    if args.workload == "lognormal_injection":
+        return main_injection(args)
     import torch
     res = run_gpu_arm(args, rank, world, local)
     fp = res["fp64"]
@@ -471,7 +471,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": max_t / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "config2: 200x100x20 lognormal-K field (sigma2 lnK 1, 10 m/2 m), FP64 CG heads, "
+        "config": {"workload": "lognormal_slab: 200x100x20 lognormal-K field (sigma2 lnK 1, 10 m/2 m), FP64 CG heads, "
                                f"{args.particles} particles from the inlet slab, step = one 10-day interval "
                                "(advance + GPKDE reconstruction on the 1 m grid, density and histogram to host)",
                    "particles_per_gpu": args.particles, "interval_days": INTERVAL_D,
@@ -523,8 +523,8 @@ def main():
     print(json.dumps(line))
 
 
-def main_config5(args):
-    """The large single run (workloads.config5): 12.5e6 cells, particles
+def main_injection(args):
+    """The large single run (workloads.lognormal_injection): 12.5e6 cells, particles
     released over 50 days, tracked to 500 days in 25-day intervals, each
     followed by a GPKDE reconstruction on the 250x250x25 grid with 5
     optimisation loops.  Run whole in FP64, then in MIXED on the same
@@ -534,7 +534,7 @@ def main_config5(args):
     from mprw import workloads as W
     from mprw.model import MIXED
     t_setup = time.perf_counter()
-    g, f, p, opt, info = W.config5(n_particles=args.config5_particles, use_torch=True)
+    g, f, p, opt, info = W.lognormal_injection(n_particles=args.injection_particles, use_torch=True)
     t_setup = time.perf_counter() - t_setup
     stream = torch.cuda.Stream()
     hbm, peak_kind = peaks()
@@ -581,7 +581,7 @@ def main_config5(args):
     line = {"metric": METRIC, "value": res["fp64"]["value"], "unit": UNIT, "n_gpus": 1, "steps": 20, "warmup": 0,
             "ms_per_step": res["fp64"]["ms_total"] / 20, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "config5: 500x500x50 lognormal-K field (sigma2 lnK 2, 20 m / 2 m), "
+            "config": {"workload": "lognormal_injection: 500x500x50 lognormal-K field (sigma2 lnK 2, 20 m / 2 m), "
                                    f"{p.n} particles released over 50 d from a 20x20x10 m source, tracked to "
                                    "500 d in 20 intervals of 25 d, each followed by GPKDE on 250x250x25 (5 loops); "
                                    "the whole run is timed (no warm-up interval)",
@@ -601,7 +601,7 @@ def main_reference(args, rank, world):
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "ms_per_step": cb["seconds"] * 1e3 / args.steps,
-            "config": {"workload": "config2 (same field and release), bounded particle sample",
+            "config": {"workload": "lognormal_slab (same field and release), bounded particle sample",
                        "particles": args.cpu_sample, "interval_days": INTERVAL_D},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -260,7 +260,7 @@ def release_in_box(grid: Grid, n: int, x0, x1, y0, y1, z0, z1, seed=1000, t0=0.0
                      id=np.arange(n, dtype=np.uint64), rng_ctr=np.zeros(n, np.uint64))
 
 
-def config1(n_particles=100_000, pure_advection=False, precision=FP64):
+def uniform_pulse(n_particles=100_000, pure_advection=False, precision=FP64):
     """200x1x1 uniform flow, v = 1 m/d, pulse at x = 10 m, Courant 0.1 (ADV)."""
     aL, aT = (0.0, 0.0) if pure_advection else (0.1, 0.01)
     g, f = uniform_flow(ncol=200, q=0.3, porosity=0.3, alpha_l=aL, alpha_t=aT, dm=0.0)
@@ -273,12 +273,12 @@ def config1(n_particles=100_000, pure_advection=False, precision=FP64):
     return g, f, p, opt
 
 
-def config2(n_particles=1_000_000, nlay=20, nrow=100, ncol=200, seed=0, precision=FP64, use_torch=None,
+def lognormal_slab(n_particles=1_000_000, nlay=20, nrow=100, ncol=200, seed=0, precision=FP64, use_torch=None,
             mf6_dir=None):
     """200x100x20 lognormal K (sigma2 1, 10 m / 2 m), 1e6 particles in the 10 m inlet slab.
 
     With ``mf6_dir`` the solved flow is written there as MODFLOW 6 binary files
-    (``config2.grb/.hds/.bud``: FLOW-JA-FACE and a CHD list) and the flow
+    (``lognormal_slab.grb/.hds/.bud``: FLOW-JA-FACE and a CHD list) and the flow
     returned is the one read back from them, as a MODFLOW 6 run would feed
     the tracker; ``info["mf6_files"]`` names the files."""
     g, f, info = heterogeneous_flow(nlay, nrow, ncol, sigma2=1.0, kg=10.0, lh=10.0, lv=2.0, porosity=0.25,
@@ -286,7 +286,7 @@ def config2(n_particles=1_000_000, nlay=20, nrow=100, ncol=200, seed=0, precisio
     if mf6_dir is not None:
         import os
         from . import mf6io
-        files = mf6io.write_flow_files(os.path.join(os.fspath(mf6_dir), "config2"), g, f, spdis=False)
+        files = mf6io.write_flow_files(os.path.join(os.fspath(mf6_dir), "lognormal_slab"), g, f, spdis=False)
         f = mf6io.flow_from_mf6(mf6io.read_grb(files[0]), mf6io.read_heads(files[1]), mf6io.read_budget(files[2]),
                                 1, 1, porosity=f.porosity, retardation=f.retardation, alpha_l=f.alpha_l,
                                 alpha_t=f.alpha_t, dm_eff=f.dm_eff, uniform_dispersion=f.uniform_dispersion)
@@ -298,7 +298,7 @@ def config2(n_particles=1_000_000, nlay=20, nrow=100, ncol=200, seed=0, precisio
     return g, f, p, opt, info
 
 
-def config3_params(n_real=64, scale=1.0):
+def ensemble_params(n_real=64, scale=1.0):
     """Per-realization draws of the ensemble: realization r draws, from
     numpy's default_rng(r), the grid (ncol in [100, 400], nrow in [50, 200],
     nlay in [10, 20], each uniform), sigma2 lnK in U[0.5, 2], alphaL in
@@ -316,13 +316,13 @@ def config3_params(n_real=64, scale=1.0):
     return out
 
 
-def config3(n_real=64, scale=1.0, precision=MIXED, use_torch=None, members=None):
-    """Ensemble of config-2-generator realizations (config3_params): per member
+def lognormal_ensemble(n_real=64, scale=1.0, precision=MIXED, use_torch=None, members=None):
+    """Ensemble of lognormal-slab-generator realizations (ensemble_params): per member
     (grid, flow, particles); field seed r, placement seed 1000 + r; particle
     ids (r << 40) + index, so every member has its own random streams and a
     separate run of the member with the same ids draws the same ones.
     ``members`` overrides the parameter list (for smaller ensembles)."""
-    params = config3_params(n_real, scale) if members is None else members
+    params = ensemble_params(n_real, scale) if members is None else members
     ens = []
     for prm in params:
         g, f, info = heterogeneous_flow(prm["nlay"], prm["nrow"], prm["ncol"], sigma2=prm["sigma2"], kg=10.0, lh=10.0,
@@ -337,10 +337,10 @@ def config3(n_real=64, scale=1.0, precision=MIXED, use_torch=None, members=None)
     return ens, opt, params
 
 
-def config5(n_particles=100_000_000, nlay=50, nrow=500, ncol=500, seed=5, precision=FP64, use_torch=None,
+def lognormal_injection(n_particles=100_000_000, nlay=50, nrow=500, ncol=500, seed=5, precision=FP64, use_torch=None,
             source=((10.0, 30.0), (240.0, 260.0), (20.0, 30.0)), release_days=50.0):
     """Large single run with continuous injection: 500x500x50 cells of 1 m,
-    ln K as config 2 with sigma2 2 and correlation lengths 20 m / 2 m, heads
+    ln K as the lognormal slab with sigma2 2 and correlation lengths 20 m / 2 m, heads
     1 m / 0 m at the x ends; n_particles released at a constant rate over
     release_days (pending particles with uniform release times) from a
     20x20x10 m source (x, y, z ranges of ``source``, model coordinates)."""

@@ -60,7 +60,7 @@ def save_case(name, p, q, steps, intervals, **extra):
 
 def flow_case():
     """The lognormal-field flow of the small heterogeneous cases, as MODFLOW 6 files."""
-    g, f, p, opt, info = W.config2(n_particles=400, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=400, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
     mf6io.write_flow_files(HERE / "hetero_small", g, f, spdis=False)
     return opt
 
@@ -74,18 +74,18 @@ def load_flow_case():
 
 
 def main():
-    # 1. config 1, pure advection: trajectories
-    g, f, p, opt = W.config1(n_particles=300, pure_advection=True)
+    # 1. the uniform column pulse, pure advection: trajectories
+    g, f, p, opt = W.uniform_pulse(n_particles=300, pure_advection=True)
     p = spread(p, 5, 40, 3)
     iv = [(0.0, 25.0), (25.0, 50.0)]
     q, s = run(g, f, opt, p, iv)
-    save_case("config1_advection", p, q, s, iv)
-    # 2. config 1 with dispersion on the shared Philox stream
-    g, f, p, opt = W.config1(n_particles=300)
+    save_case("uniform_advection", p, q, s, iv)
+    # 2. the same with dispersion on the shared Philox stream
+    g, f, p, opt = W.uniform_pulse(n_particles=300)
     p = spread(p, 5, 40, 5)
     iv = [(0.0, 10.0), (10.0, 25.0)]
     q, s = run(g, f, opt, p, iv)
-    save_case("config1_dispersion", p, q, s, iv)
+    save_case("uniform_dispersion", p, q, s, iv)
     # 3. heterogeneous field from MODFLOW 6 files, weak-sink stops
     opt = flow_case()
     g, f = load_flow_case()
@@ -104,8 +104,8 @@ def main():
     iv = [(0.0, 30.0)]
     q, s = run(g, f, opt, p, iv)
     save_case("graded_exponential", p, q, s, iv)
-    # 5. GPKDE, 1-D: config-1 plume positions after 50 days
-    g, f, p, opt = W.config1(n_particles=5000)
+    # 5. GPKDE, 1-D: the uniform column's plume after 50 days
+    g, f, p, opt = W.uniform_pulse(n_particles=5000)
     q, _ = run(g, f, opt, p, [(0.0, 50.0)])
     gx, gy, gz = O.global_xyz(g, f, q)
     act = q.status == 1

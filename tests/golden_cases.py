@@ -44,10 +44,10 @@ def case(name):
     """(grid, flow, options, particles, intervals, fixture) of a tracking case."""
     d = load(name)
     iv = [tuple(r) for r in d["intervals"]]
-    if name == "config1_advection":
-        g, f, _, opt = W.config1(n_particles=1, pure_advection=True)
-    elif name == "config1_dispersion":
-        g, f, _, opt = W.config1(n_particles=1)
+    if name == "uniform_advection":
+        g, f, _, opt = W.uniform_pulse(n_particles=1, pure_advection=True)
+    elif name == "uniform_dispersion":
+        g, f, _, opt = W.uniform_pulse(n_particles=1)
     elif name == "hetero_small":
         g, f = hetero_flow()
         opt = Options(time_step_kind=MIN_ADV_DISP, ts_param=(0.1, 0.1), advection_kind=EULERIAN,
@@ -60,4 +60,4 @@ def case(name):
     return g, f, opt, particles_in(d), iv, d
 
 
-TRACKING_CASES = ("config1_advection", "config1_dispersion", "hetero_small", "graded_exponential")
+TRACKING_CASES = ("uniform_advection", "uniform_dispersion", "hetero_small", "graded_exponential")

@@ -26,8 +26,8 @@ def _expected(n, t, nx=200, x0=10.0, v=1.0, d=0.1):
 
 
 @pytest.mark.parametrize("precision", [FP64, MIXED])
-def test_config1_concentrations_match_the_gaussian(gpu_lib, precision):
-    g, f, p, opt = W.config1(n_particles=100_000, precision=precision)
+def test_uniform_pulse_concentrations_match_the_gaussian(gpu_lib, precision):
+    g, f, p, opt = W.uniform_pulse(n_particles=100_000, precision=precision)
     tr = mprw.Tracker(g, opt)
     tr.load_flow(f)
     tr.set_particles(p)

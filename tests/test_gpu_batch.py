@@ -19,7 +19,7 @@ def _members(precision):
     """Three realizations of different sizes: two lognormal fields and a uniform column."""
     out = []
     for k, (nl, nr, nc) in enumerate(((4, 12, 30), (3, 8, 20), (5, 10, 24))):
-        g, f, p, opt, info = W.config2(n_particles=1500 + 700 * k, nlay=nl, nrow=nr, ncol=nc, seed=10 + k,
+        g, f, p, opt, info = W.lognormal_slab(n_particles=1500 + 700 * k, nlay=nl, nrow=nr, ncol=nc, seed=10 + k,
                                        precision=precision, use_torch=False)
         p.id = (np.uint64(k) << np.uint64(40)) + np.arange(p.n, dtype=np.uint64)
         out.append((g, f, p))
@@ -73,7 +73,7 @@ def test_batch_members_equal_separate_runs(gpu_lib, precision):
 def test_batch_member_against_oracle_and_without_ids(gpu_lib):
     """A member against the oracle (same ids); without ids every member draws
     the streams of its batch index, so two copies of one realization differ."""
-    g, f, p, opt, info = W.config2(n_particles=2000, nlay=4, nrow=12, ncol=30, seed=3, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=2000, nlay=4, nrow=12, ncol=30, seed=3, use_torch=False)
     u, fu = W.uniform_flow(ncol=50, q=0.3)
     pu = W.release_in_box(u, 800, 5.0, 6.0, 0.0, 1.0, 0.0, 1.0, seed=9)
     p.id = np.arange(p.n, dtype=np.uint64)
@@ -109,7 +109,7 @@ def test_batch_member_against_oracle_and_without_ids(gpu_lib):
 
 
 def test_batch_state_errors(gpu_lib):
-    g, f, p, opt, info = W.config2(n_particles=100, nlay=2, nrow=4, ncol=6, seed=0, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=100, nlay=2, nrow=4, ncol=6, seed=0, use_torch=False)
     b = mprw.Batch([g, g], opt)
     b.load_flow(0, f)
     with pytest.raises(mprw.MprwError, match="member 1"):
@@ -137,7 +137,7 @@ def test_batch_state_errors(gpu_lib):
 def test_batch_member_observations_and_empty_member(gpu_lib):
     """Observation records of a member that does not start at cell 0 equal a
     separate handle's; a member without particles is carried along."""
-    g, f, p, opt, info = W.config2(n_particles=4000, nlay=4, nrow=12, ncol=30, seed=7, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=4000, nlay=4, nrow=12, ncol=30, seed=7, use_torch=False)
     u, fu = W.uniform_flow(ncol=20, q=0.3)
     empty = W.release_in_box(u, 0, 1.0, 2.0, 0.0, 1.0, 0.0, 1.0)
     k, i, j = np.meshgrid(np.arange(g.nlay), np.arange(g.nrow), np.arange(g.ncol), indexing="ij")

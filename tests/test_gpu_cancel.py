@@ -16,7 +16,7 @@ from mprw.model import ACTIVE
 
 
 def _tracker(n=200000):
-    g, f, p, opt, info = W.config2(n_particles=n, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=n, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
     opt.stop_weak_sinks = False   # nothing stops: the advance runs to its end time
     tr = mprw.Tracker(g, opt)
     tr.load_flow(f)

@@ -14,7 +14,7 @@ from mprw.model import FP64, MIXED
 
 @pytest.mark.parametrize("precision", [FP64, MIXED])
 def test_resume_is_bit_exact(gpu_lib, tmp_path, precision):
-    g, f, p, opt, info = W.config2(n_particles=20000, nlay=4, nrow=12, ncol=30, seed=3, precision=precision,
+    g, f, p, opt, info = W.lognormal_slab(n_particles=20000, nlay=4, nrow=12, ncol=30, seed=3, precision=precision,
                                    use_torch=False)
     a = mprw.Tracker(g, opt)
     a.load_flow(f)

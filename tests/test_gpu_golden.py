@@ -33,12 +33,12 @@ def _track(g, f, opt, p, iv):
 def test_tracking_against_golden(gpu_lib, name):
     g, f, opt, p, iv, d = case(name)
     out, steps = _track(g, f, opt, p, iv)
-    if name in ("config1_advection", "graded_exponential"):
+    if name in ("uniform_advection", "graded_exponential"):
         assert steps == int(d["steps"])
         np.testing.assert_array_equal(out["cell"], d["out_cell"])
         np.testing.assert_array_equal(out["status"], d["out_status"])
         np.testing.assert_allclose(out["t"], d["out_t"], rtol=1e-12, atol=0)
-        tol = 1e-10 if name == "config1_advection" else 1e-9
+        tol = 1e-10 if name == "uniform_advection" else 1e-9
         for k in ("lx", "ly", "lz"):
             np.testing.assert_allclose(out[k], d[f"out_{k}"], rtol=tol, atol=tol)
     else:
@@ -54,7 +54,7 @@ def test_tracking_against_golden(gpu_lib, name):
 def test_gpkde_against_golden(gpu_lib, name):
     d = load(name)
     if name == "gpkde_1d":
-        g, f, _, opt = W.config1(n_particles=1)
+        g, f, _, opt = W.uniform_pulse(n_particles=1)
         kw, tol = {}, 1e-10
     else:
         g, f = hetero_flow()

@@ -18,8 +18,8 @@ def _positions(tr):
     return np.stack([out["gx"], out["gy"], out["gz"]], 1)[act]
 
 
-def test_gpkde_1d_config1(gpu_lib):
-    g, f, p, opt = W.config1(n_particles=20000)
+def test_gpkde_1d_uniform_pulse(gpu_lib):
+    g, f, p, opt = W.uniform_pulse(n_particles=20000)
     tr = mprw.Tracker(g, opt)
     tr.load_flow(f)
     tr.set_particles(p)
@@ -38,7 +38,7 @@ def test_gpkde_1d_config1(gpu_lib):
 
 
 def test_gpkde_3d_heterogeneous(gpu_lib):
-    g, f, p, opt, info = W.config2(n_particles=4000, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=4000, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
     tr = mprw.Tracker(g, opt)
     tr.load_flow(f)
     tr.set_particles(p)
@@ -54,7 +54,7 @@ def test_gpkde_3d_heterogeneous(gpu_lib):
 
 
 def test_gpkde_scaling_and_empty(gpu_lib):
-    g, f, p, opt = W.config1(n_particles=2000)
+    g, f, p, opt = W.uniform_pulse(n_particles=2000)
     tr = mprw.Tracker(g, opt)
     tr.load_flow(f)
     tr.set_particles(p)
@@ -76,10 +76,10 @@ def test_gpkde_fp32_against_fp64(gpu_lib, case):
     maximum, the mass conserved to FP32 rounding."""
     from mprw.model import MIXED
     if case == "1d":
-        g, f, p, opt = W.config1(n_particles=20000)
+        g, f, p, opt = W.uniform_pulse(n_particles=20000)
         t1, dom, lo = 50.0, (200.0, 1.0, 1.0), 10
     else:
-        g, f, p, opt, info = W.config2(n_particles=20000, nlay=6, nrow=20, ncol=40, seed=1, use_torch=False)
+        g, f, p, opt, info = W.lognormal_slab(n_particles=20000, nlay=6, nrow=20, ncol=40, seed=1, use_torch=False)
         t1, dom, lo = 30.0, (40.0, 20.0, 6.0), 10
     tr = mprw.Tracker(g, opt)
     tr.load_flow(f)

@@ -20,7 +20,7 @@ from oracle import oracle as O
 
 
 def _case():
-    g, f, p, opt, info = W.config2(n_particles=6000, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=6000, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
     opt.stop_weak_sinks = True
     rng = np.random.default_rng(4)
     p.mass = rng.uniform(0.5, 1.5, p.n)

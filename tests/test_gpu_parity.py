@@ -60,7 +60,7 @@ INTERVALS = [(0.0, 25.0), (25.0, 50.0), (50.0, 100.0)]
 
 
 def test_pure_advection_trajectories(gpu_lib):
-    g, f, p, opt = W.config1(n_particles=3000, pure_advection=True)
+    g, f, p, opt = W.uniform_pulse(n_particles=3000, pure_advection=True)
     p = spread_start(p, g)
     gp, gs = run_gpu(g, f, opt, p, INTERVALS)
     op, os_ = run_oracle(g, f, opt, p, INTERVALS)
@@ -86,7 +86,7 @@ def _compare_same_rng(gp, op, g, f, tol=1e-6, min_frac=0.999):
 
 
 def test_dispersion_shared_rng_uniform(gpu_lib):
-    g, f, p, opt = W.config1(n_particles=4000)
+    g, f, p, opt = W.uniform_pulse(n_particles=4000)
     p = spread_start(p, g, seed=5)
     iv = [(0.0, 10.0), (10.0, 25.0)]
     gp, gs = run_gpu(g, f, opt, p, iv)
@@ -98,7 +98,7 @@ def test_dispersion_shared_rng_uniform(gpu_lib):
 def test_dispersion_shared_rng_plume_moments_100d(gpu_lib):
     """Over 100 days individual trajectories may drift apart by more than 1e-6
     (rounding amplified by reflections), but the plume is the same plume."""
-    g, f, p, opt = W.config1(n_particles=4000)
+    g, f, p, opt = W.uniform_pulse(n_particles=4000)
     p = spread_start(p, g, seed=5)
     gp, gs = run_gpu(g, f, opt, p, INTERVALS)
     op, os_ = run_oracle(g, f, opt, p, INTERVALS)
@@ -114,7 +114,7 @@ def test_dispersion_shared_rng_plume_moments_100d(gpu_lib):
 
 @pytest.mark.parametrize("seed", [0, 1])
 def test_dispersion_shared_rng_heterogeneous(gpu_lib, seed):
-    g, f, p, opt, info = W.config2(n_particles=3000, nlay=4, nrow=12, ncol=30, seed=seed, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=3000, nlay=4, nrow=12, ncol=30, seed=seed, use_torch=False)
     iv = [(0.0, 20.0), (20.0, 60.0)]
     gp, gs = run_gpu(g, f, opt, p, iv)
     op, os_ = run_oracle(g, f, opt, p, iv)
@@ -129,8 +129,8 @@ def test_heterogeneous_flow_read_from_mf6_files(gpu_lib, tmp_path):
     """The lognormal-field flow written as MODFLOW 6 .grb/.hds/.bud and read
     back (all-zero boundary faces and ICELLTYPE arrays instead of absent ones)
     tracks on the GPU like the oracle does on the solver's own arrays."""
-    g, f, p, opt, info = W.config2(n_particles=3000, nlay=4, nrow=12, ncol=30, seed=2, use_torch=False)
-    _, f6, _, _, info6 = W.config2(n_particles=10, nlay=4, nrow=12, ncol=30, seed=2, use_torch=False,
+    g, f, p, opt, info = W.lognormal_slab(n_particles=3000, nlay=4, nrow=12, ncol=30, seed=2, use_torch=False)
+    _, f6, _, _, info6 = W.lognormal_slab(n_particles=10, nlay=4, nrow=12, ncol=30, seed=2, use_torch=False,
                                    mf6_dir=tmp_path)
     assert f6.boundary_flows is not None and f6.celltype is not None
     iv = [(0.0, 20.0), (20.0, 60.0)]
@@ -140,7 +140,7 @@ def test_heterogeneous_flow_read_from_mf6_files(gpu_lib, tmp_path):
 
 
 def test_histogram_bit_exact(gpu_lib):
-    g, f, p, opt = W.config1(n_particles=20000)
+    g, f, p, opt = W.uniform_pulse(n_particles=20000)
     tr = mprw.Tracker(g, opt)
     tr.load_flow(f)
     tr.set_particles(p)
@@ -164,7 +164,7 @@ def test_histogram_bit_exact(gpu_lib):
 
 
 def test_histogram_weighted_ordered(gpu_lib):
-    g, f, p, opt = W.config1(n_particles=5000)
+    g, f, p, opt = W.uniform_pulse(n_particles=5000)
     rng = np.random.default_rng(9)
     p.mass = rng.uniform(0.1, 2.0, p.n)
     tr = mprw.Tracker(g, opt)
@@ -182,7 +182,7 @@ def test_histogram_weighted_ordered(gpu_lib):
 
 
 def test_mixed_precision_moments(gpu_lib):
-    g, f, p, opt = W.config1(n_particles=50000)
+    g, f, p, opt = W.uniform_pulse(n_particles=50000)
     iv = [(0.0, 50.0), (50.0, 100.0)]
     gp, _ = run_gpu(g, f, opt, p, iv)
     opt.precision = MIXED
@@ -243,7 +243,7 @@ def test_exponential_advection_graded_field(gpu_lib):
 
 def test_exponential_dispersion_heterogeneous(gpu_lib):
     from mprw.model import EXPONENTIAL
-    g, f, p, opt, info = W.config2(n_particles=3000, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=3000, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
     opt.advection_kind = EXPONENTIAL
     iv = [(0.0, 20.0), (20.0, 60.0)]
     gp, gs = run_gpu(g, f, opt, p, iv)
@@ -258,7 +258,7 @@ def test_axisymmetric_dispersion_heterogeneous(gpu_lib, advection):
     TrackSubCell.F90:3117-3303, 750-806, 3306-3604) against the oracle on the
     shared random stream."""
     from mprw.model import EXPONENTIAL
-    g, f, p, opt, info = W.config2(n_particles=3000, nlay=4, nrow=12, ncol=30, seed=1, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=3000, nlay=4, nrow=12, ncol=30, seed=1, use_torch=False)
     f.alpha_lv = np.array([0.2])
     f.alpha_tv = np.array([0.01])
     opt.dispersion_model = 1

@@ -17,7 +17,7 @@ def _state(tr):
 
 @pytest.mark.parametrize("precision", [FP64, MIXED])
 def test_autotune_is_invisible_to_results(gpu_lib, precision):
-    g, f, p, opt, info = W.config2(n_particles=20000, nlay=4, nrow=12, ncol=30, seed=5, precision=precision,
+    g, f, p, opt, info = W.lognormal_slab(n_particles=20000, nlay=4, nrow=12, ncol=30, seed=5, precision=precision,
                                    use_torch=False)
     ref = mprw.Tracker(g, opt)
     ref.load_flow(f)
@@ -57,7 +57,7 @@ def test_autotune_is_invisible_to_results(gpu_lib, precision):
 
 
 def test_autotune_on_a_batch(gpu_lib):
-    g, f, p, opt, info = W.config2(n_particles=5000, nlay=3, nrow=8, ncol=20, seed=6, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=5000, nlay=3, nrow=8, ncol=20, seed=6, use_torch=False)
     u, fu = W.uniform_flow(ncol=40, q=0.3)
     pu = W.release_in_box(u, 3000, 2.0, 3.0, 0.0, 1.0, 0.0, 1.0, seed=2)
     b = mprw.Batch([g, u], opt)

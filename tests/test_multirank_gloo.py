@@ -21,7 +21,7 @@ def _free_port():
 
 def _workload():
     from mprw import workloads as W
-    return W.config2(n_particles=900, nlay=3, nrow=8, ncol=20, seed=5, use_torch=False)
+    return W.lognormal_slab(n_particles=900, nlay=3, nrow=8, ncol=20, seed=5, use_torch=False)
 
 
 HIST = ((0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (20, 8, 3))

@@ -4,7 +4,7 @@
   TrackSubCell.F90:2557-2691, 4016-4138);
 * pure advection is exact: a particle moves v*t and sits on cell faces
   exactly (ConvertFromNeighbor, RectangularGridDisMf6.f90:50-108);
-* the plume of config 1 against the analytic 1-D Gaussian ADE solution,
+* the uniform-column pulse against the analytic 1-D Gaussian ADE solution,
   with the tolerance the reference's interface-forcing scheme needs;
 * release / status logic of the driver (MPathRW.F90:1256-1302);
 * counter-based streams make results independent of the thread count.
@@ -18,7 +18,7 @@ from oracle import oracle as O
 
 
 def test_uniform_flow_cell_record():
-    g, f, p, opt = W.config1(n_particles=1)
+    g, f, p, opt = W.uniform_pulse(n_particles=1)
     r = O.cell_record(g, f, opt, 50)
     np.testing.assert_allclose(r["vface"], [1, 1, 0, 0, 0, 0], rtol=0, atol=1e-15)
     assert r["dtcell"] == pytest.approx(0.1, rel=1e-15)
@@ -35,7 +35,7 @@ def test_uniform_flow_cell_record():
 
 
 def test_pure_advection_exact():
-    g, f, p, opt = W.config1(n_particles=3, pure_advection=True)
+    g, f, p, opt = W.uniform_pulse(n_particles=3, pure_advection=True)
     p.lx[:] = [0.0, 0.25, 0.5]
     q, steps = O.advance(g, f, opt, p, 0.0, 25.0)
     gx, gy, gz = O.global_xyz(g, f, q)
@@ -46,9 +46,9 @@ def test_pure_advection_exact():
     assert steps >= 3 * 250
 
 
-def test_analytic_gaussian_config1():
+def test_analytic_gaussian_uniform_pulse():
     n = 6000
-    g, f, p, opt = W.config1(n_particles=n)
+    g, f, p, opt = W.uniform_pulse(n_particles=n)
     q, _ = O.advance(g, f, opt, p, 0.0, 50.0, rng_kind=O.RNG_PHILOX, nthreads=8)
     gx, _, _ = O.global_xyz(g, f, q)
     mean, var = 10.0 + 50.0, 2.0 * 0.1 * 1.0 * 50.0
@@ -59,7 +59,7 @@ def test_analytic_gaussian_config1():
 
 
 def test_release_and_status_logic():
-    g, f, p, opt = W.config1(n_particles=4, pure_advection=True)
+    g, f, p, opt = W.uniform_pulse(n_particles=4, pure_advection=True)
     p.t[:] = [0.0, 5.0, 50.0, -1.0]      # released now, later in interval, after, before interval
     p.status[:] = PENDING
     q, _ = O.advance(g, f, opt, p, 0.0, 10.0)
@@ -74,13 +74,13 @@ def test_release_and_status_logic():
 
 
 def test_empty_particle_set():
-    g, f, p, opt = W.config1(n_particles=0)
+    g, f, p, opt = W.uniform_pulse(n_particles=0)
     q, steps = O.advance(g, f, opt, p, 0.0, 10.0)
     assert q.n == 0 and steps == 0
 
 
 def test_thread_count_invariance_with_counter_based_rng():
-    g, f, p, opt, _ = W.config2(n_particles=400, nlay=3, nrow=8, ncol=20, seed=2, use_torch=False)
+    g, f, p, opt, _ = W.lognormal_slab(n_particles=400, nlay=3, nrow=8, ncol=20, seed=2, use_torch=False)
     a, sa = O.advance(g, f, opt, p, 0.0, 30.0, rng_kind=O.RNG_PHILOX, nthreads=1)
     b, sb = O.advance(g, f, opt, p, 0.0, 30.0, rng_kind=O.RNG_PHILOX, nthreads=8)
     assert sa == sb
@@ -90,7 +90,7 @@ def test_thread_count_invariance_with_counter_based_rng():
 
 
 def test_heterogeneous_weak_sink_stops():
-    g, f, p, opt, info = W.config2(n_particles=600, nlay=3, nrow=8, ncol=20, seed=1, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=600, nlay=3, nrow=8, ncol=20, seed=1, use_torch=False)
     q, _ = O.advance(g, f, opt, p, 0.0, 200.0, rng_kind=O.RNG_PHILOX, nthreads=8)
     counts = np.bincount(q.status, minlength=10)
     assert counts[WEAK_SINK] > 0

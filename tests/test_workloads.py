@@ -42,7 +42,7 @@ def test_lognormal_field_statistics():
 
 
 def test_release_box_maps_to_model_coordinates():
-    g, f, p, opt, info = W.config2(n_particles=2000, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
+    g, f, p, opt, info = W.lognormal_slab(n_particles=2000, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
     gx, gy, gz = O.global_xyz(g, f, p)
     assert gx.min() >= 0.0 and gx.max() <= 10.0
     assert gy.min() >= 0.0 and gy.max() <= 12.0

@@ -60,7 +60,7 @@ def _device_particles(out):
 
 def test_noalloc_histogram_matches_histogram(gpu_lib):
     fn = _bind(gpu_lib)
-    g, f, p, opt = W.config1(n_particles=20000)
+    g, f, p, opt = W.uniform_pulse(n_particles=20000)
     tr = mprw.Tracker(g, opt)
     tr.load_flow(f)
     tr.set_particles(p)
