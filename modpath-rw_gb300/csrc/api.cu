@@ -431,8 +431,27 @@ int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *f) {
   if (f->nja < nc || f->ia[0] != 1 || f->ia[nc] - 1 != f->nja)
     return fail(h, MPRW_E_INVAL, "mprw_load_flow: IA/JA inconsistent with the grid");
   for (int64_t c = 0; c < nc; ++c) {
-    if (f->porosity[c] <= 0.0 || f->retardation[c] <= 0.0)
-      return fail(h, MPRW_E_INVAL, "mprw_load_flow: porosity and retardation must be > 0");
+    if (!(f->porosity[c] > 0.0) || !(f->retardation[c] > 0.0) || !std::isfinite(f->porosity[c]) ||
+        !std::isfinite(f->retardation[c]))
+      return fail(h, MPRW_E_INVAL, "mprw_load_flow: porosity and retardation must be finite and > 0");
+  }
+  // non-finite inputs: the reference runs with -ffpe-trap=invalid and stops on
+  // the first NaN; a library call rejects them before any device work
+  {
+    auto finite = [](const double *a, int64_t n) {
+      if (!a) return true;
+      for (int64_t i = 0; i < n; ++i)
+        if (!std::isfinite(a[i])) return false;
+      return true;
+    };
+    const int64_t nd = f->uniform_dispersion ? 1 : nc;
+    if (!finite(f->flowja, f->nja) || !finite(f->boundary_flows, 6 * nc) || !finite(f->source_flow, nc) ||
+        !finite(f->sink_flow, nc) || !finite(f->alpha_l, nd) || !finite(f->alpha_t, nd) ||
+        !finite(f->dm_eff, nd) || !finite(f->alpha_lv, nd) || !finite(f->alpha_tv, nd))
+      return fail(h, MPRW_E_INVAL, "mprw_load_flow: non-finite face flow, boundary flow, source/sink or dispersion value");
+    if (f->heads)
+      for (int64_t c = 0; c < nc; ++c)
+        if (std::isnan(f->heads[c])) return fail(h, MPRW_E_INVAL, "mprw_load_flow: NaN head");
   }
   for (int64_t p = 0; p < f->nja; ++p)
     if (f->ja[p] < 1 || f->ja[p] > nc) return fail(h, MPRW_E_INVAL, "mprw_load_flow: JA entry out of range");

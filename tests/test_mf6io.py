@@ -226,3 +226,23 @@ def test_flow_files_round_trip_iface_boundaries(tmp_path):
     np.testing.assert_array_equal(r.boundary_flows, f.boundary_flows)
     np.testing.assert_array_equal(r.flowja, f.flowja)
     assert not r.source_flow.any() and not r.sink_flow.any()
+
+
+def test_truncated_and_corrupt_files_are_rejected(tmp_path, hetero):
+    g, f = hetero
+    M.write_flow_files(tmp_path / "t", g, f)
+    raw = (tmp_path / "t.bud").read_bytes()
+    (tmp_path / "cut.bud").write_bytes(raw[: len(raw) - 100])
+    with pytest.raises(ValueError):
+        M.read_budget(tmp_path / "cut.bud")
+    raw = (tmp_path / "t.hds").read_bytes()
+    (tmp_path / "cut.hds").write_bytes(raw[: len(raw) // 2 + 3])
+    with pytest.raises(ValueError):
+        M.read_heads(tmp_path / "cut.hds")
+    raw = (tmp_path / "t.grb").read_bytes()
+    (tmp_path / "cut.grb").write_bytes(raw[: len(raw) - 8])
+    with pytest.raises(ValueError):
+        M.read_grb(tmp_path / "cut.grb")
+    (tmp_path / "junk.bud").write_bytes(b"\x07" * 4096)
+    with pytest.raises(ValueError):
+        M.read_budget(tmp_path / "junk.bud")
