@@ -136,5 +136,16 @@ enum : int32_t {
 // Safety cap on time-loop passes in one cell visit: a pathological record
 // (for example a NaN time step) ends as status 9 instead of spinning.
 constexpr int64_t kMaxStepsPerVisit = 1000000;
+// Safety cap on consecutive cell exits that take no time: a particle sitting
+// on a face where the flow turns back (possible when the random walk is
+// restricted to fewer dimensions than the flow) can cross back and forth at
+// the same instant forever -- the reference's cell loop has no cap.  Past this
+// many such exits the particle ends as status 9.
+constexpr int kMaxZeroTimeExits = 1000;
+// ... and on the cell visits of one particle in one advance call, so that no
+// lane can keep crossing faces for ever (a particle crosses about one cell
+// per Courant-limited handful of steps; a million visits in one tracking
+// interval is far beyond any physical path).
+constexpr int64_t kMaxVisitsPerAdvance = 1000000;
 
 }  // namespace mprw

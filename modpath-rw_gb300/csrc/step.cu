@@ -733,6 +733,8 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
   V.passes = 0;
   uint32_t massb = 0;
   int32_t conn6[6] = {-1, -1, -1, -1, -1, -1};
+  int zero_exits = 0;  // consecutive cell exits without time advancing
+  int64_t visits = 0;  // cell exits of the current particle in this launch
 
   unsigned iter = 0;
   for (;;) {
@@ -794,6 +796,8 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
             ctr = a.ctr[p];
             lc = c; lx = ex; ly = ey; lz = ez; lt = et;
             need_cell = true;
+            zero_exits = 0;
+            visits = 0;
           }
         }
       }
@@ -859,6 +863,12 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
         a.ctr[p] = ctr;
         p = -1;
       } else if (r == PASS_UNDEFINED) {
+        a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
+        a.status[p] = ST_UNDEFINED;
+        a.ctr[p] = ctr;
+        p = -1;
+      } else if (r == PASS_EXIT && ((zero_exits = (V.t == V.tinit) ? zero_exits + 1 : 0) > kMaxZeroTimeExits ||
+                                    ++visits > kMaxVisitsPerAdvance)) {
         a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
         a.status[p] = ST_UNDEFINED;
         a.ctr[p] = ctr;

@@ -1018,6 +1018,8 @@ static double rw_time_step(const subcell_t *s, const orc_options *o) {
 enum { SC_UNDEFINED = 0, SC_EXIT_CELL_FACE, SC_EXIT_INTERNAL, SC_MAXTIME, SC_NO_EXIT, SC_INACTIVE };
 
 #define ORC_MAX_PASSES_PER_VISIT 1000000
+#define ORC_MAX_ZERO_TIME_EXITS 1000 /* the GPU kernel's kMaxZeroTimeExits */
+#define ORC_MAX_VISITS 1000000        /* the GPU kernel's kMaxVisitsPerAdvance */
 
 typedef struct {
   int status, exitFace, conn;
@@ -1269,6 +1271,8 @@ static int track_path(const grid_t *g, const orc_options *o, const int *dims, in
                       double maximumTime, rng_t *rng, loc_t *out, int64_t *steps) {
   const orc_flow *f = g->f;
   loc_t last = loc; /* last point in LocBuffP */
+  int zero_time_exits = 0; /* consecutive cell exits that took no time (shared cap with the GPU kernel) */
+  int64_t visits = 0;      /* cell exits in this call (shared cap with the GPU kernel) */
   for (;;) {
     int n = loc.cell;
     cdata c;
@@ -1315,6 +1319,10 @@ static int track_path(const grid_t *g, const orc_options *o, const int *dims, in
       case SC_INACTIVE: *out = loc; return ORC_INACTIVE;
       case SC_NO_EXIT: *out = loc; return ORC_NO_EXIT;
       case SC_EXIT_CELL_FACE: {
+        /* a particle that keeps crossing faces without time advancing would loop
+         * forever (the reference has no cap on its cell loop): end it as undefined */
+        zero_time_exits = (r.t == loc.t) ? zero_time_exits + 1 : 0;
+        if (zero_time_exits > ORC_MAX_ZERO_TIME_EXITS || ++visits > ORC_MAX_VISITS) { *out = last; return ORC_UNDEFINED; }
         last.cell = n; last.x = r.x; last.y = r.y; last.z = r.z; last.t = r.t;
         int next = r.conn;
         if (next > 0 && f->iboundts[next - 1] != 0) {
