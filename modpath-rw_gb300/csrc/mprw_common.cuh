@@ -146,6 +146,6 @@ constexpr int kMaxZeroTimeExits = 1000;
 // lane can keep crossing faces for ever (a particle crosses about one cell
 // per Courant-limited handful of steps; a million visits in one tracking
 // interval is far beyond any physical path).
-constexpr int64_t kMaxVisitsPerAdvance = 1000000;
+constexpr int kMaxVisitsPerAdvance = 1000000;
 
 }  // namespace mprw

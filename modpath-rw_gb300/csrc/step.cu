@@ -733,8 +733,10 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
   V.passes = 0;
   uint32_t massb = 0;
   int32_t conn6[6] = {-1, -1, -1, -1, -1, -1};
-  int zero_exits = 0;  // consecutive cell exits without time advancing
-  int64_t visits = 0;  // cell exits of the current particle in this launch
+  // cell exits of the current particle in this launch (bits 0-19) and how
+  // many of the last ones took no time (bits 20-30): one register for both caps
+  static_assert(kMaxVisitsPerAdvance < (1 << 20) - 1 && kMaxZeroTimeExits < (1 << 11) - 1, "exit counter bits");
+  uint32_t exits = 0;
 
   unsigned iter = 0;
   for (;;) {
@@ -796,8 +798,7 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
             ctr = a.ctr[p];
             lc = c; lx = ex; ly = ey; lz = ez; lt = et;
             need_cell = true;
-            zero_exits = 0;
-            visits = 0;
+            exits = 0;
           }
         }
       }
@@ -867,8 +868,10 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
         a.status[p] = ST_UNDEFINED;
         a.ctr[p] = ctr;
         p = -1;
-      } else if (r == PASS_EXIT && ((zero_exits = (V.t == V.tinit) ? zero_exits + 1 : 0) > kMaxZeroTimeExits ||
-                                    ++visits > kMaxVisitsPerAdvance)) {
+      } else if (r == PASS_EXIT &&
+                 ((exits = ((exits & 0xFFFFFu) + 1u) | ((V.t == V.tinit) ? ((exits >> 20) + 1u) << 20 : 0u)) >> 20 >
+                      (uint32_t)kMaxZeroTimeExits ||
+                  (exits & 0xFFFFFu) > (uint32_t)kMaxVisitsPerAdvance)) {
         a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
         a.status[p] = ST_UNDEFINED;
         a.ctr[p] = ctr;
