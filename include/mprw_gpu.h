@@ -52,6 +52,7 @@ extern "C" {
 #define MPRW_E_OOM -3     /* device allocation failed                        */
 #define MPRW_E_STATE -4   /* call out of order (e.g. advance before flow)    */
 #define MPRW_E_ABORTED -5 /* a kernel hit its iteration cap and set an error */
+#define MPRW_E_SIZE -6    /* an output buffer is too small; the size needed is returned */
 
 #define MPRW_FP64 0  /* positions, velocities, dispersion all in FP64        */
 #define MPRW_MIXED 1 /* int32 cell + FP32 local coordinates and arithmetic,  */
@@ -206,6 +207,75 @@ int mprw_observe_resident(mprw_handle *h, int64_t *count, double *mass);
  * capacity records are copied; n_records receives how many there are. */
 int mprw_observe_sinks(mprw_handle *h, int64_t capacity, int32_t *obs, uint64_t *id, double *time,
                        double *mass, int64_t *n_records);
+
+/* 1-D GPKDE of an observation time series (breakthrough curve): the
+ * reconstruction the observation post-process runs on the record times of
+ * one solute (MPathRW.F90:1773-2000 resident, 2000-2840 sink observations),
+ * i.e. GridProjectedKDE%Initialize with a 1-D domain and
+ * databaseOptimization = .false. followed by ComputeDensity with weights
+ * (GridProjectedKDE.F90:354-998, 3598-4392; Histogram.F90:276-720).  Every
+ * kernel is set up from its bin's exact smoothing.
+ *
+ * times[n], weights[n] are HOST arrays (the record times and the weights the
+ * driver gives them: mass / retardation for resident records, mass / |Q| for
+ * sink records).  counts[capacity] receives the histogram the driver reads
+ * (Histogram%counts), wcounts[capacity] (may be NULL) the weighted counts of
+ * effective-weight formats 2 and 3 (zeros otherwise), density[capacity] (may
+ * be NULL) the reconstruction (densityEstimateGrid; zeros for a histogram
+ * only), all after the reference's closing scalings.  res receives the grid
+ * actually used: n_bins, the first bin's offset in the domain grid
+ * (deltaBinsOrigin; bin m's centre is (m + delta_bins_origin - 1/2) *
+ * bin_size + origin), the bin size (estimated for bin formats 0 and 1), the
+ * histogram origin, the optimisation loops run and the active bins.  When
+ * n_bins > capacity nothing is reconstructed and MPRW_E_SIZE is returned
+ * with res filled: call again with a larger buffer.
+ *
+ * Inputs the reference stops on return MPRW_E_INVAL: no points, non-finite
+ * times or weights, a bin size that is not positive (a Scott or
+ * Freedman-Diaconis estimate of identical times), a grid of fewer than two
+ * bins, a sub-grid larger than the domain grid, a net roughness that is zero
+ * everywhere.  Freedman-Diaconis needs two points (the reference reads
+ * element 0 of the sorted array for one).  Grids of more than 2^20 bins and
+ * an initial smoothing whose support spans more than 2^20 bins are refused.
+ * The work runs on `stream` (a cudaStream_t, NULL = the default stream); the
+ * call returns when the results are on the host. */
+typedef struct {
+  double origin;               /* domainOrigin(1), 0 for times                  */
+  double domain_size;          /* domainSize(1); 0 with adapt_grid: from data  */
+  double bin_size;             /* binSize(1) for bin_format 2 and 3            */
+  int32_t bin_format;          /* histogramBinFormat: 0 Scott, 1 Freedman-     */
+                               /* Diaconis, 2/3 the given bin_size             */
+  double bin_size_fraction;    /* binSizeFraction (formats 0, 1), in (0, 2]    */
+  int32_t adapt_grid;          /* adaptGridToCoords                            */
+  int32_t exact_point;         /* exactPoint (resident records: a time on a    */
+                               /* bin boundary opens that bin)                 */
+  int32_t effective_weight_format; /* 0 Kish, 1 mean weight, 2 counts and     */
+                               /* weights, 3 effective counts and weights      */
+  int32_t initial_smoothing_selection; /* 0 Silverman, 1 factor * bin size, */
+                               /* 2 twice the bin size                         */
+  double initial_smoothing_factor; /* initialSmoothingFactor                   */
+  int32_t apply_initial_factor; /* selection 0: the factor scales Silverman's  */
+                               /* estimate (applyInitialSmoothingFactor)       */
+  int32_t n_opt_loops;         /* nOptimizationLoops                           */
+  double rel_err_convergence;  /* relativeErrorConvergence                     */
+  int32_t skip_error_convergence;
+  int32_t only_histogram;      /* onlyHistogram                                */
+  int32_t compute_raw_density; /* computeRawDensity: histogram / bin size      */
+  int32_t unit_volume;         /* unitVolume: density * bin size               */
+} mprw_series_options;
+
+typedef struct {
+  int32_t n_bins;
+  int32_t delta_bins_origin;
+  double bin_size;
+  double grid_origin;
+  int32_t loops_done;
+  int32_t active_bins;
+} mprw_series_result;
+
+int mprw_gpkde_series(const double *times, const double *weights, int64_t n, const mprw_series_options *opt,
+                      int32_t capacity, double *counts, double *wcounts, double *density,
+                      mprw_series_result *res, void *stream);
 
 /* Allocation-free unit-mass histogram.  No counterpart in the reference: it
  * exists for callers that cannot allocate device memory when they bin -- a

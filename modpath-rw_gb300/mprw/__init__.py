@@ -61,6 +61,21 @@ class GpkdeOptions(C.Structure):
                 ("precision", C.c_int32)]
 
 
+class SeriesOptions(C.Structure):
+    _fields_ = [("origin", C.c_double), ("domain_size", C.c_double), ("bin_size", C.c_double),
+                ("bin_format", C.c_int32), ("bin_size_fraction", C.c_double), ("adapt_grid", C.c_int32),
+                ("exact_point", C.c_int32), ("effective_weight_format", C.c_int32),
+                ("initial_smoothing_selection", C.c_int32), ("initial_smoothing_factor", C.c_double),
+                ("apply_initial_factor", C.c_int32), ("n_opt_loops", C.c_int32), ("rel_err_convergence", C.c_double),
+                ("skip_error_convergence", C.c_int32), ("only_histogram", C.c_int32),
+                ("compute_raw_density", C.c_int32), ("unit_volume", C.c_int32)]
+
+
+class SeriesResult(C.Structure):
+    _fields_ = [("n_bins", C.c_int32), ("delta_bins_origin", C.c_int32), ("bin_size", C.c_double),
+                ("grid_origin", C.c_double), ("loops_done", C.c_int32), ("active_bins", C.c_int32)]
+
+
 class FlowDesc(C.Structure):
     _fields_ = [("ia", _ip), ("ja", _ip), ("nja", C.c_int64), ("flowja", _dp), ("boundary_flows", _dp),
                 ("porosity", _dp), ("retardation", _dp), ("iboundts", _ip), ("icboundts", _ip),
@@ -108,6 +123,8 @@ def load_library() -> C.CDLL:
         "mprw_get_tuning": (C.c_int, [H, _ip, _ip, _ip]),
         "mprw_autotune": (C.c_int, [H, C.c_double, C.c_double, _ip, _ip, _dp]),
         "mprw_last_error": (C.c_char_p, [H]),
+        "mprw_gpkde_series": (C.c_int, [_dp, _dp, C.c_int64, C.POINTER(SeriesOptions), C.c_int32, _dp, _dp, _dp,
+                                        C.POINTER(SeriesResult), C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -548,3 +565,51 @@ class Batch:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def gpkde_series(times, weights, *, origin=0.0, domain_size=0.0, bin_size=0.0, bin_format=2, bin_size_fraction=1.0,
+                 adapt_grid=False, exact_point=False, eff_format=0, init_selection=0, init_factor=2.0,
+                 apply_init_factor=False, n_opt_loops=10, rel_err=0.02, skip_error=False, only_histogram=False,
+                 raw_density=False, unit_volume=False, stream=None) -> dict:
+    """1-D GPKDE of a weighted time series on the GPU (``mprw_gpkde_series``):
+    GridProjectedKDE with a 1-D domain and the kernel database off, as the
+    observation post-process runs it (MPathRW.F90:1773-2840).
+
+    Returns a dict with ``counts``, ``wcounts`` (effective-weight formats 2
+    and 3, else None), ``density`` (None for a histogram only), ``n_bins``,
+    ``delta_bins_origin``, ``bin_size``, ``grid_origin``, ``coordinates``
+    (bin centres), ``loops`` and ``active_bins``."""
+    lib = load_library()
+    t = _f64(times).ravel()
+    w = _f64(weights).ravel()
+    if t.shape != w.shape:
+        raise ValueError("times and weights differ in length")
+    o = SeriesOptions(origin=float(origin), domain_size=float(domain_size), bin_size=float(bin_size),
+                      bin_format=int(bin_format), bin_size_fraction=float(bin_size_fraction),
+                      adapt_grid=int(bool(adapt_grid)), exact_point=int(bool(exact_point)),
+                      effective_weight_format=int(eff_format), initial_smoothing_selection=int(init_selection),
+                      initial_smoothing_factor=float(init_factor), apply_initial_factor=int(bool(apply_init_factor)),
+                      n_opt_loops=int(n_opt_loops), rel_err_convergence=float(rel_err),
+                      skip_error_convergence=int(bool(skip_error)), only_histogram=int(bool(only_histogram)),
+                      compute_raw_density=int(bool(raw_density)), unit_volume=int(bool(unit_volume)))
+    res = SeriesResult()
+    cap = 1024
+    while True:
+        counts = np.zeros(cap)
+        wcounts = np.zeros(cap)
+        dens = np.zeros(cap)
+        rc = lib.mprw_gpkde_series(_p(t, _dp), _p(w, _dp), t.shape[0], C.byref(o), cap, _p(counts, _dp),
+                                   _p(wcounts, _dp), _p(dens, _dp), C.byref(res), stream)
+        if rc == -6 and res.n_bins > cap:
+            cap = int(res.n_bins)
+            continue
+        if rc != 0:
+            raise MprwError(f"mprw_gpkde_series: rc={rc}")
+        break
+    nb = int(res.n_bins)
+    coords = (np.arange(1, nb + 1, dtype=np.float64) + res.delta_bins_origin - 0.5) * res.bin_size + float(origin)
+    return dict(counts=counts[:nb].copy(), wcounts=wcounts[:nb].copy() if eff_format in (2, 3) else None,
+                density=None if only_histogram else dens[:nb].copy(), n_bins=nb,
+                delta_bins_origin=int(res.delta_bins_origin), bin_size=float(res.bin_size),
+                grid_origin=float(res.grid_origin), coordinates=coords, loops=int(res.loops_done),
+                active_bins=int(res.active_bins))

@@ -17,10 +17,12 @@ Reference quirks kept: the second-derivative kernels are never rescaled
 `if (...) matrix = 0; return` line returns unconditionally before the scaling,
 KernelMultiGaussian.f90:865-887, 969-993, 1071-1097); the 3-D shape
 normalisation uses the single-precision exponent 0.333 (GridProjectedKDE.F90:5654).
-Only the default options MODPATH-RW uses are restated: kernel database on
-(logarithmic), bounded kernel sizes (format 0), minimum-roughness format 3,
-effective-weight format 0 (Kish), not isotropic, no sliced reconstruction,
-grid fixed to the domain.  ``np.add.at`` accumulates repeated indices in
+The options MODPATH-RW uses are restated: for the spatial reconstruction the
+kernel database on (logarithmic), bounded kernel sizes (format 0),
+minimum-roughness format 3, effective-weight format 0 (Kish), not isotropic,
+no sliced reconstruction, grid fixed to the domain; for the observation time
+series (``series_oracle.py``) the database off and the grid optionally
+adapted to the data.  ``np.add.at`` accumulates repeated indices in
 array order, the reference's loop order.
 """
 from __future__ import annotations
@@ -202,7 +204,14 @@ def _rev(start, stop):
 # --------------------------------------------------------------------------
 class GPKDE:
     def __init__(self, domain_size, bin_size, origin=(0.0, 0.0, 0.0), n_opt_loops=10, min_hod=0.3,
-                 delta_hod=0.3, max_hod=15.0, rel_err=0.02, skip_error=False, isotropic=False):
+                 delta_hod=0.3, max_hod=15.0, rel_err=0.02, skip_error=False, isotropic=False, database=True,
+                 n_bins=None):
+        """``database=False`` sets every kernel up from its exact smoothing
+        (prSetKernelBrute / prSetKernelSigmaBrute / prSetKernelSD1DBrute,
+        GridProjectedKDE.F90:6224-6317) instead of the database entry.
+        ``n_bins`` overrides the reconstruction grid (a sub-grid adapted to the
+        data, :3903-3960); the kernel-size bounds keep following the domain
+        grid size (:1296-1310)."""
         self.domain_size = np.asarray(domain_size, np.float64)
         self.bin_size = np.asarray(bin_size, np.float64)
         self.origin = np.asarray(origin, np.float64)
@@ -210,7 +219,8 @@ class GPKDE:
         for d in range(3):
             if self.bin_size[d] != 0.0:
                 gs[d] = int(self.domain_size[d] / self.bin_size[d] + 0.5)
-        self.nbins = gs
+        self.nbins = gs if n_bins is None else np.asarray(n_bins, np.int64)
+        self.database = database
         self.mask = np.array([0 if gs[d] == 1 else 1 for d in range(3)])
         self.ndim = int(self.mask.sum())
         self.dims = [d for d in range(3) if self.mask[d]]
@@ -345,12 +355,26 @@ class GPKDE:
             if check_negative and np.any(s < 0.0):
                 continue
             gid = act[n]
-            gsl, k = self._kernel_span(self._w_db(self._w_indexes(s)), gid)
+            gsl, k = self._kernel_span(self._w_kernel(s), gid)
             dens[gsl] = dens[gsl] + counts[gid[0] - 1, gid[1] - 1, gid[2] - 1] * k
         return dens / self.bin_volume
 
+    def _w_kernel(self, smoothing):
+        """The W kernel (range 3) of a bin's smoothing: the database entry, or
+        set up from the exact values (inactive dimensions have no extent)."""
+        if self.database:
+            return self._w_db(self._w_indexes(smoothing))
+        return w_matrix(np.asarray(smoothing, np.float64), self.bin_size, self.ndim, 3)
+
+    def _sd_kernel(self, axis, h):
+        if self.database:
+            return self._sd_db(axis, self._log_index(h, axis))
+        inp = np.zeros(3)
+        inp[axis] = h
+        return sd_matrix(axis, inp, self.bin_size, self.ndim, 4)
+
     def _sigma_gather(self, field, gid, scale):
-        gsl, k = self._kernel_span(self._w_db(self._w_indexes(np.full(3, scale))), gid)
+        gsl, k = self._kernel_span(self._w_kernel(np.full(3, scale)), gid)
         return float((field[gsl] * k).sum())
 
     def _optimize(self, counts, act, init, npts):
@@ -460,7 +484,7 @@ class GPKDE:
                 if self.ndim == 1 and (h < 0.0 or h != h):
                     continue
                 gid = act[n]
-                gsl, k = self._kernel_span(self._sd_db(d, self._log_index(h, d)), gid)
+                gsl, k = self._kernel_span(self._sd_kernel(d, h), gid)
                 c[gsl] = c[gsl] + counts[gid[0] - 1, gid[1] - 1, gid[2] - 1] * k
             c = c / self.bin_volume
             c = c / (self.bin_size[d] ** 2.0)
@@ -478,7 +502,7 @@ class GPKDE:
         cxy, cxz, cyz = curv[0] * curv[1], curv[0] * curv[2], curv[1] * curv[2]
         for n in range(nb):
             gid = act[n]
-            gsl, k = self._kernel_span(self._w_db(self._w_indexes(np.full(3, support[n]))), gid)
+            gsl, k = self._kernel_span(self._w_kernel(np.full(3, support[n])), gid)
             rxx[n] = float((curv[0][gsl] * k).sum())
             ryy[n] = float((curv[1][gsl] * k).sum())
             rzz[n] = float((curv[2][gsl] * k).sum())
