@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-btc", action="store_true",
+                    help="skip the breakthrough-curve leg (1-D GPKDE of 10^6 sink records)")
     ap.add_argument("--realizations", type=int, default=16,
                     help="ensemble size of the batched leg (realizations 0..R-1 of the 64-member ensemble)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
@@ -417,6 +419,43 @@ def e2e_run(args, g, f, p, opt, origin, bins, domain, flush):
                 tot_ms=tot_ms)
 
 
+def btc_run(args, n_records=1_000_000, repeats=5):
+    """Breakthrough-curve leg: the observation post-process's 1-D GPKDE
+    (Freedman-Diaconis bins at fraction 0.75, raw density, kernel database
+    off) of n_records seeded sink arrivals (lognormal times, median 100 d,
+    over a 400-day run), timed end to end through mprw_gpkde_series (host
+    arrays in and out); the numpy restatement on the host times one call on
+    the same records."""
+    import time as _t
+    import mprw
+    rng = np.random.default_rng(2024)
+    t = rng.lognormal(np.log(100.0), 0.35, n_records)
+    w = rng.uniform(0.5, 1.5, n_records) / 3.0
+    kw = dict(domain_size=400.0, bin_format=1, bin_size_fraction=0.75, init_factor=3.0, raw_density=True,
+              rel_err=0.01)
+    for _ in range(2):
+        r = mprw.gpkde_series(t, w, **kw)
+    ms = []
+    for _ in range(repeats):
+        t0 = _t.perf_counter()
+        r = mprw.gpkde_series(t, w, **kw)
+        ms.append((_t.perf_counter() - t0) * 1e3)
+    out = {"records": n_records, "ms": float(np.median(ms)), "records_per_s": n_records / (np.median(ms) / 1e3),
+           "n_bins": r["n_bins"], "active_bins": r["active_bins"], "loops": r["loops"], "bin_size_d": r["bin_size"],
+           "timing": "median of %d calls, host arrays in and out (H2D of 16 B per record inside)" % repeats}
+    if not args.no_cpu:
+        from oracle import series_oracle as SO
+        t0 = _t.perf_counter()
+        ref = SO.gpkde_series(t, w, **kw)
+        cpu_ms = (_t.perf_counter() - t0) * 1e3
+        out["cpu_baseline"] = {"ms": cpu_ms, "records_per_s": n_records / (cpu_ms / 1e3), "kind": "port",
+                               "cores": 1, "sample": "one reconstruction of the same 10^6 records (numpy restatement)"}
+        d = ref["density"]
+        out["max_abs_diff_vs_port"] = float(np.abs(r["density"] - d).max() / np.abs(d).max())
+        out["loops_port"] = ref["loops"]
+    return out
+
+
 def cpu_baseline(g, f, p, opt, n_sample, t_begin_steps, steps):
     """The oracle (C restatement of the reference, OpenMP on all host threads)
     on the first n_sample particles, from t=0 over warmup+steps intervals."""
@@ -542,6 +581,8 @@ def main():
     if not args.no_cpu:
         g, f, p, opt = res["geom"]
         line["cpu_baseline"] = cpu_baseline(g, f, p, opt, args.cpu_sample, args.warmup, min(args.steps, 5))
+    if not args.no_btc:
+        line["btc"] = btc_run(args)
     print(json.dumps(line))
 
 
