@@ -69,6 +69,10 @@ struct mprw_handle {
   void *d_x = nullptr, *d_y = nullptr, *d_z = nullptr;
   double *d_t = nullptr, *d_mass = nullptr, *d_stage = nullptr;
   uint64_t *d_ctr = nullptr, *d_id = nullptr;
+  // random counters at the start of the last advance (their increments are
+  // the passes each particle took: the next sort puts the heaviest first)
+  uint64_t *d_ctr_prev = nullptr;
+  bool ctr_prev_valid = false;
   uint32_t *d_perm = nullptr;
   bool unit_mass = true;
   bool has_id = false;
@@ -170,6 +174,7 @@ void free_all(mprw_handle *h) {
     h->d_x = h->d_y = h->d_z = nullptr;
     h->d_t = h->d_mass = h->d_stage = nullptr;
     h->d_ctr = h->d_id = nullptr;
+    h->d_ctr_prev = nullptr;
     h->d_perm = nullptr;
   }
   for (mprw_handle *m : h->members) {
@@ -188,7 +193,7 @@ void free_all(mprw_handle *h) {
                   h->d_src, h->d_snk, h->d_aL, h->d_aT, h->d_dm, h->d_aLV, h->d_aTV, h->d_ibts, h->d_icb, h->d_ctype,
                   h->d_zones, h->base.q, h->base.dz, h->base.conn, h->base.flags, h->d_massb, h->d_rec64,
                   h->d_rec32, h->d_cell, h->d_status, h->d_x, h->d_y, h->d_z, h->d_t, h->d_mass,
-                  h->d_stage, h->d_ctr, h->d_id, h->d_perm, h->d_counters, h->scratch};
+                  h->d_stage, h->d_ctr, h->d_ctr_prev, h->d_id, h->d_perm, h->d_counters, h->scratch};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->h_counters) cudaFreeHost(h->h_counters);
@@ -574,6 +579,7 @@ int upload_particles(mprw_handle *h, int64_t n, const int32_t *cell, const doubl
     CK(dalloc(&h->d_t, c));
     CK(dalloc(&h->d_mass, c));
     CK(dalloc(&h->d_ctr, c));
+    CK(dalloc(&h->d_ctr_prev, c));
     CK(dalloc(&h->d_id, c));
     CK(dalloc(&h->d_perm, c));
     if (mixed) CK(dalloc(&h->d_stage, c));
@@ -581,6 +587,7 @@ int upload_particles(mprw_handle *h, int64_t n, const int32_t *cell, const doubl
   }
   h->n = n;
   h->perm_valid = false;
+  h->ctr_prev_valid = false;
   h->advance_count = 0;
   if (n == 0) return MPRW_OK;
   cudaStream_t s = h->stream;
@@ -813,7 +820,9 @@ int launch_step(mprw_handle *h, double t_begin, double t_end, int bps, bool use_
 }
 
 int sort_particles(mprw_handle *h) {
-  CK(sort_cells(h->d_cell, h->d_perm, h->n, h->ncell_bits, &h->scratch, &h->scratch_bytes, h->stream));
+  const uint64_t per_pass = 3ull * (uint64_t)h->ndim;  // Philox blocks per pass: 3 per normal, ndim normals
+  CK(sort_cells(h->d_cell, h->d_ctr, h->ctr_prev_valid ? h->d_ctr_prev : nullptr, per_pass, h->d_perm, h->n,
+                h->ncell_bits, &h->scratch, &h->scratch_bytes, h->stream));
   h->launches += 2;
   h->perm_valid = true;
   return MPRW_OK;
@@ -855,6 +864,10 @@ int mprw_advance(mprw_handle *h, double t_begin, double t_end, int64_t *steps_do
     if (rc != MPRW_OK) return rc;
   }
   ++h->advance_count;
+  if (h->d_ctr_prev) {
+    CK(cudaMemcpyAsync(h->d_ctr_prev, h->d_ctr, 8 * (size_t)h->n, cudaMemcpyDeviceToDevice, h->stream));
+    h->ctr_prev_valid = true;
+  }
   const int bps = h->blocks_per_sm > 0 ? h->blocks_per_sm : default_blocks_per_sm(h);
   float ms = 0;
   int64_t steps = 0;

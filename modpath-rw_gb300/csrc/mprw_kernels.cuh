@@ -123,7 +123,14 @@ cudaError_t launch_resident(const ObsArgs &a, unsigned long long *count, double 
 cudaError_t ordered_bin_sums(const int64_t *bin_of, const double *mass, const int32_t *status, int64_t n,
                              int64_t nbins, double *counts, double *total_mass, double *sum_w2,
                              void **scratch, size_t *scratch_bytes, cudaStream_t s);
-cudaError_t sort_cells(const int32_t *cell, uint32_t *perm, int64_t n, int ncell_bits, void **scratch,
-                       size_t *scratch_bytes, cudaStream_t s);
+// processing order: by cell, or -- given the random counters at the start of
+// the previous advance -- heaviest first in buckets of kPassBucket passes
+// of that advance, by cell within a bucket
+constexpr int kPassBucket = 8;
+constexpr int kPassBucketBits = 4;
+constexpr int kPassBuckets = 1 << kPassBucketBits;
+cudaError_t sort_cells(const int32_t *cell, const uint64_t *ctr, const uint64_t *ctr_prev, uint64_t ctr_per_pass,
+                       uint32_t *perm, int64_t n, int ncell_bits, void **scratch, size_t *scratch_bytes,
+                       cudaStream_t s);
 
 }  // namespace mprw

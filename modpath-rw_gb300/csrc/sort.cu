@@ -1,7 +1,10 @@
 // sort.cu -- radix sorts used around the hot path (CUB, header-only part of
 // the CUDA toolkit):
 //   * sort_cells: particle processing order by cell, so the warps of the step
-//     kernel read neighbouring cell records;
+//     kernel read neighbouring cell records; with the passes of the previous
+//     interval known, heaviest first in buckets of kPassBucket passes (cell
+//     order within a bucket), so the persistent kernel's queue does not end on
+//     a few long particles;
 //   * ordered_bin_sums: per-bin sums of non-unit particle weights in particle
 //     order, bit-identical to the reference's sequential loop
 //     (Histogram.F90:302-325) together with the sequential totals
@@ -30,19 +33,37 @@ __global__ void iota_keys_kernel(const int32_t *cell, uint32_t *keys, uint32_t *
   }
 }
 
+// keys (15 - bucket of the previous interval's passes, cell): passes are the
+// random-counter increments over `unit` (counter blocks per pass times the
+// bucket width)
+__global__ void lpt_keys_kernel(const int32_t *cell, const uint64_t *ctr, const uint64_t *ctr_prev, uint64_t unit,
+                                int ncell_bits, uint32_t *keys, uint32_t *vals, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t d = (ctr[i] >= ctr_prev[i]) ? ctr[i] - ctr_prev[i] : 0;
+    const uint64_t b = d / unit;
+    const uint32_t bucket = (b > (uint64_t)kPassBuckets - 1) ? (uint32_t)kPassBuckets - 1 : (uint32_t)b;
+    keys[i] = (((uint32_t)kPassBuckets - 1 - bucket) << ncell_bits) | (uint32_t)cell[i];
+    vals[i] = (uint32_t)i;
+  }
+}
+
 static int grid_for(int64_t n) {
   int64_t b = (n + 255) / 256;
   if (b > 152 * 16) b = 152 * 16;
   return b < 1 ? 1 : (int)b;
 }
 
-cudaError_t sort_cells(const int32_t *cell, uint32_t *perm, int64_t n, int ncell_bits, void **scratch,
-                       size_t *scratch_bytes, cudaStream_t s) {
+cudaError_t sort_cells(const int32_t *cell, const uint64_t *ctr, const uint64_t *ctr_prev, uint64_t ctr_per_pass,
+                       uint32_t *perm, int64_t n, int ncell_bits, void **scratch, size_t *scratch_bytes,
+                       cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  // pass buckets only when the key still fits 32 bits
+  const bool lpt = ctr && ctr_prev && ctr_per_pass > 0 && ncell_bits + kPassBucketBits <= 32;
+  const int bits = lpt ? ncell_bits + kPassBucketBits : ncell_bits;
   size_t temp = 0;
   cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, temp, (const uint32_t *)nullptr, (uint32_t *)nullptr,
                                                   (const uint32_t *)nullptr, (uint32_t *)nullptr, (int)n, 0,
-                                                  ncell_bits, s);
+                                                  bits, s);
   if (e != cudaSuccess) return e;
   size_t arr = ((size_t)n * 4 + 255) / 256 * 256;
   e = ensure(scratch, scratch_bytes, 3 * arr + temp);
@@ -50,10 +71,14 @@ cudaError_t sort_cells(const int32_t *cell, uint32_t *perm, int64_t n, int ncell
   char *b = (char *)*scratch;
   uint32_t *kin = (uint32_t *)b, *kout = (uint32_t *)(b + arr), *vin = (uint32_t *)(b + 2 * arr);
   void *tmp = b + 3 * arr;
-  iota_keys_kernel<<<grid_for(n), 256, 0, s>>>(cell, kin, vin, n);
+  if (lpt)
+    lpt_keys_kernel<<<grid_for(n), 256, 0, s>>>(cell, ctr, ctr_prev, ctr_per_pass * (uint64_t)kPassBucket,
+                                                ncell_bits, kin, vin, n);
+  else
+    iota_keys_kernel<<<grid_for(n), 256, 0, s>>>(cell, kin, vin, n);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return cub::DeviceRadixSort::SortPairs(tmp, temp, kin, kout, vin, perm, (int)n, 0, ncell_bits, s);
+  return cub::DeviceRadixSort::SortPairs(tmp, temp, kin, kout, vin, perm, (int)n, 0, bits, s);
 }
 
 __global__ void ordered_keys_kernel(const int64_t *bin_of, int64_t n, unsigned long long *keys) {

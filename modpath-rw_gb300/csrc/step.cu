@@ -451,6 +451,20 @@ struct Visit {
 
 enum : int { PASS_CONTINUE = 0, PASS_MAXTIME = 1, PASS_EXIT = 2, PASS_UNDEFINED = 3 };
 
+// component k (0, 1, 2) of three values, by selects (no local-memory array)
+template <typename T>
+__device__ __forceinline__ T pick3(int k, T a, T b, T c) {
+  return (k == 0) ? a : ((k == 1) ? b : c);
+}
+
+// bit k set when component k of the proposed position is outside [0, 1]
+template <typename R>
+__device__ __forceinline__ unsigned axes_outside(R nx, R ny, R nz) {
+  const R zero = R(0), one = R(1);
+  return ((nx > one || nx < zero) ? 1u : 0u) | ((ny > one || ny < zero) ? 2u : 0u) |
+         ((nz > one || nz < zero) ? 4u : 0u);
+}
+
 #define MPRW_OUTSIDE(a, b, c) \
   (((a) > one) || ((a) < zero) || ((b) > one) || ((b) < zero) || ((c) > one) || ((c) < zero))
 
@@ -534,12 +548,23 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
       int efx = 0, efy = 0, efz = 0;
       bool ret = false;
       V.t = V.t - dt;
-      if (!ret && ((nx > one) || (nx < zero)))
-        ret = newton_axis(nx, x, dX, vx, dvx, ddx, bx, 1, 2, dt, dtx, efx, V.exitFace, dt);
-      if (!ret && ((ny > one) || (ny < zero)))
-        ret = newton_axis(ny, y, dY, vy, dvy, ddy, by, 3, 4, dt, dty, efy, V.exitFace, dt);
-      if (!ret && ((nz > one) || (nz < zero)))
-        ret = newton_axis(nz, z, dZ, vz, dvz, ddz, bz, 5, 6, dt, dtz, efz, V.exitFace, dt);
+      // the axes the step leaves through, x then y then z, solved in one
+      // shared block: the first axis of every leaving lane together, then
+      // the second (a warp's leaving lanes mostly leave through different
+      // axes; three per-axis branches would each run with a few lanes)
+      unsigned need = axes_outside(nx, ny, nz);
+      while (!ret && need) {
+        const int k = __ffs(need) - 1;
+        need &= need - 1;
+        double dta = 0.0;
+        int efa = 0;
+        ret = newton_axis((double)pick3(k, nx, ny, nz), (double)pick3(k, x, y, z), (double)pick3(k, dX, dY, dZ),
+                          (double)pick3(k, vx, vy, vz), pick3(k, dvx, dvy, dvz), (double)pick3(k, ddx, ddy, ddz),
+                          (double)pick3(k, bx, by, bz), 2 * k + 1, 2 * k + 2, dt, dta, efa, V.exitFace, dt);
+        if (k == 0) { dtx = dta; efx = efa; }
+        else if (k == 1) { dty = dta; efy = efa; }
+        else { dtz = dta; efz = efa; }
+      }
       if (!ret) {
         if (dtx == 0.0 && dty == 0.0 && dtz == 0.0) {
           V.t = V.t + dt;
@@ -560,12 +585,31 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
       int efx = 0, efy = 0, efz = 0;
       bool ret = false;
       V.t = V.t - dt;
-      if (!ret && ((nx > one) || (nx < zero)))
-        ret = quad_axis(nx, x, dX, vx, ddx, bx, 1, 2, dt, dtx, efx, V.exitFace, dt);
-      if (!ret && ((ny > one) || (ny < zero)))
-        ret = quad_axis(ny, y, dY, vy, ddy, by, 3, 4, dt, dty, efy, V.exitFace, dt);
-      if (!ret && ((nz > one) || (nz < zero)))
-        ret = quad_axis(nz, z, dZ, vz, ddz, bz, 5, 6, dt, dtz, efz, V.exitFace, dt);
+      if constexpr (sizeof(R) == 8) {
+        // FP64: the leaving axes solved in one shared block (as for
+        // EXPONENTIAL); the FP32 solve is cheap enough that the extra
+        // registers of the shared block cost more than the divergence
+        unsigned need = axes_outside(nx, ny, nz);
+        while (!ret && need) {
+          const int k = __ffs(need) - 1;
+          need &= need - 1;
+          R dta = zero;
+          int efa = 0;
+          ret = quad_axis(pick3(k, nx, ny, nz), pick3(k, x, y, z), pick3(k, dX, dY, dZ), pick3(k, vx, vy, vz),
+                          pick3(k, ddx, ddy, ddz), pick3(k, bx, by, bz), 2 * k + 1, 2 * k + 2, dt, dta, efa,
+                          V.exitFace, dt);
+          if (k == 0) { dtx = dta; efx = efa; }
+          else if (k == 1) { dty = dta; efy = efa; }
+          else { dtz = dta; efz = efa; }
+        }
+      } else {
+        if (!ret && ((nx > one) || (nx < zero)))
+          ret = quad_axis(nx, x, dX, vx, ddx, bx, 1, 2, dt, dtx, efx, V.exitFace, dt);
+        if (!ret && ((ny > one) || (ny < zero)))
+          ret = quad_axis(ny, y, dY, vy, ddy, by, 3, 4, dt, dty, efy, V.exitFace, dt);
+        if (!ret && ((nz > one) || (nz < zero)))
+          ret = quad_axis(nz, z, dZ, vz, ddz, bz, 5, 6, dt, dtz, efz, V.exitFace, dt);
+      }
       if (!ret) {
         if (dtx == zero && dty == zero && dtz == zero) {
           V.t = V.t + dt;
@@ -596,7 +640,19 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
     advect();
     V.reachedMax = false;
     int ef = V.exitFace;
-    if (ef == 1 || ef == 2) {
+    if (ef >= 1 && ef <= 6 && sizeof(R) == 8) {
+      // FP64: the step of the truncated time on every axis (one shared
+      // block), then the exit axis pinned to its face
+      const R dxc = ax + ddx * rdt + bx * sdt;
+      const R dyc = ay + ddy * rdt + by * sdt;
+      const R dzc = az + ddz * rdt + bz * sdt;
+      const R nxc = x + dxc * iX, nyc = y + dyc * iY, nzc = z + dzc * iZ;
+      const int fa = (ef - 1) >> 1;
+      const R pin = (ef & 1) ? zero : one;
+      if (fa != 0) { dxrw = dxc; nx = nxc; } else { nx = pin; }
+      if (fa != 1) { dyrw = dyc; ny = nyc; } else { ny = pin; }
+      if (fa != 2) { dzrw = dzc; nz = nzc; } else { nz = pin; }
+    } else if (ef == 1 || ef == 2) {
       nx = (ef == 1) ? zero : one;
       dyrw = ay + ddy * rdt + by * sdt;
       ny = y + dyrw * iY;
