@@ -73,8 +73,9 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-btc", action="store_true",
                     help="skip the breakthrough-curve leg (1-D GPKDE of 10^6 sink records)")
-    ap.add_argument("--realizations", type=int, default=16,
-                    help="ensemble size of the batched leg (realizations 0..R-1 of the 64-member ensemble)")
+    ap.add_argument("--realizations", type=int, default=64,
+                    help="ensemble size of the batched leg (realizations 0..R-1 of the 64-member ensemble; "
+                         "64 = the whole ensemble)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default launch tuning instead of mprw_autotune before the warm-up")
     ap.add_argument("--workload", default="lognormal_slab", choices=["lognormal_slab", "lognormal_injection"],
