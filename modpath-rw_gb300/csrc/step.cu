@@ -468,6 +468,89 @@ __device__ __forceinline__ unsigned axes_outside(R nx, R ny, R nz) {
 #define MPRW_OUTSIDE(a, b, c) \
   (((a) > one) || ((a) < zero) || ((b) > one) || ((b) < zero) || ((c) > one) || ((c) < zero))
 
+// The first interface iteration's exit-face solves of the leaving lanes of
+// `grp`, dealt out to every lane of `grp` (FP64).  Each (leaving lane,
+// leaving axis) pair is a task; tasks in axis-major order go to the group's
+// lanes by rank (a second round only past one task per lane), every lane
+// solves one with its owner's values (quad_axis is a pure function of them),
+// and each owner gets back, per leaving axis, whether the solve returned at
+// once (bit k of rbits), its exit face and its time.  Without this, a warp
+// solves its lanes' first leaving axes together and then their second axes
+// (corner crossings) in a second round of one or two lanes.  Every lane of
+// grp calls it together.
+__device__ __forceinline__ void warp_exit_solves(unsigned grp, unsigned need, double nx, double ny, double nz,
+                                                 double x, double y, double z, double dX, double dY, double dZ,
+                                                 double vx, double vy, double vz, double ddx, double ddy,
+                                                 double ddz, double bx, double by, double bz, double dt,
+                                                 unsigned &rbits, double &tx, double &ty, double &tz, int &fx,
+                                                 int &fy, int &fz) {
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  const unsigned m0 = __ballot_sync(grp, need & 1u), m1 = __ballot_sync(grp, need & 2u);
+  const unsigned m2 = __ballot_sync(grp, need & 4u);
+  const int c0 = __popc(m0), c1 = __popc(m1), total = c0 + c1 + __popc(m2);
+  const int nw = __popc(grp), rank = __popc(grp & below);
+  // this lane's own tasks, one per leaving axis
+  const int t0 = __popc(m0 & below), t1 = c0 + __popc(m1 & below), t2 = c0 + c1 + __popc(m2 & below);
+  rbits = 0u;
+  tx = ty = tz = 0.0;
+  fx = fy = fz = 0;
+  for (int base = 0; base < total; base += nw) {
+    const int t = base + rank;
+    int a = 0, owner = lane;
+    if (t < total) {
+      if (t < c0) {
+        owner = __fns(m0, 0, t + 1);
+      } else if (t < c0 + c1) {
+        a = 1;
+        owner = __fns(m1, 0, t - c0 + 1);
+      } else {
+        a = 2;
+        owner = __fns(m2, 0, t - c0 - c1 + 1);
+      }
+    }
+    // the owner's values on all three axes, the task's axis picked after
+    const double onx = __shfl_sync(grp, nx, owner), ony = __shfl_sync(grp, ny, owner);
+    const double onz = __shfl_sync(grp, nz, owner);
+    const double ox = __shfl_sync(grp, x, owner), oy = __shfl_sync(grp, y, owner), oz = __shfl_sync(grp, z, owner);
+    const double odX = __shfl_sync(grp, dX, owner), odY = __shfl_sync(grp, dY, owner);
+    const double odZ = __shfl_sync(grp, dZ, owner);
+    const double ovx = __shfl_sync(grp, vx, owner), ovy = __shfl_sync(grp, vy, owner);
+    const double ovz = __shfl_sync(grp, vz, owner);
+    const double oddx = __shfl_sync(grp, ddx, owner), oddy = __shfl_sync(grp, ddy, owner);
+    const double oddz = __shfl_sync(grp, ddz, owner);
+    const double obx = __shfl_sync(grp, bx, owner), oby = __shfl_sync(grp, by, owner);
+    const double obz = __shfl_sync(grp, bz, owner);
+    const double odt = __shfl_sync(grp, dt, owner);
+    bool r = false;
+    double dta = 0.0;
+    int efa = 0;
+    if (t < total) {
+      int ef_unused = 0;
+      double dt_unused = 0.0;
+      r = quad_axis<double>(pick3(a, onx, ony, onz), pick3(a, ox, oy, oz), pick3(a, odX, odY, odZ),
+                            pick3(a, ovx, ovy, ovz), pick3(a, oddx, oddy, oddz), pick3(a, obx, oby, obz),
+                            2 * a + 1, 2 * a + 2, odt, dta, efa, ef_unused, dt_unused);
+    }
+    // results back to their owners, one axis at a time
+    const unsigned packed = (r ? 8u : 0u) | (unsigned)efa;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const int tb = (b == 0) ? t0 : ((b == 1) ? t1 : t2);
+      const bool mine = ((need >> b) & 1u) && tb >= base && tb < base + nw;
+      const int wl = mine ? (int)__fns(grp, 0, tb - base + 1) : lane;
+      const unsigned pk = __shfl_sync(grp, packed, wl);
+      const double dv = __shfl_sync(grp, dta, wl);
+      if (mine) {
+        if (pk & 8u) rbits |= 1u << b;
+        if (b == 0) { tx = dv; fx = (int)(pk & 7u); }
+        else if (b == 1) { ty = dv; fy = (int)(pk & 7u); }
+        else { tz = dv; fz = (int)(pk & 7u); }
+      }
+    }
+  }
+}
+
 // One pass of the `do while (continueTimeLoop)` body, TrackSubCell.F90:956-1368.
 // On PASS_MAXTIME / PASS_EXIT the final location is (ox,oy,oz,V.t); on
 // PASS_UNDEFINED the caller uses the last recorded point.
@@ -475,6 +558,7 @@ template <typename R, bool EXP, bool AXI>
 __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double maxTime, int ndim, int d1, int d2,
                        uint64_t seed, uint64_t id, uint64_t &ctr, R &ox, R &oy, R &oz) {
   const R zero = R(0), one = R(1), half = R(0.5);
+  const unsigned grp = __activemask();  // the lanes running this pass together
   const double dtRed = (double)0.1f;  // dtReductionFactor, a single-precision literal (:850)
   double dt = V.dtcell;
   R rdt = V.rdt_cell, sdt = V.sqrt_dtcell;  // FP32 copies: no conversion on the common pass
@@ -538,6 +622,17 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
     V.reachedMax = false;
   }
   R nx = x + dxrw * iX, ny = y + dyrw * iY, nz = z + dzrw * iZ;
+  // FP64 EULERIAN: the first interface iteration's exit-face solves of the
+  // leaving lanes, spread over every lane of the pass
+  unsigned pre_r = 0u;
+  double pre_tx = 0.0, pre_ty = 0.0, pre_tz = 0.0;
+  int pre_fx = 0, pre_fy = 0, pre_fz = 0;
+  if constexpr (sizeof(R) == 8 && !EXP) {
+    __syncwarp(grp);
+    warp_exit_solves(grp, MPRW_OUTSIDE(nx, ny, nz) ? axes_outside(nx, ny, nz) : 0u, nx, ny, nz, x, y, z, dX, dY,
+                     dZ, vx, vy, vz, ddx, ddy, ddz, bx, by, bz, dt, pre_r, pre_tx, pre_ty, pre_tz, pre_fx, pre_fy,
+                     pre_fz);
+  }
   // particleLeavingCell (:1025-1316)
   int intLoop = 0;
   while (MPRW_OUTSIDE(nx, ny, nz)) {
@@ -586,10 +681,25 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
       bool ret = false;
       V.t = V.t - dt;
       if constexpr (sizeof(R) == 8) {
-        // FP64: the leaving axes solved in one shared block (as for
-        // EXPONENTIAL); the FP32 solve is cheap enough that the extra
-        // registers of the shared block cost more than the divergence
+        // FP64: the first iteration takes the warp-wide solves (the same
+        // inputs: nothing has moved yet); later ones solve the leaving axes
+        // in one shared block (as for EXPONENTIAL).  The FP32 solve is cheap
+        // enough that the extra registers of either cost more than the
+        // divergence.
         unsigned need = axes_outside(nx, ny, nz);
+        if (intLoop == 1) {
+          while (!ret && need) {
+            const int k = __ffs(need) - 1;
+            need &= need - 1;
+            if ((pre_r >> k) & 1u) {
+              V.exitFace = pick3(k, pre_fx, pre_fy, pre_fz);
+              dt = 0.0;
+              ret = true;
+            } else if (k == 0) { dtx = pre_tx; efx = pre_fx; }
+            else if (k == 1) { dty = pre_ty; efy = pre_fy; }
+            else { dtz = pre_tz; efz = pre_fz; }
+          }
+        }
         while (!ret && need) {
           const int k = __ffs(need) - 1;
           need &= need - 1;
