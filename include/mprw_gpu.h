@@ -125,7 +125,11 @@ int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *flow);
 /* Copy n particles (host arrays) to the device.  cell is 1-based; t is the
  * TrackingTime (the release time for pending particles); mass may be NULL
  * (unit mass); id may be NULL (id = index); rng_ctr may be NULL (zeros).
- * Replaces the particle arrays of ParticleGroups (Particle.f90:7-17). */
+ * Replaces the particle arrays of ParticleGroups (Particle.f90:7-17).
+ * The next advance processes the particles heaviest first by the passes each
+ * took in the previous advance (their rng_ctr increments) when n is
+ * unchanged -- a host that hands back the particles mprw_get_particles gave
+ * it keeps that order; results never depend on the order. */
 int mprw_set_particles(mprw_handle *h, int64_t n, const int32_t *cell, const double *lx,
                        const double *ly, const double *lz, const double *t,
                        const int32_t *status, const double *mass, const uint64_t *id,

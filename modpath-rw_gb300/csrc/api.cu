@@ -585,9 +585,12 @@ int upload_particles(mprw_handle *h, int64_t n, const int32_t *cell, const doubl
     if (mixed) CK(dalloc(&h->d_stage, c));
     h->cap = n;
   }
+  // the pass counts of the last advance (counter increments) still order the
+  // next one when the host hands the same particles back; for other
+  // particles of the same count they only give a poorer order
+  if (n != h->n) h->ctr_prev_valid = false;
   h->n = n;
   h->perm_valid = false;
-  h->ctr_prev_valid = false;
   h->advance_count = 0;
   if (n == 0) return MPRW_OK;
   cudaStream_t s = h->stream;
