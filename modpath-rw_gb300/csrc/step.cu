@@ -35,12 +35,40 @@ struct Lane {
   __device__ __forceinline__ R operator()(int f) const { return p[f * stride]; }
 };
 
+// The staged fields are the record's first NFIELDS values and records are
+// 16-byte aligned, so they are read with 16-byte loads (FP32: 16 float4 and
+// one float2; FP64: 33 double2) and scattered to the lane's SoA slots.
+static_assert(NFIELDS == 66, "stage_record reads 66 leading fields");
 template <typename R>
-__device__ __forceinline__ void stage_record(const CellRec<R> *__restrict__ recs, int32_t c, R *sm,
-                                             int stride) {
-  const R *src = reinterpret_cast<const R *>(recs + c);
-#pragma unroll 8
-  for (int f = 0; f < NFIELDS; ++f) sm[f * stride] = __ldg(src + f);
+__device__ __forceinline__ void stage_record(const CellRec<R> *__restrict__ recs, int32_t c, R *sm, int stride);
+
+template <>
+__device__ __forceinline__ void stage_record<float>(const CellRec<float> *__restrict__ recs, int32_t c, float *sm,
+                                                    int stride) {
+  const float4 *src = reinterpret_cast<const float4 *>(recs + c);
+#pragma unroll 4
+  for (int q = 0; q < 16; ++q) {
+    const float4 v = __ldg(src + q);
+    sm[(4 * q + 0) * stride] = v.x;
+    sm[(4 * q + 1) * stride] = v.y;
+    sm[(4 * q + 2) * stride] = v.z;
+    sm[(4 * q + 3) * stride] = v.w;
+  }
+  const float2 t = __ldg(reinterpret_cast<const float2 *>(src + 16));
+  sm[64 * stride] = t.x;
+  sm[65 * stride] = t.y;
+}
+
+template <>
+__device__ __forceinline__ void stage_record<double>(const CellRec<double> *__restrict__ recs, int32_t c,
+                                                     double *sm, int stride) {
+  const double2 *src = reinterpret_cast<const double2 *>(recs + c);
+#pragma unroll 4
+  for (int q = 0; q < 33; ++q) {
+    const double2 v = __ldg(src + q);
+    sm[(2 * q + 0) * stride] = v.x;
+    sm[(2 * q + 1) * stride] = v.y;
+  }
 }
 
 template <typename R>
