@@ -926,7 +926,6 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
   V.reachedMax = false;
   V.passes = 0;
   uint32_t massb = 0;
-  int32_t conn6[6] = {-1, -1, -1, -1, -1, -1};
   // cell exits of the current particle in this launch (bits 0-19) and how
   // many of the last ones took no time (bits 20-30): one register for both caps
   static_assert(kMaxVisitsPerAdvance < (1 << 20) - 1 && kMaxZeroTimeExits < (1 << 11) - 1, "exit counter bits");
@@ -1016,8 +1015,6 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
         } else {
           stage_record(a.recs, c, sm, stride);
           massb = rec->massb;
-#pragma unroll
-          for (int f = 0; f < 6; ++f) conn6[f] = rec->conn[f];
           V.x = ex; V.y = ey; V.z = ez;
           V.ix = ex; V.iy = ey; V.iz = ez;
           V.t = et; V.tinit = et;
@@ -1074,7 +1071,9 @@ __global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1
         // the exit point becomes the last pathline point
         const int face = V.exitFace;
         lc = c; lx = ox; ly = oy; lz = oz; lt = V.t;
-        const int32_t nc = conn6[face - 1];
+        // the neighbour through the exit face, read from the cell's record
+        // (not held in registers through the visit)
+        const int32_t nc = __ldg(&a.recs[c].conn[face - 1]);
         // ConvertFromNeighbor: the exit coordinate must sit exactly on the face
         const bool bad = (face == 2 && ox != one) || (face == 1 && ox != zero) || (face == 4 && oy != one) ||
                          (face == 3 && oy != zero) || (face == 6 && oz != one) || (face == 5 && oz != zero);
