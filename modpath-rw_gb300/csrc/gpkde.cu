@@ -260,15 +260,27 @@ __global__ void key_assign_kernel(KdeParams P, KdeBinsT<T> B, int kind, int *bin
     sc[k] = 0;
   }
   __syncthreads();
-  auto record = [&](int key, const int lev[3], const int g[3]) {
+  // Neighbouring bins mostly share a key, so the lanes of a warp with the
+  // same key first reduce their bounding box and count among themselves
+  // (min, max and count do not depend on the order) and one lane of each
+  // group updates the block's shared accumulators.  key < 0: nothing to record.
+  auto record = [&](unsigned act, int key, const int lev[3], const int g[3]) {
+    const unsigned grp = __match_any_sync(act, key);
+    int lo[3], hi[3];
     for (int d = 0; d < 3; ++d) {
-      atomicMin(&sb[key][2 * d], g[d]);
-      atomicMax(&sb[key][2 * d + 1], g[d]);
+      lo[d] = __reduce_min_sync(grp, g[d]);
+      hi[d] = __reduce_max_sync(grp, g[d]);
+    }
+    if (key < 0 || (int)(threadIdx.x & 31) != __ffs(grp) - 1) return;
+    for (int d = 0; d < 3; ++d) {
+      atomicMin(&sb[key][2 * d], lo[d]);
+      atomicMax(&sb[key][2 * d + 1], hi[d]);
       sl[key][d] = lev[d];  // every bin of the key writes the same levels
     }
-    atomicAdd(&sc[key], 1);
+    atomicAdd(&sc[key], __popc(grp));
   };
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
+    const unsigned act = __activemask();
     const int g[3] = {B.gx[b], B.gy[b], B.gz[b]};
     if (kind == 1) {
       const T s = B.support[b];
@@ -277,17 +289,18 @@ __global__ void key_assign_kernel(KdeParams P, KdeBinsT<T> B, int kind, int *bin
         if (P.mask[d]) lev[d] = log_index<T>(P, s, d);
       const int key = lev[0] + lev[1] + lev[2] - 3;
       bin_key[b] = key;
-      record(key, lev, g);
+      record(act, key, lev, g);
     } else {
       for (int a = 0; a < 3; ++a) {
         int key = -1;
+        int n = 1;
         const T h = B.cb[a * B.n + b];
         if (P.mask[a] && h == h) {
-          const int n = log_index<T>(P, h, a);
-          const int lev[3] = {n, n, n};
+          n = log_index<T>(P, h, a);
           key = a * KDE_MAXDB + n - 1;
-          record(key, lev, g);
         }
+        const int lev[3] = {n, n, n};
+        record(act, key, lev, g);
         bin_key[a * B.n + b] = key;
       }
     }
@@ -1094,7 +1107,10 @@ cudaError_t KdeState::ensure_bins(int n) {
   partial = nullptr;
   bin_key = wlev = nullptr;
   cap = 0;
-  const size_t c = (size_t)n;
+  // a quarter of headroom: a spreading plume activates more bins at almost
+  // every reconstruction, and each regrowth frees and allocates ~20 arrays
+  // (cudaFree synchronises the device)
+  const size_t c = (size_t)n + (size_t)n / 4;
   cudaError_t e = cudaSuccess;
   auto I = [&](int **p, size_t k) {
     if (e == cudaSuccess) e = cudaMalloc((void **)p, sizeof(int) * k);
@@ -1108,7 +1124,7 @@ cudaError_t KdeState::ensure_bins(int n) {
   D(&bins.net, c); D(&bins.dens_old, c); D(&bins.scale_old, c);
   D(&partial, 3 * 152 * 8 + 16);
   if (e != cudaSuccess) return e;
-  cap = n;
+  cap = (int)std::min<size_t>(c, (size_t)INT_MAX);
   bins.n = n;
   return cudaSuccess;
 }
