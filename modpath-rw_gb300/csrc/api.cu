@@ -714,8 +714,9 @@ int max_blocks_per_sm(mprw_handle *h) {
   const bool mixed = h->opt.precision == MPRW_MIXED;
   const bool exp_adv = h->opt.advection_kind == 1, axi = h->opt.dispersion_model == 1;
   int nb = 0;
-  cudaError_t e = mixed ? advance_occupancy<float>(exp_adv, axi, kStepThreads, &nb)
-                        : advance_occupancy<double>(exp_adv, axi, kStepThreads, &nb);
+  const int threads = step_threads(!mixed, exp_adv != 0);
+  cudaError_t e = mixed ? advance_occupancy<float>(exp_adv, axi, threads, &nb)
+                        : advance_occupancy<double>(exp_adv, axi, threads, &nb);
   if (e != cudaSuccess || nb < 1) nb = 1;
   return nb;
 }
@@ -730,7 +731,7 @@ int default_blocks_per_sm(mprw_handle *h) {
 int launch_step(mprw_handle *h, double t_begin, double t_end, int bps, bool use_perm, float *ms, int64_t *steps) {
   cudaStream_t s = h->stream;
   CK(cudaMemsetAsync(h->d_counters, 0, 4 * sizeof(unsigned long long), s));
-  const int threads = kStepThreads;
+  const int threads = step_threads(h->opt.precision != MPRW_MIXED, h->opt.advection_kind == 1);
   int64_t need = (h->n + threads - 1) / threads;
   int64_t blocks = (int64_t)h->sms * bps;
   if (need < blocks) blocks = need;

@@ -5,6 +5,10 @@
 namespace mprw {
 
 constexpr int kStepThreads = 256;
+// FP64 EULERIAN step kernel: 384 threads per block (12 warps per SM fit in
+// 168 registers; the FP64 pipe is fuller than with 8 warps at 236)
+constexpr int kStepThreadsF64 = 384;
+constexpr int step_threads(bool fp64, bool exp_adv) { return (fp64 && !exp_adv) ? kStepThreadsF64 : kStepThreads; }
 constexpr int kAbortPoll = 256;  // main-loop iterations between two reads of the cancel flag
 
 template <typename R>

@@ -895,7 +895,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
 // runs with every tracking lane active; the loop ends when no lane of the warp
 // has work.
 template <typename R, bool EXP, bool AXI>
-__global__ void __launch_bounds__(kStepThreads, (sizeof(R) == 4 && !EXP) ? 3 : 1) rwpt_advance_kernel(AdvanceArgs<R> a) {
+__global__ void __launch_bounds__(step_threads(sizeof(R) == 8, EXP), (sizeof(R) == 4 && !EXP) ? 3 : 1) rwpt_advance_kernel(AdvanceArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw) + threadIdx.x;
   const int stride = blockDim.x;
