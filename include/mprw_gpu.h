@@ -359,11 +359,13 @@ int mprw_gpkde_batch(mprw_handle *batch, const mprw_gpkde_options *opts, double 
  * is `!$omp parallel do schedule(dynamic,1)`).  blocks_per_sm: resident
  * blocks per SM of the persistent step kernel (0 = the variant's default: 3
  * for EULERIAN MIXED, else 1; at most what its registers allow, which
- * mprw_get_tuning reports as max_blocks); sort_interval: the particles are
- * sorted by cell before every k-th advance and processed in that order
- * until the next sort (1 = every advance, the default; 0 = never).  Results
- * do not depend on the tuning: each particle's steps use only its own state
- * and its own counter-based random numbers.
+ * mprw_get_tuning reports as max_blocks; blocks of 384 threads for the FP64
+ * EULERIAN kernel, 256 otherwise); sort_interval: the particles are sorted
+ * -- by the passes each took in the previous advance, heaviest first in
+ * buckets of 8, then by cell -- before every k-th advance and processed in
+ * that order until the next sort (1 = every advance, the default; 0 =
+ * never).  Results do not depend on the tuning: each particle's steps use
+ * only its own state and its own counter-based random numbers.
  *
  * mprw_autotune picks both on the handle's real work: from the current
  * particle state it runs one advance over [t_begin, t_end] per candidate
