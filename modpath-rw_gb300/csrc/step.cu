@@ -212,9 +212,11 @@ __device__ __forceinline__ void random_displacement(const Lane<R> &F, int ndim, 
 
 // One axis of pr_DetectExitFaceAndUpdateTimeStepQuadratic (:1622-1710).
 // Returns true when the routine must return at once (exitFace, dt set).
-template <typename R>
+// The step length dt comes in the type T of its comparison: FP64 compares in
+// double as the reference; MIXED passes the FP32 copy of dt (no FP64 op).
+template <typename R, typename T>
 __device__ __forceinline__ bool quad_axis(R npos, R pos, R d, R v, R divD, R dB, int faceLo, int faceHi,
-                                          double dt, R &dtaxis, int &exitAxis, int &exitFace,
+                                          T dt, R &dtaxis, int &exitAxis, int &exitFace,
                                           double &dtout) {
   const R zero = R(0), one = R(1);
   R dI;
@@ -269,7 +271,7 @@ __device__ __forceinline__ bool quad_axis(R npos, R pos, R d, R v, R divD, R dB,
       }
     }
   }
-  if ((double)dtaxis > dt) dtaxis = zero;
+  if ((T)dtaxis > dt) dtaxis = zero;
   return false;
 }
 
@@ -637,6 +639,28 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
   R dyrw = ay + ddy * rdt + by * sdt;
   R dzrw = az + ddz * rdt + bz * sdt;
   // jump limiter (:989-1013)
+  if constexpr (sizeof(R) == 4 && !EXP) {
+    // MIXED: the cut step stays in FP32 (rdt = 0.1 rdt) and the simulation
+    // time is corrected once after the loop.  The loop runs with a few
+    // lanes, and every FP64 operation in it would cost a whole warp
+    // instruction on the narrow FP64 pipe.
+    const double dt0 = dt;
+    bool cut = false;
+    while ((fabs(dxrw * iX) > half) || (fabs(dyrw * iY) > half) || (fabs(dzrw * iZ) > half)) {
+      rdt = R(0.1f) * rdt;
+      sdt = sqrt(rdt);
+      advect();
+      dxrw = ax + ddx * rdt + bx * sdt;
+      dyrw = ay + ddy * rdt + by * sdt;
+      dzrw = az + ddz * rdt + bz * sdt;
+      cut = true;
+    }
+    if (cut) {
+      dt = (double)rdt;
+      V.t = (V.t - dt0) + dt;
+      V.reachedMax = false;
+    }
+  } else
   while ((fabs(dxrw * iX) > half) || (fabs(dyrw * iY) > half) || (fabs(dzrw * iZ) > half)) {
     V.t = V.t - dt;
     dt = dtRed * dt;
@@ -742,11 +766,11 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
         }
       } else {
         if (!ret && ((nx > one) || (nx < zero)))
-          ret = quad_axis(nx, x, dX, vx, ddx, bx, 1, 2, dt, dtx, efx, V.exitFace, dt);
+          ret = quad_axis(nx, x, dX, vx, ddx, bx, 1, 2, rdt, dtx, efx, V.exitFace, dt);
         if (!ret && ((ny > one) || (ny < zero)))
-          ret = quad_axis(ny, y, dY, vy, ddy, by, 3, 4, dt, dty, efy, V.exitFace, dt);
+          ret = quad_axis(ny, y, dY, vy, ddy, by, 3, 4, rdt, dty, efy, V.exitFace, dt);
         if (!ret && ((nz > one) || (nz < zero)))
-          ret = quad_axis(nz, z, dZ, vz, ddz, bz, 5, 6, dt, dtz, efz, V.exitFace, dt);
+          ret = quad_axis(nz, z, dZ, vz, ddz, bz, 5, 6, rdt, dtz, efz, V.exitFace, dt);
       }
       if (!ret) {
         if (dtx == zero && dty == zero && dtz == zero) {
