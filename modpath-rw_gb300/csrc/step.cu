@@ -731,7 +731,9 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
       // ExitFaceAndUpdateTimeStep (quadratic, :1576-1892)
       int efx = 0, efy = 0, efz = 0;
       bool ret = false;
-      V.t = V.t - dt;
+      // MIXED takes the time back only when the step changes (below)
+      const double dt_in = dt;
+      if constexpr (sizeof(R) == 8) V.t = V.t - dt;
       if constexpr (sizeof(R) == 8) {
         // FP64: the first iteration takes the warp-wide solves (the same
         // inputs: nothing has moved yet); later ones solve the leaving axes
@@ -774,7 +776,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
       }
       if (!ret) {
         if (dtx == zero && dty == zero && dtz == zero) {
-          V.t = V.t + dt;
+          if constexpr (sizeof(R) == 8) V.t = V.t + dt;
         } else {
           int im = -1;
           R best = zero;
@@ -783,8 +785,16 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
           if (dtz > zero && (im < 0 || dtz < best)) { im = 2; best = dtz; }
           dt = (double)best;
           V.exitFace = (im == 0) ? efx : (im == 1 ? efy : efz);
-          V.t = V.t + dt;
+          if constexpr (sizeof(R) == 8) {
+            V.t = V.t + dt;
+          } else {
+            V.t = (V.t - dt_in) + dt;
+            rdt = best;
+          }
         }
+      } else if constexpr (sizeof(R) == 4) {
+        V.t = V.t - dt_in;
+        rdt = zero;
       }
     }
     if (intLoop > 5) {
@@ -797,7 +807,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
       }
       break;
     }
-    rdt = (R)dt;
+    if constexpr (sizeof(R) == 8 || EXP) rdt = (R)dt;  // MIXED EULERIAN: rdt set above
     sdt = sqrt(rdt);
     advect();
     V.reachedMax = false;
