@@ -5,8 +5,9 @@ code that owns a fixed device-memory budget, or one running where cudaMalloc
 would synchronise the device or is forbidden): its only scratch is a fixed
 array inside the library.  These tests call it through the C ABI on device
 buffers and check that it gives exactly the counts of mprw_histogram, the
-handle-based entry point, with unit masses -- on consecutive calls, so that a
-call never sees what the previous one left in the shared array.  The file is
+handle-based entry point, with unit masses, and exactly the counts of the
+oracle's restatement of the reference's histogram -- on consecutive calls, so
+that a call never sees what the previous one left in the shared array.  The file is
 named so that pytest collects it last; it passes both alone in a fresh process
 (where its first call does the once-per-device set-up) and after every other
 test.
@@ -20,6 +21,8 @@ pytestmark = pytest.mark.gpu
 
 import mprw
 from mprw import workloads as W
+from mprw.model import ACTIVE
+from oracle import gpkde_oracle as GO
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -70,7 +73,10 @@ def test_noalloc_histogram_matches_histogram(gpu_lib):
     try:
         for t0, t1 in ((0.0, 30.0), (30.0, 60.0)):
             tr.advance(t0, t1)
-            dev = _device_particles(tr.get_particles())
+            out = tr.get_particles()
+            dev = _device_particles(out)
+            act = out["status"] == ACTIVE
+            coords = np.stack([out["gx"], out["gy"], out["gz"]], 1)[act]
             # the same grids twice in a row, then a larger grid after a smaller one
             for origin, bins, nb in grids + grids[:1]:
                 ref, ref_binned, _ = tr.histogram(origin, bins, nb)
@@ -78,6 +84,10 @@ def test_noalloc_histogram_matches_histogram(gpu_lib):
                 np.testing.assert_array_equal(got, ref)
                 assert got_binned == ref_binned
                 assert ref_binned > 0
+                # and against the oracle's histogram of the same active particles
+                orc, orc_binned, _ = GO.histogram_weighted(coords, np.ones(coords.shape[0]), origin, bins, nb)
+                np.testing.assert_array_equal(got, orc)
+                assert got_binned == orc_binned
     finally:
         tr.close()
 
