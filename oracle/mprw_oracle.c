@@ -75,6 +75,17 @@ void orc_xoro_seed_stream(int k, uint64_t s[2]) {
   for (int i = 0; i < k; ++i) xoro_jump(s);
 }
 
+/* The streams live for the whole run, as the reference's module state does:
+ * rng_init seeds one stream per OpenMP thread once, in
+ * pr_InitializeRandomWalk (TrackSubCell.F90:613-620, called from
+ * trackingEngine%Initialize), and every tracking interval continues them.
+ * orc_xoro_reset() starts a new run (stream k = base jumped k times again). */
+#define ORC_MAX_THREADS 512
+static uint64_t g_xoro_state[ORC_MAX_THREADS][2];
+static int g_xoro_seeded[ORC_MAX_THREADS];
+
+void orc_xoro_reset(void) { memset(g_xoro_seeded, 0, sizeof g_xoro_seeded); }
+
 /* rng_int64_to_real64, rng_par_zig.f90:67-74 */
 double orc_xoro_uniform(uint64_t s[2]) {
   uint64_t x = orc_xoro_next(s);
@@ -1370,6 +1381,7 @@ int orc_advance(const orc_flow *f, const orc_options *o, int64_t n, int *cell, d
   if (ndim == 0) { grid_free(&g); return -2; }
   int64_t steps_total = 0;
   int nthreads = o->nthreads > 0 ? o->nthreads : 1;
+  if (nthreads > ORC_MAX_THREADS) { grid_free(&g); return -3; }
 #ifdef _OPENMP
 #pragma omp parallel num_threads(nthreads) reduction(+ : steps_total)
 #endif
@@ -1381,7 +1393,15 @@ int orc_advance(const orc_flow *f, const orc_options *o, int64_t n, int *cell, d
     rng_t rng;
     rng.kind = o->rng_kind;
     rng.seed = o->seed;
-    if (o->rng_kind == 0) orc_xoro_seed_stream(tid, rng.xs);
+    if (o->rng_kind == 0) {
+      /* continue this thread's stream of the run (seeded on first use) */
+      if (!g_xoro_seeded[tid]) {
+        orc_xoro_seed_stream(tid, g_xoro_state[tid]);
+        g_xoro_seeded[tid] = 1;
+      }
+      rng.xs[0] = g_xoro_state[tid][0];
+      rng.xs[1] = g_xoro_state[tid][1];
+    }
     /* the reference's particle loop: schedule(dynamic,1) (MPathRW.F90:1207) */
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 1)
@@ -1409,6 +1429,10 @@ int orc_advance(const orc_flow *f, const orc_options *o, int64_t n, int *cell, d
       steps_total += st;
       cell[p] = out.cell; lx[p] = out.x; ly[p] = out.y; lz[p] = out.z; t[p] = out.t;
       status[p] = s;
+    }
+    if (o->rng_kind == 0) {
+      g_xoro_state[tid][0] = rng.xs[0];
+      g_xoro_state[tid][1] = rng.xs[1];
     }
   }
   if (steps_out) *steps_out = steps_total;

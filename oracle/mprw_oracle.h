@@ -96,6 +96,9 @@ int orc_cell_record(const orc_flow *f, const orc_options *o, int cell,
 
 /* RNG restatements (rng_par_zig.f90, TrackSubCell.F90:3631-3663). */
 void     orc_xoro_seed_stream(int k, uint64_t s[2]);      /* base seed jumped k times */
+void     orc_xoro_reset(void);  /* rng_kind 0: start a new run; the thread streams otherwise
+                                   continue across orc_advance calls, as rng_init seeds them
+                                   once per run in the reference (TrackSubCell.F90:613-620) */
 uint64_t orc_xoro_next(uint64_t s[2]);
 double   orc_xoro_uniform(uint64_t s[2]);
 double   orc_xoro_normal_ih12(uint64_t s[2]);

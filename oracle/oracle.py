@@ -69,6 +69,8 @@ def lib() -> C.CDLL:
     L.orc_cell_record.argtypes = [C.POINTER(OrcFlow), C.POINTER(OrcOptions), C.c_int, _dp, _dp, _dp, _dp, _dp,
                                   _ip, _ip]
     L.orc_xoro_seed_stream.argtypes = [C.c_int, _up]
+    L.orc_xoro_reset.restype = None
+    L.orc_xoro_reset.argtypes = []
     L.orc_xoro_next.restype = C.c_uint64
     L.orc_xoro_next.argtypes = [_up]
     L.orc_xoro_uniform.restype = C.c_double
@@ -126,8 +128,19 @@ class _Inputs:
         self.o = o
 
 
+def reset_xoroshiro():
+    """Start a new run of the reference's RNG: the xoroshiro128+ thread streams
+    (rng_kind RNG_XOROSHIRO) are seeded again on their next use.  Otherwise
+    they continue across advance() calls, as the reference seeds them once per
+    run (TrackSubCell.F90:613-620) and every tracking interval draws on."""
+    lib().orc_xoro_reset()
+
+
 def advance(grid, flow, opt, particles, t_begin, t_end, rng_kind=RNG_PHILOX, nthreads=1):
-    """Advance a copy of ``particles``; returns (particles, particle_steps)."""
+    """Advance a copy of ``particles``; returns (particles, particle_steps).
+    With RNG_XOROSHIRO the thread streams continue from the previous call
+    (reset_xoroshiro() starts a new run); with nthreads=1 the result is the
+    reference's single-threaded run, deterministic."""
     L = lib()
     inp = _Inputs(grid, flow, opt, rng_kind, nthreads)
     p = particles.copy()

@@ -1,12 +1,23 @@
 """Config 1 on the GPU against the analytic 1-D Gaussian solution of the
 advection-dispersion equation (v = 1 m/d, D = alphaL v = 0.1 m2/d, pulse at
-x = 10 m): the GPKDE concentrations on the 1 m grid at 25, 50 and 100 days,
-in FP64 and MIXED.  Particles expected per bin: N (Phi((x+1-mu)/s) -
-Phi((x-mu)/s)), mu = 10 + v t, s^2 = 2 D t.  The scheme's interface-forcing
-exit time biases the mean drift slightly (-0.25 m at 100 days, also in the
-oracle), hence the tolerances on the moments; the profile's L1 distance
-holds the GPKDE smoothing and the sampling noise of 1e5 particles."""
+x = 10 m), with the scheme's own bias measured and pinned.
+
+The analytic plume has mean 10 + v t and variance 2 D t.  The reference's
+random walk departs from it by a bias of the scheme itself (the exit time
+that forces a step onto a cell face, TrackSubCell.F90:1025-1316, and the
+Irwin-Hall normals): measured on the oracle with the reference's own RNG at
+1,000,000 particles (tests/golden/mc_uniform_pulse.npz), the mean lags by
+0.024, 0.100 and 0.252 m at 25, 50 and 100 days and the variance is 4.3 %
+low (Monte-Carlo standard errors 0.002-0.004 m and 0.14 %).  The GPU (1e5
+particles, FP64 and MIXED) must reproduce that biased plume within 4.5
+combined standard errors -- about 0.065 m on the mean and 2 % on the
+variance at 100 days -- and the bias itself must stand out against those
+errors.  On the GPKDE concentrations on the 1 m grid: mass conserved, the
+L1 distance of the profile from the analytic one below 10 % of the mass
+(the scheme's bias, the smoothing and the sampling noise), the
+reconstructed variance within 25 % (the kernel widens it)."""
 import math
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -16,6 +27,9 @@ pytestmark = pytest.mark.gpu
 import mprw
 from mprw import workloads as W
 from mprw.model import FP64, MIXED
+
+FIXTURE = Path(__file__).resolve().parent / "golden" / "mc_uniform_pulse.npz"
+Z = 4.5
 
 
 def _expected(n, t, nx=200, x0=10.0, v=1.0, d=0.1):
@@ -27,27 +41,39 @@ def _expected(n, t, nx=200, x0=10.0, v=1.0, d=0.1):
 
 @pytest.mark.parametrize("precision", [FP64, MIXED])
 def test_uniform_pulse_concentrations_match_the_gaussian(gpu_lib, precision):
+    fx = np.load(FIXTURE)
     g, f, p, opt = W.uniform_pulse(n_particles=100_000, precision=precision)
     tr = mprw.Tracker(g, opt)
     tr.load_flow(f)
     tr.set_particles(p)
     t = 0.0
     centres = np.arange(200) + 0.5
-    for t_out in (25.0, 50.0, 100.0):
+    for k, t_out in enumerate((25.0, 50.0, 100.0)):
         tr.advance(t, t_out)
         t = t_out
+        ref, mu, var = _expected(p.n, t_out)
+        # the particles: the oracle's biased plume, within Monte-Carlo bounds
+        x = tr.get_particles()["gx"]
+        n1, m1, v1 = x.size, float(x.mean()), float(x.var())
+        m41 = float(((x - m1) ** 4).mean())
+        n2, m2, v2 = int(fx[f"t{k}_n"]), float(fx[f"t{k}_mean_x"]), float(fx[f"t{k}_var_x"])
+        m42 = float(fx[f"t{k}_m4_x"])
+        se_m = math.sqrt(v1 / n1 + v2 / n2)
+        se_v = math.sqrt((m41 - v1 * v1) / n1 + (m42 - v2 * v2) / n2)
+        assert abs(m1 - m2) < Z * se_m, (t_out, m1, m2, se_m)
+        assert abs(v1 - v2) < Z * se_v, (t_out, v1, v2, se_v)
+        # the scheme's bias is real: the oracle's plume lags the analytic mean and
+        # is narrower than 2 D t by many standard errors of the oracle sample
+        if t_out == 100.0:
+            assert mu - m2 > 20 * math.sqrt(v2 / n2)
+            assert var - v2 > 20 * math.sqrt((m42 - v2 * v2) / n2)
+        # the reconstruction
         dens, hist, loops = tr.gpkde((200.0, 1.0, 1.0), (1.0, 1.0, 1.0), precision=precision)
         c = dens.reshape(-1)                       # particles per bin (unit volume x bin volume)
-        ref, mu, var = _expected(p.n, t_out)
         assert abs(c.sum() - p.n) < 1e-6 * p.n     # mass
         m = (c * centres).sum() / c.sum()
         v = (c * (centres - m) ** 2).sum() / c.sum()
-        assert abs(m - mu) < 0.5
-        # the reconstruction widens the plume by its kernel: compare the raw
-        # histogram's variance with the analytic one, the density's within 25 %
-        h = hist.reshape(-1)
-        vh = (h * (centres - (h * centres).sum() / h.sum()) ** 2).sum() / h.sum() - 1.0 / 12.0
-        assert abs(vh - var) / var < 0.12
+        assert abs(m - m1) < 1e-2
         assert abs(v - var) / var < 0.25
         assert np.abs(c - ref).sum() / p.n < 0.10
     tr.close()

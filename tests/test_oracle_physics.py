@@ -47,15 +47,33 @@ def test_pure_advection_exact():
 
 
 def test_analytic_gaussian_uniform_pulse():
-    n = 6000
+    """The oracle on the reference's RNG path (xoroshiro128+ thread streams,
+    8 threads, 20,000 particles) against its 1,000,000-particle single-thread
+    run (tests/golden/mc_uniform_pulse.npz): two samples of one process, within
+    Monte-Carlo bounds (tests/mc_stats.py) at 25 and 50 days.  Against the
+    analytic Gaussian the scheme is biased: the mean lags by 0.10 m at
+    50 days and the variance is 4.3 % low, and both stand out against the
+    large run's standard errors."""
+    import math
+    from pathlib import Path
+
+    import mc_stats as S
+    fx = np.load(Path(__file__).resolve().parent / "golden" / "mc_uniform_pulse.npz")
+    n = 20000
     g, f, p, opt = W.uniform_pulse(n_particles=n)
-    q, _ = O.advance(g, f, opt, p, 0.0, 50.0, rng_kind=O.RNG_PHILOX, nthreads=8)
-    gx, _, _ = O.global_xyz(g, f, q)
+    O.reset_xoroshiro()
+    q = p
+    for k, (a, b) in enumerate([(0.0, 25.0), (25.0, 50.0)]):
+        q, _ = O.advance(g, f, opt, q, a, b, rng_kind=O.RNG_XOROSHIRO, nthreads=8)
+        gx, gy, gz = O.global_xyz(g, f, q)
+        assert np.all(q.status == ACTIVE)
+        got = S.summarize(q.status, gx, gy, gz, q.t, np.arange(201, dtype=np.float64))
+        bad = S.compare(got, S.from_npz(fx, f"t{k}_"), f"interval {k}")
+        assert not bad, bad
+    m, v, big = float(fx["t1_mean_x"]), float(fx["t1_var_x"]), int(fx["t1_n"])
     mean, var = 10.0 + 50.0, 2.0 * 0.1 * 1.0 * 50.0
-    assert np.all(q.status == ACTIVE)
-    # the scheme's interface forcing biases the drift by a few tenths of a metre
-    assert abs(gx.mean() - mean) < 0.5
-    assert abs(gx.var() - var) / var < 0.12
+    assert -0.15 < m - mean < -0.05 and (mean - m) > 20 * math.sqrt(v / big)
+    assert -0.06 < (v - var) / var < -0.03
 
 
 def test_release_and_status_logic():

@@ -122,3 +122,25 @@ def test_ih12_moments():
     assert abs(vals.mean()) < 0.03
     assert abs(vals.var() - 1.0) < 0.04
     assert vals.min() > -6 and vals.max() < 6
+
+
+def test_xoroshiro_streams_continue_across_intervals():
+    """The reference seeds its thread streams once per run (rng_init in
+    pr_InitializeRandomWalk, TrackSubCell.F90:613-620) and every tracking
+    interval continues them: two intervals of one run draw different numbers,
+    and a single-threaded run is deterministic."""
+    from mprw import workloads as W
+    g, f, p, opt = W.uniform_pulse(n_particles=50)
+
+    def run(reset_between):
+        O.reset_xoroshiro()
+        q, _ = O.advance(g, f, opt, p, 0.0, 5.0, rng_kind=O.RNG_XOROSHIRO, nthreads=1)
+        if reset_between:
+            O.reset_xoroshiro()
+        q, _ = O.advance(g, f, opt, q, 5.0, 10.0, rng_kind=O.RNG_XOROSHIRO, nthreads=1)
+        return q
+
+    a, b, c = run(False), run(False), run(True)
+    assert np.array_equal(a.lx, b.lx) and np.array_equal(a.cell, b.cell)
+    # restarting the streams replays the first interval's draws: another trajectory
+    assert not np.array_equal(a.lx, c.lx)
