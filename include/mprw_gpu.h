@@ -177,19 +177,54 @@ typedef struct {
   int32_t precision;           /* MPRW_FP64 (the reference's arithmetic) or    */
                                /* MPRW_MIXED (FP32 smoothing passes and        */
                                /* per-bin updates, FP64 convergence sums)      */
+  int32_t isotropic;           /* gpkdeIsotropicKernels (0 = anisotropic, the  */
+                               /* default; ModpathSimulationData.f90:1065-1075)*/
 } mprw_gpkde_options;
 
 /* GPKDE reconstruction of the ACTIVE particles (weights = particle masses).
  * Replaces gpkde%ComputeDensity (GridProjectedKDE.F90:3598-4392) with the
  * kernel database on, bounded kernel sizes, Kish effective weights and
- * anisotropic kernels, for 1-D and 3-D grids (a grid whose three
- * dimensions all have more than one bin, or exactly one).
+ * anisotropic (or, with isotropic != 0, isotropic) kernels, for 1-D, 2-D
+ * and 3-D grids (the dimensions with more than one bin are active).
  * density: nx*ny*nz doubles, x fastest (nx = int(domain/bin + 0.5)),
  * scaled as the reference exports it (x binVolume if unit_volume, x
  * scaling_factor); histogram (may be NULL): mass per bin; n_bins_out (may be
  * NULL): the grid; loops_done (may be NULL): optimisation loops run. */
 int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *opt, double *density, double *histogram,
                int32_t n_bins_out[3], int32_t *loops_done);
+
+/* Reconstruction from histograms summed over several trackers: the
+ * collective of a multi-GPU run.  The reference reconstructs from all
+ * particles at once (ComputeDensity on the active particles gathered at
+ * MPathRW.F90:1568-1624); when the particles are split over trackers (one per
+ * GPU), each bins its own particles and the reconstruction needs only
+ * summable quantities: the mass per bin and the sums below.  Summed over the
+ * trackers (an all-reduce) they give exactly the histogram, effective mass
+ * (Histogram.F90:276-350) and coordinate statistics (GridProjectedKDE.F90:
+ * 4023-4030) that mprw_gpkde computes from all particles, up to the rounding
+ * of the sums.
+ *   mprw_gpkde_partial      this tracker's part on the options' grid:
+ *                           mass_per_bin (prod n_bins doubles, host, x
+ *                           fastest: the summed masses of its ACTIVE
+ *                           particles per bin) and sums
+ *   mprw_gpkde_from_counts  the reconstruction of mprw_gpkde from summed
+ *                           parts (host arrays): the same outputs; it uses
+ *                           the handle's device memory and stream, not its
+ *                           particles (any handle of the run may do it)
+ * The coordinate sums are taken about the domain centre origin +
+ * domain_size/2 of the options, so every tracker must use the same options. */
+typedef struct {
+  double n_active;   /* ACTIVE particles                                   */
+  double sum_w;      /* sum of their masses                                */
+  double sum_w2;     /* sum of their squared masses                        */
+  double sum_dx[3];  /* sum of (model coordinate - domain centre)          */
+  double sum_dx2[3]; /* sum of (model coordinate - domain centre)^2        */
+} mprw_gpkde_sums;
+
+int mprw_gpkde_partial(mprw_handle *h, const mprw_gpkde_options *opt, double *mass_per_bin, mprw_gpkde_sums *sums);
+int mprw_gpkde_from_counts(mprw_handle *h, const mprw_gpkde_options *opt, const double *mass_per_bin,
+                           const mprw_gpkde_sums *sums, double *density, double *histogram, int32_t n_bins_out[3],
+                           int32_t *loops_done);
 
 /* Observation cells (TrackingOptions%isObservation / idObservation;
  * Observation.f90:7-60).  cells[i] (1-based) belongs to observation obs[i]
@@ -288,21 +323,24 @@ int mprw_gpkde_series(const double *times, const double *weights, int64_t n, con
  * device or is forbidden.  It needs no handle and calls no cudaMalloc,
  * cudaFree or allocating library routine.
  *
- * All pointers are DEVICE pointers: gx/gy/gz are model coordinates (as
- * mprw_get_particles returns them), status the particle statuses; only
- * ACTIVE (1) particles are counted.  counts (prod n_bins doubles, x fastest)
- * receives the particle count per bin, identical to mprw_histogram's with
- * unit masses; n_binned (one int64, may be NULL) the particles binned.  The
- * work is queued on `stream` (a cudaStream_t, NULL = the default stream) and
- * the call returns without waiting for it.
+ * gx, gy, gz, status, counts and n_binned are DEVICE pointers: gx/gy/gz are
+ * model coordinates (as mprw_get_particles returns them), status the particle
+ * statuses; only ACTIVE (1) particles are counted.  counts (prod n_bins
+ * doubles, x fastest) receives the particle count per bin, identical to
+ * mprw_histogram's with unit masses; n_binned (one int64, may be NULL) the
+ * particles binned.  origin, bin_size and n_bins are HOST arrays of 3, read
+ * during the call.  The work is queued on `stream` (a cudaStream_t, NULL =
+ * the default stream) and the call returns without waiting for it.
  *
- * Limit: prod(n_bins) <= MPRW_NOALLOC_MAX_BINS, else MPRW_E_INVAL.  The
- * scratch (MPRW_NOALLOC_MAX_BINS + 2 32-bit words, about 4 MiB) is a fixed
- * array in the library's device image that every GPU loading the library
- * holds until the process exits.  The first call on each device looks up the
- * array's device address (with that device current), so make that first
- * call before any stream capture.  All calls share the array and each clears
- * it before counting; calls that overlap on the GPU race on it. */
+ * Limits: prod(n_bins) <= MPRW_NOALLOC_MAX_BINS and n < 2^32 (the bin
+ * counters are 32-bit), else MPRW_E_INVAL.  The scratch
+ * (MPRW_NOALLOC_MAX_BINS 32-bit bin counters plus a 64-bit binned-particle
+ * counter, about 4 MiB) is a fixed array in the library's device image that
+ * every GPU loading the library holds until the process exits.  The first
+ * call on each device (and the first after a device reset) looks up the
+ * array's device address in the current context, so make that first call
+ * before any stream capture.  All calls share the array and each clears it
+ * before counting; calls that overlap on the GPU race on it. */
 #define MPRW_NOALLOC_MAX_BINS (1 << 20)
 int mprw_histogram_noalloc(const double *gx, const double *gy, const double *gz, const int32_t *status,
                            int64_t n, const double origin[3], const double bin_size[3],

@@ -1077,10 +1077,25 @@ int mprw_get_particles(mprw_handle *h, int32_t *cell, double *lx, double *ly, do
 
 namespace {
 
+// h->d_counts holds at least nbins doubles (and nbins 32-bit counters after them)
+int ensure_counts(mprw_handle *h, int64_t nbins) {
+  if (nbins > h->counts_cap) {
+    if (h->d_counts) cudaFree(h->d_counts);
+    h->d_counts = nullptr;
+    h->counts_cap = 0;
+    CK(cudaMalloc(&h->d_counts, sizeof(double) * nbins + sizeof(unsigned int) * nbins));
+    h->counts_cap = nbins;
+  }
+  return MPRW_OK;
+}
+
 // Histogram of the active particles into h->d_counts (counts / effMass, the
-// reference's histogram%counts after ComputeCountsWeighted).
+// reference's histogram%counts after ComputeCountsWeighted; with raw, the
+// mass per bin, not divided).  wsums (may be NULL) receives the sum of the
+// weights and of their squares that the effective mass comes from (NaN for
+// unit masses, whose effective mass is 1).
 int histogram_device(mprw_handle *h, const double origin[3], const double bin_size[3], const int32_t n_bins[3],
-                     int64_t *n_binned, double *eff_mass, double *n_active) {
+                     int64_t *n_binned, double *eff_mass, double *wsums, bool raw = false) {
   int64_t nbins = 1;
   HistArgs a{};
   for (int d = 0; d < 3; ++d) {
@@ -1096,13 +1111,7 @@ int histogram_device(mprw_handle *h, const double origin[3], const double bin_si
   if (nbins > ((int64_t)1 << 31)) return fail(h, MPRW_E_INVAL, "histogram: too many bins");
   cudaStream_t s = h->stream;
   const int64_t n = h->n;
-  if (nbins > h->counts_cap) {
-    if (h->d_counts) cudaFree(h->d_counts);
-    h->d_counts = nullptr;
-    h->counts_cap = 0;
-    CK(cudaMalloc(&h->d_counts, sizeof(double) * nbins + sizeof(unsigned int) * nbins));
-    h->counts_cap = nbins;
-  }
+  if (ensure_counts(h, nbins) != MPRW_OK) return MPRW_E_OOM;
   a.geo = geometry(h);
   a.n = n;
   a.cell = h->d_cell;
@@ -1139,8 +1148,10 @@ int histogram_device(mprw_handle *h, const double origin[3], const double bin_si
     if (e == cudaSuccess && total != 0.0) {
       double neff = total * total / sw2;  // Kish (Histogram.F90:338-340)
       eff = total / neff;
-      div_kernel<<<grid1d(nbins), 256, 0, s>>>(h->d_counts, nbins, eff);
-      e = cudaGetLastError();
+      if (!raw) {
+        div_kernel<<<grid1d(nbins), 256, 0, s>>>(h->d_counts, nbins, eff);
+        e = cudaGetLastError();
+      }
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaFree(tmp);
@@ -1150,7 +1161,10 @@ int histogram_device(mprw_handle *h, const double origin[3], const double bin_si
   }
   if (n_binned) *n_binned = nb_out;
   if (eff_mass) *eff_mass = eff;
-  (void)n_active;
+  if (wsums) {
+    wsums[0] = h->unit_mass ? NAN : total;
+    wsums[1] = h->unit_mass ? NAN : sw2;
+  }
   return MPRW_OK;
 }
 
@@ -1179,33 +1193,39 @@ int mprw_histogram(mprw_handle *h, const double origin[3], const double bin_size
   return MPRW_OK;
 }
 
-int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, double *histogram,
-               int32_t n_bins_out[3], int32_t *loops_done) {
-  NvtxRange nvtx_("mprw_gpkde");
-  if (!h) return MPRW_E_INVAL;
-  if (!h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_gpkde on a batch: use a member view");
-  if (!o || !density) return fail(h, MPRW_E_INVAL, "mprw_gpkde: null argument");
-  // prInitialize (GridProjectedKDE.F90:354-998)
-  KdeParams P{};
-  int32_t nb[3];
+}  // extern "C"
+
+namespace {
+
+// The constants of a reconstruction grid from its options: prInitialize
+// (GridProjectedKDE.F90:354-998), the kernel database (prInitializeKernel-
+// DatabaseFlat, prGenerateLogSpaceData) and the kernel-size bounds.  Returns
+// MPRW_OK, or the failure recorded on h.
+int gpkde_params(mprw_handle *h, const mprw_gpkde_options *o, const char *who, KdeParams &P, int32_t nb[3]) {
+  P = KdeParams{};
   for (int d = 0; d < 3; ++d) {
-    if (o->bin_size[d] < 0.0 || o->domain_size[d] < 0.0) return fail(h, MPRW_E_INVAL, "mprw_gpkde: negative size");
+    if (o->bin_size[d] < 0.0 || o->domain_size[d] < 0.0) return fail(h, MPRW_E_INVAL, std::string(who) + ": negative size");
     nb[d] = (o->bin_size[d] != 0.0) ? (int32_t)(o->domain_size[d] / o->bin_size[d] + 0.5) : 1;
-    if (nb[d] < 1) return fail(h, MPRW_E_INVAL, "mprw_gpkde: grid size < 1");
+    if (nb[d] < 1) return fail(h, MPRW_E_INVAL, std::string(who) + ": grid size < 1");
     P.nb[d] = nb[d];
     P.bin[d] = o->bin_size[d];
     P.mask[d] = (nb[d] != 1) ? 1 : 0;
   }
   P.ndim = P.mask[0] + P.mask[1] + P.mask[2];
-  if (P.ndim != 1 && P.ndim != 3)
-    return fail(h, MPRW_E_INVAL, "mprw_gpkde: only 1-D and 3-D reconstruction grids are supported");
+  if (P.ndim < 1) return fail(h, MPRW_E_INVAL, std::string(who) + ": the grid has no dimension with more than one bin");
+  // idDim1 < idDim2: the active dimensions of a 2-D grid (GridProjectedKDE.F90 prInitialize)
+  P.d1 = P.d2 = -1;
+  for (int d = 0; d < 3; ++d)
+    if (P.mask[d]) {
+      if (P.d1 < 0) P.d1 = d;
+      else if (P.d2 < 0) P.d2 = d;
+    }
+  if (o->isotropic != 0 && o->isotropic != 1) return fail(h, MPRW_E_INVAL, std::string(who) + ": isotropic must be 0 or 1");
+  P.isotropic = o->isotropic;
   if (!(o->min_hover_delta > 0.0) || !(o->max_hover_delta > o->min_hover_delta) || !(o->delta_hover_delta > 0.0))
-    return fail(h, MPRW_E_INVAL, "mprw_gpkde: invalid kernel database parameters");
+    return fail(h, MPRW_E_INVAL, std::string(who) + ": invalid kernel database parameters");
   if (o->precision != MPRW_FP64 && o->precision != MPRW_MIXED)
-    return fail(h, MPRW_E_INVAL, "mprw_gpkde: precision");
-  const int fp32 = o->precision == MPRW_MIXED;
-  if (n_bins_out)
-    for (int d = 0; d < 3; ++d) n_bins_out[d] = nb[d];
+    return fail(h, MPRW_E_INVAL, std::string(who) + ": precision");
   double binvol = 1.0;
   int hd = 0;
   for (int d = 0; d < 3; ++d)
@@ -1230,7 +1250,7 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
   // logarithmic database (prInitializeKernelDatabaseFlat, prGenerateLogSpaceData)
   const int ndelta = (int)std::ceil(std::log10(o->max_hover_delta / o->min_hover_delta) /
                                     std::log10(1 + o->delta_hover_delta)) + 1;
-  if (ndelta > KDE_MAXDB || ndelta < 2) return fail(h, MPRW_E_INVAL, "mprw_gpkde: kernel database too large");
+  if (ndelta > KDE_MAXDB || ndelta < 2) return fail(h, MPRW_E_INVAL, std::string(who) + ": kernel database too large");
   P.ndelta = ndelta;
   {
     const double li = std::log10(o->min_hover_delta), le = std::log10(o->max_hover_delta);
@@ -1241,7 +1261,7 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
       acc = acc + de;
     }
   }
-  if (o->max_hover_delta * 4 * 2 + 1 > KDE_MAXLEN) return fail(h, MPRW_E_INVAL, "mprw_gpkde: maxHOverDelta too large");
+  if (o->max_hover_delta * 4 * 2 + 1 > KDE_MAXLEN) return fail(h, MPRW_E_INVAL, std::string(who) + ": maxHOverDelta too large");
   P.min_hod = o->min_hover_delta;
   P.dlog = std::log(P.hod[1] / P.hod[0]);
   // bounded kernel sizes (boundKernelSizeFormat 0)
@@ -1257,51 +1277,45 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
     if (P.max_k[d] > 0.0 && (maxd < 0 || P.max_k[d] < P.max_k[maxd])) maxd = d;
   for (int d = 0; d < 3; ++d)
     if (P.min_k[d] > 0.0 && (mind < 0 || P.min_k[d] > P.min_k[mind])) mind = d;
-  if (maxd < 0 || mind < 0) return fail(h, MPRW_E_INVAL, "mprw_gpkde: grid too small for bounded kernels");
+  if (maxd < 0 || mind < 0) return fail(h, MPRW_E_INVAL, std::string(who) + ": grid too small for bounded kernels");
   P.max_dim = maxd;
   P.min_dim = mind;
+  return MPRW_OK;
+}
 
+// Sums over the ACTIVE particles' model coordinates, fixed-order per block
+// and summed on the host in block order: pass 0 the coordinates and the
+// count, pass 2 the coordinates minus m and the count, pass 1 the squares of
+// the coordinates minus m (acc[3] unused).
+int coord_sums(mprw_handle *h, int pass, const double m[3], double acc[4]) {
   cudaStream_t s = h->stream;
-  h->launches = 0;
-  h->kdep->launches = 0;
-  CK(cudaEventRecord(h->ev2, s));
-  // histogram (counts / effective mass)
-  int64_t nbinned = 0;
-  double eff = 1.0;
-  int rc = histogram_device(h, o->origin, o->bin_size, nb, &nbinned, &eff, nullptr);
-  if (rc != MPRW_OK) return rc;
+  if (!h->d_kpart) CK(cudaMalloc(&h->d_kpart, sizeof(double) * 4 * 152 * 4));
+  int nblk = 0;
+  const double zero[3] = {0, 0, 0};
+  CK(launch_coord_sums(geometry(h), h->n, h->d_cell, h->d_status, h->d_x, h->d_y, h->d_z,
+                       h->opt.precision == MPRW_MIXED, pass, m ? m : zero, h->d_kpart, &nblk, s));
+  std::vector<double> part(4 * (size_t)nblk);
+  CK(cudaMemcpyAsync(part.data(), h->d_kpart, sizeof(double) * 4 * nblk, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int k = 0; k < 4; ++k) acc[k] = 0.0;
+  for (int i = 0; i < nblk; ++i)
+    for (int k = 0; k < 4; ++k) acc[k] += part[4 * i + k];
+  h->launches += 1;
+  return MPRW_OK;
+}
+
+// The reconstruction from the histogram in h->d_counts (counts / effMass,
+// the grid of P) and the statistics of the reconstructed points (standard
+// deviation per dimension, their number npts): active bins, factor tables,
+// the optimisation loop, the exported density and, when asked, the
+// histogram (mass per bin) to the host.  The caller has recorded h->ev2.
+int gpkde_reconstruct(mprw_handle *h, const mprw_gpkde_options *o, KdeParams &P, const int32_t nb[3], double eff,
+                      const double sd[3], double npts, double *density, double *histogram, int32_t *loops_done) {
+  cudaStream_t s = h->stream;
+  const int fp32 = o->precision == MPRW_MIXED;
   const int64_t ngrid = (int64_t)nb[0] * nb[1] * nb[2];
-  // statistics of the active particles' coordinates (GridProjectedKDE.F90:4023-4030)
-  CK(h->kdep->ensure_grid(ngrid));
-  double mean[3] = {0, 0, 0}, sd[3] = {0, 0, 0}, npts = 0.0;
-  {
-    std::vector<double> part;
-    int nblk = 0;
-    if (!h->d_kpart) CK(cudaMalloc(&h->d_kpart, sizeof(double) * 4 * 152 * 4));
-    double *dpart = h->d_kpart;
-    cudaError_t e = launch_coord_sums(geometry(h), h->n, h->d_cell, h->d_status, h->d_x, h->d_y, h->d_z,
-                                      h->opt.precision == MPRW_MIXED, 0, mean, dpart, &nblk, s);
-    part.resize(4 * nblk);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), dpart, sizeof(double) * 4 * nblk, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    double acc[4] = {0, 0, 0, 0};
-    for (int i = 0; i < nblk && e == cudaSuccess; ++i)
-      for (int k = 0; k < 4; ++k) acc[k] += part[4 * i + k];
-    npts = acc[3];
-    if (npts > 0)
-      for (int d = 0; d < 3; ++d) mean[d] = acc[d] / npts;
-    if (e == cudaSuccess)
-      e = launch_coord_sums(geometry(h), h->n, h->d_cell, h->d_status, h->d_x, h->d_y, h->d_z,
-                            h->opt.precision == MPRW_MIXED, 1, mean, dpart, &nblk, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), dpart, sizeof(double) * 4 * nblk, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    double sq[3] = {0, 0, 0};
-    for (int i = 0; i < nblk && e == cudaSuccess; ++i)
-      for (int k = 0; k < 3; ++k) sq[k] += part[4 * i + k];
-    for (int d = 0; d < 3; ++d) sd[d] = (P.mask[d] && npts > 0) ? std::sqrt(sq[d] / npts) : 0.0;
-    h->launches += 2;
-    CK(e);
-  }
+  const double nd = (double)P.ndim;
+  double binvol = P.binvol;
   // active bins
   int nactive = 0;
   CK(kde_collect_active(*h->kdep, P, h->d_counts, s, &nactive));
@@ -1390,6 +1404,128 @@ int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, dou
   h->launches += h->kdep->launches + 2;
   if (loops_done) *loops_done = loops;
   return MPRW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+
+int mprw_gpkde(mprw_handle *h, const mprw_gpkde_options *o, double *density, double *histogram,
+               int32_t n_bins_out[3], int32_t *loops_done) {
+  NvtxRange nvtx_("mprw_gpkde");
+  if (!h) return MPRW_E_INVAL;
+  if (!h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_gpkde on a batch: use a member view");
+  if (!o || !density) return fail(h, MPRW_E_INVAL, "mprw_gpkde: null argument");
+  KdeParams P;
+  int32_t nb[3];
+  int rc = gpkde_params(h, o, "mprw_gpkde", P, nb);
+  if (rc != MPRW_OK) return rc;
+  if (n_bins_out)
+    for (int d = 0; d < 3; ++d) n_bins_out[d] = nb[d];
+  cudaStream_t s = h->stream;
+  h->launches = 0;
+  h->kdep->launches = 0;
+  CK(cudaEventRecord(h->ev2, s));
+  // histogram (counts / effective mass)
+  int64_t nbinned = 0;
+  double eff = 1.0;
+  rc = histogram_device(h, o->origin, o->bin_size, nb, &nbinned, &eff, nullptr);
+  if (rc != MPRW_OK) return rc;
+  const int64_t ngrid = (int64_t)nb[0] * nb[1] * nb[2];
+  // statistics of the active particles' coordinates (GridProjectedKDE.F90:4023-4030)
+  CK(h->kdep->ensure_grid(ngrid));
+  double mean[3] = {0, 0, 0}, sd[3] = {0, 0, 0}, acc[4];
+  rc = coord_sums(h, 0, nullptr, acc);
+  if (rc != MPRW_OK) return rc;
+  const double npts = acc[3];
+  if (npts > 0)
+    for (int d = 0; d < 3; ++d) mean[d] = acc[d] / npts;
+  rc = coord_sums(h, 1, mean, acc);
+  if (rc != MPRW_OK) return rc;
+  for (int d = 0; d < 3; ++d) sd[d] = (P.mask[d] && npts > 0) ? std::sqrt(acc[d] / npts) : 0.0;
+  return gpkde_reconstruct(h, o, P, nb, eff, sd, npts, density, histogram, loops_done);
+}
+
+int mprw_gpkde_partial(mprw_handle *h, const mprw_gpkde_options *o, double *mass_per_bin, mprw_gpkde_sums *sums) {
+  NvtxRange nvtx_("mprw_gpkde_partial");
+  if (!h) return MPRW_E_INVAL;
+  if (!h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_gpkde_partial on a batch: use a member view");
+  if (!o || !mass_per_bin || !sums) return fail(h, MPRW_E_INVAL, "mprw_gpkde_partial: null argument");
+  KdeParams P;
+  int32_t nb[3];
+  int rc = gpkde_params(h, o, "mprw_gpkde_partial", P, nb);
+  if (rc != MPRW_OK) return rc;
+  cudaStream_t s = h->stream;
+  h->launches = 0;
+  double wsums[2];
+  rc = histogram_device(h, o->origin, o->bin_size, nb, nullptr, nullptr, wsums, true);
+  if (rc != MPRW_OK) return rc;
+  const int64_t ngrid = (int64_t)nb[0] * nb[1] * nb[2];
+  CK(cudaMemcpyAsync(mass_per_bin, h->d_counts, sizeof(double) * ngrid, cudaMemcpyDeviceToHost, s));
+  double c[3], acc[4];
+  for (int d = 0; d < 3; ++d) c[d] = o->origin[d] + 0.5 * o->domain_size[d];
+  rc = coord_sums(h, 2, c, acc);
+  if (rc != MPRW_OK) return rc;
+  sums->n_active = acc[3];
+  for (int d = 0; d < 3; ++d) sums->sum_dx[d] = acc[d];
+  rc = coord_sums(h, 1, c, acc);
+  if (rc != MPRW_OK) return rc;
+  for (int d = 0; d < 3; ++d) sums->sum_dx2[d] = acc[d];
+  // unit masses: the weights are the particles themselves
+  sums->sum_w = h->unit_mass ? sums->n_active : wsums[0];
+  sums->sum_w2 = h->unit_mass ? sums->n_active : wsums[1];
+  CK(cudaStreamSynchronize(s));
+  return MPRW_OK;
+}
+
+int mprw_gpkde_from_counts(mprw_handle *h, const mprw_gpkde_options *o, const double *mass_per_bin,
+                           const mprw_gpkde_sums *sums, double *density, double *histogram, int32_t n_bins_out[3],
+                           int32_t *loops_done) {
+  NvtxRange nvtx_("mprw_gpkde_from_counts");
+  if (!h) return MPRW_E_INVAL;
+  if (!h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_gpkde_from_counts on a batch: use a member view");
+  if (!o || !mass_per_bin || !sums || !density) return fail(h, MPRW_E_INVAL, "mprw_gpkde_from_counts: null argument");
+  KdeParams P;
+  int32_t nb[3];
+  int rc = gpkde_params(h, o, "mprw_gpkde_from_counts", P, nb);
+  if (rc != MPRW_OK) return rc;
+  const double n = sums->n_active;
+  if (!(n >= 0.0) || !std::isfinite(n) || !(sums->sum_w2 >= 0.0) || !std::isfinite(sums->sum_w) ||
+      !std::isfinite(sums->sum_w2))
+    return fail(h, MPRW_E_INVAL, "mprw_gpkde_from_counts: invalid sums");
+  for (int d = 0; d < 3; ++d)
+    if (!std::isfinite(sums->sum_dx[d]) || !std::isfinite(sums->sum_dx2[d]))
+      return fail(h, MPRW_E_INVAL, "mprw_gpkde_from_counts: invalid sums");
+  if (n_bins_out)
+    for (int d = 0; d < 3; ++d) n_bins_out[d] = nb[d];
+  cudaStream_t s = h->stream;
+  h->launches = 0;
+  h->kdep->launches = 0;
+  CK(cudaEventRecord(h->ev2, s));
+  const int64_t ngrid = (int64_t)nb[0] * nb[1] * nb[2];
+  if (ensure_counts(h, ngrid) != MPRW_OK) return fail(h, MPRW_E_OOM, "mprw_gpkde_from_counts: device memory");
+  CK(h->kdep->ensure_grid(ngrid));
+  CK(cudaMemcpyAsync(h->d_counts, mass_per_bin, sizeof(double) * ngrid, cudaMemcpyHostToDevice, s));
+  // Kish effective mass of the summed weights (Histogram.F90:338-340); the
+  // mass per bin becomes histogram%counts
+  double eff = 1.0;
+  if (sums->sum_w != 0.0 && sums->sum_w2 != sums->sum_w) {
+    const double neff = sums->sum_w * sums->sum_w / sums->sum_w2;
+    eff = sums->sum_w / neff;
+    div_kernel<<<grid1d(ngrid), 256, 0, s>>>(h->d_counts, ngrid, eff);
+    CK(cudaGetLastError());
+    h->launches += 1;
+  }
+  // mean and standard deviation from the sums about the domain centre
+  double sd[3] = {0, 0, 0};
+  for (int d = 0; d < 3; ++d) {
+    if (!P.mask[d] || n <= 0.0) continue;
+    const double m = sums->sum_dx[d] / n;
+    const double v = sums->sum_dx2[d] / n - m * m;
+    sd[d] = v > 0.0 ? std::sqrt(v) : 0.0;
+  }
+  return gpkde_reconstruct(h, o, P, nb, eff, sd, n, density, histogram, loops_done);
 }
 
 int mprw_gpkde_batch(mprw_handle *h, const mprw_gpkde_options *opts, double *const *density,

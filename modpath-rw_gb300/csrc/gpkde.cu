@@ -106,6 +106,16 @@ struct Span {
 // bins share no kernel and each warp folds its bin's three factors in shared
 // memory and adds count * fy fz * fx over the span (atomics, one multiply per
 // cell with the row products cached).
+//
+// The atomics add 64-bit fixed-point integers, not floating-point values:
+// each contribution is scaled by 2^shift and rounded to an integer once, and
+// integer sums do not depend on the order in which the warps' atomics land,
+// so the density is bit-for-bit repeatable (FP64 atomicAdd is not).  Every
+// bin's folded kernel sums to at most one, so the grid's total is at most the
+// total count, which the host bounds by the active particles; shift is chosen
+// so that this bound times 2^shift stays below 2^62 (no overflow), and the
+// rounding error of one contribution is 2^-(shift+1) -- about 2e-13 counts
+// for a million particles.
 constexpr int kWarpsW = 4;
 constexpr int kRowCache = 256;
 
@@ -118,9 +128,17 @@ __global__ void wlevel_kernel(KdeParams P, KdeBinsT<T> B, int *wlev) {
   for (int d = 0; d < 3; ++d) wlev[d * B.n + b] = P.mask[d] ? log_index<T>(P, B.ks[d * B.n + b], d) : 1;
 }
 
+__device__ __forceinline__ unsigned long long to_fixed(double v, double scale) {
+  return (unsigned long long)__double2ll_rn(v * scale);
+}
+__device__ __forceinline__ unsigned long long to_fixed(float v, float scale) {
+  return (unsigned long long)__float2ll_rn(v * scale);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, KdeBinsT<T> B, KdeTableT<T> tab,
-                                                                int stride, const int *wlev, T *grid) {
+                                                                int stride, const int *wlev, T fscale,
+                                                                unsigned long long *grid) {
   __shared__ T sv_all[kWarpsW][3 * KDE_MAXLEN];
   __shared__ int sm_all[kWarpsW][3], sofs_all[kWarpsW][3];
   __shared__ T crow_all[kWarpsW][kRowCache];
@@ -159,7 +177,7 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
   const int n0 = S.n[0], n1 = S.n[1], rows = S.n[1] * S.n[2];
   const T *fx = sv + S.k0[0], *fy = sv + KDE_MAXLEN + S.k0[1], *fz = sv + 2 * KDE_MAXLEN + S.k0[2];
   const int64_t sy = P.nb[0], sz = (int64_t)P.nb[0] * P.nb[1];
-  T *gbase = grid + (S.g0[0] - 1) + sy * (S.g0[1] - 1) + sz * (S.g0[2] - 1);
+  unsigned long long *gbase = grid + (S.g0[0] - 1) + sy * (S.g0[1] - 1) + sz * (S.g0[2] - 1);
   // count * fy * fz per row (y fastest), cached when the span has few rows
   T *crow = crow_all[w];
   const bool cached = rows <= kRowCache;
@@ -178,7 +196,7 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
     int iz = r0 / n1, iy = r0 - iz * n1;
     for (int r = r0; r < rows; r += rpi) {
       const T c = cached ? crow[r] : cnt * (fy[iy] * fz[iz]);
-      atomicAdd(gbase + ix + sy * iy + sz * iz, c * fxv);
+      atomicAdd(gbase + ix + sy * iy + sz * iz, to_fixed(c * fxv, fscale));
       iy += rpi;
       while (iy >= n1) {
         iy -= n1;
@@ -189,7 +207,7 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
     for (int r = 0; r < rows; ++r) {
       const int iz = r / n1, iy = r - iz * n1;
       const T c = cached ? crow[r] : cnt * (fy[iy] * fz[iz]);
-      for (int ix = lane; ix < n0; ix += 32) atomicAdd(gbase + ix + sy * iy + sz * iz, c * fx[ix]);
+      for (int ix = lane; ix < n0; ix += 32) atomicAdd(gbase + ix + sy * iy + sz * iz, to_fixed(c * fx[ix], fscale));
     }
   }
 }
@@ -197,16 +215,18 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
 // density grid = raw scatter / binVolume, and the density at every bin
 // (GridProjectedKDE.F90:4662-4667), both from the raw grid
 // (and S[S_DMAX] = max density, zeroed before)
+// (the raw grid is the fixed-point scatter; inv_scale = 2^-shift)
 template <typename T>
-__global__ void scale_pick_kernel(KdeParams P, KdeBinsT<T> B, const T *raw, T *grid, int64_t ngrid, double *S) {
+__global__ void scale_pick_kernel(KdeParams P, KdeBinsT<T> B, const unsigned long long *raw, double inv_scale,
+                                  T *grid, int64_t ngrid, double *S) {
   const int64_t n = ngrid > B.n ? ngrid : (int64_t)B.n;
   const T bv = T(P.binvol);
   double dmax = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    if (i < ngrid) grid[i] = raw[i] / bv;
+    if (i < ngrid) grid[i] = T((double)(long long)raw[i] * inv_scale) / bv;
     if (i < B.n) {
       const int64_t g = (int64_t)(B.gx[i] - 1) + (int64_t)P.nb[0] * ((B.gy[i] - 1) + (int64_t)P.nb[1] * (B.gz[i] - 1));
-      const T d = raw[g] / bv;
+      const T d = T((double)(long long)raw[g] * inv_scale) / bv;
       B.dens[i] = d;
       dmax = fmax(dmax, (double)d);
     }
@@ -279,29 +299,48 @@ __global__ void key_assign_kernel(KdeParams P, KdeBinsT<T> B, int kind, int *bin
     }
     atomicAdd(&sc[key], __popc(grp));
   };
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
-    const unsigned act = __activemask();
-    const int g[3] = {B.gx[b], B.gy[b], B.gz[b]};
+  // The loop runs the same number of times on every lane of a warp (its
+  // bound depends on the block, not the lane; blockDim is a multiple of 32),
+  // so every lane reaches each record() and the full mask is exact; lanes
+  // past the last bin take part with key -1.
+  for (int base = blockIdx.x * blockDim.x; base < B.n; base += gridDim.x * blockDim.x) {
+    const int b = base + threadIdx.x;
+    const bool in = b < B.n;
+    const unsigned act = 0xffffffffu;
+    const int g[3] = {in ? B.gx[b] : 0, in ? B.gy[b] : 0, in ? B.gz[b] : 0};
     if (kind == 1) {
-      const T s = B.support[b];
       int lev[3] = {1, 1, 1};
-      for (int d = 0; d < 3; ++d)
-        if (P.mask[d]) lev[d] = log_index<T>(P, s, d);
-      const int key = lev[0] + lev[1] + lev[2] - 3;
-      bin_key[b] = key;
+      int key = -1;
+      if (in) {
+        const T s = B.support[b];
+        for (int d = 0; d < 3; ++d)
+          if (P.mask[d]) lev[d] = log_index<T>(P, s, d);
+        key = lev[0] + lev[1] + lev[2] - 3;
+        bin_key[b] = key;
+      }
       record(act, key, lev, g);
     } else {
+      // 2-D: a bin with a NaN bandwidth adds to neither curvature
+      // (GridProjectedKDE.F90:1967-1968; negative bandwidths are clipped to
+      // the minimum before this point)
+      // (only the active axes' bandwidths are defined)
+      bool skip2 = false;
+      if (in && P.ndim == 2)
+        for (int a = 0; a < 3; ++a)
+          if (P.mask[a]) skip2 = skip2 || !(B.cb[a * B.n + b] == B.cb[a * B.n + b]);
       for (int a = 0; a < 3; ++a) {
         int key = -1;
         int n = 1;
-        const T h = B.cb[a * B.n + b];
-        if (P.mask[a] && h == h) {
-          n = log_index<T>(P, h, a);
-          key = a * KDE_MAXDB + n - 1;
+        if (in) {
+          const T h = B.cb[a * B.n + b];
+          if (P.mask[a] && h == h && !skip2) {
+            n = log_index<T>(P, h, a);
+            key = a * KDE_MAXDB + n - 1;
+          }
+          bin_key[a * B.n + b] = key;
         }
         const int lev[3] = {n, n, n};
         record(act, key, lev, g);
-        bin_key[a * B.n + b] = key;
       }
     }
   }
@@ -529,6 +568,18 @@ __global__ void gather_x_kernel(KdeParams P, const SepPlan *pl, const T *val, Fi
   }
 }
 
+// 2-D: the product of the two curvatures, then their squares
+// (GridProjectedKDE.F90:2134-2138; the 3-D form below squares first)
+template <typename T>
+__global__ void products2d_kernel(T *c1, T *c2, T *c12, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T a = c1[i], b = c2[i];
+    c12[i] = a * b;
+    c1[i] = a * a;
+    c2[i] = b * b;
+  }
+}
+
 // pairwise products of the squared curvatures (GridProjectedKDE.F90:2466-2468)
 template <typename T>
 __global__ void products_kernel(const T *cx, const T *cy, const T *cz, T *cxy, T *cxz, T *cyz, int64_t n) {
@@ -633,21 +684,38 @@ __global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, c
         if (out2) out2[b] = acc[0];
         net = (double)acc[0];
       }
+    } else if constexpr (NC == 3) {
+      // 2-D (GridProjectedKDE.F90:2168-2228): roughness of the two active
+      // dimensions and the gathered product of their curvatures
+      const T r1 = acc[0], r2 = acc[1], r12 = acc[2];
+      T *rr[3] = {B.rxx, B.ryy, B.rzz};
+      for (int d = 0; d < 3; ++d) rr[d][b] = T(0);
+      rr[P.d1][b] = r1;
+      rr[P.d2][b] = r2;
+      const T v = P.isotropic ? T(2) * r12 + r1 + r2 : T(2) * r12 + T(2) * sqrt(r1 * r2);
+      B.net[b] = v;
+      net = (double)v;
     } else {
       const T rxx = acc[0], ryy = acc[1], rzz = acc[2], rxy = acc[3], rxz = acc[4], ryz = acc[5];
       B.rxx[b] = rxx;
       B.ryy[b] = ryy;
       B.rzz[b] = rzz;
-      const T third = T(1.0 / 3.0), sixth = T(1.0 / 6.0);
-      T v = T(3) * pow(rxx * ryy * rzz, third);
-      if (ryz > T(0)) v = v + T(2) * ryz * pow(rxx * rxx / ryy / rzz, sixth);
-      if (rxz > T(0)) v = v + T(2) * rxz * pow(ryy * ryy / rxx / rzz, sixth);
-      if (rxy > T(0)) v = v + T(2) * rxy * pow(rzz * rzz / rxx / ryy, sixth);
+      T v;
+      if (P.isotropic) {
+        // GridProjectedKDE.F90:2675-2676
+        v = rxx + T(2) * rxy + T(2) * rxz + ryy + T(2) * ryz + rzz;
+      } else {
+        const T third = T(1.0 / 3.0), sixth = T(1.0 / 6.0);
+        v = T(3) * pow(rxx * ryy * rzz, third);
+        if (ryz > T(0)) v = v + T(2) * ryz * pow(rxx * rxx / ryy / rzz, sixth);
+        if (rxz > T(0)) v = v + T(2) * rxz * pow(ryy * ryy / rxx / rzz, sixth);
+        if (rxy > T(0)) v = v + T(2) * rxy * pow(rzz * rzz / rxx / ryy, sixth);
+      }
       B.net[b] = v;
       net = (double)v;
     }
   }
-  if (NC == 6 || mode == GZ_NET) {  // block-uniform: every lane takes part
+  if (NC != 1 || mode == GZ_NET) {  // block-uniform: every lane takes part
     warp_max_pos(S + S_NETMAX, net);
     warp_min_pos(S + S_NETMINPOS, net);
   }
@@ -732,9 +800,11 @@ __global__ void scatter_y_kernel(KdeParams P, const SepPlan *pl, const T *val, c
 // Scatter pass 3 (z) of every key of one axis into that axis's curvature
 // grid (zeroed before; only the union of the keys' output regions is
 // written), keys in increasing order, then the normalisation
-// ((c / binVolume) / binSize^2)^2 (GridProjectedKDE.F90:2366-2461).
+// (c / binVolume) / binSize^2 (GridProjectedKDE.F90:2366-2461), squared
+// when `square` (1-D and 3-D; the 2-D form multiplies the curvatures first).
 template <typename T>
-__global__ void scatter_z_kernel(KdeParams P, const SepPlan *pl, const T *val, const T *V2, T *c0, T *c1, T *c2) {
+__global__ void scatter_z_kernel(KdeParams P, const SepPlan *pl, const T *val, const T *V2, T *c0, T *c1, T *c2,
+                                 int square) {
   const int axis = blockIdx.y;
   T *out = axis == 0 ? c0 : (axis == 1 ? c1 : c2);
   const T bs2 = T(P.bin[axis] * P.bin[axis]), bv = T(P.binvol);
@@ -766,7 +836,7 @@ __global__ void scatter_z_kernel(KdeParams P, const SepPlan *pl, const T *val, c
     }
     T c = acc / bv;
     c = c / bs2;
-    out[g] = c * c;
+    out[g] = square ? c * c : c;
   }
 }
 
@@ -929,11 +999,18 @@ __global__ void optimal_phase0_kernel(KdeParams P, KdeBinsT<T> B, double *S, int
     const T min_pos_net = T(S[S_NETMINPOS]);
     const T nd = T(P.ndim), iso = T(P.iso_threshold);
     T net = B.net[b];
-    if (P.ndim == 3) {
+    if (P.ndim == 3 && !P.isotropic) {
       T sm = B.rxx[b] + B.ryy[b] + B.rzz[b];
       if (sm == T(0)) sm = min_pos_net;
       if ((B.rxx[b] / sm > iso) || (B.ryy[b] / sm > iso) || (B.rzz[b] / sm > iso))
         net = (T(1) - T(0.5)) * net + T(0.5) * sm;
+      B.net[b] = net;
+    } else if (P.ndim == 2 && !P.isotropic) {
+      const T *rr[3] = {B.rxx, B.ryy, B.rzz};
+      const T r1 = rr[P.d1][b], r2 = rr[P.d2][b];
+      T sm = r1 + r2;
+      if (sm == T(0)) sm = min_pos_net;
+      if ((r1 / sm > iso) || (r2 / sm > iso)) net = (T(1) - T(0.5)) * net + T(0.5) * sm;
       B.net[b] = net;
     }
     T sc = T(0);
@@ -956,7 +1033,21 @@ __global__ void optimal_phase1_kernel(KdeParams P, KdeBinsT<T> B, const double *
     B.scale[b] = sc;
   }
   T sh[3] = {T(1), T(1), T(1)};
-  if (P.ndim == 3) {
+  if (P.ndim == 2 && !P.isotropic) {
+    // bounded kernels (GridProjectedKDE.F90:5557-5578)
+    const T *rr[3] = {B.rxx, B.ryy, B.rzz};
+    const T r1 = rr[P.d1][b], r2 = rr[P.d2][b], net = B.net[b];
+    if (!(r1 == T(0) || r2 == T(0))) {
+      const T s1 = fmax(pow(net / r1, T(1.0 / 8.0)), T(P.min_k[P.d1]) / sc);
+      const T s2 = T(1) / s1;
+      const T ns = sqrt(s1 * s2);
+      if (ns != T(0)) {
+        sh[P.d1] = s1 / ns;
+        sh[P.d2] = s2 / ns;
+      }
+    }
+  }
+  if (P.ndim == 3 && !P.isotropic) {
     const T rxx = B.rxx[b], ryy = B.ryy[b], rzz = B.rzz[b], net = B.net[b];
     if (!(rxx == T(0) || ryy == T(0) || rzz == T(0))) {
       const T twelfth = T(1.0 / 12.0);
@@ -1311,7 +1402,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   double *S = st.d_scalars, *h = st.h_scalars;
   *overflow = false;
   // typed views of the grids and pass buffers, the factor values
-  T *dens_grid = reinterpret_cast<T *>(st.dens_grid), *dens_raw = reinterpret_cast<T *>(st.dens_raw);
+  T *dens_grid = reinterpret_cast<T *>(st.dens_grid);
   T *cx = reinterpret_cast<T *>(st.cx), *cy = reinterpret_cast<T *>(st.cy), *cz = reinterpret_cast<T *>(st.cz);
   T *cxy = reinterpret_cast<T *>(st.cxy), *cxz = reinterpret_cast<T *>(st.cxz), *cyz = reinterpret_cast<T *>(st.cyz);
   T *t1 = reinterpret_cast<T *>(st.t1), *t2 = reinterpret_cast<T *>(st.t2);
@@ -1321,11 +1412,22 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   // a stride near n/61 coprime with n (a permutation of the bins)
   int wstride = nb / 61 + 1;
   while (std::gcd(wstride, nb) != 1) ++wstride;
+  // fixed-point scale of the density scatter: the total count is at most
+  // npts (the active particles), and npts * 2^shift < 2^62
+  int shift = 61;
+  {
+    int e = 0;
+    std::frexp(std::max(npts, 1.0), &e);  // npts < 2^e
+    shift = 61 - e;
+  }
+  const double fscale = std::ldexp(1.0, shift), inv_fscale = std::ldexp(1.0, -shift);
+  unsigned long long *raw_fixed = reinterpret_cast<unsigned long long *>(st.dens_raw);
   auto density = [&](void) -> cudaError_t {
-    KCK(cudaMemsetAsync(dens_raw, 0, sizeof(T) * ngrid, s));
+    KCK(cudaMemsetAsync(raw_fixed, 0, sizeof(unsigned long long) * ngrid, s));
     wlevel_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, st.wlev);
-    wscatter_kernel<T><<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, wtab, wstride, st.wlev, dens_raw);
-    scale_pick_kernel<T><<<blocks_for(npick), kThreads, 0, s>>>(P, B, dens_raw, dens_grid, ngrid, S);
+    wscatter_kernel<T><<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, wtab, wstride, st.wlev, T(fscale),
+                                                                            raw_fixed);
+    scale_pick_kernel<T><<<blocks_for(npick), kThreads, 0, s>>>(P, B, raw_fixed, inv_fscale, dens_grid, ngrid, S);
     st.launches += 3;
     return cudaGetLastError();
   };
@@ -1380,17 +1482,25 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     // and the curvature bandwidths
     KCK(plan(1, 1));
     KCK(gather1(dens_grid, GZ_SUPPORT, nullptr, nullptr));
-    KCK(plan(1, P.ndim == 3 ? 6 : 1));
+    KCK(plan(1, P.ndim == 3 ? 6 : (P.ndim == 2 ? 3 : 1)));
     KCK(gather1(dens_grid, GZ_NEST, nullptr, nullptr));
     // curvatures: second-derivative scatters of the counts, squared (every
     // cell of the three grids is written, zero outside the keys' regions)
     KCK(plan(2, 1));
     scatter_x_kernel<T><<<pgrid, kThreads, 0, s>>>(P, B, plan2, val, st.cell_bin, key2, t1);
     scatter_y_kernel<T><<<pgrid, kThreads, 0, s>>>(P, plan2, val, t1, t2);
-    scatter_z_kernel<T><<<dim3(gb, 3), kThreads, 0, s>>>(P, plan2, val, t2, cx, cy, cz);
+    scatter_z_kernel<T><<<dim3(gb, 3), kThreads, 0, s>>>(P, plan2, val, t2, cx, cy, cz, P.ndim != 2);
     st.launches += 3;
     // net roughness: smoothing-kernel gathers of the squared curvatures
-    if (P.ndim == 3) {
+    if (P.ndim == 2) {
+      T *cg[3] = {cx, cy, cz};
+      T *c1 = cg[P.d1], *c2 = cg[P.d2];
+      products2d_kernel<T><<<gb, kThreads, 0, s>>>(c1, c2, cxy, ngrid);
+      gather_x_kernel<T, 3><<<pgrid, kThreads, 0, s>>>(P, plan1, val, Fields<T>{{c1, c2, cxy}}, t1);
+      gather_y_kernel<T, 3><<<pgrid, kThreads, 0, s>>>(P, plan1, val, t1, t2);
+      gather_z_kernel<T, 3><<<bb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, GZ_OUT, nullptr, nullptr, S);
+      st.launches += 4;
+    } else if (P.ndim == 3) {
       products_kernel<T><<<gb, kThreads, 0, s>>>(cx, cy, cz, cxy, cxz, cyz, ngrid);
       gather_x_kernel<T, 6><<<pgrid, kThreads, 0, s>>>(P, plan1, val, Fields<T>{{cx, cy, cz, cxy, cxz, cyz}}, t1);
       gather_y_kernel<T, 6><<<pgrid, kThreads, 0, s>>>(P, plan1, val, t1, t2);

@@ -25,6 +25,8 @@ struct KdeParams {
   double support_c, alpha_c, beta_c, one_over_nd4, minus_one_over_nd6, one_plus_nd_q;
   double four_pi_half_nd;  // (4 pi)**(0.5 nDim)
   double max_sigma_growth, iso_threshold;
+  int isotropic;  // isotropic kernels (gpkdeIsotropicKernels): no shapes, isotropic net roughness
+  int d1, d2;     // 2-D grids: the two active dimensions (idDim1 < idDim2)
 };
 
 // 1-D factor table: for dimension d and database index n (0-based),

@@ -80,6 +80,8 @@ __global__ void coord_sums_kernel(Geometry geo, int64_t n, const int32_t *cell, 
     model_xyz<R>(geo, cell[p], x[p], y[p], z[p], X, Y, Z);
     if (pass == 0) {
       a[0] += X; a[1] += Y; a[2] += Z; a[3] += 1.0;
+    } else if (pass == 2) {  // centred on (m0, m1, m2)
+      a[0] += X - m0; a[1] += Y - m1; a[2] += Z - m2; a[3] += 1.0;
     } else {
       a[0] += (X - m0) * (X - m0); a[1] += (Y - m1) * (Y - m1); a[2] += (Z - m2) * (Z - m2);
     }

@@ -58,7 +58,12 @@ class GpkdeOptions(C.Structure):
                 ("n_opt_loops", C.c_int32), ("min_hover_delta", C.c_double), ("delta_hover_delta", C.c_double),
                 ("max_hover_delta", C.c_double), ("rel_err_convergence", C.c_double),
                 ("skip_error_convergence", C.c_int32), ("unit_volume", C.c_int32), ("scaling_factor", C.c_double),
-                ("precision", C.c_int32)]
+                ("precision", C.c_int32), ("isotropic", C.c_int32)]
+
+
+class GpkdeSums(C.Structure):
+    _fields_ = [("n_active", C.c_double), ("sum_w", C.c_double), ("sum_w2", C.c_double),
+                ("sum_dx", C.c_double * 3), ("sum_dx2", C.c_double * 3)]
 
 
 class SeriesOptions(C.Structure):
@@ -105,6 +110,9 @@ def load_library() -> C.CDLL:
         "mprw_get_particles": (C.c_int, [H, _ip, _dp, _dp, _dp, _dp, _ip, _up, _dp, _dp, _dp]),
         "mprw_histogram": (C.c_int, [H, _dp, _dp, _ip, _dp, C.POINTER(C.c_int64), _dp]),
         "mprw_gpkde": (C.c_int, [H, C.POINTER(GpkdeOptions), _dp, _dp, _ip, _ip]),
+        "mprw_gpkde_partial": (C.c_int, [H, C.POINTER(GpkdeOptions), _dp, C.POINTER(GpkdeSums)]),
+        "mprw_gpkde_from_counts": (C.c_int, [H, C.POINTER(GpkdeOptions), _dp, C.POINTER(GpkdeSums), _dp, _dp, _ip,
+                                             _ip]),
         "mprw_set_observations": (C.c_int, [H, C.c_int32, _ip, _ip, C.c_int32, _ip]),
         "mprw_observe_resident": (C.c_int, [H, C.POINTER(C.c_int64), _dp]),
         "mprw_observe_sinks": (C.c_int, [H, C.c_int64, _ip, _up, _dp, _dp, C.POINTER(C.c_int64)]),
@@ -297,9 +305,9 @@ class Tracker:
     @staticmethod
     def gpkde_options(domain_size, bin_size, origin=(0.0, 0.0, 0.0), n_opt_loops=10, kdb=(0.3, 0.3, 15.0),
                       rel_err=0.02, skip_error=False, unit_volume=True, scaling_factor=1.0,
-                      precision=FP64) -> "GpkdeOptions":
+                      precision=FP64, isotropic=False) -> "GpkdeOptions":
         """The mprw_gpkde_options of a reconstruction grid (defaults: the reference's GPKDE input
-        defaults, FP64 arithmetic)."""
+        defaults, anisotropic kernels, FP64 arithmetic)."""
         o = GpkdeOptions()
         for d in range(3):
             o.origin[d], o.domain_size[d], o.bin_size[d] = float(origin[d]), float(domain_size[d]), float(bin_size[d])
@@ -310,14 +318,16 @@ class Tracker:
         o.unit_volume = int(unit_volume)
         o.scaling_factor = float(scaling_factor)
         o.precision = int(precision)
+        o.isotropic = int(bool(isotropic))
         return o
 
     def gpkde(self, domain_size, bin_size, origin=(0.0, 0.0, 0.0), n_opt_loops=10, kdb=(0.3, 0.3, 15.0),
-              rel_err=0.02, skip_error=False, unit_volume=True, scaling_factor=1.0, precision=FP64):
+              rel_err=0.02, skip_error=False, unit_volume=True, scaling_factor=1.0, precision=FP64,
+              isotropic=False):
         """GPKDE reconstruction of the active particles.  Returns (density, histogram,
         loops) with the grids shaped (nz, ny, nx)."""
         o = self.gpkde_options(domain_size, bin_size, origin, n_opt_loops, kdb, rel_err, skip_error, unit_volume,
-                               scaling_factor, precision)
+                               scaling_factor, precision, isotropic)
         nb = [int(domain_size[d] / bin_size[d] + 0.5) if bin_size[d] != 0 else 1 for d in range(3)]
         dens = np.empty(int(np.prod(nb)))
         hist = np.empty(int(np.prod(nb)))
@@ -325,6 +335,34 @@ class Tracker:
         loops = C.c_int32(0)
         self._check(self.lib.mprw_gpkde(self.h, C.byref(o), _p(dens, _dp), _p(hist, _dp), _p(nbo, _ip),
                                         C.byref(loops)), "mprw_gpkde")
+        shp = (nb[2], nb[1], nb[0])
+        return dens.reshape(shp), hist.reshape(shp), loops.value
+
+    def gpkde_partial(self, domain_size, bin_size, origin=(0.0, 0.0, 0.0), **kw):
+        """This tracker's summable part of a reconstruction (mprw_gpkde_partial):
+        (mass per bin shaped (nz, ny, nx), GpkdeSums)."""
+        o = self.gpkde_options(domain_size, bin_size, origin, **kw)
+        nb = [int(domain_size[d] / bin_size[d] + 0.5) if bin_size[d] != 0 else 1 for d in range(3)]
+        mass = np.empty(int(np.prod(nb)))
+        sums = GpkdeSums()
+        self._check(self.lib.mprw_gpkde_partial(self.h, C.byref(o), _p(mass, _dp), C.byref(sums)),
+                    "mprw_gpkde_partial")
+        return mass.reshape(nb[2], nb[1], nb[0]), sums
+
+    def gpkde_from_counts(self, domain_size, bin_size, mass, sums, origin=(0.0, 0.0, 0.0), **kw):
+        """The reconstruction of summed parts (mprw_gpkde_from_counts): (density, histogram, loops)."""
+        o = self.gpkde_options(domain_size, bin_size, origin, **kw)
+        nb = [int(domain_size[d] / bin_size[d] + 0.5) if bin_size[d] != 0 else 1 for d in range(3)]
+        m = np.ascontiguousarray(mass, np.float64).reshape(-1)
+        if m.shape[0] != int(np.prod(nb)):
+            raise ValueError("mass per bin does not match the grid")
+        dens = np.empty(int(np.prod(nb)))
+        hist = np.empty(int(np.prod(nb)))
+        nbo = np.zeros(3, np.int32)
+        loops = C.c_int32(0)
+        self._check(self.lib.mprw_gpkde_from_counts(self.h, C.byref(o), _p(m, _dp), C.byref(sums), _p(dens, _dp),
+                                                    _p(hist, _dp), _p(nbo, _ip), C.byref(loops)),
+                    "mprw_gpkde_from_counts")
         shp = (nb[2], nb[1], nb[0])
         return dens.reshape(shp), hist.reshape(shp), loops.value
 

@@ -4,8 +4,11 @@ Particles are independent within a tracking interval
 (MPathRW.F90:1207-1539), so ranks take contiguous id ranges and keep the
 global particle ids as Philox keys: a particle's trajectory does not depend
 on which rank tracks it.  The only exchange is the sum of the per-rank GPKDE
-histograms before the smoothing (integer-valued for unit masses, so the sum
-is exact in float64 below 2^53 particles per bin).
+parts before the smoothing: the mass per bin (integer-valued for unit
+masses, so the sum is exact in float64 below 2^53 particles per bin) and the
+sums behind the effective mass and the coordinate statistics
+(mprw_gpkde_partial); one sum-all-reduce per reconstruction, after which any
+rank reconstructs (mprw_gpkde_from_counts).
 """
 from __future__ import annotations
 
@@ -42,3 +45,29 @@ def allreduce_histogram(counts: np.ndarray, group=None) -> np.ndarray:
         t = t.cuda()
     dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
     return t.cpu().numpy().reshape(counts.shape)
+
+
+def allreduce_sums(sums, group=None):
+    """Sum a GpkdeSums record over all ranks (in place) and return it."""
+    import torch
+    import torch.distributed as dist
+    v = torch.tensor([sums.n_active, sums.sum_w, sums.sum_w2, *sums.sum_dx, *sums.sum_dx2], dtype=torch.float64)
+    if dist.get_backend(group) == "nccl":
+        v = v.cuda()
+    dist.all_reduce(v, op=dist.ReduceOp.SUM, group=group)
+    v = v.cpu().tolist()
+    sums.n_active, sums.sum_w, sums.sum_w2 = v[0], v[1], v[2]
+    for d in range(3):
+        sums.sum_dx[d], sums.sum_dx2[d] = v[3 + d], v[6 + d]
+    return sums
+
+
+def gpkde_allreduce(tracker, domain_size, bin_size, origin=(0.0, 0.0, 0.0), group=None, **kw):
+    """GPKDE of the particles of every rank's tracker: each rank's part
+    (mprw_gpkde_partial) is summed over the ranks, then every rank
+    reconstructs the same density from the sums (mprw_gpkde_from_counts).
+    Returns (density, histogram, loops) as Tracker.gpkde."""
+    mass, sums = tracker.gpkde_partial(domain_size, bin_size, origin, **kw)
+    total = allreduce_histogram(mass, group)
+    allreduce_sums(sums, group)
+    return tracker.gpkde_from_counts(domain_size, bin_size, total, sums, origin, **kw)

@@ -6,8 +6,11 @@ Follows lib/gpkde of the reference (paths relative to its src/ directory):
 * GPKDE              -- GridProjectedKDE.F90 prInitialize (354-998),
   prComputeDensity (3598-4392), prComputeDensityOptimization (4396-5160),
   smoothing scale (5164-5203), curvature bandwidth (5207-5275), net
-  roughness 1-D (1666-1903) and 3-D (2295-2709), optimal smoothing and shape
-  (5404-5724), kernel database and indexes (3138-3528, 5727-5962, 6467-6500);
+  roughness 1-D (1666-1903), 2-D (1905-2289) and 3-D (2295-2709), optimal
+  smoothing and shape (5404-5724), kernel database and indexes (3138-3528,
+  5727-5962, 6467-6500), the isotropic-kernel option (gpkdeIsotropicKernels,
+  passed at MPathRW.F90:1639: no isotropy correction, unit shapes, and the
+  isotropic net-roughness sums 2182-2228, 2660-2676);
 * kernels            -- KernelMultiGaussian.f90: W matrix (720-790), second
   derivative matrices (794-1110), spans and boundary reflection (209-390),
   unfold (516-546), SetupMatrix (549-590).
@@ -16,11 +19,13 @@ Reference quirks kept: the second-derivative kernels are never rescaled
 (their balance coefficient needs a positive sum of negative entries, and the
 `if (...) matrix = 0; return` line returns unconditionally before the scaling,
 KernelMultiGaussian.f90:865-887, 969-993, 1071-1097); the 3-D shape
-normalisation uses the single-precision exponent 0.333 (GridProjectedKDE.F90:5654).
+normalisation uses the single-precision exponent 0.333 (GridProjectedKDE.F90:5654);
+the 2-D net roughness multiplies the two curvatures before squaring them
+(2134-2138) where the 3-D one squares them first (2463-2468).
 The options MODPATH-RW uses are restated: for the spatial reconstruction the
 kernel database on (logarithmic), bounded kernel sizes (format 0),
-minimum-roughness format 3, effective-weight format 0 (Kish), not isotropic,
-no sliced reconstruction, grid fixed to the domain; for the observation time
+minimum-roughness format 3, effective-weight format 0 (Kish), anisotropic
+or isotropic kernels, no sliced reconstruction, grid fixed to the domain; for the observation time
 series (``series_oracle.py``) the database off and the grid optionally
 adapted to the data.  ``np.add.at`` accumulates repeated indices in
 array order, the reference's loop order.
@@ -421,7 +426,9 @@ class GPKDE:
                 support[n] = ssc
             cb = self._curvature_bandwidth(darr, nest, scale, shape, support)
             rxx, ryy, rzz, netr = self._net_roughness(counts, act, cb, support)
-            ks, scale, shape = self._optimal_smoothing(nest, netr, rxx, ryy, rzz)
+            # the isotropy correction changes netRoughnessArray in place (intent(inout),
+            # GridProjectedKDE.F90:5420, 5496-5518): the ALMISE below reads the corrected values
+            ks, scale, shape, netr = self._optimal_smoothing(nest, netr, rxx, ryy, rzz)
             dens = self._density(counts, act, ks)
             darr = np.array([dens[g[0] - 1, g[1] - 1, g[2] - 1] for g in act])
             e = np.where(darr_old != 0.0, np.abs(darr / darr.max() - darr_old / darr_old.max())
@@ -474,6 +481,8 @@ class GPKDE:
         return cb
 
     def _net_roughness(self, counts, act, cb, support):
+        """prComputeNetRoughness1D/2D/3D (GridProjectedKDE.F90:1666-1904,
+        1905-2289, 2295-2709), local (not global) smoothing."""
         nb = act.shape[0]
         curv = {}
         axes = self.dims if self.ndim != 3 else [0, 1, 2]
@@ -483,22 +492,43 @@ class GPKDE:
                 h = cb[d, n]
                 if self.ndim == 1 and (h < 0.0 or h != h):
                     continue
+                # 2-D: a bin with any negative or NaN bandwidth adds to neither curvature (:1967-1968)
+                if self.ndim == 2 and (np.any(cb[:, n] < 0.0) or np.any(cb[:, n] != cb[:, n])):
+                    continue
                 gid = act[n]
                 gsl, k = self._kernel_span(self._sd_kernel(d, h), gid)
                 c[gsl] = c[gsl] + counts[gid[0] - 1, gid[1] - 1, gid[2] - 1] * k
             c = c / self.bin_volume
             c = c / (self.bin_size[d] ** 2.0)
-            curv[d] = c * c
+            curv[d] = c
         rxx = np.zeros(nb); ryy = np.zeros(nb); rzz = np.zeros(nb); net = np.zeros(nb)
         r = {0: rxx, 1: ryy, 2: rzz}
         if self.ndim == 1:
             d = self.dims[0]
+            c2 = curv[d] * curv[d]
             for n in range(nb):
-                r[d][n] = self._sigma_gather(curv[d], act[n], support[n])
+                r[d][n] = self._sigma_gather(c2, act[n], support[n])
             net[:] = r[d]
             return rxx, ryy, rzz, net
-        if self.ndim != 3:
-            raise NotImplementedError("2-D reconstruction is not restated")
+        if self.ndim == 2:
+            # the 2-D form multiplies the curvatures before squaring them (:2134-2138)
+            d1, d2 = self.dims
+            c12 = curv[d1] * curv[d2]
+            c1, c2 = curv[d1] * curv[d1], curv[d2] * curv[d2]
+            for n in range(nb):
+                gsl, k = self._kernel_span(self._w_kernel(np.full(3, support[n])), act[n])
+                r1 = float((c1[gsl] * k).sum())
+                r2 = float((c2[gsl] * k).sum())
+                r12 = float((c12[gsl] * k).sum())
+                r[d1][n], r[d2][n] = r1, r2
+                if self.isotropic:
+                    net[n] = 2.0 * r12 + r1 + r2
+                else:
+                    net[n] = 2.0 * r12 + 2.0 * math.sqrt(r1 * r2)
+            return rxx, ryy, rzz, net
+        # the 3-D form squares the curvatures, then multiplies the squares (:2463-2468)
+        for d in (0, 1, 2):
+            curv[d] = curv[d] * curv[d]
         cxy, cxz, cyz = curv[0] * curv[1], curv[0] * curv[2], curv[1] * curv[2]
         for n in range(nb):
             gid = act[n]
@@ -509,6 +539,10 @@ class GPKDE:
             rxy = float((cxy[gsl] * k).sum())
             rxz = float((cxz[gsl] * k).sum())
             ryz = float((cyz[gsl] * k).sum())
+            if self.isotropic:
+                # :2675-2676
+                net[n] = rxx[n] + 2.0 * rxy + 2.0 * rxz + ryy[n] + 2.0 * ryz + rzz[n]
+                continue
             v = 3.0 * (rxx[n] * ryy[n] * rzz[n]) ** (1.0 / 3.0)
             if ryz > 0.0:
                 v = v + 2.0 * ryz * (rxx[n] ** 2.0 / ryy[n] / rzz[n]) ** (1.0 / 6.0)
@@ -525,6 +559,14 @@ class GPKDE:
         if netr.max() == 0.0:
             raise RuntimeError("net roughness is zero everywhere")
         netr = netr.copy()
+        r = {0: rxx, 1: ryy, 2: rzz}
+        if self.ndim == 2 and not self.isotropic:
+            # :5476-5500
+            r1, r2 = r[self.dims[0]], r[self.dims[1]]
+            sm = r1 + r2
+            sm = np.where(sm == 0.0, netr[netr > 0.0].min(), sm)
+            iso = (r1 / sm > self.iso_threshold) | (r2 / sm > self.iso_threshold)
+            netr = np.where(iso, (1.0 - 0.5) * netr + 0.5 * sm, netr)
         if self.ndim == 3 and not self.isotropic:
             sm = rxx + ryy + rzz
             sm = np.where(sm == 0.0, netr[netr > 0.0].min(), sm)
@@ -537,6 +579,19 @@ class GPKDE:
         if zero.any():
             scale[zero] = scale[scale > 0.0].max()
         shape = np.ones((3, nb))
+        if self.ndim == 2 and not self.isotropic:
+            # bounded kernels (:5557-5578)
+            d1, d2 = self.dims
+            r1, r2 = r[d1], r[d2]
+            for n in range(nb):
+                if r1[n] == 0.0 or r2[n] == 0.0:
+                    continue
+                s1 = max((netr[n] / r1[n]) ** (1.0 / 8.0), self.min_k[d1] / scale[n])
+                s2 = 1.0 / s1
+                ns = math.sqrt(s1 * s2)
+                if ns == 0.0:
+                    continue
+                shape[d1, n], shape[d2, n] = s1 / ns, s2 / ns
         if self.ndim == 3 and not self.isotropic:
             for n in range(nb):
                 if rxx[n] == 0.0 or ryy[n] == 0.0 or rzz[n] == 0.0:
@@ -564,4 +619,4 @@ class GPKDE:
                 ks[d] = np.where(ks[d] < self.min_k[d], self.min_k[d], ks[d])
         if update:
             scale = self._smoothing_scale(ks)
-        return ks, scale, shape
+        return ks, scale, shape, netr

@@ -93,3 +93,89 @@ def test_gpkde_fp32_against_fp64(gpu_lib, case):
     assert l32 == l64
     assert np.abs(d32 - d64).max() <= 1e-3 * d64.max()
     assert abs(d32.sum() - n) < 1e-4 * n
+
+
+@pytest.mark.parametrize("case", ["uniform_pulse", "lognormal_field"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gpkde_is_bitwise_repeatable(gpu_lib, case, precision):
+    """The same reconstruction of the same particles, run three times, gives
+    the same density to the last bit and the same number of optimisation
+    loops: the density scatter adds fixed-point integers, so the order in
+    which its atomics land does not matter.  The uniform pulse at 50 days
+    (1e5 particles, 1-D) and the lognormal slab (200x100x20 cells, 1e6
+    particles) after 20 days (3-D)."""
+    from mprw.model import MIXED
+    prec = MIXED if precision == "mixed" else 0
+    if case == "uniform_pulse":
+        g, f, p, opt = W.uniform_pulse(n_particles=100_000)
+        t1, dom = 50.0, (200.0, 1.0, 1.0)
+    else:
+        g, f, p, opt, info = W.lognormal_slab(n_particles=1_000_000, seed=0, use_torch=True)
+        t1, dom = 20.0, (200.0, 100.0, 20.0)
+    tr = mprw.Tracker(g, opt)
+    tr.load_flow(f)
+    tr.set_particles(p)
+    tr.advance(0.0, t1)
+    runs = [tr.gpkde(dom, (1.0, 1.0, 1.0), precision=prec) for _ in range(3)]
+    tr.close()
+    d0, h0, l0 = runs[0]
+    assert d0.max() > 0 and l0 > 0
+    for d, h, lo in runs[1:]:
+        assert lo == l0
+        np.testing.assert_array_equal(h, h0)
+        assert np.array_equal(d.view(np.uint64), d0.view(np.uint64))
+
+
+@pytest.mark.parametrize("isotropic", [False, True], ids=["anisotropic", "isotropic"])
+def test_gpkde_2d_on_the_reference_example_grid(gpu_lib, isotropic):
+    """2-D reconstruction on the grid of the reference's GPKDE example
+    (examples/ex07_mf6/ex07a_mf6.gpkde: 250 x 50 x 1 bins of 1 m), on a 2-D
+    lognormal field of that shape (the lognormal-slab generator with one
+    layer) after 40 days: the same loop count as the numpy restatement
+    (prComputeNetRoughness2D, the 2-D isotropy correction and shapes), the
+    density within 1e-10 of its maximum, mass conserved."""
+    g, f, p, opt, info = W.lognormal_slab(n_particles=20000, nlay=1, nrow=50, ncol=250, seed=3, use_torch=False)
+    tr = mprw.Tracker(g, opt)
+    tr.load_flow(f)
+    tr.set_particles(p)
+    tr.advance(0.0, 40.0)
+    co = _positions(tr)
+    dens, hist, loops = tr.gpkde((250.0, 50.0, 1.0), (1.0, 1.0, 1.0), isotropic=isotropic)
+    tr.close()
+    G = GO.GPKDE((250.0, 50.0, 1.0), (1.0, 1.0, 1.0), isotropic=isotropic)
+    assert G.ndim == 2
+    ref, _ = G.compute_density(co, np.ones(co.shape[0]))
+    assert loops == G.loops
+    np.testing.assert_allclose(dens, ref.transpose(2, 1, 0), rtol=0, atol=1e-10 * ref.max())
+    assert abs(dens.sum() - co.shape[0]) < 1e-8 * co.shape[0]
+
+
+def test_gpkde_2d_xz_and_3d_isotropic(gpu_lib):
+    """The other 2-D orientation (x-z: one row) and the isotropic option in
+    3-D, against the numpy restatement."""
+    g, f, p, opt, info = W.lognormal_slab(n_particles=6000, nlay=8, nrow=1, ncol=60, seed=4, use_torch=False)
+    tr = mprw.Tracker(g, opt)
+    tr.load_flow(f)
+    tr.set_particles(p)
+    tr.advance(0.0, 30.0)
+    co = _positions(tr)
+    dens, _, loops = tr.gpkde((60.0, 1.0, 8.0), (1.0, 1.0, 1.0))
+    tr.close()
+    G = GO.GPKDE((60.0, 1.0, 8.0), (1.0, 1.0, 1.0))
+    assert G.dims == [0, 2]
+    ref, _ = G.compute_density(co, np.ones(co.shape[0]))
+    assert loops == G.loops
+    np.testing.assert_allclose(dens, ref.transpose(2, 1, 0), rtol=0, atol=1e-10 * ref.max())
+
+    g, f, p, opt, info = W.lognormal_slab(n_particles=4000, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
+    tr = mprw.Tracker(g, opt)
+    tr.load_flow(f)
+    tr.set_particles(p)
+    tr.advance(0.0, 20.0)
+    co = _positions(tr)
+    dens, _, loops = tr.gpkde((30.0, 12.0, 4.0), (1.0, 1.0, 1.0), n_opt_loops=5, isotropic=True)
+    tr.close()
+    G = GO.GPKDE((30.0, 12.0, 4.0), (1.0, 1.0, 1.0), n_opt_loops=5, isotropic=True)
+    ref, _ = G.compute_density(co, np.ones(co.shape[0]))
+    assert loops == G.loops
+    np.testing.assert_allclose(dens, ref.transpose(2, 1, 0), rtol=0, atol=1e-9 * ref.max())
