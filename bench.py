@@ -31,6 +31,16 @@ bounded sample -- without the GPKDE reconstruction, whose CPU restatement is
 numpy test code and not representative, so the CPU figure is an upper bound
 on the reference's pipeline rate.
 
+Also in the line: ``lognormal_slab_btc_150m`` = the breakthrough counts at
+the x = 150 m control plane after every advance; ``uniform_pulse`` = the
+uniform-column pulse (1e5 particles, 100 days, FP64 and MIXED) with its
+plume against the analytic Gaussian; ``batched`` = the ensemble as one batch
+in MIXED, the same batch in FP64, and the plain FP64 path (every
+realization on its own handle, one after another): the spec ratio
+``speedup_vs_plain_fp64``, and per realization the moment errors and the
+L1 error of the breakthrough curve at x = 30 m of the MIXED batch against
+the plain FP64 run of the same seed.
+
 ``--impl reference`` times the reference's CPU algorithm (the C restatement:
 the Fortran reference cannot be compiled on these machines) instead.
 """
@@ -71,6 +81,7 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-pulse", action="store_true", help="skip the uniform-pulse leg (1e5 particles, 100 days)")
     ap.add_argument("--no-btc", action="store_true",
                     help="skip the breakthrough-curve leg (1-D GPKDE of 10^6 sink records)")
     ap.add_argument("--realizations", type=int, default=64,
@@ -189,6 +200,55 @@ def moments(out):
     return m, int(act.sum())
 
 
+def plane_observations(g, x_plane):
+    """Observations of a control plane at x = x_plane: observation 0 (resident)
+    = the cells of the columns at or beyond the plane except the last column,
+    observation 1 (sink) = the last column, the constant-head outlet whose
+    weak-sink stops end the particles that reach it."""
+    xe = np.concatenate([[0.0], np.cumsum(g.delr)])
+    cols = np.nonzero(xe[:-1] >= x_plane - 1e-9)[0]
+    cols = cols[cols < g.ncol - 1]
+    k, i, j = np.meshgrid(np.arange(g.nlay), np.arange(g.nrow), cols, indexing="ij")
+    res = g.node(k.ravel(), i.ravel(), j.ravel())
+    k, i = np.meshgrid(np.arange(g.nlay), np.arange(g.nrow), indexing="ij")
+    out = g.node(k.ravel(), i.ravel(), np.full(k.size, g.ncol - 1))
+    cells = np.concatenate([res, out]).astype(np.int32)
+    obs = np.concatenate([np.zeros(res.size, np.int32), np.ones(out.size, np.int32)])
+    return cells, obs, np.array([1, 2], np.int32)
+
+
+def sink_count(tr):
+    """Number of sink-observation records of the tracker's last advance (none copied)."""
+    import ctypes as C
+    n = C.c_int64(0)
+    rc = tr.lib.mprw_observe_sinks(tr.h, 0, None, None, None, None, C.byref(n))
+    if rc != 0:
+        raise RuntimeError(tr.lib.mprw_last_error(tr.h).decode())
+    return int(n.value)
+
+
+class PlaneCounter:
+    """Breakthrough at a control plane: after every advance, the ACTIVE particles
+    beyond the plane plus every particle stopped so far at the outlet."""
+
+    def __init__(self, tr, g, x_plane):
+        tr.set_observations(*plane_observations(g, x_plane))
+        self.tr, self.arrived, self.curve = tr, 0, []
+
+    def after_advance(self, t):
+        self.arrived += sink_count(self.tr)
+        cnt, _ = self.tr.observe_resident()
+        self.curve.append((float(t), int(cnt[0]) + self.arrived))
+
+
+def btc_l1(a, b):
+    """L1 distance of two breakthrough curves sampled at the same times, relative to b's."""
+    ca = np.array([c for _, c in a], np.float64)
+    cb = np.array([c for _, c in b], np.float64)
+    den = cb.sum()
+    return float(np.abs(ca - cb).sum() / den) if den > 0 else (0.0 if ca.sum() == 0 else float("inf"))
+
+
 def barrier():
     """Align the ranks around a timed region (no-op for one process)."""
     import torch.distributed as dist
@@ -218,9 +278,13 @@ def run_gpu_arm(args, rank, world, local):
         tr.load_flow(f)
         tr.set_particles(p)
         tuning = tr.autotune(0.0, INTERVAL_D) if args.autotune else tr.tuning()
+        # breakthrough at the x = 150 m control plane, counted after every advance
+        # outside the timed events (two small device reductions)
+        plane = PlaneCounter(tr, g, 150.0)
         t = 0.0
         for _ in range(warmup):
             tr.advance(t, t + INTERVAL_D)
+            plane.after_advance(t + INTERVAL_D)
             tr.gpkde(domain, bins, origin, precision=kde_prec)
             t += INTERVAL_D
         torch.cuda.synchronize()
@@ -240,6 +304,7 @@ def run_gpu_arm(args, rank, world, local):
             ev[k][2].record(stream)
             torch.cuda.synchronize()
             wall_ms.append((time.perf_counter() - t0) * 1e3)
+            plane.after_advance(t + INTERVAL_D)
             kern_ms.append(tm["step_ms"])
             kde_ms.append(tk["gpkde_ms"])
             loops.append(nl)
@@ -259,7 +324,8 @@ def run_gpu_arm(args, rank, world, local):
                        "max_rel": float(np.abs(dens - d64).max() / d64.max())}
         tr.close()
         return dict(ms=ms, adv_ms=adv_ms, kern_ms=kern_ms, kde_ms=kde_ms, wall_ms=wall_ms, steps=steps_done,
-                    launches=launches, out=out, t_end=t, loops=loops, dens=dens, kde_err=kde_err, tuning=tuning)
+                    launches=launches, out=out, t_end=t, loops=loops, dens=dens, kde_err=kde_err, tuning=tuning,
+                    btc150=plane.curve)
 
     with ClockSampler(local) as clk:
         fp64 = timed_run(MIXED if args.precision == "mixed" else 0, args.steps, args.warmup)
@@ -269,19 +335,27 @@ def run_gpu_arm(args, rank, world, local):
     if not args.no_e2e:
         res["e2e"] = e2e_run(args, g, f, p, opt, origin, bins, domain, flush)
     res["geom"] = (g, f, p, opt)
+    res["flush"] = flush
     res["mf6_bytes"] = info["mf6_bytes"]
     if not args.no_batched and rank == 0:
         res["batched"] = batched_run(args, flush)
     return res
 
 
+BATCH_PLANE_X = 30.0   # control plane of the ensemble's breakthrough curves (20 m past the inlet slab)
+
+
 def batched_run(args, flush):
     """The ensemble (mprw.workloads.lognormal_ensemble, the first R realizations) as ONE
     batch: each step advances every realization's particles in one persistent
     launch and reconstructs every realization with GPKDE.  Timed in MIXED
-    precision (FP32 advance + FP32 reconstruction) and, on the same particles
-    and random streams, in FP64; the plume moments of the two are compared
-    per realization."""
+    precision (FP32 advance + FP32 reconstruction), in FP64 as the same batch,
+    and in FP64 as the plain path -- every realization on its own handle, one
+    after another -- with the same particles and random streams.  Per
+    realization, the plume moments and the breakthrough curve at the control
+    plane x = 30 m (ACTIVE particles beyond the plane plus those stopped at the
+    outlet, after every step) of the MIXED batch are compared with the plain
+    FP64 run, the separate FP64 run of the same seed."""
     import torch
     import mprw
     from mprw import workloads as W
@@ -302,10 +376,13 @@ def batched_run(args, flush):
             b.load_flow(k, f)
         b.set_particles([e[2] for e in ens])
         tuning = b.autotune(0.0, INTERVAL_D) if args.autotune else b.tuning()
+        planes = [PlaneCounter(b.member(k), g, BATCH_PLANE_X) for k, (g, _, _) in enumerate(ens)]
         t = 0.0
 
         def one_step(t):
             s = b.advance(t, t + INTERVAL_D)
+            for pc in planes:
+                pc.after_advance(t + INTERVAL_D)
             b.gpkde(doms, bins, precision=precision, concurrency=args.kde_streams)
             return s
         for _ in range(args.warmup):
@@ -326,6 +403,8 @@ def batched_run(args, flush):
             launches += b.timings()["launches"]
             ev[k][2].record(stream)
             torch.cuda.synchronize()
+            for pc in planes:          # outside the timed events
+                pc.after_advance(t + INTERVAL_D)
             steps += s
             t += INTERVAL_D
         ms = sum(a.elapsed_time(c) for a, _, c in ev)
@@ -333,25 +412,71 @@ def batched_run(args, flush):
         outs = b.get_particles()
         b.close()
         return dict(steps=steps, ms=ms, adv_ms=adv, kern_ms=float(np.sum(adv_kern)), launches=launches, outs=outs,
-                    t_end=t, tuning=tuning)
+                    t_end=t, tuning=tuning, btc=[pc.curve for pc in planes])
+
+    def run_plain():
+        """Plain FP64: each realization on its own handle, one after another, the
+        same steps (warm-up untimed), advance + GPKDE per step timed with events."""
+        opt.precision = 0
+        steps, ms, adv_ms, launches, outs, btc = 0, 0.0, 0.0, 0, [], []
+        for k, (g, f, p) in enumerate(ens):
+            tr = mprw.Tracker(g, opt)
+            tr.set_stream(stream.cuda_stream)
+            tr.load_flow(f)
+            tr.set_particles(p)
+            pc = PlaneCounter(tr, g, BATCH_PLANE_X)
+            t = 0.0
+            for _ in range(args.warmup):
+                tr.advance(t, t + INTERVAL_D)
+                pc.after_advance(t + INTERVAL_D)
+                tr.gpkde(doms[k], bins)
+                t += INTERVAL_D
+            for _ in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+                e[0].record(stream)
+                steps += tr.advance(t, t + INTERVAL_D)
+                launches += tr.timings()["launches"]
+                e[1].record(stream)
+                tr.gpkde(doms[k], bins)
+                launches += tr.timings()["launches"]
+                e[2].record(stream)
+                torch.cuda.synchronize()
+                pc.after_advance(t + INTERVAL_D)
+                ms += e[0].elapsed_time(e[2])
+                adv_ms += e[0].elapsed_time(e[1])
+                t += INTERVAL_D
+            outs.append(tr.get_particles())
+            btc.append(pc.curve)
+            tr.close()
+        return dict(steps=steps, ms=ms, adv_ms=adv_ms, launches=launches, outs=outs, btc=btc)
 
     mx = run(MIXED)
     fp = run(0)
+    pl = run_plain()
     errs = []
     for k, (g, f, p) in enumerate(ens):
         m32, n32 = moments(mx["outs"][k])
-        m64, n64 = moments(fp["outs"][k])
+        m64, n64 = moments(pl["outs"][k])
         x0 = 5.0  # centre of the 10 m inlet slab: first moments are taken as displacement from it
         e = {"mean_disp_x_rel": abs(m32["gx"][0] - m64["gx"][0]) / max(abs(m64["gx"][0] - x0), 1e-30)}
         for ax in ("gx", "gy", "gz"):
             e[f"var_{ax[1]}_rel"] = abs(m32[ax][1] - m64[ax][1]) / max(m64[ax][1], 1e-30)
         # Monte-Carlo standard error of a variance estimate, relative: sqrt(2 / n)
         e["mc_var_rel_se"] = float(np.sqrt(2.0 / max(n64, 1)))
+        e["btc_l1_rel"] = btc_l1(mx["btc"][k], pl["btc"][k])
+        e["btc_final"] = [mx["btc"][k][-1][1], pl["btc"][k][-1][1]]
         e["active"] = [n32, n64]
         errs.append(e)
-    worst = {key: max(e[key] for e in errs) for key in ("mean_disp_x_rel", "var_x_rel", "var_y_rel", "var_z_rel")}
+    worst = {key: max(e[key] for e in errs)
+             for key in ("mean_disp_x_rel", "var_x_rel", "var_y_rel", "var_z_rel", "btc_l1_rel")}
+    # the batch in FP64 reproduces the separate FP64 runs particle for particle
+    same = all(np.array_equal(a["cell"], b_["cell"]) and np.array_equal(a["lx"], b_["lx"]) and
+               np.array_equal(a["status"], b_["status"]) for a, b_ in zip(fp["outs"], pl["outs"]))
     v32 = mx["steps"] / (mx["ms"] / 1e3)
     v64 = fp["steps"] / (fp["ms"] / 1e3)
+    vpl = pl["steps"] / (pl["ms"] / 1e3)
     return {"workload": f"realizations 0..{len(ens) - 1} of the 64-member ensemble (the lognormal-slab generator; grids "
                         "U[100..400]x[50..200]x[10..20], sigma2 lnK U[0.5,2], alphaL U[0.1,1], alphaT = alphaL/10, "
                         "particles log-U[1e5,4e6]), one batch: one advance launch for all realizations + one "
@@ -361,12 +486,63 @@ def batched_run(args, flush):
             "value": v32, "unit": UNIT, "ms_per_step": mx["ms"] / args.steps,
             "advance_ms_per_step": mx["adv_ms"] / args.steps, "advance_kernel_ms_per_step": mx["kern_ms"] / args.steps,
             "gpkde_ms_per_step": (mx["ms"] - mx["adv_ms"]) / args.steps, "gpu_launches": mx["launches"],
-            "fp64": {"value": v64, "ms_per_step": fp["ms"] / args.steps,
-                     "advance_ms_per_step": fp["adv_ms"] / args.steps, "tuning": fp["tuning"]},
+            "fp64_plain": {"value": vpl, "ms_per_step": pl["ms"] / args.steps,
+                           "advance_ms_per_step": pl["adv_ms"] / args.steps, "gpu_launches": pl["launches"],
+                           "path": "every realization on its own handle (FP64 advance + FP64 GPKDE), one after "
+                                   "another, default launch tuning"},
+            "fp64_batched": {"value": v64, "ms_per_step": fp["ms"] / args.steps,
+                             "advance_ms_per_step": fp["adv_ms"] / args.steps, "tuning": fp["tuning"],
+                             "identical_to_plain": bool(same)},
             "tuning": mx["tuning"],
-            "speedup_vs_fp64_same_ensemble": v32 / v64,
-            "moment_error_vs_fp64": {"worst_over_realizations": worst, "per_realization": errs},
+            "speedup_vs_plain_fp64": v32 / vpl,
+            "speedup_vs_fp64_batched": v32 / v64,
+            "control_plane_x_m": BATCH_PLANE_X,
+            "error_vs_plain_fp64": {"worst_over_realizations": worst, "per_realization": errs},
             "t_end_days": mx["t_end"]}
+
+
+def pulse_run(args, flush):
+    """The uniform-column pulse (200x1x1 cells of 1 m, v = 1 m/d, alphaL 0.1 m,
+    alphaT 0.01 m, Courant 0.1, 1e5 particles at x = 10 m): advance to 25, 50
+    and 100 days, each followed by GPKDE on the 1 m grid, FP64 and MIXED,
+    timed with CUDA events; the plume against the analytic Gaussian (mean
+    10 + t, variance 0.2 t)."""
+    import torch
+    import mprw
+    from mprw import workloads as W
+    from mprw.model import MIXED
+    out = {"workload": "uniform pulse: 200x1x1 cells, v 1 m/d, alphaL 0.1 m, 1e5 particles at x = 10 m, "
+                       "intervals to 25, 50, 100 d, GPKDE on the 1 m grid after each"}
+    stream = torch.cuda.Stream()
+    for name, prec in (("fp64", 0), ("mixed", MIXED)):
+        g, f, p, opt = W.uniform_pulse(n_particles=100_000, precision=prec)
+        tr = mprw.Tracker(g, opt)
+        tr.set_stream(stream.cuda_stream)
+        tr.load_flow(f)
+        tr.set_particles(p)
+        flush.zero_()
+        torch.cuda.synchronize()
+        steps, ms, t, plume = 0, 0.0, 0.0, []
+        for t_out in (25.0, 50.0, 100.0):
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            e[0].record(stream)
+            steps += tr.advance(t, t_out)
+            tr.gpkde((200.0, 1.0, 1.0), (1.0, 1.0, 1.0), precision=prec)
+            e[1].record(stream)
+            torch.cuda.synchronize()
+            ms += e[0].elapsed_time(e[1])
+            x = tr.get_particles()["gx"]
+            plume.append({"t": t_out, "mean_minus_analytic_m": float(x.mean() - (10.0 + t_out)),
+                          "var_rel_to_analytic": float(x.var() / (0.2 * t_out) - 1.0)})
+            t = t_out
+        tr.close()
+        out[name] = {"value": steps / (ms / 1e3), "unit": UNIT, "particle_steps": steps, "ms": ms, "plume": plume}
+    out["mixed_speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["note"] = ("one small launch per interval with few particles per SM: this configuration is launch- and "
+                   "latency-bound on one GB300; the scheme's own bias against the analytic Gaussian (interface "
+                   "forcing at the cell faces) is -0.25 m on the mean and -4.3 % on the variance at 100 d, "
+                   "measured on the reference's RNG path at 1e6 particles")
+    return out
 
 
 def e2e_run(args, g, f, p, opt, origin, bins, domain, flush):
@@ -468,6 +644,7 @@ def cpu_baseline(g, f, p, opt, n_sample, t_begin_steps, steps):
                   rng_ctr=np.zeros(n_sample, np.uint64))
     opt.precision = 0
     th = O.cpu_count()
+    O.reset_xoroshiro()   # one run: the thread streams are seeded once and continue across intervals
     t = 0.0
     tot, nsteps = 0.0, 0
     for it in range(t_begin_steps + steps):
@@ -546,6 +723,10 @@ def main():
                      "kernel": "rwpt_advance_kernel<double>", "kernel_ms": kern_avg_ms,
                      "bytes_model": "1008 B per particle-step (state 96 B + cell record 912 B)",
                      "fp64_pipe_active_pct_ncu": ncu_figure("fp64_pipe_active_pct"),
+                     "traffic_source": "not measured in this run: the ncu DRAM bytes per particle-step of the "
+                                       "committed 200,000-particle capture (profiles/rwpt_advance_kernel_"
+                                       "lognormal_slab.md) times this run's particle-steps per launch; "
+                                       "fp64_pipe_active_pct_ncu is read from the same capture",
                      "note": "the step kernel is bound by the FP64 pipe (GB300: 2 FP64 lane-operations per clock "
                              "per SM), not HBM: the records stay in L2; traffic is ncu DRAM bytes"},
         "clocks": res["clocks"],
@@ -576,9 +757,16 @@ def main():
                          "active_mixed": n32, "kernel_ms": float(np.mean(mx["kern_ms"])),
                          "gpkde_ms": float(np.mean(mx["kde_ms"])), "gpkde_precision": "fp32", "tuning": mx["tuning"],
                          "gpkde_fp32_vs_fp64_same_particles": mx["kde_err"]}
+    line["lognormal_slab_btc_150m"] = {
+        "curve": fp["btc150"], "control_plane_x_m": 150.0,
+        "counts": "after every 10-day advance (warm-up included): ACTIVE particles at or beyond x = 150 m plus "
+                  "those stopped at the outlet; the mean plume (v ~ 0.2 m/d) does not reach the plane in this "
+                  "run, only fast-channel early arrivals do"}
+    if not args.no_pulse:
+        line["uniform_pulse"] = pulse_run(args, res["flush"])
     if "batched" in res:
         line["batched"] = res["batched"]
-        line["batched"]["speedup_vs_plain_fp64"] = res["batched"]["value"] / value_rank
+        line["batched"]["headline_fp64_value"] = value_rank
     if not args.no_cpu:
         g, f, p, opt = res["geom"]
         line["cpu_baseline"] = cpu_baseline(g, f, p, opt, args.cpu_sample, args.warmup, min(args.steps, 5))
