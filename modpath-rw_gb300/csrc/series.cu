@@ -200,24 +200,28 @@ __global__ void __launch_bounds__(kRed) ser_var_kernel(const double *x, int64_t 
 
 // Histogram%ComputeCounts{Weighted,AndWeights} / ComputeEffectiveCountsAndWeights
 // (Histogram.F90:276-490): bin = floor((t - origin)/binSize) + 1 (+ 0 for an
-// exact point), points outside [1, G] skipped.
+// exact point), points outside [1, G] skipped.  The sums are 64-bit
+// fixed-point integers (scale 2^shift_c for counts, 2^shift_w for wcounts,
+// chosen by the host from the totals so that no sum overflows): integer
+// additions do not depend on the order of the atomics, so the histogram is
+// bit-for-bit repeatable; ser_fixed_kernel turns them into doubles.
 __global__ void ser_hist_kernel(const double *x, const double *w, int64_t n, double origin, double b, int G,
-                                int exact, int fmt, double *counts, double *wcounts) {
+                                int exact, int fmt, double sc, double sw, unsigned long long *counts,
+                                unsigned long long *wcounts) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double q = floor((x[i] - origin) / b) + (exact ? 0.0 : 1.0);
     if (!(q >= 1.0 && q <= (double)G)) continue;
     const int k = (int)q - 1;
     const double wi = w[i];
-    if (fmt == 2) {
-      atomicAdd(counts + k, 1.0);
-      atomicAdd(wcounts + k, wi);
-    } else if (fmt == 3) {
-      atomicAdd(counts + k, wi * wi);
-      atomicAdd(wcounts + k, wi);
-    } else {
-      atomicAdd(counts + k, wi);
-    }
+    const double c = fmt == 2 ? 1.0 : (fmt == 3 ? wi * wi : wi);
+    atomicAdd(counts + k, (unsigned long long)__double2ll_rn(c * sc));
+    if (fmt >= 2) atomicAdd(wcounts + k, (unsigned long long)__double2ll_rn(wi * sw));
   }
+}
+
+__global__ void ser_fixed_kernel(const unsigned long long *a, double inv, double *out, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = (double)(long long)a[i] * inv;
 }
 
 // mode 0: a /= f; mode 1: a *= f; mode 2: format 3's effective counts
@@ -273,20 +277,60 @@ __global__ void ser_init_kernel(SerBins B, double hs) {
   B.netr[i] = 0.0;
 }
 
-// density: scatter of (w)counts times the folded W taps of kernelSmoothing;
-// check_negative skips a negative smoothing (the first estimate, :4640).
-__global__ void __launch_bounds__(kThreads) ser_density_kernel(SerParams P, SerBins B, const double *val,
-                                                               int check_negative, double *dens) {
+// density: the sum of (w)counts times the folded W taps of kernelSmoothing
+// (check_negative skips a negative smoothing, the first estimate, :4640).
+// The reference scatters bin by bin in ascending order; here each grid
+// position gathers the bins whose folded kernel reaches it, in the same
+// ascending order, so the sums are the reference's and repeatable.  First the
+// taps of every bin (one warp per bin; m = -1 for a bin that adds nothing)
+// and the largest half-width, then the gather.
+__global__ void __launch_bounds__(kThreads) ser_wtap_kernel(SerParams P, SerBins B, int check_negative, WTap *taps,
+                                                            int *mmax) {
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * kWarps + (threadIdx.x >> 5);
   if (i >= B.na) return;
   const double h = B.ks[i];
-  if ((check_negative && h < 0.0) || h == 0.0) return;
+  if ((check_negative && h < 0.0) || h == 0.0) {
+    if (lane == 0) taps[i].m = -1;
+    return;
+  }
   const WTap t = make_w(h, P.b, lane);
-  const int g = B.act[i] + 1;
-  const int q0 = max(g - t.m, 1), q1 = min(g + t.m, P.G);
-  const double c = val[i];
-  for (int q = q0 + lane; q <= q1; q += 32) atomicAdd(dens + q - 1, c * folded(t, q, g, P.G, t.sum));
+  if (lane == 0) {
+    taps[i] = t;
+    atomicMax(mmax, t.m);
+  }
+}
+
+// the first active bin index whose grid position (1-based) is >= g
+__device__ inline int first_bin_at(const SerBins &B, int g) {
+  int lo = 0, hi = B.na;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (B.act[mid] + 1 < g) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// out[q-1] = sum over the bins i reaching q, ascending, of val[i] * folded taps
+template <typename Tap, bool NORM>
+__global__ void ser_gather_kernel(SerParams P, SerBins B, const Tap *taps, const int *mmax, const double *val,
+                                  double *out) {
+  const int M = *mmax;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x + 1; q <= P.G; q += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    if (M >= 0) {
+      for (int i = first_bin_at(B, q - M); i < B.na && B.act[i] + 1 <= q + M; ++i) {
+        const Tap t = taps[i];
+        const int g = B.act[i] + 1;
+        if (t.m < 0 || q < g - t.m || q > g + t.m) continue;
+        double norm = 0.0;
+        if constexpr (NORM) norm = t.sum;
+        acc += val[i] * folded(t, q, g, P.G, norm);
+      }
+    }
+    out[q - 1] = acc;
+  }
 }
 
 // nEstimate with the current support, the support update, nEstimate again
@@ -330,25 +374,35 @@ __global__ void ser_cb_kernel(SerParams P, SerBins B) {
   B.cb[i] = cb;
 }
 
-// curvature: scatter of counts times the second-derivative taps of the
-// curvature bandwidth (prComputeNetRoughness1D, GridProjectedKDE.F90:1666-1760)
-__global__ void __launch_bounds__(kThreads) ser_curv_kernel(SerParams P, SerBins B, double *curv) {
+// curvature: the sum of counts times the second-derivative taps of the
+// curvature bandwidth (prComputeNetRoughness1D, GridProjectedKDE.F90:1666-1760),
+// as a gather like the density: the taps of every bin (m = -1 where the
+// reference skips the bin: a negative, NaN or zero bandwidth, or a kernel
+// whose sum of squares is zero), then ser_gather_kernel<SdTap, false>.
+__global__ void __launch_bounds__(kThreads) ser_sdtap_kernel(SerParams P, SerBins B, SdTap *taps, int *mmax) {
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * kWarps + (threadIdx.x >> 5);
   if (i >= B.na) return;
   const double h = B.cb[i];
-  if (h < 0.0 || h != h || h == 0.0) return;
+  if (h < 0.0 || h != h || h == 0.0) {
+    if (lane == 0) taps[i].m = -1;
+    return;
+  }
   const SdTap t = make_sd(h, P.b, P.sd_c0);
   double s = 0.0;  // the sum of squares decides a zero kernel
   for (int j = -t.m + lane; j <= t.m; j += 32) {
     const double v = t.zp(j < 0 ? -j : j);
     s += v * v;
   }
-  if (warp_sum(s) <= 0.0) return;
-  const int g = B.act[i] + 1;
-  const int q0 = max(g - t.m, 1), q1 = min(g + t.m, P.G);
-  const double c = B.cnt[i];
-  for (int q = q0 + lane; q <= q1; q += 32) atomicAdd(curv + q - 1, c * folded(t, q, g, P.G, 0.0));
+  const double ss = warp_sum(s);
+  if (lane == 0) {
+    if (ss <= 0.0) {
+      taps[i].m = -1;
+    } else {
+      taps[i] = t;
+      atomicMax(mmax, t.m);
+    }
+  }
 }
 
 // curvature / binVolume / binSize^2, squared
@@ -620,17 +674,39 @@ extern "C" int mprw_gpkde_series(const double *times, const double *weights, int
   res->grid_origin = gorigin;
   if (nb > capacity) return MPRW_E_SIZE;
 
-  // weighted histogram (Histogram.F90:276-490)
+  // weighted histogram (Histogram.F90:276-490), fixed-point sums: a bin's
+  // sum is at most the total over all records (weights are >= 0), and
+  // 2^shift times that stays below 2^62
   const bool wfmt = (fmt >= 2);
   double *counts, *wcounts = nullptr;
   SCK(mem.alloc(&counts, nb));
-  SCK(cudaMemsetAsync(counts, 0, sizeof(double) * nb, s));
+  if (wfmt) SCK(mem.alloc(&wcounts, nb));
+  unsigned long long *fc, *fw = nullptr;
+  SCK(mem.alloc(&fc, nb));
+  SCK(cudaMemsetAsync(fc, 0, sizeof(unsigned long long) * nb, s));
   if (wfmt) {
-    SCK(mem.alloc(&wcounts, nb));
-    SCK(cudaMemsetAsync(wcounts, 0, sizeof(double) * nb, s));
+    SCK(mem.alloc(&fw, nb));
+    SCK(cudaMemsetAsync(fw, 0, sizeof(unsigned long long) * nb, s));
   }
-  ser_hist_kernel<<<blocks_of(n, kThreads), kThreads, 0, s>>>(dx, dw, n, gorigin, b, nb, o->exact_point ? 1 : 0,
-                                                               fmt, counts, wcounts);
+  auto shift_for = [](double bound) {
+    int e = 0;
+    std::frexp(std::max(bound, 1e-300), &e);
+    return 61 - e;
+  };
+  {
+    double tw = 0.0, tw2 = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+      tw += std::fabs(weights[i]);
+      tw2 += weights[i] * weights[i];
+    }
+    const double cb = fmt == 2 ? (double)n : (fmt == 3 ? tw2 : tw);
+    const int shc = shift_for(cb), shw = shift_for(tw);
+    ser_hist_kernel<<<blocks_of(n, kThreads), kThreads, 0, s>>>(dx, dw, n, gorigin, b, nb, o->exact_point ? 1 : 0,
+                                                                 fmt, std::ldexp(1.0, shc), std::ldexp(1.0, shw), fc,
+                                                                 fw);
+    ser_fixed_kernel<<<blocks_of(nb, kThreads), kThreads, 0, s>>>(fc, std::ldexp(1.0, -shc), counts, nb);
+    if (wfmt) ser_fixed_kernel<<<blocks_of(nb, kThreads), kThreads, 0, s>>>(fw, std::ldexp(1.0, -shw), wcounts, nb);
+  }
   double eff = 1.0;
   if (!wfmt) {
     const double total = h[S_SUMW];
@@ -703,6 +779,12 @@ extern "C" int mprw_gpkde_series(const double *times, const double *weights, int
   double *dens, *curv;
   SCK(mem.alloc(&dens, nb));
   SCK(mem.alloc(&curv, nb));
+  WTap *wtaps;
+  SdTap *sdtaps;
+  int *mmax;
+  SCK(mem.alloc(&wtaps, na));
+  SCK(mem.alloc(&sdtaps, na));
+  SCK(mem.alloc(&mmax, 2));
 
   // data statistics and the initial smoothing (GridProjectedKDE.F90:4020-4110)
   const double std_x = std::sqrt(var);
@@ -751,9 +833,10 @@ extern "C" int mprw_gpkde_series(const double *times, const double *weights, int
   const int eb = blocks_of(na, kThreads);      // one thread per bin
   const int wb = (na + kWarps - 1) / kWarps;   // one warp per bin
   auto density = [&](const double *val, int check_negative) -> cudaError_t {
-    cudaError_t e = cudaMemsetAsync(dens, 0, sizeof(double) * nb, s);
+    cudaError_t e = cudaMemsetAsync(mmax, 0xff, sizeof(int), s);  // -1
     if (e != cudaSuccess) return e;
-    ser_density_kernel<<<wb, kThreads, 0, s>>>(P, B, val, check_negative, dens);
+    ser_wtap_kernel<<<wb, kThreads, 0, s>>>(P, B, check_negative, wtaps, mmax);
+    ser_gather_kernel<WTap, true><<<blocks_of(nb, kThreads), kThreads, 0, s>>>(P, B, wtaps, mmax, val, dens);
     ser_dens_finish_kernel<<<blocks_of(nb, kThreads), kThreads, 0, s>>>(dens, nb, b);
     return cudaGetLastError();
   };
@@ -770,8 +853,9 @@ extern "C" int mprw_gpkde_series(const double *times, const double *weights, int
     ser_loop_init_kernel<<<eb, kThreads, 0, s>>>(B, S);
     ser_nest_kernel<<<wb, kThreads, 0, s>>>(P, B, dens);
     ser_cb_kernel<<<eb, kThreads, 0, s>>>(P, B);
-    SCK(cudaMemsetAsync(curv, 0, sizeof(double) * nb, s));
-    ser_curv_kernel<<<wb, kThreads, 0, s>>>(P, B, curv);
+    SCK(cudaMemsetAsync(mmax + 1, 0xff, sizeof(int), s));
+    ser_sdtap_kernel<<<wb, kThreads, 0, s>>>(P, B, sdtaps, mmax + 1);
+    ser_gather_kernel<SdTap, false><<<blocks_of(nb, kThreads), kThreads, 0, s>>>(P, B, sdtaps, mmax + 1, B.cnt, curv);
     ser_curv_square_kernel<<<blocks_of(nb, kThreads), kThreads, 0, s>>>(curv, nb, b);
     ser_rough_kernel<<<wb, kThreads, 0, s>>>(P, B, curv);
     ser_rough_reduce_kernel<<<1, kRed, 0, s>>>(B, S);
