@@ -61,6 +61,15 @@ module mprw_gpu
     real(c_double)     :: sum_dx(3), sum_dx2(3)     ! about the domain centre
   end type
 
+  type, bind(C) :: mprw_adj_options                ! differentiable walk
+    integer(c_int32_t) :: nzones, nsteps, checkpoint
+    real(c_double)     :: dt, velocity_floor
+    integer(c_int64_t) :: seed                     ! uint64 in C
+    real(c_double)     :: origin(3), bin_size(3)
+    integer(c_int32_t) :: n_bins(3)
+    real(c_double)     :: bandwidth(3)
+  end type
+
   type, bind(C) :: mprw_series_options             ! the observation post-process GPKDE
     real(c_double)     :: origin, domain_size, bin_size
     integer(c_int32_t) :: bin_format               ! obs%histogramBinFormat
@@ -185,6 +194,17 @@ module mprw_gpu
         bind(C, name="mprw_autotune")
       import; type(c_ptr), value :: h; real(c_double), value :: t_begin, t_end
       integer(c_int32_t) :: blocks_per_sm, sort_interval; type(c_ptr), value :: rates
+    end function
+    integer(c_int) function mprw_adj_setup(h, zones, opt) bind(C, name="mprw_adj_setup")
+      import; type(c_ptr), value :: h; integer(c_int32_t), intent(in) :: zones(*)
+      type(mprw_adj_options), intent(in) :: opt
+    end function
+    integer(c_int) function mprw_adj_forward(h, theta, density) bind(C, name="mprw_adj_forward")
+      import; type(c_ptr), value :: h; real(c_double), intent(in) :: theta(*); real(c_double) :: density(*)
+    end function
+    integer(c_int) function mprw_adj_backward(h, grad_density, grad_theta) bind(C, name="mprw_adj_backward")
+      import; type(c_ptr), value :: h; real(c_double), intent(in) :: grad_density(*)
+      real(c_double) :: grad_theta(*)
     end function
     integer(c_int) function mprw_set_timeout(h, timeout_ms) bind(C, name="mprw_set_timeout")
       import; type(c_ptr), value :: h; real(c_double), value :: timeout_ms

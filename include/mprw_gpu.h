@@ -420,6 +420,66 @@ int mprw_get_tuning(mprw_handle *h, int32_t *blocks_per_sm, int32_t *sort_interv
 int mprw_autotune(mprw_handle *h, double t_begin, double t_end, int32_t *blocks_per_sm, int32_t *sort_interval,
                   double *rates);
 
+/* Differentiable random walk and its adjoint.  No counterpart in the
+ * reference: its step is not differentiable in the parameters (a step cut at
+ * a cell face shifts every later normal to another step, TrackSubCell.F90:
+ * 956-1368, and the histogram deposit, Histogram.F90:276-350, is piecewise
+ * constant), so a gradient of a concentration misfit needs a walk whose path
+ * is continuous in the parameters.  This variant sits beside the tracking
+ * path and leaves it unchanged:
+ *   - fields on the lattice of cell corners, interpolated trilinearly: pore
+ *     velocity u = s q / (phi R) from the Darcy flux of the loaded flow
+ *     (averaged over the faces that meet at a corner), the drift correction
+ *     div(phi D) / phi by central differences of the corner values of phi D
+ *     (the reference's div D term, TrackSubCell.F90:2695-2818), alphaL,
+ *     alphaT and Dm of each corner's share of the zones;
+ *   - D = (alphaT r + Dm/R) I + (alphaL - alphaT) u u^T / r with r =
+ *     sqrt(|u|^2 + velocity_floor^2): the reference's tensor where the
+ *     velocity is well above the floor, smooth where it vanishes;
+ *   - a fixed time step dt: x' = x + (u + div term) dt + B xi sqrt(dt), with
+ *     B B^T = 2 D (TrackSubCell.F90:2821-2928) and B smooth in u;
+ *     reflection at every domain wall;
+ *   - xi: normals keyed by (seed, particle id, step): a perturbed run draws
+ *     the same numbers (common random numbers);
+ *   - the density on a grid: a deposit of a product biweight kernel of
+ *     half-width bandwidth[d] per dimension (dimensions with one bin are
+ *     integrated over), per unit length / area / volume.
+ * Parameters theta (3 nzones + 1 doubles): alphaL of each zone, alphaT of
+ * each zone, porosity of each zone, then a velocity scale s (1 = the loaded
+ * flow).  The grid must be uniform (equal cell sizes) with one retardation.
+ * The pathwise gradient is exact for this discrete model; it is a useful
+ * estimate of the gradient of the expected misfit while the particles travel
+ * a few correlation lengths of the velocity field at most -- over longer
+ * runs in a heterogeneous field the paths' sensitivities grow fast.
+ *   mprw_adj_setup     zones (one 0-based zone per cell, < nzones), the walk
+ *                      and density grid; the walkers are the handle's
+ *                      particles that are ACTIVE or PENDING (pending ones
+ *                      start at the first step), from their positions now
+ *   mprw_adj_forward   runs nsteps steps for theta, storing the positions
+ *                      every `checkpoint` steps, and returns the density
+ *                      (prod n_bins doubles, x fastest); repeatable to the
+ *                      last bit
+ *   mprw_adj_backward  given dL/d density of the last forward run, the
+ *                      gradient dL/d theta (3 nzones + 1 doubles): the
+ *                      hand-written reverse sweep of every step, each
+ *                      segment recomputed from its checkpoint */
+typedef struct {
+  int32_t nzones;        /* 1..64                                          */
+  int32_t nsteps;        /* steps of a run                                 */
+  int32_t checkpoint;    /* steps between stored positions (1..nsteps)     */
+  double dt;             /* time step                                      */
+  double velocity_floor; /* > 0, in the velocity's units                   */
+  uint64_t seed;         /* Philox key of the normals                      */
+  double origin[3];      /* density grid                                   */
+  double bin_size[3];
+  int32_t n_bins[3];
+  double bandwidth[3];   /* biweight half-width per dimension              */
+} mprw_adj_options;
+
+int mprw_adj_setup(mprw_handle *h, const int32_t *zones, const mprw_adj_options *opt);
+int mprw_adj_forward(mprw_handle *h, const double *theta, double *density);
+int mprw_adj_backward(mprw_handle *h, const double *grad_density, double *grad_theta);
+
 /* Cancellation of mprw_advance (the reference has none: its loops end by
  * their own caps).  The step kernel reads a cancel flag in mapped host memory
  * every few hundred iterations of each warp.  mprw_set_timeout: an advance

@@ -27,6 +27,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include "../../include/mprw_gpu.h"
+#include "adjoint.cuh"
 #include "gpkde.cuh"
 #include "mprw_kernels.cuh"
 
@@ -63,6 +64,8 @@ struct mprw_handle {
   CellRec<double> *d_rec64 = nullptr;
   CellRec<float> *d_rec32 = nullptr;
   bool flow_loaded = false;
+  bool dm_uniform = true;             // dm_eff of the loaded flow holds one value
+  AdjState *adj = nullptr;            // differentiable walk (mprw_adj_*), made on first set-up
   // particles
   int64_t n = 0, cap = 0;
   int32_t *d_cell = nullptr, *d_status = nullptr;
@@ -164,6 +167,11 @@ cudaError_t upload(mprw_handle *h, T **p, const T *src, size_t count) {
 }
 
 void free_all(mprw_handle *h) {
+  if (h->adj) {
+    h->adj->release();
+    delete h->adj;
+    h->adj = nullptr;
+  }
   if (h->parent) {
     // slices of the batch's arrays
     h->d_rec64 = nullptr;
@@ -467,6 +475,7 @@ int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *f) {
   if (f->boundary_flows) CK(upload(h, &h->d_bflow, f->boundary_flows, 6 * nc));
   CK(upload(h, &h->d_por, f->porosity, nc));
   CK(upload(h, &h->d_ret, f->retardation, nc));
+  h->dm_uniform = f->uniform_dispersion != 0;
   if (h->parent)
     CK(cudaMemcpyAsync(h->d_ibts, f->iboundts, sizeof(int32_t) * nc, cudaMemcpyHostToDevice, h->stream));
   else
@@ -1713,6 +1722,114 @@ int mprw_destroy(mprw_handle *h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   free_all(h);
   delete h;
+  return MPRW_OK;
+}
+
+// ---- differentiable walk and its adjoint (adjoint.cu) ----
+int mprw_adj_setup(mprw_handle *h, const int32_t *zones, const mprw_adj_options *o) {
+  NvtxRange nvtx_("mprw_adj_setup");
+  if (!h) return MPRW_E_INVAL;
+  if (h->parent || !h->members.empty()) return fail(h, MPRW_E_STATE, "mprw_adj_setup: not on a batch or member");
+  if (!zones || !o) return fail(h, MPRW_E_INVAL, "mprw_adj_setup: null argument");
+  if (!h->flow_loaded) return fail(h, MPRW_E_STATE, "mprw_adj_setup before mprw_load_flow");
+  const GridDims g = h->g;
+  const int64_t ncell = g.ncell;
+  // a uniform grid: equal column widths, row widths and cell thicknesses
+  std::vector<double> delr(g.ncol), delc(g.nrow), botm(ncell), ret(ncell);
+  CK(cudaMemcpy(delr.data(), h->d_delr, sizeof(double) * g.ncol, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(delc.data(), h->d_delc, sizeof(double) * g.nrow, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(botm.data(), h->d_botm, sizeof(double) * ncell, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(ret.data(), h->d_ret, sizeof(double) * ncell, cudaMemcpyDeviceToHost));
+  const double dx = delr[0], dy = delc[0], dz = h->h_top_cell[0] - botm[0];
+  bool uniform = dx > 0.0 && dy > 0.0 && dz > 0.0;
+  for (double v : delr) uniform = uniform && v == dx;
+  for (double v : delc) uniform = uniform && v == dy;
+  for (int64_t c = 0; c < ncell && uniform; ++c)
+    uniform = std::fabs((h->h_top_cell[c] - botm[c]) - dz) <= 1e-12 * dz && botm[c] == botm[(c / g.ncpl) * g.ncpl];
+  if (!uniform) return fail(h, MPRW_E_INVAL, "mprw_adj_setup: the walk needs a uniform grid (equal cell sizes)");
+  for (int64_t c = 0; c < ncell; ++c)
+    if (ret[c] != ret[0]) return fail(h, MPRW_E_INVAL, "mprw_adj_setup: the walk needs a uniform retardation");
+  AdjInputs in{};
+  in.g = g;
+  in.geo = geometry(h);
+  in.base = h->base;
+  in.iboundts = h->d_ibts;
+  in.dm = h->d_dm;
+  in.dm_uniform = h->dm_uniform ? 1 : 0;
+  in.R = ret[0];
+  in.lo[0] = 0.0;
+  in.lo[1] = 0.0;
+  in.lo[2] = botm[(int64_t)(g.nlay - 1) * g.ncpl];
+  in.d[0] = dx;
+  in.d[1] = dy;
+  in.d[2] = dz;
+  in.n = h->n;
+  in.cell = h->d_cell;
+  in.status = h->d_status;
+  in.x = h->d_x;
+  in.y = h->d_y;
+  in.z = h->d_z;
+  in.mixed = h->opt.precision == MPRW_MIXED;
+  in.mass = h->unit_mass ? nullptr : h->d_mass;
+  in.id = h->has_id ? h->d_id : nullptr;
+  AdjOptions ao{};
+  ao.nzones = o->nzones;
+  ao.dt = o->dt;
+  ao.eps = o->velocity_floor;
+  ao.nsteps = o->nsteps;
+  ao.checkpoint = o->checkpoint;
+  ao.seed = o->seed;
+  for (int d = 0; d < 3; ++d) {
+    ao.origin[d] = o->origin[d];
+    ao.bin[d] = o->bin_size[d];
+    ao.h[d] = o->bandwidth[d];
+    ao.nb[d] = o->n_bins[d];
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  if (!h->adj) h->adj = new AdjState();
+  std::vector<char> err;
+  const cudaError_t e = h->adj->setup(in, ao, zones, err);
+  if (e == cudaErrorInvalidValue && !err.empty()) return fail(h, MPRW_E_INVAL, std::string("mprw_adj_setup: ") + err.data());
+  if (e == cudaErrorMemoryAllocation) return fail(h, MPRW_E_OOM, "mprw_adj_setup: device memory");
+  CK(e);
+  return MPRW_OK;
+}
+
+int mprw_adj_forward(mprw_handle *h, const double *theta, double *density) {
+  NvtxRange nvtx_("mprw_adj_forward");
+  if (!h) return MPRW_E_INVAL;
+  if (!h->adj) return fail(h, MPRW_E_STATE, "mprw_adj_forward before mprw_adj_setup");
+  if (!theta || !density) return fail(h, MPRW_E_INVAL, "mprw_adj_forward: null argument");
+  const int nz = h->adj->o.nzones;
+  for (int k = 0; k < 3 * nz + 1; ++k)
+    if (!std::isfinite(theta[k])) return fail(h, MPRW_E_INVAL, "mprw_adj_forward: non-finite parameter");
+  for (int z = 0; z < nz; ++z)
+    if (!(theta[2 * nz + z] > 0.0) || theta[z] < 0.0 || theta[nz + z] < 0.0)
+      return fail(h, MPRW_E_INVAL, "mprw_adj_forward: porosity must be > 0 and dispersivities >= 0");
+  CK(cudaEventRecord(h->ev0, h->stream));
+  CK(h->adj->forward(theta, density, h->stream));
+  CK(cudaEventRecord(h->ev1, h->stream));
+  CK(cudaEventSynchronize(h->ev1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  h->step_ms = ms;
+  h->launches = h->adj->launches;
+  return MPRW_OK;
+}
+
+int mprw_adj_backward(mprw_handle *h, const double *grad_density, double *grad_theta) {
+  NvtxRange nvtx_("mprw_adj_backward");
+  if (!h) return MPRW_E_INVAL;
+  if (!h->adj || !h->adj->forward_done) return fail(h, MPRW_E_STATE, "mprw_adj_backward before mprw_adj_forward");
+  if (!grad_density || !grad_theta) return fail(h, MPRW_E_INVAL, "mprw_adj_backward: null argument");
+  CK(cudaEventRecord(h->ev0, h->stream));
+  CK(h->adj->backward(grad_density, grad_theta, h->stream));
+  CK(cudaEventRecord(h->ev1, h->stream));
+  CK(cudaEventSynchronize(h->ev1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  h->step_ms = ms;
+  h->launches = h->adj->launches;
   return MPRW_OK;
 }
 

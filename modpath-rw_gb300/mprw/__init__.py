@@ -66,6 +66,12 @@ class GpkdeSums(C.Structure):
                 ("sum_dx", C.c_double * 3), ("sum_dx2", C.c_double * 3)]
 
 
+class AdjOptions(C.Structure):
+    _fields_ = [("nzones", C.c_int32), ("nsteps", C.c_int32), ("checkpoint", C.c_int32), ("dt", C.c_double),
+                ("velocity_floor", C.c_double), ("seed", C.c_uint64), ("origin", C.c_double * 3),
+                ("bin_size", C.c_double * 3), ("n_bins", C.c_int32 * 3), ("bandwidth", C.c_double * 3)]
+
+
 class SeriesOptions(C.Structure):
     _fields_ = [("origin", C.c_double), ("domain_size", C.c_double), ("bin_size", C.c_double),
                 ("bin_format", C.c_int32), ("bin_size_fraction", C.c_double), ("adapt_grid", C.c_int32),
@@ -111,6 +117,9 @@ def load_library() -> C.CDLL:
         "mprw_histogram": (C.c_int, [H, _dp, _dp, _ip, _dp, C.POINTER(C.c_int64), _dp]),
         "mprw_gpkde": (C.c_int, [H, C.POINTER(GpkdeOptions), _dp, _dp, _ip, _ip]),
         "mprw_gpkde_partial": (C.c_int, [H, C.POINTER(GpkdeOptions), _dp, C.POINTER(GpkdeSums)]),
+        "mprw_adj_setup": (C.c_int, [H, _ip, C.POINTER(AdjOptions)]),
+        "mprw_adj_forward": (C.c_int, [H, _dp, _dp]),
+        "mprw_adj_backward": (C.c_int, [H, _dp, _dp]),
         "mprw_gpkde_from_counts": (C.c_int, [H, C.POINTER(GpkdeOptions), _dp, C.POINTER(GpkdeSums), _dp, _dp, _ip,
                                              _ip]),
         "mprw_set_observations": (C.c_int, [H, C.c_int32, _ip, _ip, C.c_int32, _ip]),
@@ -365,6 +374,39 @@ class Tracker:
                     "mprw_gpkde_from_counts")
         shp = (nb[2], nb[1], nb[0])
         return dens.reshape(shp), hist.reshape(shp), loops.value
+
+    def adj_setup(self, zones, nzones, dt, nsteps, checkpoint, origin, bin_size, n_bins, bandwidth, velocity_floor,
+                  seed=0):
+        """The differentiable walk of this handle's particles (mprw_adj_setup)."""
+        z = _i32(zones)
+        if z.shape[0] != self.grid.ncell:
+            raise ValueError("one zone per cell")
+        o = AdjOptions()
+        o.nzones, o.nsteps, o.checkpoint, o.dt, o.seed = int(nzones), int(nsteps), int(checkpoint), float(dt), int(seed)
+        o.velocity_floor = float(velocity_floor)
+        for d in range(3):
+            o.origin[d], o.bin_size[d], o.n_bins[d], o.bandwidth[d] = (float(origin[d]), float(bin_size[d]),
+                                                                      int(n_bins[d]), float(bandwidth[d]))
+        self._adj = dict(nz=int(nzones), nb=tuple(int(v) for v in n_bins))
+        self._check(self.lib.mprw_adj_setup(self.h, _p(z, _ip), C.byref(o)), "mprw_adj_setup")
+
+    def adj_forward(self, theta):
+        """Density (shaped (nz, ny, nx)) of the walk for theta = (alphaL per zone, alphaT per zone,
+        porosity per zone, velocity scale)."""
+        th = _f64(theta)
+        if th.shape[0] != 3 * self._adj["nz"] + 1:
+            raise ValueError("theta: 3 nzones + 1 values")
+        nb = self._adj["nb"]
+        dens = np.empty(int(np.prod(nb)))
+        self._check(self.lib.mprw_adj_forward(self.h, _p(th, _dp), _p(dens, _dp)), "mprw_adj_forward")
+        return dens.reshape(nb[2], nb[1], nb[0])
+
+    def adj_backward(self, grad_density):
+        """dL/dtheta from dL/d(density) of the last adj_forward."""
+        g = _f64(np.asarray(grad_density).reshape(-1))
+        out = np.empty(3 * self._adj["nz"] + 1)
+        self._check(self.lib.mprw_adj_backward(self.h, _p(g, _dp), _p(out, _dp)), "mprw_adj_backward")
+        return out
 
     def set_observations(self, cells, obs, style):
         """Observation cells: cells (1-based) belong to observations obs (0-based);

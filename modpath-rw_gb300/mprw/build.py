@@ -18,7 +18,8 @@ SRC_DIR = PKG_DIR.parent / "csrc"
 BUILD_DIR = PKG_DIR.parent / "build"
 LIB_PATH = PKG_DIR / "libmprw_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "prep.cu", "step.cu", "hist.cu", "sort.cu", "gpkde.cu", "noalloc.cu", "obs.cu", "series.cu"]
+SOURCES = ["api.cu", "prep.cu", "step.cu", "hist.cu", "sort.cu", "gpkde.cu", "noalloc.cu", "obs.cu", "series.cu",
+           "adjoint.cu"]
 # The per-cell records and model coordinates follow the reference's operation
 # order exactly, so these units are compiled without multiply-add contraction.
 NO_FMAD = {"prep.cu", "hist.cu", "noalloc.cu"}

@@ -48,5 +48,10 @@ int main(void) {
   F(mprw_gpkde_sums, n_active); F(mprw_gpkde_sums, sum_w); F(mprw_gpkde_sums, sum_w2);
   F(mprw_gpkde_sums, sum_dx); F(mprw_gpkde_sums, sum_dx2);
   END(mprw_gpkde_sums);
+  F(mprw_adj_options, nzones); F(mprw_adj_options, nsteps); F(mprw_adj_options, checkpoint);
+  F(mprw_adj_options, dt); F(mprw_adj_options, velocity_floor); F(mprw_adj_options, seed);
+  F(mprw_adj_options, origin); F(mprw_adj_options, bin_size); F(mprw_adj_options, n_bins);
+  F(mprw_adj_options, bandwidth);
+  END(mprw_adj_options);
   return 0;
 }

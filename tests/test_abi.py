@@ -74,7 +74,8 @@ def _ctypes_mirrors():
     import mprw
     return {"mprw_grid_desc": mprw.GridDesc, "mprw_options": mprw.OptionsDesc, "mprw_flow_desc": mprw.FlowDesc,
             "mprw_gpkde_options": mprw.GpkdeOptions, "mprw_series_options": mprw.SeriesOptions,
-            "mprw_series_result": mprw.SeriesResult, "mprw_gpkde_sums": mprw.GpkdeSums}
+            "mprw_series_result": mprw.SeriesResult, "mprw_gpkde_sums": mprw.GpkdeSums,
+            "mprw_adj_options": mprw.AdjOptions}
 
 
 def test_header_structs_are_all_probed(c_layout):
