@@ -43,7 +43,7 @@ constexpr double kSqrt2 = 1.4142135623730951;
 
 enum {
   S_SUMX, S_MINX, S_MAXX, S_SUMW, S_SUMW2, S_BAD, S_SUMDX2,
-  S_MAXD, S_MAXD_OLD, S_ERRD, S_ERRS, S_ALMISE, S_NETMAX, S_MAXSCALE, S_NA,
+  S_MAXD, S_MAXD_OLD, S_ERRD, S_ERRS, S_ALMISE, S_NETMAX, S_MAXSCALE, S_NA, S_SUMABSW,
   S_COUNT
 };
 
@@ -156,7 +156,7 @@ __device__ inline double w_gather(const double *field, double h, int g, const Se
 __global__ void __launch_bounds__(kRed) ser_stats_kernel(const double *x, const double *w, int64_t n, double *S) {
   using BR = cub::BlockReduce<double, kRed>;
   __shared__ typename BR::TempStorage tmp;
-  double sx = 0.0, mn = INFINITY, mx = -INFINITY, sw = 0.0, sw2 = 0.0, bad = 0.0;
+  double sx = 0.0, mn = INFINITY, mx = -INFINITY, sw = 0.0, sw2 = 0.0, bad = 0.0, swa = 0.0;
   for (int64_t i = threadIdx.x; i < n; i += kRed) {
     const double xi = x[i], wi = w[i];
     if (!isfinite(xi) || !isfinite(wi)) bad += 1.0;
@@ -165,6 +165,7 @@ __global__ void __launch_bounds__(kRed) ser_stats_kernel(const double *x, const 
     mx = fmax(mx, xi);
     sw += wi;
     sw2 += wi * wi;
+    swa += fabs(wi);
   }
   double r;
   r = BR(tmp).Sum(sx);
@@ -184,6 +185,9 @@ __global__ void __launch_bounds__(kRed) ser_stats_kernel(const double *x, const 
   __syncthreads();
   r = BR(tmp).Sum(bad);
   if (threadIdx.x == 0) S[S_BAD] = r;
+  __syncthreads();
+  r = BR(tmp).Sum(swa);
+  if (threadIdx.x == 0) S[S_SUMABSW] = r;
 }
 
 __global__ void __launch_bounds__(kRed) ser_var_kernel(const double *x, int64_t n, double mean, double *S) {
@@ -312,25 +316,30 @@ __device__ inline int first_bin_at(const SerBins &B, int g) {
   return lo;
 }
 
-// out[q-1] = sum over the bins i reaching q, ascending, of val[i] * folded taps
+// out[q-1] = sum over the bins i reaching q of val[i] * folded taps: one warp
+// per grid position, lane l taking the candidate bins l, l+32, ... in
+// ascending order, then a fixed shuffle tree -- a fixed order, so the sum is
+// the same on every run.
 template <typename Tap, bool NORM>
-__global__ void ser_gather_kernel(SerParams P, SerBins B, const Tap *taps, const int *mmax, const double *val,
-                                  double *out) {
+__global__ void __launch_bounds__(kThreads) ser_gather_kernel(SerParams P, SerBins B, const Tap *taps,
+                                                              const int *mmax, const double *val, double *out) {
   const int M = *mmax;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x + 1; q <= P.G; q += gridDim.x * blockDim.x) {
-    double acc = 0.0;
-    if (M >= 0) {
-      for (int i = first_bin_at(B, q - M); i < B.na && B.act[i] + 1 <= q + M; ++i) {
-        const Tap t = taps[i];
-        const int g = B.act[i] + 1;
-        if (t.m < 0 || q < g - t.m || q > g + t.m) continue;
-        double norm = 0.0;
-        if constexpr (NORM) norm = t.sum;
-        acc += val[i] * folded(t, q, g, P.G, norm);
-      }
+  const int lane = threadIdx.x & 31;
+  const int q = blockIdx.x * kWarps + (threadIdx.x >> 5) + 1;
+  if (q > P.G) return;  // warp-uniform
+  double acc = 0.0;
+  if (M >= 0) {
+    for (int i = first_bin_at(B, q - M) + lane; i < B.na && B.act[i] + 1 <= q + M; i += 32) {
+      const Tap t = taps[i];
+      const int g = B.act[i] + 1;
+      if (t.m < 0 || q < g - t.m || q > g + t.m) continue;
+      double norm = 0.0;
+      if constexpr (NORM) norm = t.sum;
+      acc += val[i] * folded(t, q, g, P.G, norm);
     }
-    out[q - 1] = acc;
   }
+  acc = warp_sum(acc);
+  if (lane == 0) out[q - 1] = acc;
 }
 
 // nEstimate with the current support, the support update, nEstimate again
@@ -694,11 +703,8 @@ extern "C" int mprw_gpkde_series(const double *times, const double *weights, int
     return 61 - e;
   };
   {
-    double tw = 0.0, tw2 = 0.0;
-    for (int64_t i = 0; i < n; ++i) {
-      tw += std::fabs(weights[i]);
-      tw2 += weights[i] * weights[i];
-    }
+    // totals of the statistics pass (with a margin for their rounding)
+    const double tw = 1.0001 * h[S_SUMABSW], tw2 = 1.0001 * h[S_SUMW2];
     const double cb = fmt == 2 ? (double)n : (fmt == 3 ? tw2 : tw);
     const int shc = shift_for(cb), shw = shift_for(tw);
     ser_hist_kernel<<<blocks_of(n, kThreads), kThreads, 0, s>>>(dx, dw, n, gorigin, b, nb, o->exact_point ? 1 : 0,
@@ -836,7 +842,7 @@ extern "C" int mprw_gpkde_series(const double *times, const double *weights, int
     cudaError_t e = cudaMemsetAsync(mmax, 0xff, sizeof(int), s);  // -1
     if (e != cudaSuccess) return e;
     ser_wtap_kernel<<<wb, kThreads, 0, s>>>(P, B, check_negative, wtaps, mmax);
-    ser_gather_kernel<WTap, true><<<blocks_of(nb, kThreads), kThreads, 0, s>>>(P, B, wtaps, mmax, val, dens);
+    ser_gather_kernel<WTap, true><<<(nb + kWarps - 1) / kWarps, kThreads, 0, s>>>(P, B, wtaps, mmax, val, dens);
     ser_dens_finish_kernel<<<blocks_of(nb, kThreads), kThreads, 0, s>>>(dens, nb, b);
     return cudaGetLastError();
   };
@@ -855,7 +861,8 @@ extern "C" int mprw_gpkde_series(const double *times, const double *weights, int
     ser_cb_kernel<<<eb, kThreads, 0, s>>>(P, B);
     SCK(cudaMemsetAsync(mmax + 1, 0xff, sizeof(int), s));
     ser_sdtap_kernel<<<wb, kThreads, 0, s>>>(P, B, sdtaps, mmax + 1);
-    ser_gather_kernel<SdTap, false><<<blocks_of(nb, kThreads), kThreads, 0, s>>>(P, B, sdtaps, mmax + 1, B.cnt, curv);
+    ser_gather_kernel<SdTap, false><<<(nb + kWarps - 1) / kWarps, kThreads, 0, s>>>(P, B, sdtaps, mmax + 1, B.cnt,
+                                                                                   curv);
     ser_curv_square_kernel<<<blocks_of(nb, kThreads), kThreads, 0, s>>>(curv, nb, b);
     ser_rough_kernel<<<wb, kThreads, 0, s>>>(P, B, curv);
     ser_rough_reduce_kernel<<<1, kRed, 0, s>>>(B, S);
