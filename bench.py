@@ -263,6 +263,7 @@ def barrier():
 def run_gpu_arm(args, rank, world, local):
     import torch
     import mprw
+    from mprw import shard
     from mprw.model import MIXED
 
     torch.cuda.set_device(local)
@@ -289,7 +290,10 @@ def run_gpu_arm(args, rank, world, local):
         for _ in range(warmup):
             tr.advance(t, t + INTERVAL_D)
             plane.after_advance(t + INTERVAL_D)
-            tr.gpkde(domain, bins, origin, precision=kde_prec)
+            if world > 1:
+                shard.gpkde_allreduce(tr, domain, bins, origin, precision=kde_prec)
+            else:
+                tr.gpkde(domain, bins, origin, precision=kde_prec)
             t += INTERVAL_D
         torch.cuda.synchronize()
         barrier()
@@ -303,7 +307,12 @@ def run_gpu_arm(args, rank, world, local):
             s = tr.advance(t, t + INTERVAL_D)
             tm = tr.timings()
             ev[k][1].record(stream)
-            dens, _, nl = tr.gpkde(domain, bins, origin, precision=kde_prec)
+            if world > 1:
+                # one reconstruction of every rank's particles: the per-rank
+                # parts summed by an all-reduce, then smoothed on every rank
+                dens, _, nl = shard.gpkde_allreduce(tr, domain, bins, origin, precision=kde_prec)
+            else:
+                dens, _, nl = tr.gpkde(domain, bins, origin, precision=kde_prec)
             tk = tr.timings()
             ev[k][2].record(stream)
             torch.cuda.synchronize()
@@ -789,7 +798,8 @@ def main():
                                f"{args.particles} particles from the inlet slab, step = one 10-day interval "
                                "(advance + GPKDE reconstruction on the 1 m grid, density and histogram to host)",
                    "particles_per_gpu": args.particles, "interval_days": INTERVAL_D,
-                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"particles x{world}",
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"particles x{world}" + (
+                       ", one GPKDE of all ranks' particles per step (per-rank parts all-reduced)" if world > 1 else ""),
                    "flow_input": f"MODFLOW 6 binary .grb/.hds/.bud ({res['mf6_bytes']} B: FLOW-JA-FACE imeth 1, "
                                  "CHD imeth 6) written from the CG solve and read back by mprw.mf6io"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
