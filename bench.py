@@ -567,8 +567,8 @@ def adjoint_run(args, g, f, flush):
     same run with every parameter +10 %.  Forward and adjoint (the reverse
     sweep with every segment recomputed from its checkpoint) timed with CUDA
     events; five gradient components checked against central differences
-    (relative step 1e-4, common random numbers) on this run and on a short
-    run of the same particles (120 steps of 0.02 d)."""
+    (relative steps 1e-4 and 1e-5, common random numbers) on this run and on
+    a short run of the same particles (120 steps of 0.02 d)."""
     import mprw
     from mprw import workloads as W
     from mprw.model import ACTIVE, EULERIAN, MIN_ADV_DISP, Options
@@ -599,12 +599,15 @@ def adjoint_run(args, g, f, flush):
         check = {}
         for kk, name in ((0, "alphaL_zone0"), (nz, "alphaT_zone0"), (2 * nz, "porosity_zone0"),
                          (3 * nz - 1, "porosity_zone7"), (3 * nz, "velocity_scale")):
-            h = 1e-4 * abs(theta[kk])
-            e = np.zeros_like(theta)
-            e[kk] = h
-            fd = (loss(theta + e) - loss(theta - e)) / (2 * h)
-            check[name] = {"adjoint": float(gr[kk]), "central_difference": fd,
-                           "rel_error": abs(gr[kk] - fd) / max(abs(fd), 1e-300)}
+            c = {"adjoint": float(gr[kk])}
+            for rel in (1e-4, 1e-5):
+                h = rel * abs(theta[kk])
+                e = np.zeros_like(theta)
+                e[kk] = h
+                fd = (loss(theta + e) - loss(theta - e)) / (2 * h)
+                c[f"central_difference_{rel:g}"] = fd
+                c[f"rel_error_{rel:g}"] = abs(gr[kk] - fd) / max(abs(fd), 1e-300)
+            check[name] = c
         tr.close()
         return dict(fwd=float(np.median(fwd_ms[-2:] if timed else fwd_ms)),
                     bwd=float(np.median(bwd_ms[-2:] if timed else bwd_ms)), check=check,
@@ -623,10 +626,10 @@ def adjoint_run(args, g, f, flush):
             "gradient_check_100d": full["check"],
             "gradient_check_2.4d": short["check"],
             "note": "the adjoint is the exact derivative of the discrete walk (tests: torch autograd of an "
-                    "independent restatement to 1e-9); how well central differences reproduce it depends on how "
-                    "far the plume travels through the heterogeneous field -- over 100 days (about 20 cells) the "
-                    "paths' sensitivities grow fast and a relative step of 1e-4 no longer resolves them, over "
-                    "2.4 days (a few cells) it does"}
+                    "independent restatement to 1e-9); central differences approach it as their step shrinks "
+                    "(truncation error), more slowly the farther the plume travels through the heterogeneous "
+                    "field: over 100 days (about 20 cells) the paths' sensitivities grow fast and the misfit's "
+                    "higher derivatives with them"}
 
 
 def e2e_run(args, g, f, p, opt, origin, bins, domain, flush):
