@@ -1243,6 +1243,10 @@ int gpkde_params(mprw_handle *h, const mprw_gpkde_options *o, const char *who, K
       ++hd;
     }
   P.binvol = binvol;
+  {
+    int e = 0;
+    P.inv_binvol = (binvol > 0.0 && std::frexp(binvol, &e) == 0.5) ? 1.0 / binvol : 0.0;
+  }
   P.bin_distance = std::pow(binvol, 1.0 / (double)hd);
   const double nd = (double)P.ndim;
   P.support_c = std::pow((nd + 2.0) * std::pow(8.0 * PI_D, 0.5 * nd), 0.25);
@@ -1273,6 +1277,8 @@ int gpkde_params(mprw_handle *h, const mprw_gpkde_options *o, const char *who, K
   if (o->max_hover_delta * 4 * 2 + 1 > KDE_MAXLEN) return fail(h, MPRW_E_INVAL, std::string(who) + ": maxHOverDelta too large");
   P.min_hod = o->min_hover_delta;
   P.dlog = std::log(P.hod[1] / P.hod[0]);
+  for (int d = 0; d < 3; ++d) P.lscale[d] = P.bin[d] > 0.0 ? (float)(1.0 / (P.bin[d] * P.min_hod)) : 0.0f;
+  P.linv = (float)(1.0 / P.dlog);
   // bounded kernel sizes (boundKernelSizeFormat 0)
   int maxd = -1, mind = -1;
   for (int d = 0; d < 3; ++d) {

@@ -40,13 +40,67 @@ constexpr int kThreads = 256;
 constexpr int kBinThreads = 64;   // per-bin elementwise kernels: spread few bins over all SMs
 constexpr int kPassBlocks = 1216; // blocks of a separable pass: 8 per SM, grid-stride over all keys' regions
 
+// The database level of a kernel size h along dimension d:
+// floor(log(h / bin / minHOverDelta) / dlog) + 1, clamped to the database.
+// GB300 issues two FP64 lane-operations per clock per SM, and a double
+// logarithm is a few dozen of them, so in FP64 the quotient is first
+// estimated in FP32 (within 1e-4 of the FP64 value: the FP32 rounding of h
+// and the FP32 logarithm); the FP64 expression runs only when the estimate
+// lies within 1e-3 of an integer or is not finite.  The level is the FP64
+// expression's in every case.
 template <typename T>
 __device__ __forceinline__ int log_index(const KdeParams &P, T h, int d) {
   if (h <= T(0)) return 1;
-  int i = (int)floor(log(h / T(P.bin[d]) / T(P.min_hod)) / T(P.dlog)) + 1;
+  int i;
+  if constexpr (sizeof(T) == 8) {
+    const float v = logf((float)h * P.lscale[d]) * P.linv;
+    if (isfinite(v) && fabsf(v - rintf(v)) > 1e-3f) i = (int)floorf(v) + 1;
+    else i = (int)floor(log(h / T(P.bin[d]) / T(P.min_hod)) / T(P.dlog)) + 1;
+  } else {
+    i = (int)floor(log(h / T(P.bin[d]) / T(P.min_hod)) / T(P.dlog)) + 1;
+  }
   if (i < 1) i = 1;
   if (i > P.ndelta) i = P.ndelta;
   return i;
+}
+
+// Powers of the optimisation loop.  The reference raises to real exponents
+// (x**0.25, x**(1/(nDim+4)), ...), which its compiler evaluates with the C
+// library's pow.  Here each is its identity in square and cube roots where
+// the exponent allows (x^0.25 = sqrt(sqrt(x)), x^(1/6) = cbrt(sqrt(x)),
+// x^-(1/9) = 1/cbrt(cbrt(x)), ...) and exp(y log x) otherwise: a few
+// rounding errors (1e-15 relative for the exponents and arguments here)
+// instead of a pow that costs several times as many FP64 operations.  Every
+// argument is >= 0 (products and quotients of smoothed squares, densities
+// and kernel sizes); for x < 0 the forms give NaN as pow does, and x = 0
+// gives 0 (positive exponents) or +inf (negative ones) as pow does.
+template <typename T>
+__device__ __forceinline__ T root4(T x) { return sqrt(sqrt(x)); }
+template <typename T>
+__device__ __forceinline__ T pow_general(T x, T y) { return exp(y * log(x)); }
+// x^(1/nd)
+template <typename T>
+__device__ __forceinline__ T pow_inv_nd(T x, int nd) { return nd == 3 ? cbrt(x) : (nd == 2 ? sqrt(x) : x); }
+// x^(1 + nd/4)
+template <typename T>
+__device__ __forceinline__ T pow_one_plus_nd_q(T x, int nd) {
+  const T r = sqrt(x);
+  return nd == 3 ? x * r * sqrt(r) : (nd == 2 ? x * r : x * sqrt(r));
+}
+// x^(1/(nd+4))
+template <typename T>
+__device__ __forceinline__ T pow_one_over_nd4(T x, int nd, double y) {
+  return nd == 2 ? cbrt(sqrt(x)) : pow_general(x, T(y));
+}
+// x^(-1/(nd+6))
+template <typename T>
+__device__ __forceinline__ T pow_minus_one_over_nd6(T x, int nd, double y) {
+  return nd == 3 ? T(1) / cbrt(cbrt(x)) : (nd == 2 ? T(1) / sqrt(sqrt(sqrt(x))) : pow_general(x, T(y)));
+}
+// x^(2/((nd+4)(nd+6)))
+template <typename T>
+__device__ __forceinline__ T pow_beta(T x, int nd, double y) {
+  return nd == 2 ? cbrt(sqrt(sqrt(sqrt(x)))) : pow_general(x, T(y));
 }
 
 // Device scalars of one reconstruction (S, FP64): slot meanings
@@ -119,15 +173,6 @@ struct Span {
 constexpr int kWarpsW = 4;
 constexpr int kRowCache = 256;
 
-// database level of every bin's W kernel per dimension (one thread per bin:
-// the logarithm and divisions run on full warps)
-template <typename T>
-__global__ void wlevel_kernel(KdeParams P, KdeBinsT<T> B, int *wlev) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B.n) return;
-  for (int d = 0; d < 3; ++d) wlev[d * B.n + b] = P.mask[d] ? log_index<T>(P, B.ks[d * B.n + b], d) : 1;
-}
-
 __device__ __forceinline__ unsigned long long to_fixed(double v, double scale) {
   return (unsigned long long)__double2ll_rn(v * scale);
 }
@@ -135,9 +180,30 @@ __device__ __forceinline__ unsigned long long to_fixed(float v, float scale) {
   return (unsigned long long)__float2ll_rn(v * scale);
 }
 
+// round(a * b / 2^63) for a < 2^63, b <= 2^63 (the 128-bit product, rounded
+// to nearest), on the integer pipe
+__device__ __forceinline__ unsigned long long mulq63(unsigned long long a, unsigned long long b) {
+  const unsigned long long lo = a * b, lo2 = lo + (1ull << 62);
+  const unsigned long long hi = __umul64hi(a, b) + (lo2 < lo ? 1ull : 0ull);
+  return (hi << 1) | (lo2 >> 63);
+}
+
+// FP64 path of the density scatter on the integer pipe.  GB300 issues two FP64
+// lane-operations per clock per SM against 64 integer ones, and the scatter's
+// per-cell work is a product and a conversion to fixed point, so the folded
+// factors are converted once per bin to 63-bit fixed point (fx, fy, fz <= 1)
+// and the count to the grid's fixed point (|count| 2^shift < 2^62), and every
+// cell's contribution is the rounded integer product |count| fz fy fx:
+// three roundings of at most half a unit of 2^-shift, where the FP64 product
+// carried a relative 2^-53 -- the same density to far below the tolerance of
+// its FP64 reference.
+__device__ __forceinline__ unsigned long long fixed63(double f) {
+  return __double2ull_rn(f * 9223372036854775808.0);  // 2^63
+}
+
 template <typename T>
 __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, KdeBinsT<T> B, KdeTableT<T> tab,
-                                                                int stride, const int *wlev, T fscale,
+                                                                int stride, T fscale,
                                                                 unsigned long long *grid) {
   __shared__ T sv_all[kWarpsW][3 * KDE_MAXLEN];
   __shared__ int sm_all[kWarpsW][3], sofs_all[kWarpsW][3];
@@ -153,7 +219,8 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
   const int gid[3] = {B.gx[b], B.gy[b], B.gz[b]};
   if (lane < 3) {
     const int d = lane;
-    const int idx = wlev[d * B.n + b];
+    // the W kernel's database level along d (lanes 0-2, one dimension each)
+    const int idx = P.mask[d] ? log_index<T>(P, B.ks[d * B.n + b], d) : 1;
     sm_all[w][d] = tab.m[d * KDE_MAXDB + idx - 1];
     sofs_all[w][d] = tab.ofs[d * KDE_MAXDB + idx - 1];
   }
@@ -178,6 +245,54 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
   const T *fx = sv + S.k0[0], *fy = sv + KDE_MAXLEN + S.k0[1], *fz = sv + 2 * KDE_MAXLEN + S.k0[2];
   const int64_t sy = P.nb[0], sz = (int64_t)P.nb[0] * P.nb[1];
   unsigned long long *gbase = grid + (S.g0[0] - 1) + sy * (S.g0[1] - 1) + sz * (S.g0[2] - 1);
+  if constexpr (sizeof(T) == 8) {
+    // the factors to fixed point in place (each lane converts the entries it
+    // owns, then the warp reads them as integers)
+    unsigned long long *q = reinterpret_cast<unsigned long long *>(sv);
+    for (int d = 0; d < 3; ++d) {
+      const int len = 2 * sm_all[w][d] + 1;
+      for (int k = lane; k < len; k += 32) q[d * KDE_MAXLEN + k] = fixed63((double)sv[d * KDE_MAXLEN + k]);
+    }
+    __syncwarp();
+    const unsigned long long *qx = q + S.k0[0], *qy = q + KDE_MAXLEN + S.k0[1], *qz = q + 2 * KDE_MAXLEN + S.k0[2];
+    const long long ci = __double2ll_rn((double)cnt * (double)fscale);
+    const unsigned long long cm = (unsigned long long)(ci < 0 ? -ci : ci);
+    const bool neg = ci < 0;
+    auto row_val = [&](int iy, int iz) { return mulq63(mulq63(cm, qz[iz]), qy[iy]); };
+    auto emit = [&](unsigned long long *dst, unsigned long long r, int ix) {
+      const unsigned long long v = mulq63(r, qx[ix]);
+      if (v) atomicAdd(dst, neg ? (unsigned long long)(-(long long)v) : v);
+    };
+    unsigned long long *crq = reinterpret_cast<unsigned long long *>(crow_all[w]);
+    const bool cached = rows <= kRowCache;
+    if (cached) {
+      for (int r = lane; r < rows; r += 32) {
+        const int iz = r / n1, iy = r - iz * n1;
+        crq[r] = row_val(iy, iz);
+      }
+      __syncwarp();
+    }
+    if (n0 <= 32) {
+      const int rpi = 32 / n0, ix = lane % n0, r0 = lane / n0;
+      if (r0 >= rpi) return;
+      int iz = r0 / n1, iy = r0 - iz * n1;
+      for (int r = r0; r < rows; r += rpi) {
+        emit(gbase + ix + sy * iy + sz * iz, cached ? crq[r] : row_val(iy, iz), ix);
+        iy += rpi;
+        while (iy >= n1) {
+          iy -= n1;
+          ++iz;
+        }
+      }
+    } else {
+      for (int r = 0; r < rows; ++r) {
+        const int iz = r / n1, iy = r - iz * n1;
+        const unsigned long long rv = cached ? crq[r] : row_val(iy, iz);
+        for (int ix = lane; ix < n0; ix += 32) emit(gbase + ix + sy * iy + sz * iz, rv, ix);
+      }
+    }
+    return;
+  }
   // count * fy * fz per row (y fastest), cached when the span has few rows
   T *crow = crow_all[w];
   const bool cached = rows <= kRowCache;
@@ -221,12 +336,18 @@ __global__ void scale_pick_kernel(KdeParams P, KdeBinsT<T> B, const unsigned lon
                                   T *grid, int64_t ngrid, double *S) {
   const int64_t n = ngrid > B.n ? ngrid : (int64_t)B.n;
   const T bv = T(P.binvol);
+  // x / binVolume; a power-of-two volume (1 m^3, 0.5 m^3, ...) divides
+  // exactly as a product with its reciprocal, which costs one FP64 operation
+  // instead of a division's dozen (the host sets inv_binvol only then)
+  const bool pow2 = P.inv_binvol != 0.0;
+  const T ibv = T(P.inv_binvol);
+  auto per_vol = [&](T x) { return pow2 ? x * ibv : x / bv; };
   double dmax = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    if (i < ngrid) grid[i] = T((double)(long long)raw[i] * inv_scale) / bv;
+    if (i < ngrid) grid[i] = per_vol(T((double)(long long)raw[i] * inv_scale));
     if (i < B.n) {
       const int64_t g = (int64_t)(B.gx[i] - 1) + (int64_t)P.nb[0] * ((B.gy[i] - 1) + (int64_t)P.nb[1] * (B.gz[i] - 1));
-      const T d = T((double)(long long)raw[g] * inv_scale) / bv;
+      const T d = per_vol(T((double)(long long)raw[g] * inv_scale));
       B.dens[i] = d;
       dmax = fmax(dmax, (double)d);
     }
@@ -472,12 +593,28 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, KeyAcc 
   }
 }
 
+// A 64-bit integer division is a long software sequence on the GPU (longer
+// than a pass element's whole tap loop); pass elements and grid cells are
+// numbered below 2^31 in practice, where two 32-bit divisions do.
+__device__ __forceinline__ void split3(long long i, int nx, int ny, int &a, int &b, int &c) {
+  if (i <= 0x7fffffffLL) {
+    const unsigned ui = (unsigned)i, q = ui / (unsigned)nx, z = q / (unsigned)ny;
+    a = (int)(ui - q * (unsigned)nx);
+    b = (int)(q - z * (unsigned)ny);
+    c = (int)z;
+  } else {
+    const long long q = i / nx, z = q / ny;
+    a = (int)(i - q * nx);
+    b = (int)(q - z * ny);
+    c = (int)z;
+  }
+}
+
 __device__ __forceinline__ void region_xyz(const int r[6], long long i, int &x, int &y, int &z) {
-  const int nx = r[1] - r[0] + 1, ny = r[3] - r[2] + 1;
-  const long long q = i / nx;
-  x = r[0] + (int)(i - q * nx);
-  y = r[2] + (int)(q % ny);
-  z = r[4] + (int)(q / ny);
+  split3(i, r[1] - r[0] + 1, r[3] - r[2] + 1, x, y, z);
+  x += r[0];
+  y += r[2];
+  z += r[4];
 }
 
 __device__ __forceinline__ long long region_vol(const int r[6]) {
@@ -657,6 +794,8 @@ __global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, c
   // np == 0: the plan did not fit, the attempt is discarded
   const bool valid = b < B.n && pl->np != 0;
   double net = 0.0;
+  T acc[NC];
+  for (int c = 0; c < NC; ++c) acc[c] = T(0);
   if (valid) {
     const int j = pl->slot_of[bin_key[b]];
     const int m = pl->m[j][2], n = P.nb[2];
@@ -664,8 +803,6 @@ __global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, c
     const int *r2 = pl->r2[j];
     const T *in = T2 + pl->o2[j] * NC;
     const int bx = B.gx[b], by = B.gy[b], bz = B.gz[b];
-    T acc[NC];
-    for (int c = 0; c < NC; ++c) acc[c] = T(0);
     for (int t = 0; t <= 2 * m; ++t) {
       const int p = reflect_pos(bz - m + t, n);
       if (p < 1) continue;
@@ -673,6 +810,8 @@ __global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, c
       const long long l = region_loc(r2, bx, by, p) * NC;
       for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
     }
+  }
+  if (valid) {
     if constexpr (NC == 1) {
       if (mode == GZ_SUPPORT) {
         support_update<T>(P, B, b, acc[0]);
@@ -705,11 +844,11 @@ __global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, c
         // GridProjectedKDE.F90:2675-2676
         v = rxx + T(2) * rxy + T(2) * rxz + ryy + T(2) * ryz + rzz;
       } else {
-        const T third = T(1.0 / 3.0), sixth = T(1.0 / 6.0);
-        v = T(3) * pow(rxx * ryy * rzz, third);
-        if (ryz > T(0)) v = v + T(2) * ryz * pow(rxx * rxx / ryy / rzz, sixth);
-        if (rxz > T(0)) v = v + T(2) * rxz * pow(ryy * ryy / rxx / rzz, sixth);
-        if (rxy > T(0)) v = v + T(2) * rxy * pow(rzz * rzz / rxx / ryy, sixth);
+        // x^(1/3) = cbrt(x), x^(1/6) = cbrt(sqrt(x))
+        v = T(3) * cbrt(rxx * ryy * rzz);
+        if (ryz > T(0)) v = v + T(2) * ryz * cbrt(sqrt(rxx * rxx / ryy / rzz));
+        if (rxz > T(0)) v = v + T(2) * rxz * cbrt(sqrt(ryy * ryy / rxx / rzz));
+        if (rxy > T(0)) v = v + T(2) * rxy * cbrt(sqrt(rzz * rzz / rxx / ryy));
       }
       B.net[b] = v;
       net = (double)v;
@@ -814,25 +953,49 @@ __global__ void scatter_z_kernel(KdeParams P, const SepPlan *pl, const T *val, c
   const bool any = P.mask[axis] && u[0] <= u[1];
   const long long ngrid = (long long)P.nb[0] * P.nb[1] * P.nb[2];
   const int np = pl->np, n = P.nb[2];
+  // this axis's keys (consecutive slots: a key is axis * KDE_MAXDB + level
+  // and the slots are in key order) staged in shared memory once per block
+  __shared__ int s_r2[KDE_MAXDB][6], s_m[KDE_MAXDB], s_f[KDE_MAXDB];
+  __shared__ long long s_o2[KDE_MAXDB];
+  __shared__ int s_j0, s_nk;
+  if (threadIdx.x == 0) {
+    int j0 = 0;
+    while (j0 < np && pl->key[j0] < axis * KDE_MAXDB) ++j0;
+    int j1 = j0;
+    while (j1 < np && pl->key[j1] < (axis + 1) * KDE_MAXDB) ++j1;
+    s_j0 = j0;
+    s_nk = j1 - j0;
+  }
+  __syncthreads();
+  const int nk = s_nk;
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+    const int j = s_j0 + k;
+    for (int i = 0; i < 6; ++i) s_r2[k][i] = pl->r2[j][i];
+    s_m[k] = pl->m[j][2];
+    s_f[k] = pl->fofs[j][2];
+    s_o2[k] = pl->o2[j];
+  }
+  __syncthreads();
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ngrid; g += (long long)gridDim.x * blockDim.x) {
-    const int x = 1 + (int)(g % P.nb[0]);
-    const long long q = g / P.nb[0];
-    const int y = 1 + (int)(q % P.nb[1]), z = 1 + (int)(q / P.nb[1]);
+    int x, y, z;
+    split3(g, P.nb[0], P.nb[1], x, y, z);
+    ++x;
+    ++y;
+    ++z;
     if (!any || x < u[0] || x > u[1] || y < u[2] || y > u[3] || z < u[4] || z > u[5]) {
       out[g] = T(0);
       continue;
     }
     T acc = T(0);
-    for (int j = 0; j < np; ++j) {
-      if (pl->key[j] / KDE_MAXDB != axis) continue;
-      const int *r2 = pl->r2[j];
+    for (int k = 0; k < nk; ++k) {
+      const int *r2 = s_r2[k];
       if (x < r2[0] || x > r2[1] || y < r2[2] || y > r2[3]) continue;
-      const int m = pl->m[j][2];
+      const int m = s_m[k];
       if (z < r2[4] - m || z > r2[5] + m) continue;
       const long long sz = (long long)(r2[1] - r2[0] + 1) * (r2[3] - r2[2] + 1);
       const long long base = region_loc(r2, x, y, r2[4]) - (long long)r2[4] * sz;
-      acc += scatter_taps<T>(val + pl->fofs[j][2], m, z, n, r2[4], r2[5], V2 + pl->o2[j], sz, base, nullptr,
-                             nullptr, 0, nullptr);
+      acc += scatter_taps<T>(val + s_f[k], m, z, n, r2[4], r2[5], V2 + s_o2[k], sz, base, nullptr, nullptr, 0,
+                             nullptr);
     }
     T c = acc / bv;
     c = c / bs2;
@@ -849,7 +1012,7 @@ __device__ __forceinline__ T smoothing_scale(const KdeParams &P, const T ks[3]) 
     if (ks[d] != T(0)) out = out * ks[d];
     else dimc = dimc - 1;
   }
-  return (dimc != 0) ? pow(out, T(1.0 / (double)P.ndim)) : T(0);
+  return (dimc != 0) ? pow_inv_nd<T>(out, P.ndim) : T(0);
 }
 
 template <typename T>
@@ -875,7 +1038,7 @@ template <typename T>
 __device__ void support_update(const KdeParams &P, const KdeBinsT<T> &B, int b, T ne1) {
   const T dn = B.dens[b];
   // nEstimate**0.5: the correctly rounded square root (as the C library's pow)
-  T ssc = sqrt(ne1) * pow(B.scale[b], T(P.one_plus_nd_q)) / pow(T(4) * dn, T(0.25)) * T(P.support_c);
+  T ssc = sqrt(ne1) * pow_one_plus_nd_q<T>(B.scale[b], P.ndim) / root4<T>(T(4) * dn) * T(P.support_c);
   const T grow = T(P.max_sigma_growth) * B.support[b];
   if (ssc > grow) ssc = grow;
   ssc = fmin(ssc, T(P.max_k[P.max_dim]));
@@ -895,7 +1058,7 @@ __device__ void curvature_bandwidth(const KdeParams &P, const KdeBinsT<T> &B, in
     for (int k = 0; k < P.ndim; ++k) p = (k == 0) ? base : p * base;  // integer power, left to right
     if (P.ndim == 3) p = base * (base * base);
     const T ne = B.nest[b];
-    nvpb = pow(p * (ne * ne) / dn, T(P.beta_c));
+    nvpb = pow_beta<T>(p * (ne * ne) / dn, P.ndim, P.beta_c);
   }
   for (int d = 0; d < 3; ++d) {
     if (!P.mask[d]) continue;
@@ -907,7 +1070,9 @@ __device__ void curvature_bandwidth(const KdeParams &P, const KdeBinsT<T> &B, in
     }
     const T shd = B.shape[d * B.n + b];
     T term = T(0);
-    if (shd != T(0)) term = pow((T(P.one_over_nd4) / pow(shd, T(4))) * tsum, T(P.minus_one_over_nd6));
+    const T sh2 = shd * shd;
+    if (shd != T(0)) term = pow_minus_one_over_nd6<T>((T(P.one_over_nd4) / (sh2 * sh2)) * tsum, P.ndim,
+                                                      P.minus_one_over_nd6);
     T c = T(P.alpha_c) * nvpb * term * B.scale[b];
     if (c > T(P.max_sd[d])) c = T(P.max_sd[d]);
     if (c < T(P.min_sd[d])) c = T(P.min_sd[d]);
@@ -938,7 +1103,6 @@ __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBi
   __shared__ double red[kThreads / 32][3];
   double a[3] = {0.0, 0.0, 0.0};
   const double mx = S[S_DMAX], mx_old = S[S_DMAXOLD];
-  const T nd = T(P.ndim);
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
     if (what == RED_END) {
       const double dn = (double)B.dens[b], dold = (double)B.dens_old[b];
@@ -954,7 +1118,9 @@ __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBi
     }
     const T sc = B.scale[b];
     if (sc != T(0)) {
-      const T e = (B.nest[b] / (pow(sc, nd) * T(P.four_pi_half_nd)) + T(0.25) * B.net[b] * pow(sc, T(4))) / T(npts2);
+      const T sc2 = sc * sc;
+      const T scn = P.ndim == 3 ? sc2 * sc : (P.ndim == 2 ? sc2 : sc);
+      const T e = (B.nest[b] / (scn * T(P.four_pi_half_nd)) + T(0.25) * B.net[b] * (sc2 * sc2)) / T(npts2);
       a[2] += (double)e * (double)e;
     }
   }
@@ -1014,7 +1180,7 @@ __global__ void optimal_phase0_kernel(KdeParams P, KdeBinsT<T> B, double *S, int
       B.net[b] = net;
     }
     T sc = T(0);
-    if (net > T(0)) sc = pow(nd * B.nest[b] / (T(P.four_pi_half_nd) * net), T(P.one_over_nd4));
+    if (net > T(0)) sc = pow_one_over_nd4<T>(nd * B.nest[b] / (T(P.four_pi_half_nd) * net), P.ndim, P.one_over_nd4);
     B.scale[b] = sc;
     scv = (double)sc;
   }
@@ -1038,7 +1204,7 @@ __global__ void optimal_phase1_kernel(KdeParams P, KdeBinsT<T> B, const double *
     const T *rr[3] = {B.rxx, B.ryy, B.rzz};
     const T r1 = rr[P.d1][b], r2 = rr[P.d2][b], net = B.net[b];
     if (!(r1 == T(0) || r2 == T(0))) {
-      const T s1 = fmax(pow(net / r1, T(1.0 / 8.0)), T(P.min_k[P.d1]) / sc);
+      const T s1 = fmax(sqrt(sqrt(sqrt(net / r1))), T(P.min_k[P.d1]) / sc);  // ^(1/8)
       const T s2 = T(1) / s1;
       const T ns = sqrt(s1 * s2);
       if (ns != T(0)) {
@@ -1050,11 +1216,12 @@ __global__ void optimal_phase1_kernel(KdeParams P, KdeBinsT<T> B, const double *
   if (P.ndim == 3 && !P.isotropic) {
     const T rxx = B.rxx[b], ryy = B.ryy[b], rzz = B.rzz[b], net = B.net[b];
     if (!(rxx == T(0) || ryy == T(0) || rzz == T(0))) {
-      const T twelfth = T(1.0 / 12.0);
-      const T s1 = fmax(pow(net / rxx, twelfth), T(P.min_k[0]) / sc);
-      const T s2 = fmax(pow(net / ryy, twelfth), T(P.min_k[1]) / sc);
+      // ^(1/12) = cbrt(sqrt(sqrt()))
+      const T s1 = fmax(cbrt(root4<T>(net / rxx)), T(P.min_k[0]) / sc);
+      const T s2 = fmax(cbrt(root4<T>(net / ryy)), T(P.min_k[1]) / sc);
       const T s3 = T(1) / s1 / s2;
-      const T ns = pow(s1 * s2 * s3, T(0.333f));
+      // the reference's exponent is the single-precision literal 0.333
+      const T ns = pow_general<T>(s1 * s2 * s3, T(0.333f));
       if (ns != T(0)) {
         sh[0] = s1 / ns;
         sh[1] = s2 / ns;
@@ -1160,10 +1327,8 @@ __global__ void active_write_kernel(const double *counts, int64_t nbins, const i
     if (g >= nbins) break;
     const double v = counts[g];
     if (v == 0.0) continue;
-    const int ix = (int)(g % P.nb[0]);
-    const int64_t r = g / P.nb[0];
-    const int iy = (int)(r % P.nb[1]);
-    const int iz = (int)(r / P.nb[1]);
+    int ix, iy, iz;
+    split3(g, P.nb[0], P.nb[1], ix, iy, iz);
     B.gx[o] = ix + 1;
     B.gy[o] = iy + 1;
     B.gz[o] = iz + 1;
@@ -1191,12 +1356,12 @@ cudaError_t KdeState::ensure_bins(int n) {
   }
   void *old[] = {bins.gx, bins.gy, bins.gz, bins.count, bins.ks, bins.scale, bins.shape, bins.support, bins.nest,
                  bins.dens, bins.cb, bins.rxx, bins.ryy, bins.rzz, bins.net, bins.dens_old, bins.scale_old,
-                 partial, bin_key, wlev};
+                 partial, bin_key};
   for (void *p : old)
     if (p) cudaFree(p);
   bins = KdeBins{};
   partial = nullptr;
-  bin_key = wlev = nullptr;
+  bin_key = nullptr;
   cap = 0;
   // a quarter of headroom: a spreading plume activates more bins at almost
   // every reconstruction, and each regrowth frees and allocates ~20 arrays
@@ -1209,7 +1374,7 @@ cudaError_t KdeState::ensure_bins(int n) {
   auto D = [&](double **p, size_t k) {
     if (e == cudaSuccess) e = cudaMalloc((void **)p, sizeof(double) * k);
   };
-  I(&bins.gx, c); I(&bins.gy, c); I(&bins.gz, c); I(&bin_key, 4 * c); I(&wlev, 3 * c);
+  I(&bins.gx, c); I(&bins.gy, c); I(&bins.gz, c); I(&bin_key, 4 * c);
   D(&bins.count, c); D(&bins.ks, 3 * c); D(&bins.scale, c); D(&bins.shape, 3 * c); D(&bins.support, c);
   D(&bins.nest, c); D(&bins.dens, c); D(&bins.cb, 3 * c); D(&bins.rxx, c); D(&bins.ryy, c); D(&bins.rzz, c);
   D(&bins.net, c); D(&bins.dens_old, c); D(&bins.scale_old, c);
@@ -1277,7 +1442,7 @@ void KdeState::release() {
   void *ptrs[] = {bins.gx, bins.gy, bins.gz, bins.count, bins.ks, bins.scale, bins.shape, bins.support, bins.nest,
                   bins.dens, bins.cb, bins.rxx, bins.ryy, bins.rzz, bins.net, bins.dens_old, bins.scale_old,
                   partial, dens_grid, cx, cy, cz, d_scalars, d_flag, d_blockcnt, d_val, d_valf, d_meta, cell_bin,
-                  bin_key, d_keys, d_plan, t1, t2, dens_raw, d_need, wlev, cxy, cxz, cyz, dens_out};
+                  bin_key, d_keys, d_plan, t1, t2, dens_raw, d_need, cxy, cxz, cyz, dens_out};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_scalars) cudaFreeHost(h_scalars);
@@ -1424,11 +1589,10 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   unsigned long long *raw_fixed = reinterpret_cast<unsigned long long *>(st.dens_raw);
   auto density = [&](void) -> cudaError_t {
     KCK(cudaMemsetAsync(raw_fixed, 0, sizeof(unsigned long long) * ngrid, s));
-    wlevel_kernel<T><<<bb, kBinThreads, 0, s>>>(P, B, st.wlev);
-    wscatter_kernel<T><<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, wtab, wstride, st.wlev, T(fscale),
+    wscatter_kernel<T><<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, wtab, wstride, T(fscale),
                                                                             raw_fixed);
     scale_pick_kernel<T><<<blocks_for(npick), kThreads, 0, s>>>(P, B, raw_fixed, inv_fscale, dens_grid, ngrid, S);
-    st.launches += 3;
+    st.launches += 2;
     return cudaGetLastError();
   };
   // plans: [0] smoothing kernels (kind 1), [1] second-derivative kernels (kind 2)

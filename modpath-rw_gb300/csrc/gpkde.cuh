@@ -17,9 +17,11 @@ constexpr double SQRT8PI_D = 5.01325654926724104;  // sqrt(8*pi)
 struct KdeParams {
   int ndim, mask[3], nb[3];
   double bin[3], binvol, bin_distance;
+  double inv_binvol;  // 1 / binvol when binvol is a power of two (exact), else 0
   int ndelta;
   double hod[KDE_MAXDB];
   double min_hod, dlog;  // log database: index = floor(log(h/bin/min)/dlog)+1
+  float lscale[3], linv;  // FP32 estimate of the index: 1/(bin*min_hod), 1/dlog
   double max_k[3], min_k[3], max_sd[3], min_sd[3];
   int max_dim, min_dim;
   double support_c, alpha_c, beta_c, one_over_nd4, minus_one_over_nd6, one_plus_nd_q;
@@ -95,7 +97,6 @@ struct KdeState {
   int *d_flag = nullptr, *d_blockcnt = nullptr;
   int *cell_bin = nullptr;          // per grid cell: active bin index or -1
   int *bin_key = nullptr;           // per bin: smoothing key (n) and SD keys per axis (3n)
-  int *wlev = nullptr;              // per bin: W kernel database level per dimension (3n)
   KeyAcc *d_keys = nullptr;
   SepPlan *d_plan = nullptr;
   double *t1 = nullptr, *t2 = nullptr;
