@@ -787,23 +787,32 @@ enum { GZ_OUT = 0, GZ_SUPPORT = 1, GZ_NEST = 2, GZ_NET = 3 };
 
 // GZ_NET (1-D): out[b] = out2[b] = the roughness, which is the net roughness;
 // NC = 6 and GZ_NET also fold max(net) and min(net > 0) into S.
+// FP32: LPB = 4 lanes per bin split the taps (lane s of the group takes t =
+// s, s + 4, ...) and a fixed shuffle tree adds their sums (the same order on
+// every run): four times the warps of one thread per bin, whose tap loops
+// wait on L2 loads.  FP64: one thread per bin -- the bin's finish (roots and
+// quotients) is FP64-pipe work, which must run on full warps.
+template <typename T>
+constexpr int gz_lanes() { return sizeof(T) == 4 ? 4 : 1; }
+
 template <typename T, int NC>
 __global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, const T *val, const int *bin_key,
                                 const T *T2, int mode, T *out, T *out2, double *S) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int LPB = gz_lanes<T>();
+  const int b = (blockIdx.x * blockDim.x + threadIdx.x) / LPB, sub = threadIdx.x % LPB;
   // np == 0: the plan did not fit, the attempt is discarded
-  const bool valid = b < B.n && pl->np != 0;
+  const bool inb = b < B.n && pl->np != 0;
   double net = 0.0;
   T acc[NC];
   for (int c = 0; c < NC; ++c) acc[c] = T(0);
-  if (valid) {
+  if (inb) {
     const int j = pl->slot_of[bin_key[b]];
     const int m = pl->m[j][2], n = P.nb[2];
     const T *f = val + pl->fofs[j][2];
     const int *r2 = pl->r2[j];
     const T *in = T2 + pl->o2[j] * NC;
     const int bx = B.gx[b], by = B.gy[b], bz = B.gz[b];
-    for (int t = 0; t <= 2 * m; ++t) {
+    for (int t = sub; t <= 2 * m; t += LPB) {
       const int p = reflect_pos(bz - m + t, n);
       if (p < 1) continue;
       const T w = f[t];
@@ -811,6 +820,12 @@ __global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, c
       for (int c = 0; c < NC; ++c) acc[c] += w * in[l + c];
     }
   }
+  if constexpr (LPB > 1) {
+    // every lane of the warp takes part (lanes past the last bin add zeros)
+    for (int o = 1; o < LPB; o <<= 1)
+      for (int c = 0; c < NC; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+  }
+  const bool valid = inb && sub == 0;
   if (valid) {
     if constexpr (NC == 1) {
       if (mode == GZ_SUPPORT) {
@@ -1560,6 +1575,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   const int nb = B.n;
   const int64_t ngrid = (int64_t)P.nb[0] * P.nb[1] * P.nb[2];
   const int bb = (nb + kBinThreads - 1) / kBinThreads;
+  const int gzb = (int)(((long long)nb * gz_lanes<T>() + kBinThreads - 1) / kBinThreads);
   const int gb = blocks_for(ngrid);
   const int rb = std::min(blocks_for(nb), kRedBlocks);
   const int kb = std::min((nb + kThreads - 1) / kThreads, 2 * kRedBlocks);
@@ -1614,7 +1630,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   auto gather1 = [&](const T *field, int mode, T *out, T *out2) -> cudaError_t {
     gather_x_kernel<T, 1><<<pgrid, kThreads, 0, s>>>(P, plan1, val, Fields<T>{{field}}, t1);
     gather_y_kernel<T, 1><<<pgrid, kThreads, 0, s>>>(P, plan1, val, t1, t2);
-    gather_z_kernel<T, 1><<<bb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, mode, out, out2, S);
+    gather_z_kernel<T, 1><<<gzb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, mode, out, out2, S);
     st.launches += 3;
     return cudaGetLastError();
   };
@@ -1662,13 +1678,13 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
       products2d_kernel<T><<<gb, kThreads, 0, s>>>(c1, c2, cxy, ngrid);
       gather_x_kernel<T, 3><<<pgrid, kThreads, 0, s>>>(P, plan1, val, Fields<T>{{c1, c2, cxy}}, t1);
       gather_y_kernel<T, 3><<<pgrid, kThreads, 0, s>>>(P, plan1, val, t1, t2);
-      gather_z_kernel<T, 3><<<bb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, GZ_OUT, nullptr, nullptr, S);
+      gather_z_kernel<T, 3><<<gzb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, GZ_OUT, nullptr, nullptr, S);
       st.launches += 4;
     } else if (P.ndim == 3) {
       products_kernel<T><<<gb, kThreads, 0, s>>>(cx, cy, cz, cxy, cxz, cyz, ngrid);
       gather_x_kernel<T, 6><<<pgrid, kThreads, 0, s>>>(P, plan1, val, Fields<T>{{cx, cy, cz, cxy, cxz, cyz}}, t1);
       gather_y_kernel<T, 6><<<pgrid, kThreads, 0, s>>>(P, plan1, val, t1, t2);
-      gather_z_kernel<T, 6><<<bb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, GZ_OUT, nullptr, nullptr, S);
+      gather_z_kernel<T, 6><<<gzb, kBinThreads, 0, s>>>(P, B, plan1, val, key1, t2, GZ_OUT, nullptr, nullptr, S);
       st.launches += 4;
     } else {
       int a = 0;
