@@ -1402,8 +1402,8 @@ cudaError_t KdeState::ensure_bins(int n) {
 
 cudaError_t KdeState::ensure_grid(int64_t ngrid) {
   if (!d_scalars) {
-    cudaError_t e = cudaMalloc((void **)&d_scalars, 16 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMallocHost((void **)&h_scalars, 16 * sizeof(double));
+    cudaError_t e = cudaMalloc((void **)&d_scalars, 32 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&h_scalars, 32 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_keys, sizeof(KeyAcc));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_plan, 2 * sizeof(SepPlan));
@@ -1566,6 +1566,68 @@ void kde_build_tables(const KdeParams &P, std::vector<double> &val, std::vector<
     if (e_ != cudaSuccess) return e_;     \
   } while (0)
 
+// The optimisation loop on the device.  The loop body is the body of a
+// while node of a CUDA graph; its last kernel (one thread) takes the host
+// loop's convergence decision from the device scalars -- the same FP64
+// operations in the same order, each correctly rounded, so the same decision
+// -- and sets the node's condition.  The host reads the outcome once, after
+// the last loop, instead of synchronising on every loop.  Control slots of
+// the device scalars (after S_COUNT):
+enum { C_ALMOLD = 16, C_CUM = 17, C_CUMOLD = 18, C_LOOPS = 19, C_STATUS = 20 };
+// C_STATUS: 0 ran to convergence or to the loop limit, 1 a plan did not fit
+// its pass buffers (the attempt is discarded), 2 the net roughness is zero
+// everywhere (the reference stops, GridProjectedKDE.F90:5443-5446)
+
+__global__ void loop_ctl_init_kernel(double *S, int nb) {
+  const double alm = sqrt(S[S_ALMISE] / nb);
+  S[C_ALMOLD] = alm;
+  S[C_CUM] = alm;
+  S[C_CUMOLD] = alm;
+  S[C_LOOPS] = 0.0;
+  S[C_STATUS] = 0.0;
+}
+
+// GridProjectedKDE.F90:5000-5040: the convergence tests after a loop
+__global__ void loop_ctl_kernel(double *S, const long long *need, int nb, int n_opt_loops, double rel_err,
+                                int skip_error, cudaGraphConditionalHandle cond) {
+  const int m = (int)S[C_LOOPS] + 1;
+  S[C_LOOPS] = (double)m;
+  unsigned cont = 1;
+  if (need[2] != 0) {
+    S[C_STATUS] = 1.0;
+    cont = 0;
+  } else if (S[S_NETMAX] == 0.0) {
+    S[C_STATUS] = 2.0;
+    cont = 0;
+  } else {
+    const double err_dens = sqrt(S[S_ERRD] / nb), err_smooth = sqrt(S[S_ERRS] / nb);
+    const double alm = sqrt(S[S_ALMISE] / nb);
+    const double cum = S[C_CUM] + alm;
+    const double alm_old = S[C_ALMOLD], cum_old = S[C_CUMOLD];
+    S[C_CUM] = cum;
+    bool stop = false;
+    if (!skip_error) {
+      if (alm_old > 0.0 && fabs(alm - alm_old) / alm_old < rel_err) stop = true;
+      else if (err_dens < rel_err) stop = true;
+      else if (err_smooth < rel_err) stop = true;
+      else if (m > 7 && fabs(cum_old / (double)(m - 1) - cum / (double)m) / cum_old / (double)(m - 1) < rel_err)
+        stop = true;
+    }
+    if (stop || m >= n_opt_loops) {
+      cont = 0;
+    } else {
+      S[C_ALMOLD] = alm;
+      S[C_CUMOLD] = cum;
+    }
+  }
+  cudaGraphSetConditional(cond, cont);
+}
+
+__global__ void zero_u64_kernel(unsigned long long *a, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = 0ull;
+}
+
 // One reconstruction attempt in arithmetic type T; *overflow is set when a
 // plan found the pass buffers too small (the sizes it needed are in st.h_need).
 template <typename T>
@@ -1604,11 +1666,11 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   const double fscale = std::ldexp(1.0, shift), inv_fscale = std::ldexp(1.0, -shift);
   unsigned long long *raw_fixed = reinterpret_cast<unsigned long long *>(st.dens_raw);
   auto density = [&](void) -> cudaError_t {
-    KCK(cudaMemsetAsync(raw_fixed, 0, sizeof(unsigned long long) * ngrid, s));
+    zero_u64_kernel<<<blocks_for(ngrid), kThreads, 0, s>>>(raw_fixed, ngrid);
     wscatter_kernel<T><<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, wtab, wstride, T(fscale),
                                                                             raw_fixed);
     scale_pick_kernel<T><<<blocks_for(npick), kThreads, 0, s>>>(P, B, raw_fixed, inv_fscale, dens_grid, ngrid, S);
-    st.launches += 2;
+    st.launches += 3;
     return cudaGetLastError();
   };
   // plans: [0] smoothing kernels (kind 1), [1] second-derivative kernels (kind 2)
@@ -1655,7 +1717,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   // end of a loop that did not converge; nothing runs in between).  Every
   // data-dependent choice inside is taken on the device, so one captured
   // graph replays every loop.
-  auto body = [&](void) -> cudaError_t {
+  auto body_core = [&](void) -> cudaError_t {
     loop_init_kernel<T><<<bb, kBinThreads, 0, s>>>(B, S);
     st.launches += 1;
     // nEstimate with the current support, support update, nEstimate again
@@ -1700,7 +1762,10 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     st.launches += 3;
     // density with the new smoothing, then the convergence measures
     KCK(density());
-    KCK(reduce(RED_END));
+    return reduce(RED_END);
+  };
+  auto body = [&](void) -> cudaError_t {
+    KCK(body_core());
     return fetch_async();
   };
   KCK(cudaMemsetAsync(st.d_need, 0, 3 * sizeof(long long), s));
@@ -1709,6 +1774,63 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   st.launches += 2;
   KCK(density());
   KCK(reduce(RED_ALMISE));  // nEstimate and net roughness are zero: 0
+  {
+    // the whole loop as one graph: a while node around the captured body
+    cudaGraphExec_t dexec = nullptr;
+    int64_t dbody = 0;
+    cudaGraph_t g = nullptr;
+    if (cudaGraphCreate(&g, 0) == cudaSuccess) {
+      cudaGraphConditionalHandle cond;
+      cudaGraphNode_t node;
+      cudaGraphNodeParams cp{};
+      cp.type = cudaGraphNodeTypeConditional;
+      if (cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) == cudaSuccess) {
+        cp.conditional.handle = cond;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) == cudaSuccess &&
+            cudaStreamBeginCaptureToGraph(s, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+          const int64_t l0 = st.launches;
+          cudaError_t eb = body_core();
+          if (eb == cudaSuccess) {
+            loop_ctl_kernel<<<1, 1, 0, s>>>(S, st.d_need, nb, n_opt_loops, rel_err, skip_error ? 1 : 0, cond);
+            eb = cudaGetLastError();
+          }
+          cudaGraph_t out = nullptr;
+          const cudaError_t ee = cudaStreamEndCapture(s, &out);
+          dbody = st.launches - l0 + 1;
+          st.launches = l0;
+          if (eb == cudaSuccess && ee == cudaSuccess && cudaGraphInstantiate(&dexec, g, 0) != cudaSuccess)
+            dexec = nullptr;
+        }
+      }
+      cudaGraphDestroy(g);
+    }
+    (void)cudaGetLastError();  // a failed construction leaves no sticky error
+    if (dexec) {
+      struct ExecGuard {
+        cudaGraphExec_t e;
+        ~ExecGuard() { cudaGraphExecDestroy(e); }
+      } guard{dexec};
+      loop_ctl_init_kernel<<<1, 1, 0, s>>>(S, nb);
+      KCK(cudaGetLastError());
+      KCK(cudaGraphLaunch(dexec, s));
+      KCK(cudaMemcpyAsync(h, S, 32 * sizeof(double), cudaMemcpyDeviceToHost, s));
+      KCK(cudaMemcpyAsync(st.h_need, st.d_need, 3 * sizeof(long long), cudaMemcpyDeviceToHost, s));
+      KCK(cudaStreamSynchronize(s));
+      const int loops = (int)h[C_LOOPS];
+      st.launches += 1 + dbody * loops;
+      if (h[C_STATUS] == 1.0) {
+        *overflow = true;
+        return cudaSuccess;
+      }
+      if (h[C_STATUS] == 2.0) return cudaErrorInvalidValue;
+      if (loops_done) *loops_done = loops;
+      return cudaGetLastError();
+    }
+  }
+  // the loop driven from the host (a stream that cannot be captured)
   KCK(fetch_async());
   KCK(fetch_wait());
   double alm = std::sqrt(h[S_ALMISE] / nb);
