@@ -126,6 +126,37 @@ def test_gpkde_is_bitwise_repeatable(gpu_lib, case, precision):
         assert np.array_equal(d.view(np.uint64), d0.view(np.uint64))
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_host_driven_loop_matches_the_device_loop(gpu_lib, precision):
+    """On a stream that can be captured the optimisation loop runs on the
+    device (a while node of a CUDA graph whose last kernel takes the
+    convergence decision); on the legacy default stream, which cannot be
+    captured, the host drives it, reading the convergence scalars after every
+    loop.  Both take the same decisions from the same FP64 scalars: the same
+    loop count and the same density to the last bit (lognormal slab, 10^6
+    particles after 20 days)."""
+    from mprw.model import MIXED
+    prec = MIXED if precision == "mixed" else 0
+    g, f, p, opt, info = W.lognormal_slab(n_particles=1_000_000, seed=0, use_torch=True)
+    dom = (200.0, 100.0, 20.0)
+    tr = mprw.Tracker(g, opt)
+    tr.load_flow(f)
+    tr.set_particles(p)
+    tr.advance(0.0, 20.0)
+    d_dev, h_dev, l_dev = tr.gpkde(dom, (1.0, 1.0, 1.0), precision=prec)
+    launches_dev = tr.timings()["launches"]
+    tr.set_stream(1)  # cudaStreamLegacy
+    d_host, h_host, l_host = tr.gpkde(dom, (1.0, 1.0, 1.0), precision=prec)
+    launches_host = tr.timings()["launches"]
+    tr.set_stream(0)
+    tr.close()
+    assert l_dev == l_host > 0
+    np.testing.assert_array_equal(h_dev, h_host)
+    assert np.array_equal(d_dev.view(np.uint64), d_host.view(np.uint64))
+    # the device loop adds its decision kernel per loop
+    assert launches_dev > launches_host
+
+
 @pytest.mark.parametrize("isotropic", [False, True], ids=["anisotropic", "isotropic"])
 def test_gpkde_2d_on_the_reference_example_grid(gpu_lib, isotropic):
     """2-D reconstruction on the grid of the reference's GPKDE example
