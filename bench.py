@@ -298,7 +298,7 @@ def run_gpu_arm(args, rank, world, local):
         torch.cuda.synchronize()
         barrier()
         ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
-        kern_ms, kde_ms, wall_ms, steps_done, launches, loops = [], [], [], 0, 0, []
+        kern_ms, kde_ms, wall_ms, steps_done, launches, loops, madds = [], [], [], 0, 0, [], []
         for k in range(steps):
             flush.zero_()
             torch.cuda.synchronize()
@@ -320,6 +320,7 @@ def run_gpu_arm(args, rank, world, local):
             plane.after_advance(t + INTERVAL_D)
             kern_ms.append(tm["step_ms"])
             kde_ms.append(tk["gpkde_ms"])
+            madds.append(tk["gpkde_madds"])
             loops.append(nl)
             launches += tm["launches"] + tk["launches"]
             steps_done += s
@@ -336,7 +337,7 @@ def run_gpu_arm(args, rank, world, local):
             kde_err = {"l2_rel": float(np.linalg.norm(dens - d64) / np.linalg.norm(d64)),
                        "max_rel": float(np.abs(dens - d64).max() / d64.max())}
         tr.close()
-        return dict(ms=ms, adv_ms=adv_ms, kern_ms=kern_ms, kde_ms=kde_ms, wall_ms=wall_ms, steps=steps_done,
+        return dict(ms=ms, adv_ms=adv_ms, kern_ms=kern_ms, kde_ms=kde_ms, madds=madds, wall_ms=wall_ms, steps=steps_done,
                     launches=launches, out=out, t_end=t, loops=loops, dens=dens, kde_err=kde_err, tuning=tuning,
                     btc150=plane.curve)
 
@@ -635,6 +636,25 @@ def adjoint_run(args, g, f, flush):
                     "(about 20 cells) the paths' sensitivities grow and the differences are coarser"}
 
 
+def gpkde_roofline(madds, kde_ms, sm_mhz, fp32):
+    """The reconstruction against the issue rate of its arithmetic type: the
+    work model (multiply-adds of the reference's direct 3-D kernels, summed
+    over the optimisation loops; mprw_last_gpkde_work) per second of the
+    reconstructions' CUDA-event time, against 152 SMs x FP64 2 (FP32 128)
+    multiply-add lanes per clock at the sampled SM clock."""
+    lanes = 128 if fp32 else 2
+    peak = 152 * lanes * sm_mhz * 1e6
+    achieved = float(np.sum(madds)) / (float(np.sum(kde_ms)) / 1e3)
+    return {"bound": "fp32 issue" if fp32 else "fp64 issue", "achieved": achieved, "peak": peak,
+            "unit": "multiply-adds/s", "frac": achieved / peak,
+            "model": "per loop and active bin |K_W| + 8 |K_sigma| + 3 |K_SD| multiply-adds, |K| = prod_d "
+                     "(2 ceil(r hOverDelta_d) + 1) at the bin's database levels (r = 3; 4 for second derivatives); "
+                     "the separable passes do a fraction of it, so frac > 1 means fewer operations than direct "
+                     "kernels, not more than the hardware issues",
+            "peak_source": "nominal lanes per SM per clock at the sampled SM clock",
+            "madds_per_reconstruction": float(np.mean(madds)), "ms_per_reconstruction": float(np.mean(kde_ms))}
+
+
 def e2e_run(args, g, f, p, opt, origin, bins, domain, flush):
     """Through the C ABI with pinned host buffers; copies inside the timed region."""
     import ctypes as C
@@ -827,6 +847,8 @@ def main():
                               "advance_event_ms": float(np.sum(fp["adv_ms"])),
                               "gpkde_ms": float(np.sum(fp["kde_ms"])), "step_event_ms": float(np.sum(fp["ms"])),
                               "step_wall_ms": float(np.sum(fp["wall_ms"])), "gpkde_loops": fp["loops"]},
+        "gpkde_roofline": gpkde_roofline(fp["madds"], fp["kde_ms"], res["clocks"]["sm_mhz"] or 2070.0,
+                                         args.precision == "mixed"),
     }
     if "e2e" in res:
         e = res["e2e"]
@@ -847,7 +869,9 @@ def main():
                          "moment_error_vs_fp64": err, "active_fp64": n64,
                          "active_mixed": n32, "kernel_ms": float(np.mean(mx["kern_ms"])),
                          "gpkde_ms": float(np.mean(mx["kde_ms"])), "gpkde_precision": "fp32", "tuning": mx["tuning"],
-                         "gpkde_fp32_vs_fp64_same_particles": mx["kde_err"]}
+                         "gpkde_fp32_vs_fp64_same_particles": mx["kde_err"],
+                         "gpkde_roofline": gpkde_roofline(mx["madds"], mx["kde_ms"],
+                                                          res["clocks"]["sm_mhz"] or 2070.0, True)}
     line["lognormal_slab_btc_150m"] = {
         "curve": fp["btc150"], "control_plane_x_m": 150.0,
         "counts": "after every 10-day advance (warm-up included): ACTIVE particles at or beyond x = 150 m plus "

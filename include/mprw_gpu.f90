@@ -220,6 +220,9 @@ module mprw_gpu
       import; type(c_ptr), value :: h; real(c_double) :: step_ms, prep_ms, hist_ms, gpkde_ms
       integer(c_int64_t) :: launches
     end function
+    integer(c_int) function mprw_last_gpkde_work(h, madds) bind(C, name="mprw_last_gpkde_work")
+      import; type(c_ptr), value :: h; real(c_double) :: madds
+    end function
     integer(c_int) function mprw_destroy(h) bind(C, name="mprw_destroy")
       import; type(c_ptr), value :: h
     end function

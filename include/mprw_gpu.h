@@ -129,7 +129,9 @@ int mprw_load_flow(mprw_handle *h, const mprw_flow_desc *flow);
  * The next advance processes the particles heaviest first by the passes each
  * took in the previous advance (their rng_ctr increments) when n is
  * unchanged -- a host that hands back the particles mprw_get_particles gave
- * it keeps that order; results never depend on the order. */
+ * it keeps that order; results never depend on the order.  A cell outside
+ * 1..ncell fails with MPRW_E_INVAL (checked on the device after the copy; the
+ * handle then holds no particles until the next successful call). */
 int mprw_set_particles(mprw_handle *h, int64_t n, const int32_t *cell, const double *lx,
                        const double *ly, const double *lz, const double *t,
                        const int32_t *status, const double *mass, const uint64_t *id,
@@ -506,6 +508,15 @@ int mprw_set_stream(mprw_handle *h, void *stream);
  * NULL. */
 int mprw_last_timings(mprw_handle *h, double *step_ms, double *prep_ms, double *hist_ms,
                       double *gpkde_ms, int64_t *launches);
+
+/* Work model of the last mprw_gpkde (0 when it had no active bins): the
+ * multiply-adds of the reference's direct 3-D kernels, summed over its
+ * optimisation loops -- per loop and active bin |K_W| + 8 |K_sigma| + 3 |K_SD|
+ * with |K| = prod_d (2 ceil(r hOverDelta_d) + 1) at the bin's database levels
+ * (r = 3 for W and the smoothing kernel, 4 for the second derivatives).
+ * Divided by the reconstruction's time it is the rate a direct evaluation
+ * would need; the library's separable passes do a fraction of it. */
+int mprw_last_gpkde_work(mprw_handle *h, double *madds);
 
 int mprw_destroy(mprw_handle *h);
 

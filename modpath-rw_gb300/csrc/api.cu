@@ -80,6 +80,7 @@ struct mprw_handle {
   bool unit_mass = true;
   bool has_id = false;
   unsigned long long *d_counters = nullptr;  // [0] queue, [1] steps, [2] nbinned
+  int *d_pflags = nullptr;            // particle upload checks: [0] a cell out of range, [1] a mass other than 1
   unsigned long long *h_counters = nullptr;  // pinned
   void *scratch = nullptr;
   size_t scratch_bytes = 0;
@@ -87,6 +88,7 @@ struct mprw_handle {
   size_t hscratch_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   double step_ms = 0, prep_ms = 0, hist_ms = 0, kde_ms = 0;
+  double kde_work = 0;  // work model of the last reconstruction (multiply-adds of direct kernels)
   KdeState kde;
   // observation cells
   int32_t *d_obs_of_cell = nullptr, *d_obs_style = nullptr;
@@ -201,7 +203,8 @@ void free_all(mprw_handle *h) {
                   h->d_src, h->d_snk, h->d_aL, h->d_aT, h->d_dm, h->d_aLV, h->d_aTV, h->d_ibts, h->d_icb, h->d_ctype,
                   h->d_zones, h->base.q, h->base.dz, h->base.conn, h->base.flags, h->d_massb, h->d_rec64,
                   h->d_rec32, h->d_cell, h->d_status, h->d_x, h->d_y, h->d_z, h->d_t, h->d_mass,
-                  h->d_stage, h->d_ctr, h->d_ctr_prev, h->d_id, h->d_perm, h->d_counters, h->scratch};
+                  h->d_stage, h->d_ctr, h->d_ctr_prev, h->d_id, h->d_perm, h->d_counters, h->scratch,
+                  h->d_pflags};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->h_counters) cudaFreeHost(h->h_counters);
@@ -229,6 +232,30 @@ __global__ void f32_to_f64_kernel(const float *in, double *out, int64_t n) {
 __global__ void cell_shift_kernel(int32_t *cell, int64_t n, int32_t delta) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     cell[i] += delta;
+}
+// The uploaded cells (1-based) checked against 1..ncell and shifted to the
+// stored numbering; flag[0] is set when any is out of range.  One warp vote
+// and at most one atomic per warp.
+__global__ void cell_check_shift_kernel(int32_t *cell, int64_t n, int32_t ncell, int32_t delta, int *flag) {
+  bool bad = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c = cell[i];
+    bad = bad || c < 1 || c > ncell;
+    cell[i] = c + delta;
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+// flag set when any mass differs from 1
+__global__ void unit_mass_kernel(const double *m, int64_t n, int *flag) {
+  bool other = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    other = other || m[i] != 1.0;
+  if (__any_sync(0xffffffffu, other) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+// stored cells back to the caller's 1-based numbering
+__global__ void cell_out_kernel(const int32_t *cell, int64_t n, int32_t delta, int32_t *out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = cell[i] + delta;
 }
 __global__ void mul2_kernel(double *x, int64_t n, double a, double b) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -574,7 +601,7 @@ namespace {
 // they are too small).  Cells arrive 1-based and are stored 0-based + shift.
 int upload_particles(mprw_handle *h, int64_t n, const int32_t *cell, const double *lx, const double *ly,
                      const double *lz, const double *t, const int32_t *status, const double *mass,
-                     const uint64_t *id, const uint64_t *rng_ctr, int32_t shift) {
+                     const uint64_t *id, const uint64_t *rng_ctr, int32_t shift, int32_t ncell_check) {
   const bool mixed = h->opt.precision == MPRW_MIXED;
   const size_t rs = mixed ? sizeof(float) : sizeof(double);
   if (n > h->cap) {
@@ -603,8 +630,13 @@ int upload_particles(mprw_handle *h, int64_t n, const int32_t *cell, const doubl
   h->advance_count = 0;
   if (n == 0) return MPRW_OK;
   cudaStream_t s = h->stream;
+  if (!h->d_pflags) CK(cudaMalloc(&h->d_pflags, 2 * sizeof(int)));
+  CK(cudaMemsetAsync(h->d_pflags, 0, 2 * sizeof(int), s));
   CK(cudaMemcpyAsync(h->d_cell, cell, 4 * n, cudaMemcpyHostToDevice, s));
-  cell_shift_kernel<<<grid1d(n), 256, 0, s>>>(h->d_cell, n, shift);
+  if (ncell_check > 0)
+    cell_check_shift_kernel<<<grid1d(n), 256, 0, s>>>(h->d_cell, n, ncell_check, shift, h->d_pflags);
+  else
+    cell_shift_kernel<<<grid1d(n), 256, 0, s>>>(h->d_cell, n, shift);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(h->d_status, status, 4 * n, cudaMemcpyHostToDevice, s));
   const double *src[3] = {lx, ly, lz};
@@ -622,14 +654,23 @@ int upload_particles(mprw_handle *h, int64_t n, const int32_t *cell, const doubl
   CK(cudaMemcpyAsync(h->d_t, t, 8 * n, cudaMemcpyHostToDevice, s));
   h->unit_mass = true;
   if (mass) {
-    for (int64_t p = 0; p < n && h->unit_mass; ++p) h->unit_mass = (mass[p] == 1.0);
     CK(cudaMemcpyAsync(h->d_mass, mass, 8 * n, cudaMemcpyHostToDevice, s));
+    unit_mass_kernel<<<grid1d(n), 256, 0, s>>>(h->d_mass, n, h->d_pflags + 1);
+    CK(cudaGetLastError());
   }
   h->has_id = id != nullptr;
   if (id) CK(cudaMemcpyAsync(h->d_id, id, 8 * n, cudaMemcpyHostToDevice, s));
   if (rng_ctr) CK(cudaMemcpyAsync(h->d_ctr, rng_ctr, 8 * n, cudaMemcpyHostToDevice, s));
   else CK(cudaMemsetAsync(h->d_ctr, 0, 8 * n, s));
+  int flags[2] = {0, 0};
+  CK(cudaMemcpyAsync(flags, h->d_pflags, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  if (flags[0]) {
+    // the device arrays were overwritten: the handle holds no particles
+    h->n = 0;
+    return fail(h, MPRW_E_INVAL, "particle cell number out of range");
+  }
+  h->unit_mass = (mass == nullptr) || flags[1] == 0;
   return MPRW_OK;
 }
 
@@ -651,9 +692,9 @@ int mprw_set_particles(mprw_handle *h, int64_t n, const int32_t *cell, const dou
     if ((id != nullptr) != h->parent->has_id)
       return fail(h, MPRW_E_INVAL, "a batch member's particles carry ids exactly when the batch's do");
   }
-  for (int64_t p = 0; p < n; ++p)
-    if (cell[p] < 1 || cell[p] > h->g.ncell) return fail(h, MPRW_E_INVAL, "particle cell number out of range");
-  return upload_particles(h, n, cell, lx, ly, lz, t, status, mass, id, rng_ctr, h->cell0 - 1);
+  // the cells are checked against 1..ncell on the device (the upload fails,
+  // and the handle then holds no particles, when one is out of range)
+  return upload_particles(h, n, cell, lx, ly, lz, t, status, mass, id, rng_ctr, h->cell0 - 1, h->g.ncell);
 }
 
 int mprw_set_particles_batch(mprw_handle *h, const int64_t *counts, const int32_t *cell, const double *lx,
@@ -678,7 +719,7 @@ int mprw_set_particles_batch(mprw_handle *h, const int64_t *counts, const int32_
         if (cell[p] < 1 || cell[p] > h->members[k]->g.ncell)
           return fail(h, MPRW_E_INVAL, "member " + std::to_string(k) + ": particle cell number out of range");
   }
-  int rc = upload_particles(h, n, cell, lx, ly, lz, t, status, mass, id, rng_ctr, -1);
+  int rc = upload_particles(h, n, cell, lx, ly, lz, t, status, mass, id, rng_ctr, -1, 0);
   if (rc != MPRW_OK) return rc;
   const size_t rs = h->opt.precision == MPRW_MIXED ? sizeof(float) : sizeof(double);
   int64_t p0 = 0;
@@ -1035,7 +1076,20 @@ int mprw_get_particles(mprw_handle *h, int32_t *cell, double *lx, double *ly, do
   cudaStream_t s = h->stream;
   const bool mixed = h->opt.precision == MPRW_MIXED;
   if (cell) {
-    CK(cudaMemcpyAsync(cell, h->d_cell, 4 * n, cudaMemcpyDeviceToHost, s));
+    // back to 1-based cells on the device, through the scratch buffer
+    const size_t need = (size_t)4 * n;
+    if (h->scratch_bytes < need) {
+      if (h->scratch) cudaFree(h->scratch);
+      h->scratch = nullptr;
+      h->scratch_bytes = 0;
+      CK(cudaMalloc(&h->scratch, need));
+      h->scratch_bytes = need;
+    }
+    cell_out_kernel<<<grid1d(n), 256, 0, s>>>(h->d_cell, n, 1 - h->cell0, (int32_t *)h->scratch);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(cell, h->scratch, 4 * n, cudaMemcpyDeviceToHost, s));
+    // the scratch buffer is reused for the model coordinates below
+    if (gx || gy || gz) CK(cudaStreamSynchronize(s));
   }
   double *outs[3] = {lx, ly, lz};
   void *srcs[3] = {h->d_x, h->d_y, h->d_z};
@@ -1077,8 +1131,6 @@ int mprw_get_particles(mprw_handle *h, int32_t *cell, double *lx, double *ly, do
     if (gz) CK(cudaMemcpyAsync(gz, g2, 8 * n, cudaMemcpyDeviceToHost, s));
   }
   CK(cudaStreamSynchronize(s));
-  if (cell)
-    for (int64_t p = 0; p < n; ++p) cell[p] += 1 - h->cell0;
   return MPRW_OK;
 }
 
@@ -1335,6 +1387,7 @@ int gpkde_reconstruct(mprw_handle *h, const mprw_gpkde_options *o, KdeParams &P,
   int nactive = 0;
   CK(kde_collect_active(*h->kdep, P, h->d_counts, s, &nactive));
   int loops = 0;
+  h->kde_work = 0.0;
   if (nactive > 0) {
     // initial smoothing (initialSmoothingSelection 0: Silverman-type scale)
     double prod = 1.0;
@@ -1384,6 +1437,7 @@ int gpkde_reconstruct(mprw_handle *h, const mprw_gpkde_options *o, KdeParams &P,
                             o->skip_error_convergence != 0, fp32, s, &loops);
     if (e == cudaErrorInvalidValue) return fail(h, MPRW_E_INVAL, "mprw_gpkde: net roughness is zero everywhere");
     CK(e);
+    h->kde_work = h->kdep->work_madds;
     // effective mass, unit volume, scaling (GridProjectedKDE.F90:4292-4306, 5080-5084)
     double f = eff;
     double scale = 1.0;
@@ -1719,6 +1773,12 @@ int mprw_last_timings(mprw_handle *h, double *step_ms, double *prep_ms, double *
   if (hist_ms) *hist_ms = h->hist_ms;
   if (gpkde_ms) *gpkde_ms = h->kde_ms;
   if (launches) *launches = h->launches;
+  return MPRW_OK;
+}
+
+int mprw_last_gpkde_work(mprw_handle *h, double *madds) {
+  if (!h || !madds) return MPRW_E_INVAL;
+  *madds = h->kde_work;
   return MPRW_OK;
 }
 

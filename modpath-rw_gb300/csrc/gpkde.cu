@@ -108,8 +108,9 @@ __device__ __forceinline__ T pow_beta(T x, int nd, double y) {
 //   S_DMAX    max density                 S_DMAXOLD    max previous density
 //   S_ERRD    sum of squared density changes   S_ERRS  ... smoothing changes
 //   S_ALMISE  sum of squared ALMISE terms S_SCMAX      max positive smoothing scale
+//   S_WORK    the reconstruction's work model, summed over its loops (below)
 enum { S_NETMAX = 0, S_NETMINPOS = 2, S_DMAX = 3, S_DMAXOLD = 4, S_ERRD = 6, S_ERRS = 7, S_ALMISE = 9,
-       S_SCMAX = 11, S_COUNT = 12 };
+       S_SCMAX = 11, S_WORK = 12, S_COUNT = 13 };
 
 // Extremes of positive values by integer atomics on the IEEE bit patterns
 // (their order is the numeric order for positive doubles): order-independent,
@@ -1137,7 +1138,10 @@ __device__ __forceinline__ T smoothing_scale(const KdeParams &P, const T ks[3]) 
 template <typename T>
 __global__ void init_bins_kernel(KdeParams P, KdeBinsT<T> B, double hs, double *S) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b == 0) S[S_DMAX] = 0.0;
+  if (b == 0) {
+    S[S_DMAX] = 0.0;
+    S[S_WORK] = 0.0;
+  }
   if (b >= B.n) return;
   T ks[3];
   for (int d = 0; d < 3; ++d) ks[d] = P.mask[d] ? T(hs) : T(0);
@@ -1216,11 +1220,45 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // npts2: nPoints**fTWO, which Fortran evaluates as the product nPoints*nPoints
+// The work model of one optimisation loop (the multiply-adds of direct 3-D
+// kernels, GridProjectedKDE.F90:4620-4667, 4808-5065): per active bin its W
+// kernel, eight smoothing-kernel gathers (support update, nEstimate, six
+// roughness terms) and the three second-derivative kernels, each of
+// prod_d (2 ceil(r hod[level_d]) + 1) cells (r = 3, 4 for the second
+// derivatives) at its database levels.  The separable passes do a fraction
+// of this; dividing it by the time gives the rate a direct evaluation would
+// need.
+template <typename T>
+__device__ __forceinline__ double ksize(const KdeParams &P, T h, double range, int lev_dim) {
+  const int l = log_index<T>(P, h, lev_dim);
+  return 2.0 * ceil(range * P.hod[l - 1]) + 1.0;
+}
+template <typename T>
+__device__ double loop_work(const KdeParams &P, const KdeBinsT<T> &B, int b) {
+  double w = 1.0, sg = 1.0;
+  for (int d = 0; d < 3; ++d) {
+    if (!P.mask[d]) continue;
+    w *= ksize<T>(P, B.ks[d * B.n + b], 3.0, d);
+    sg *= ksize<T>(P, B.support[b], 3.0, d);
+  }
+  double sd = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    const T h = B.cb[a * B.n + b];
+    if (!P.mask[a] || !(h == h)) continue;
+    double k = 1.0;
+    const double m = ksize<T>(P, h, 4.0, a);
+    for (int d = 0; d < 3; ++d)
+      if (P.mask[d]) k *= m;
+    sd += k;
+  }
+  return w + 8.0 * sg + sd;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBinsT<T> B, int what, double npts2,
                                                               const double *S, double *partial) {
-  __shared__ double red[kThreads / 32][3];
-  double a[3] = {0.0, 0.0, 0.0};
+  __shared__ double red[kThreads / 32][4];
+  double a[4] = {0.0, 0.0, 0.0, 0.0};
   const double mx = S[S_DMAX], mx_old = S[S_DMAXOLD];
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
     if (what == RED_END) {
@@ -1242,17 +1280,18 @@ __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBi
       const T e = (B.nest[b] / (scn * T(P.four_pi_half_nd)) + T(0.25) * B.net[b] * (sc2 * sc2)) / T(npts2);
       a[2] += (double)e * (double)e;
     }
+    if (what == RED_END) a[3] += loop_work<T>(P, B, b);
   }
-  for (int k = 0; k < 3; ++k) a[k] = warp_sum(a[k]);
+  for (int k = 0; k < 4; ++k) a[k] = warp_sum(a[k]);
   const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0)
-    for (int k = 0; k < 3; ++k) red[w][k] = a[k];
+    for (int k = 0; k < 4; ++k) red[w][k] = a[k];
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 4; ++k) {
       double v = red[0][k];
       for (int i = 1; i < kThreads / 32; ++i) v = v + red[i][k];
-      partial[3 * blockIdx.x + k] = v;
+      partial[4 * blockIdx.x + k] = v;
     }
   }
 }
@@ -1260,14 +1299,15 @@ __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBi
 // one warp: lane l folds partials l, l+32, ... then a shuffle tree
 __global__ void bin_reduce_final_kernel(int what, int nblk, const double *partial, double *S) {
   const int l = threadIdx.x;
-  double a[3] = {0.0, 0.0, 0.0};
+  double a[4] = {0.0, 0.0, 0.0, 0.0};
   for (int i = l; i < nblk; i += 32)
-    for (int k = 0; k < 3; ++k) a[k] = a[k] + partial[3 * i + k];
-  for (int k = 0; k < 3; ++k) a[k] = warp_sum(a[k]);
+    for (int k = 0; k < 4; ++k) a[k] = a[k] + partial[4 * i + k];
+  for (int k = 0; k < 4; ++k) a[k] = warp_sum(a[k]);
   if (l != 0) return;
   if (what == RED_END) {
     S[S_ERRD] = a[0];
     S[S_ERRS] = a[1];
+    S[S_WORK] += a[3];
   }
   S[S_ALMISE] = a[2];
 }
@@ -1497,7 +1537,7 @@ cudaError_t KdeState::ensure_bins(int n) {
   D(&bins.count, c); D(&bins.ks, 3 * c); D(&bins.scale, c); D(&bins.shape, 3 * c); D(&bins.support, c);
   D(&bins.nest, c); D(&bins.dens, c); D(&bins.cb, 3 * c); D(&bins.rxx, c); D(&bins.ryy, c); D(&bins.rzz, c);
   D(&bins.net, c); D(&bins.dens_old, c); D(&bins.scale_old, c);
-  D(&partial, 3 * 152 * 8 + 16);
+  D(&partial, 4 * 152 * 8 + 16);
   if (e != cudaSuccess) return e;
   cap = (int)std::min<size_t>(c, (size_t)INT_MAX);
   bins.n = n;
@@ -1959,6 +1999,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
       }
       if (h[C_STATUS] == 2.0) return cudaErrorInvalidValue;
       if (loops_done) *loops_done = loops;
+      st.work_madds = h[S_WORK];
       return cudaGetLastError();
     }
   }
@@ -2018,6 +2059,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     cum_old = cum;
   }
   if (loops_done) *loops_done = (m > n_opt_loops) ? n_opt_loops : m;
+  st.work_madds = h[S_WORK];
   return cudaGetLastError();
 }
 

@@ -102,6 +102,7 @@ struct KdeState {
   double *t1 = nullptr, *t2 = nullptr;
   int64_t t1_cap = 0, t2_cap = 0;
   unsigned char *need1 = nullptr, *need2 = nullptr;  // FP64 gathers: the elements of the passes that are read
+  double work_madds = 0;  // the last reconstruction's work model (multiply-adds of direct kernels)
   long long *d_need = nullptr, *h_need = nullptr;  // pass-buffer sizes a plan needed, overflow flag
   KdeTable wtab{}, sdtab[3]{};
   double *d_val = nullptr;

@@ -127,6 +127,7 @@ def load_library() -> C.CDLL:
         "mprw_observe_sinks": (C.c_int, [H, C.c_int64, _ip, _up, _dp, _dp, C.POINTER(C.c_int64)]),
         "mprw_set_stream": (C.c_int, [H, C.c_void_p]),
         "mprw_last_timings": (C.c_int, [H, _dp, _dp, _dp, _dp, C.POINTER(C.c_int64)]),
+        "mprw_last_gpkde_work": (C.c_int, [H, _dp]),
         "mprw_destroy": (C.c_int, [H]),
         "mprw_create_batch": (C.c_int, [C.POINTER(H), C.c_int32, C.POINTER(GridDesc), C.POINTER(OptionsDesc)]),
         "mprw_batch_member": (C.c_int, [H, C.c_int32, C.POINTER(H)]),
@@ -471,7 +472,10 @@ class Tracker:
         n = C.c_int64()
         self._check(self.lib.mprw_last_timings(self.h, C.byref(s), C.byref(p), C.byref(h), C.byref(k), C.byref(n)),
                     "mprw_last_timings")
-        return dict(step_ms=s.value, prep_ms=p.value, hist_ms=h.value, gpkde_ms=k.value, launches=n.value)
+        w = C.c_double()
+        self._check(self.lib.mprw_last_gpkde_work(self.h, C.byref(w)), "mprw_last_gpkde_work")
+        return dict(step_ms=s.value, prep_ms=p.value, hist_ms=h.value, gpkde_ms=k.value, launches=n.value,
+                    gpkde_madds=w.value)
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
