@@ -914,9 +914,9 @@ __global__ void gather_z_kernel(KdeParams P, KdeBinsT<T> B, const SepPlan *pl, c
     const int j = pl->slot_of[bin_key[b]];
     const int m = pl->m[j][2], n = P.nb[2];
     const T *f = val + pl->fofs[j][2];
+    const int bx = B.gx[b], by = B.gy[b], bz = B.gz[b];
     const int *r2 = pl->r2[j];
     const T *in = T2 + pl->o2[j] * NC;
-    const int bx = B.gx[b], by = B.gy[b], bz = B.gz[b];
     for (int t = sub; t <= 2 * m; t += LPB) {
       const int p = reflect_pos(bz - m + t, n);
       if (p < 1) continue;
@@ -1229,29 +1229,23 @@ __device__ __forceinline__ double warp_sum(double v) {
 // of this; dividing it by the time gives the rate a direct evaluation would
 // need.
 template <typename T>
-__device__ __forceinline__ double ksize(const KdeParams &P, T h, double range, int lev_dim) {
-  const int l = log_index<T>(P, h, lev_dim);
-  return 2.0 * ceil(range * P.hod[l - 1]) + 1.0;
-}
-template <typename T>
 __device__ double loop_work(const KdeParams &P, const KdeBinsT<T> &B, int b) {
-  double w = 1.0, sg = 1.0;
+  long long w = 1, sg = 1, sd = 0;
   for (int d = 0; d < 3; ++d) {
     if (!P.mask[d]) continue;
-    w *= ksize<T>(P, B.ks[d * B.n + b], 3.0, d);
-    sg *= ksize<T>(P, B.support[b], 3.0, d);
+    w *= P.width3[log_index<T>(P, B.ks[d * B.n + b], d) - 1];
+    sg *= P.width3[log_index<T>(P, B.support[b], d) - 1];
   }
-  double sd = 0.0;
   for (int a = 0; a < 3; ++a) {
     const T h = B.cb[a * B.n + b];
     if (!P.mask[a] || !(h == h)) continue;
-    double k = 1.0;
-    const double m = ksize<T>(P, h, 4.0, a);
+    const long long m = P.width4[log_index<T>(P, h, a) - 1];
+    long long k = 1;
     for (int d = 0; d < 3; ++d)
       if (P.mask[d]) k *= m;
     sd += k;
   }
-  return w + 8.0 * sg + sd;
+  return (double)(w + 8 * sg + sd);
 }
 
 template <typename T>
