@@ -97,6 +97,10 @@ def parse():
                     help="lognormal_injection: the large continuous-injection run, whole (20 x 25 days), FP64 then MIXED; "
                          "prints its own line")
     ap.add_argument("--injection-particles", type=int, default=100_000_000)
+    ap.add_argument("--legacy-stream", action="store_true",
+                    help="run the FP64 and MIXED legs on the legacy default stream: the library then drives the "
+                         "GPKDE optimisation loop from the host, one launch per kernel (the same kernels and "
+                         "results as the device-driven loop), which a per-kernel profile of the loop needs")
     ap.add_argument("--kde-streams", type=int, default=4,
                     help="batched leg: reconstructions run concurrently (mprw_gpkde_batch concurrency)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
@@ -272,14 +276,16 @@ def run_gpu_arm(args, rank, world, local):
     origin, bins, nb = (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (g.ncol, g.nrow, g.nlay)
     domain = (float(np.sum(g.delr)), float(np.sum(g.delc)), float(g.top[0] - g.botm[-1]))
 
-    stream = torch.cuda.Stream()
+    # the legacy default stream is torch's default stream
+    stream = torch.cuda.default_stream() if args.legacy_stream else torch.cuda.Stream()
 
     def timed_run(precision, steps, warmup):
         # the MIXED pipeline reconstructs in FP32 too; FP64 is the reference's arithmetic
         kde_prec = precision
         opt.precision = precision
         tr = mprw.Tracker(g, opt)
-        tr.set_stream(stream.cuda_stream)   # launch on a stream the events below can see
+        # launch on a stream the events below can see (1: cudaStreamLegacy)
+        tr.set_stream(1 if args.legacy_stream else stream.cuda_stream)
         tr.load_flow(f)
         tr.set_particles(p)
         tuning = tr.autotune(0.0, INTERVAL_D) if args.autotune else tr.tuning()
