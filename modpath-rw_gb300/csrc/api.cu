@@ -1331,10 +1331,6 @@ int gpkde_params(mprw_handle *h, const mprw_gpkde_options *o, const char *who, K
   P.dlog = std::log(P.hod[1] / P.hod[0]);
   for (int d = 0; d < 3; ++d) P.lscale[d] = P.bin[d] > 0.0 ? (float)(1.0 / (P.bin[d] * P.min_hod)) : 0.0f;
   P.linv = (float)(1.0 / P.dlog);
-  for (int l = 0; l < P.ndelta; ++l) {
-    P.width3[l] = 2 * (int)std::ceil(3.0 * P.hod[l]) + 1;
-    P.width4[l] = 2 * (int)std::ceil(4.0 * P.hod[l]) + 1;
-  }
   // bounded kernel sizes (boundKernelSizeFormat 0)
   int maxd = -1, mind = -1;
   for (int d = 0; d < 3; ++d) {

@@ -112,6 +112,20 @@ __device__ __forceinline__ T pow_beta(T x, int nd, double y) {
 enum { S_NETMAX = 0, S_NETMINPOS = 2, S_DMAX = 3, S_DMAXOLD = 4, S_ERRD = 6, S_ERRS = 7, S_ALMISE = 9,
        S_SCMAX = 11, S_WORK = 12, S_COUNT = 13 };
 
+// The work model of one optimisation loop (the multiply-adds of direct 3-D
+// kernels, GridProjectedKDE.F90:4620-4667, 4808-5065): per active bin its W
+// kernel, eight smoothing-kernel gathers (support update, nEstimate, six
+// roughness terms) and the three second-derivative kernels, each of
+// prod_d (2 m_d + 1) cells at the bin's database kernels.  It is counted
+// where the kernels' half widths are already at hand -- per level in the
+// plans (bins per level times the level's kernel), per bin in the density
+// scatter -- as 64-bit integers in S[S_WORK] (exact, in any order), and reset
+// before the first loop.  The separable passes do a fraction of it; divided
+// by the time it is the rate a direct evaluation would need.
+__device__ __forceinline__ unsigned long long *work_counter(double *S) {
+  return reinterpret_cast<unsigned long long *>(S + S_WORK);
+}
+
 // Extremes of positive values by integer atomics on the IEEE bit patterns
 // (their order is the numeric order for positive doubles): order-independent,
 // so as repeatable as the fixed-order sums.  One atomic per warp.
@@ -205,7 +219,7 @@ __device__ __forceinline__ unsigned long long fixed63(double f) {
 template <typename T>
 __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, KdeBinsT<T> B, KdeTableT<T> tab,
                                                                 int stride, T fscale,
-                                                                unsigned long long *grid) {
+                                                                unsigned long long *grid, double *scal) {
   __shared__ T sv_all[kWarpsW][3 * KDE_MAXLEN];
   __shared__ int sm_all[kWarpsW][3], sofs_all[kWarpsW][3];
   __shared__ T crow_all[kWarpsW][kRowCache];
@@ -226,6 +240,9 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
     sofs_all[w][d] = tab.ofs[d * KDE_MAXDB + idx - 1];
   }
   __syncwarp();
+  if (lane == 0)  // the work model: the W kernel's cells
+    atomicAdd(work_counter(scal), (unsigned long long)((2 * sm_all[w][0] + 1) * (2 * sm_all[w][1] + 1) *
+                                                    (2 * sm_all[w][2] + 1)));
   for (int d = 0; d < 3; ++d) {
     const int m = sm_all[w][d], o = sofs_all[w][d];
     for (int k = lane; k < 2 * m + 1; k += 32) sv[d * KDE_MAXLEN + k] = tab.val[o + k];
@@ -494,7 +511,8 @@ static_assert(kPlanThreads >= KDE_KMAX, "one plan thread per key");
 // nothing and the host reruns the reconstruction with larger buffers.
 __global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, KeyAcc *K, KdeTable t0, KdeTable t1,
                                                             KdeTable t2, int scatter, SepPlan *pl, int nc,
-                                                            long long cap1, long long cap2, long long *need) {
+                                                            long long cap1, long long cap2, long long *need,
+                                                            double *S, int work_weight) {
   __shared__ long long sv1[kPlanThreads], sv2[kPlanThreads];
   __shared__ int sp[kPlanThreads];
   __shared__ int su[3][6];
@@ -528,6 +546,10 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, KeyAcc 
     }
     v1 = (long long)(r1[1] - r1[0] + 1) * (r1[3] - r1[2] + 1) * (r1[5] - r1[4] + 1);
     v2 = (long long)(r2[1] - r2[0] + 1) * (r2[3] - r2[2] + 1) * (r2[5] - r2[4] + 1);
+    // the work model: this level's bins times its kernel's cells
+    if (work_weight > 0)
+      atomicAdd(work_counter(S), (unsigned long long)K->cnt[k] * (unsigned long long)work_weight *
+                                     (unsigned long long)((2 * m[0] + 1) * (2 * m[1] + 1) * (2 * m[2] + 1)));
   }
   sp[k] = present ? 1 : 0;
   sv1[k] = v1;
@@ -1220,39 +1242,12 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // npts2: nPoints**fTWO, which Fortran evaluates as the product nPoints*nPoints
-// The work model of one optimisation loop (the multiply-adds of direct 3-D
-// kernels, GridProjectedKDE.F90:4620-4667, 4808-5065): per active bin its W
-// kernel, eight smoothing-kernel gathers (support update, nEstimate, six
-// roughness terms) and the three second-derivative kernels, each of
-// prod_d (2 ceil(r hod[level_d]) + 1) cells (r = 3, 4 for the second
-// derivatives) at its database levels.  The separable passes do a fraction
-// of this; dividing it by the time gives the rate a direct evaluation would
-// need.
-template <typename T>
-__device__ double loop_work(const KdeParams &P, const KdeBinsT<T> &B, int b) {
-  long long w = 1, sg = 1, sd = 0;
-  for (int d = 0; d < 3; ++d) {
-    if (!P.mask[d]) continue;
-    w *= P.width3[log_index<T>(P, B.ks[d * B.n + b], d) - 1];
-    sg *= P.width3[log_index<T>(P, B.support[b], d) - 1];
-  }
-  for (int a = 0; a < 3; ++a) {
-    const T h = B.cb[a * B.n + b];
-    if (!P.mask[a] || !(h == h)) continue;
-    const long long m = P.width4[log_index<T>(P, h, a) - 1];
-    long long k = 1;
-    for (int d = 0; d < 3; ++d)
-      if (P.mask[d]) k *= m;
-    sd += k;
-  }
-  return (double)(w + 8 * sg + sd);
-}
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBinsT<T> B, int what, double npts2,
                                                               const double *S, double *partial) {
-  __shared__ double red[kThreads / 32][4];
-  double a[4] = {0.0, 0.0, 0.0, 0.0};
+  __shared__ double red[kThreads / 32][3];
+  double a[3] = {0.0, 0.0, 0.0};
   const double mx = S[S_DMAX], mx_old = S[S_DMAXOLD];
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
     if (what == RED_END) {
@@ -1274,18 +1269,17 @@ __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBi
       const T e = (B.nest[b] / (scn * T(P.four_pi_half_nd)) + T(0.25) * B.net[b] * (sc2 * sc2)) / T(npts2);
       a[2] += (double)e * (double)e;
     }
-    if (what == RED_END) a[3] += loop_work<T>(P, B, b);
   }
-  for (int k = 0; k < 4; ++k) a[k] = warp_sum(a[k]);
+  for (int k = 0; k < 3; ++k) a[k] = warp_sum(a[k]);
   const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0)
-    for (int k = 0; k < 4; ++k) red[w][k] = a[k];
+    for (int k = 0; k < 3; ++k) red[w][k] = a[k];
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 3; ++k) {
       double v = red[0][k];
       for (int i = 1; i < kThreads / 32; ++i) v = v + red[i][k];
-      partial[4 * blockIdx.x + k] = v;
+      partial[3 * blockIdx.x + k] = v;
     }
   }
 }
@@ -1293,15 +1287,14 @@ __global__ void __launch_bounds__(kThreads) bin_reduce_kernel(KdeParams P, KdeBi
 // one warp: lane l folds partials l, l+32, ... then a shuffle tree
 __global__ void bin_reduce_final_kernel(int what, int nblk, const double *partial, double *S) {
   const int l = threadIdx.x;
-  double a[4] = {0.0, 0.0, 0.0, 0.0};
+  double a[3] = {0.0, 0.0, 0.0};
   for (int i = l; i < nblk; i += 32)
-    for (int k = 0; k < 4; ++k) a[k] = a[k] + partial[4 * i + k];
-  for (int k = 0; k < 4; ++k) a[k] = warp_sum(a[k]);
+    for (int k = 0; k < 3; ++k) a[k] = a[k] + partial[3 * i + k];
+  for (int k = 0; k < 3; ++k) a[k] = warp_sum(a[k]);
   if (l != 0) return;
   if (what == RED_END) {
     S[S_ERRD] = a[0];
     S[S_ERRS] = a[1];
-    S[S_WORK] += a[3];
   }
   S[S_ALMISE] = a[2];
 }
@@ -1531,7 +1524,7 @@ cudaError_t KdeState::ensure_bins(int n) {
   D(&bins.count, c); D(&bins.ks, 3 * c); D(&bins.scale, c); D(&bins.shape, 3 * c); D(&bins.support, c);
   D(&bins.nest, c); D(&bins.dens, c); D(&bins.cb, 3 * c); D(&bins.rxx, c); D(&bins.ryy, c); D(&bins.rzz, c);
   D(&bins.net, c); D(&bins.dens_old, c); D(&bins.scale_old, c);
-  D(&partial, 4 * 152 * 8 + 16);
+  D(&partial, 3 * 152 * 8 + 16);
   if (e != cudaSuccess) return e;
   cap = (int)std::min<size_t>(c, (size_t)INT_MAX);
   bins.n = n;
@@ -1723,6 +1716,7 @@ enum { C_ALMOLD = 16, C_CUM = 17, C_CUMOLD = 18, C_LOOPS = 19, C_STATUS = 20 };
 // everywhere (the reference stops, GridProjectedKDE.F90:5443-5446)
 
 __global__ void loop_ctl_init_kernel(double *S, int nb) {
+  *work_counter(S) = 0ull;
   const double alm = sqrt(S[S_ALMISE] / nb);
   S[C_ALMOLD] = alm;
   S[C_CUM] = alm;
@@ -1812,7 +1806,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   auto density = [&](void) -> cudaError_t {
     zero_u64_kernel<<<blocks_for(ngrid), kThreads, 0, s>>>(raw_fixed, ngrid);
     wscatter_kernel<T><<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, wtab, wstride, T(fscale),
-                                                                            raw_fixed);
+                                                                            raw_fixed, S);
     scale_pick_kernel<T><<<blocks_for(npick), kThreads, 0, s>>>(P, B, raw_fixed, inv_fscale, dens_grid, ngrid, S);
     st.launches += 3;
     return cudaGetLastError();
@@ -1821,14 +1815,17 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   SepPlan *plan1 = st.d_plan, *plan2 = st.d_plan + 1;
   int *key1 = st.bin_key, *key2 = st.bin_key + nb;
   const dim3 pgrid(kPassBlocks);
-  auto plan = [&](int kind, int nc) -> cudaError_t {
+  // work_weight: the smoothing kernels of the nEstimate plan count eight
+  // times (support update, nEstimate, six roughness terms), the second
+  // derivatives once, the support plan's not at all
+  auto plan = [&](int kind, int nc, int work_weight) -> cudaError_t {
     key_assign_kernel<T><<<kb, kThreads, 0, s>>>(P, B, kind, kind == 1 ? key1 : key2, st.d_keys);
     if (kind == 1)
       plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.wtab, st.wtab, st.wtab, 0, plan1, nc, st.t1_cap,
-                                             st.t2_cap, st.d_need);
+                                             st.t2_cap, st.d_need, S, work_weight);
     else
       plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.sdtab[0], st.sdtab[1], st.sdtab[2], 1, plan2, nc,
-                                             st.t1_cap, st.t2_cap, st.d_need);
+                                             st.t1_cap, st.t2_cap, st.d_need, S, work_weight);
     st.launches += 2;
     return cudaGetLastError();
   };
@@ -1888,15 +1885,15 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     st.launches += 1;
     // nEstimate with the current support, support update, nEstimate again
     // and the curvature bandwidths
-    KCK(plan(1, 1));
+    KCK(plan(1, 1, 0));
     KCK(needed());
     KCK(gather1(dens_grid, GZ_SUPPORT, nullptr, nullptr));
-    KCK(plan(1, P.ndim == 3 ? 6 : (P.ndim == 2 ? 3 : 1)));
+    KCK(plan(1, P.ndim == 3 ? 6 : (P.ndim == 2 ? 3 : 1), 8));
     KCK(needed());
     KCK(gather1(dens_grid, GZ_NEST, nullptr, nullptr));
     // curvatures: second-derivative scatters of the counts, squared (every
     // cell of the three grids is written, zero outside the keys' regions)
-    KCK(plan(2, 1));
+    KCK(plan(2, 1, 1));
     scatter_x_kernel<T><<<pgrid, kThreads, 0, s>>>(P, B, plan2, val, st.cell_bin, key2, t1);
     scatter_y_kernel<T><<<pgrid, kThreads, 0, s>>>(P, plan2, val, t1, t2);
     scatter_z_kernel<T><<<dim3(gb, 3), kThreads, 0, s>>>(P, plan2, val, t2, cx, cy, cz, P.ndim != 2);
@@ -1993,11 +1990,12 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
       }
       if (h[C_STATUS] == 2.0) return cudaErrorInvalidValue;
       if (loops_done) *loops_done = loops;
-      st.work_madds = h[S_WORK];
+      st.work_madds = (double)*reinterpret_cast<const unsigned long long *>(h + S_WORK);
       return cudaGetLastError();
     }
   }
   // the loop driven from the host (a stream that cannot be captured)
+  KCK(cudaMemsetAsync(S + S_WORK, 0, sizeof(double), s));
   KCK(fetch_async());
   KCK(fetch_wait());
   double alm = std::sqrt(h[S_ALMISE] / nb);
@@ -2053,7 +2051,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     cum_old = cum;
   }
   if (loops_done) *loops_done = (m > n_opt_loops) ? n_opt_loops : m;
-  st.work_madds = h[S_WORK];
+  st.work_madds = (double)*reinterpret_cast<const unsigned long long *>(h + S_WORK);
   return cudaGetLastError();
 }
 

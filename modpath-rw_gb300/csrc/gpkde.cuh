@@ -22,7 +22,6 @@ struct KdeParams {
   double hod[KDE_MAXDB];
   double min_hod, dlog;  // log database: index = floor(log(h/bin/min)/dlog)+1
   float lscale[3], linv;  // FP32 estimate of the index: 1/(bin*min_hod), 1/dlog
-  int width3[KDE_MAXDB], width4[KDE_MAXDB];  // kernel widths 2 ceil(r hod) + 1 per level, r = 3 and 4
   double max_k[3], min_k[3], max_sd[3], min_sd[3];
   int max_dim, min_dim;
   double support_c, alpha_c, beta_c, one_over_nd4, minus_one_over_nd6, one_plus_nd_q;

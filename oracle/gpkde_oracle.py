@@ -315,7 +315,10 @@ class GPKDE:
 
     # -- the reconstruction ---------------------------------------------------
     def compute_density(self, coords, weights, unit_volume=True, scaling_factor=1.0):
-        """Returns the density grid shaped (nx, ny, nz) and the smoothing per active bin."""
+        """Returns the density grid shaped (nx, ny, nz) and the smoothing per active bin.
+        Afterwards ``self.work`` holds the work model of its optimisation loops
+        (per loop and active bin |K_W| + 8 |K_sigma| + 3 |K_SD| cells)."""
+        self.work = 0
         counts_zyx, _, eff_mass = histogram_weighted(coords, weights, self.origin, self.bin_size, self.nbins)
         counts = np.ascontiguousarray(counts_zyx.transpose(2, 1, 0))   # [x, y, z]
         npts = coords.shape[0]
@@ -407,6 +410,7 @@ class GPKDE:
         almise_old, cum_old = almise, cum
         darr_old = darr.copy()
         loops = 0
+        self.work = 0
         for m in range(1, self.n_opt_loops + 1):
             loops = m
             for n in range(nb):
@@ -429,6 +433,7 @@ class GPKDE:
             # the isotropy correction changes netRoughnessArray in place (intent(inout),
             # GridProjectedKDE.F90:5420, 5496-5518): the ALMISE below reads the corrected values
             ks, scale, shape, netr = self._optimal_smoothing(nest, netr, rxx, ryy, rzz)
+            self.work += self._loop_work(ks, support, cb)
             dens = self._density(counts, act, ks)
             darr = np.array([dens[g[0] - 1, g[1] - 1, g[2] - 1] for g in act])
             e = np.where(darr_old != 0.0, np.abs(darr / darr.max() - darr_old / darr_old.max())
@@ -454,6 +459,23 @@ class GPKDE:
             scale_old = scale.copy()
         self.loops = loops
         return dens, ks
+
+    def _loop_work(self, ks, support, cb):
+        """The work model of one loop: per active bin the cells of its W kernel,
+        eight smoothing-kernel gathers and the second-derivative kernel of each
+        active axis, at the database kernels this loop used."""
+        w = 0
+        for n in range(ks.shape[1]):
+            kw = np.prod(2 * np.asarray(self._w_kernel(ks[:, n])[1]) + 1)
+            ksg = np.prod(2 * np.asarray(self._w_kernel(np.full(3, support[n]))[1]) + 1)
+            ksd = 0
+            for a in self.dims:
+                h = cb[a, n]
+                if h != h:
+                    continue
+                ksd += np.prod(2 * np.asarray(self._sd_kernel(a, h)[1]) + 1)
+            w += int(kw) + 8 * int(ksg) + int(ksd)
+        return w
 
     def _curvature_bandwidth(self, darr, nest, scale, shape, support):
         nb = darr.shape[0]

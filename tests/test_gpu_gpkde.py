@@ -53,6 +53,36 @@ def test_gpkde_3d_heterogeneous(gpu_lib):
     tr.close()
 
 
+@pytest.mark.parametrize("case", ["1d", "3d"])
+def test_gpkde_work_model_matches_the_restatement(gpu_lib, case):
+    """mprw_last_gpkde_work -- the multiply-adds direct 3-D kernels would take,
+    summed over the optimisation loops -- against the same model counted by
+    the numpy restatement from the database kernels each of its loops used
+    (the same loops, so the same levels; within 1e-3 for a level taken on
+    the other side of a boundary by rounding)."""
+    if case == "1d":
+        g, f, p, opt = W.uniform_pulse(n_particles=20000)
+        t1, dom = 50.0, (200.0, 1.0, 1.0)
+        kw = {}
+    else:
+        g, f, p, opt, info = W.lognormal_slab(n_particles=4000, nlay=4, nrow=12, ncol=30, seed=0, use_torch=False)
+        t1, dom = 20.0, (30.0, 12.0, 4.0)
+        kw = dict(n_opt_loops=5)
+    tr = mprw.Tracker(g, opt)
+    tr.load_flow(f)
+    tr.set_particles(p)
+    tr.advance(0.0, t1)
+    co = _positions(tr)
+    dens, hist, loops = tr.gpkde(dom, (1.0, 1.0, 1.0), **kw)
+    work = tr.timings()["gpkde_madds"]
+    tr.close()
+    G = GO.GPKDE(dom, (1.0, 1.0, 1.0), **kw)
+    G.compute_density(co, np.ones(co.shape[0]))
+    assert loops == G.loops
+    assert G.work > 0
+    assert abs(work - G.work) <= 1e-3 * G.work, (work, G.work)
+
+
 def test_gpkde_scaling_and_empty(gpu_lib):
     g, f, p, opt = W.uniform_pulse(n_particles=2000)
     tr = mprw.Tracker(g, opt)
