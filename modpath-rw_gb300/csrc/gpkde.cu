@@ -219,7 +219,8 @@ __device__ __forceinline__ unsigned long long fixed63(double f) {
 template <typename T>
 __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, KdeBinsT<T> B, KdeTableT<T> tab,
                                                                 int stride, T fscale,
-                                                                unsigned long long *grid, double *scal) {
+                                                                unsigned long long *grid,
+                                                                unsigned long long *wcnt) {
   __shared__ T sv_all[kWarpsW][3 * KDE_MAXLEN];
   __shared__ int sm_all[kWarpsW][3], sofs_all[kWarpsW][3];
   __shared__ T crow_all[kWarpsW][kRowCache];
@@ -240,9 +241,9 @@ __global__ void __launch_bounds__(32 * kWarpsW) wscatter_kernel(KdeParams P, Kde
     sofs_all[w][d] = tab.ofs[d * KDE_MAXDB + idx - 1];
   }
   __syncwarp();
-  if (lane == 0)  // the work model: the W kernel's cells
-    atomicAdd(work_counter(scal), (unsigned long long)((2 * sm_all[w][0] + 1) * (2 * sm_all[w][1] + 1) *
-                                                    (2 * sm_all[w][2] + 1)));
+  if (lane == 0)  // the work model: the W kernel's cells (64 counters: one address would serialise)
+    atomicAdd(wcnt + (wi & 63), (unsigned long long)((2 * sm_all[w][0] + 1) * (2 * sm_all[w][1] + 1) *
+                                                     (2 * sm_all[w][2] + 1)));
   for (int d = 0; d < 3; ++d) {
     const int m = sm_all[w][d], o = sofs_all[w][d];
     for (int k = lane; k < 2 * m + 1; k += 32) sv[d * KDE_MAXLEN + k] = tab.val[o + k];
@@ -1534,7 +1535,8 @@ cudaError_t KdeState::ensure_bins(int n) {
 cudaError_t KdeState::ensure_grid(int64_t ngrid) {
   if (!d_scalars) {
     cudaError_t e = cudaMalloc((void **)&d_scalars, 32 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMallocHost((void **)&h_scalars, 32 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_wcnt, 64 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&h_scalars, 96 * sizeof(double));  // + the 64 counters
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_keys, sizeof(KeyAcc));
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_plan, 2 * sizeof(SepPlan));
@@ -1594,7 +1596,7 @@ void KdeState::release() {
   void *ptrs[] = {bins.gx, bins.gy, bins.gz, bins.count, bins.ks, bins.scale, bins.shape, bins.support, bins.nest,
                   bins.dens, bins.cb, bins.rxx, bins.ryy, bins.rzz, bins.net, bins.dens_old, bins.scale_old,
                   partial, dens_grid, cx, cy, cz, d_scalars, d_flag, d_blockcnt, d_val, d_valf, d_meta, cell_bin,
-                  bin_key, d_keys, d_plan, t1, t2, need1, need2, dens_raw, d_need, cxy, cxz, cyz, dens_out};
+                  bin_key, d_keys, d_plan, t1, t2, need1, need2, d_wcnt, dens_raw, d_need, cxy, cxz, cyz, dens_out};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_scalars) cudaFreeHost(h_scalars);
@@ -1715,8 +1717,9 @@ enum { C_ALMOLD = 16, C_CUM = 17, C_CUMOLD = 18, C_LOOPS = 19, C_STATUS = 20 };
 // its pass buffers (the attempt is discarded), 2 the net roughness is zero
 // everywhere (the reference stops, GridProjectedKDE.F90:5443-5446)
 
-__global__ void loop_ctl_init_kernel(double *S, int nb) {
+__global__ void loop_ctl_init_kernel(double *S, unsigned long long *wcnt, int nb) {
   *work_counter(S) = 0ull;
+  for (int k = 0; k < 64; ++k) wcnt[k] = 0ull;
   const double alm = sqrt(S[S_ALMISE] / nb);
   S[C_ALMOLD] = alm;
   S[C_CUM] = alm;
@@ -1766,6 +1769,20 @@ __global__ void zero_u64_kernel(unsigned long long *a, int64_t n) {
     a[i] = 0ull;
 }
 
+// the work model after the loops: the plans' count plus the scatters' 64
+// counters (copied to h + 32 with the last read of the scalars, or here)
+static cudaError_t read_work(KdeState &st, double *h, cudaStream_t s, bool copied) {
+  if (!copied) {
+    KCK(cudaMemcpyAsync(h + 32, st.d_wcnt, 64 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    KCK(cudaStreamSynchronize(s));
+  }
+  unsigned long long t = *reinterpret_cast<const unsigned long long *>(h + S_WORK);
+  const unsigned long long *w = reinterpret_cast<const unsigned long long *>(h + 32);
+  for (int k = 0; k < 64; ++k) t += w[k];
+  st.work_madds = (double)t;
+  return cudaSuccess;
+}
+
 // One reconstruction attempt in arithmetic type T; *overflow is set when a
 // plan found the pass buffers too small (the sizes it needed are in st.h_need).
 template <typename T>
@@ -1806,7 +1823,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   auto density = [&](void) -> cudaError_t {
     zero_u64_kernel<<<blocks_for(ngrid), kThreads, 0, s>>>(raw_fixed, ngrid);
     wscatter_kernel<T><<<(nb + kWarpsW - 1) / kWarpsW, 32 * kWarpsW, 0, s>>>(P, B, wtab, wstride, T(fscale),
-                                                                            raw_fixed, S);
+                                                                            raw_fixed, st.d_wcnt);
     scale_pick_kernel<T><<<blocks_for(npick), kThreads, 0, s>>>(P, B, raw_fixed, inv_fscale, dens_grid, ngrid, S);
     st.launches += 3;
     return cudaGetLastError();
@@ -1976,11 +1993,12 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
         cudaGraphExec_t e;
         ~ExecGuard() { cudaGraphExecDestroy(e); }
       } guard{dexec};
-      loop_ctl_init_kernel<<<1, 1, 0, s>>>(S, nb);
+      loop_ctl_init_kernel<<<1, 1, 0, s>>>(S, st.d_wcnt, nb);
       KCK(cudaGetLastError());
       KCK(cudaGraphLaunch(dexec, s));
       KCK(cudaMemcpyAsync(h, S, 32 * sizeof(double), cudaMemcpyDeviceToHost, s));
       KCK(cudaMemcpyAsync(st.h_need, st.d_need, 3 * sizeof(long long), cudaMemcpyDeviceToHost, s));
+      KCK(cudaMemcpyAsync(h + 32, st.d_wcnt, 64 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
       KCK(cudaStreamSynchronize(s));
       const int loops = (int)h[C_LOOPS];
       st.launches += 1 + dbody * loops;
@@ -1990,12 +2008,13 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
       }
       if (h[C_STATUS] == 2.0) return cudaErrorInvalidValue;
       if (loops_done) *loops_done = loops;
-      st.work_madds = (double)*reinterpret_cast<const unsigned long long *>(h + S_WORK);
+      KCK(read_work(st, h, s, true));
       return cudaGetLastError();
     }
   }
   // the loop driven from the host (a stream that cannot be captured)
   KCK(cudaMemsetAsync(S + S_WORK, 0, sizeof(double), s));
+  KCK(cudaMemsetAsync(st.d_wcnt, 0, 64 * sizeof(unsigned long long), s));
   KCK(fetch_async());
   KCK(fetch_wait());
   double alm = std::sqrt(h[S_ALMISE] / nb);
@@ -2051,7 +2070,7 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     cum_old = cum;
   }
   if (loops_done) *loops_done = (m > n_opt_loops) ? n_opt_loops : m;
-  st.work_madds = (double)*reinterpret_cast<const unsigned long long *>(h + S_WORK);
+  KCK(read_work(st, h, s, false));
   return cudaGetLastError();
 }
 

@@ -103,6 +103,7 @@ struct KdeState {
   int64_t t1_cap = 0, t2_cap = 0;
   unsigned char *need1 = nullptr, *need2 = nullptr;  // FP64 gathers: the elements of the passes that are read
   double work_madds = 0;  // the last reconstruction's work model (multiply-adds of direct kernels)
+  unsigned long long *d_wcnt = nullptr;  // the density scatters' part of it, spread over 64 counters
   long long *d_need = nullptr, *h_need = nullptr;  // pass-buffer sizes a plan needed, overflow flag
   KdeTable wtab{}, sdtab[3]{};
   double *d_val = nullptr;
