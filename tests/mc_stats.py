@@ -4,7 +4,7 @@ The GPU tracks with counter-based Philox normals and the reference with
 xoroshiro128+ thread streams (rng_par_zig.f90:156-335; normals
 TrackSubCell.F90:3631-3663), so the two cannot agree particle by particle:
 they are compared as two samples of the same random-walk process.  A summary
-holds what a plume is judged by -- the stop-status counts (mass leaving
+holds what characterises a plume -- the stop-status counts (mass leaving
 through weak sinks, MPathRW.F90:1337-1403), the first, second and fourth
 central moments of the ACTIVE particles' model coordinates, their
 histogram along x, the particles past a control plane, and the

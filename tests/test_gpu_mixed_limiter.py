@@ -15,7 +15,8 @@ and by the few particles whose FP32 comparisons go the other way:
   particles end exactly at t_end);
 * the stop-status counts agree within max(3, 0.5 %) of the particles;
 * plume mean displacement within 0.5 % and variances within 1 %
-  relative (the north star's moment tolerance is 0.5 % on the mean);
+  relative (the mixed-precision target's moment tolerance is 0.5 % on
+  the mean);
 * the limiter really cut: FP64 steps per particle at least 4x the 25 an
   uncut one-day FIXED step gives over 25 days (the oracle takes ~360).
 """
