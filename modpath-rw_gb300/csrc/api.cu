@@ -1611,6 +1611,7 @@ int mprw_gpkde_batch(mprw_handle *h, const mprw_gpkde_options *opts, double *con
   if (nw > nm) nw = nm;
   while ((int)h->kde_workers.size() < nw) {
     KdeWorker *w = new KdeWorker();
+    w->kde.device_loop = false;
     h->kde_workers.push_back(w);
     CK(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
   }

@@ -38,7 +38,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kBinThreads = 64;   // per-bin elementwise kernels: spread few bins over all SMs
-constexpr int kPassBlocks = 2432; // blocks of a separable pass: 16 per SM (measured best of 4-48), grid-stride over all keys' regions
+constexpr int kPassBlocks = 2432; // most blocks of a separable pass: 16 per SM (measured best of 4-48), grid-stride over all keys' regions
 
 // The database level of a kernel size h along dimension d:
 // floor(log(h / bin / minHOverDelta) / dlog) + 1, clamped to the database.
@@ -1831,7 +1831,10 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   // plans: [0] smoothing kernels (kind 1), [1] second-derivative kernels (kind 2)
   SepPlan *plan1 = st.d_plan, *plan2 = st.d_plan + 1;
   int *key1 = st.bin_key, *key2 = st.bin_key + nb;
-  const dim3 pgrid(kPassBlocks);
+  // about one block per 20 active bins (a pass covers ~10-25 elements per
+  // bin), a multiple of the SM count: a small reconstruction (a batch's
+  // small members) does not pay for the prologue of blocks that find no work
+  const dim3 pgrid(std::min(kPassBlocks, std::max(152, (nb / 20 + 151) / 152 * 152)));
   // work_weight: the smoothing kernels of the nEstimate plan count eight
   // times (support update, nEstimate, six roughness terms), the second
   // derivatives once, the support plan's not at all
@@ -1954,8 +1957,9 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   st.launches += 2;
   KCK(density());
   KCK(reduce(RED_ALMISE));  // nEstimate and net roughness are zero: 0
-  {
-    // the whole loop as one graph: a while node around the captured body
+  if (n_opt_loops > 0 && st.device_loop) {
+    // the whole loop as one graph: a while node around the captured body (a
+    // while node runs its body at least once: no loops are the host path's)
     cudaGraphExec_t dexec = nullptr;
     int64_t dbody = 0;
     cudaGraph_t g = nullptr;

@@ -103,6 +103,11 @@ struct KdeState {
   int64_t t1_cap = 0, t2_cap = 0;
   unsigned char *need1 = nullptr, *need2 = nullptr;  // FP64 gathers: the elements of the passes that are read
   double work_madds = 0;  // the last reconstruction's work model (multiply-adds of direct kernels)
+  // run the optimisation loop as a device-side graph loop when the stream can
+  // be captured; a batch's workers drive it from the host (several small
+  // reconstructions in flight: building each one's conditional graph cost
+  // more than the host's per-loop reads)
+  bool device_loop = true;
   unsigned long long *d_wcnt = nullptr;  // the density scatters' part of it, spread over 64 counters
   long long *d_need = nullptr, *h_need = nullptr;  // pass-buffer sizes a plan needed, overflow flag
   KdeTable wtab{}, sdtab[3]{};

@@ -83,6 +83,25 @@ def test_gpkde_work_model_matches_the_restatement(gpu_lib, case):
     assert abs(work - G.work) <= 1e-3 * G.work, (work, G.work)
 
 
+def test_gpkde_without_optimisation_loops(gpu_lib):
+    """n_opt_loops = 0: the density of the initial smoothing, no loop run --
+    the device-driven loop (a while node, whose body would run at least once)
+    is not used then -- as the numpy restatement gives it."""
+    g, f, p, opt = W.uniform_pulse(n_particles=20000)
+    tr = mprw.Tracker(g, opt)
+    tr.load_flow(f)
+    tr.set_particles(p)
+    tr.advance(0.0, 50.0)
+    co = _positions(tr)
+    dens, hist, loops = tr.gpkde((200.0, 1.0, 1.0), (1.0, 1.0, 1.0), n_opt_loops=0)
+    work = tr.timings()["gpkde_madds"]
+    tr.close()
+    G = GO.GPKDE((200.0, 1.0, 1.0), (1.0, 1.0, 1.0), n_opt_loops=0)
+    ref, _ = G.compute_density(co, np.ones(co.shape[0]))
+    assert loops == 0 == G.loops and work == 0
+    np.testing.assert_allclose(dens, ref.transpose(2, 1, 0), rtol=0, atol=1e-10 * ref.max())
+
+
 def test_gpkde_scaling_and_empty(gpu_lib):
     g, f, p, opt = W.uniform_pulse(n_particles=2000)
     tr = mprw.Tracker(g, opt)
