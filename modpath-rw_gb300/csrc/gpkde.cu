@@ -393,6 +393,7 @@ __device__ __forceinline__ int reflect_pos(int p, int n) {
 }
 
 __global__ void key_init_kernel(KeyAcc *K) {
+  if (threadIdx.x == 0) K->done = 0u;
   for (int k = threadIdx.x; k < KDE_KMAX; k += blockDim.x) {
     K->box[k][0] = K->box[k][2] = K->box[k][4] = INT_MAX;
     K->box[k][1] = K->box[k][3] = K->box[k][5] = INT_MIN;
@@ -409,8 +410,15 @@ __global__ void key_init_kernel(KeyAcc *K) {
 // (GridProjectedKDE.F90:1723-1724; its 3-D path has no such test and no
 // defined kernel for NaN).  Boxes and counts are accumulated per
 // block in shared memory and merged into K once per block and key.
+__device__ void plan_body(const KdeParams &P, KeyAcc *K, const KdeTable &t0, const KdeTable &t1,
+                          const KdeTable &t2, int scatter, SepPlan *pl, int nc, long long cap1, long long cap2,
+                          long long *need, double *S, int work_weight);
+
 template <typename T>
-__global__ void key_assign_kernel(KdeParams P, KdeBinsT<T> B, int kind, int *bin_key, KeyAcc *K) {
+__global__ void __launch_bounds__(kThreads) key_assign_kernel(KdeParams P, KdeBinsT<T> B, int kind, int *bin_key,
+                                                              KeyAcc *K, KdeTable t0, KdeTable t1, KdeTable t2,
+                                                              SepPlan *pl, int nc, long long cap1, long long cap2,
+                                                              long long *need, double *S, int work_weight) {
   __shared__ int sb[KDE_KMAX][6];
   __shared__ int sl[KDE_KMAX][3];
   __shared__ int sc[KDE_KMAX];
@@ -494,6 +502,19 @@ __global__ void key_assign_kernel(KdeParams P, KdeBinsT<T> B, int kind, int *bin
     }
     atomicAdd(&K->cnt[k], sc[k]);
   }
+  // The last block to merge lays out the plan (one launch fewer per plan):
+  // every thread's merges are made visible device-wide before its block
+  // takes a ticket, and the block that takes the last ticket then sees all
+  // of them.
+  __shared__ unsigned int ticket;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) ticket = atomicAdd(&K->done, 1u);
+  __syncthreads();
+  if (ticket != gridDim.x - 1) return;
+  __threadfence();
+  if (threadIdx.x == 0) K->done = 0u;  // for the next assignment (kernel boundaries order it)
+  plan_body(P, K, t0, t1, t2, kind == 2, pl, nc, cap1, cap2, need, S, work_weight);
 }
 
 // Compact the keys present and lay out the pass regions, one thread per
@@ -510,10 +531,11 @@ static_assert(kPlanThreads >= KDE_KMAX, "one plan thread per key");
 // more than cap1 / cap2 elements (nc per region cell) records the sizes it
 // needs in need[0..1], sets need[2] and presents no key, so the passes do
 // nothing and the host reruns the reconstruction with larger buffers.
-__global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, KeyAcc *K, KdeTable t0, KdeTable t1,
-                                                            KdeTable t2, int scatter, SepPlan *pl, int nc,
-                                                            long long cap1, long long cap2, long long *need,
-                                                            double *S, int work_weight) {
+// (run by the last block of the key assignment, kPlanThreads threads; the
+// accumulators other blocks merged are read through L2)
+__device__ void plan_body(const KdeParams &P, KeyAcc *K, const KdeTable &t0, const KdeTable &t1,
+                          const KdeTable &t2, int scatter, SepPlan *pl, int nc, long long cap1, long long cap2,
+                          long long *need, double *S, int work_weight) {
   __shared__ long long sv1[kPlanThreads], sv2[kPlanThreads];
   __shared__ int sp[kPlanThreads];
   __shared__ int su[3][6];
@@ -522,18 +544,19 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, KeyAcc 
     su[k][0] = su[k][2] = su[k][4] = INT_MAX;
     su[k][1] = su[k][3] = su[k][5] = INT_MIN;
   }
-  const bool present = k < KDE_KMAX && K->cnt[k] > 0;
+  const int cntk = k < KDE_KMAX ? __ldcg(&K->cnt[k]) : 0;
+  const bool present = cntk > 0;
   int m[3] = {0, 0, 0}, fo[3] = {0, 0, 0}, bx[6], r1[6], r2[6];
   long long v1 = 0, v2 = 0;
   if (present) {
     const int axis = k / KDE_MAXDB;
     const KdeTable T = !scatter ? t0 : (axis == 0 ? t0 : (axis == 1 ? t1 : t2));
     for (int d = 0; d < 3; ++d) {
-      const int li = d * KDE_MAXDB + K->lev[k][d] - 1;
+      const int li = d * KDE_MAXDB + __ldcg(&K->lev[k][d]) - 1;
       m[d] = T.m[li];
       fo[d] = T.ofs[li];
     }
-    for (int i = 0; i < 6; ++i) bx[i] = r1[i] = r2[i] = K->box[k][i];
+    for (int i = 0; i < 6; ++i) bx[i] = r1[i] = r2[i] = __ldcg(&K->box[k][i]);
     if (!scatter) {
       r1[2] = max(1, bx[2] - m[1]);
       r1[3] = min(P.nb[1], bx[3] + m[1]);
@@ -549,7 +572,7 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(KdeParams P, KeyAcc 
     v2 = (long long)(r2[1] - r2[0] + 1) * (r2[3] - r2[2] + 1) * (r2[5] - r2[4] + 1);
     // the work model: this level's bins times its kernel's cells
     if (work_weight > 0)
-      atomicAdd(work_counter(S), (unsigned long long)K->cnt[k] * (unsigned long long)work_weight *
+      atomicAdd(work_counter(S), (unsigned long long)cntk * (unsigned long long)work_weight *
                                      (unsigned long long)((2 * m[0] + 1) * (2 * m[1] + 1) * (2 * m[2] + 1)));
   }
   sp[k] = present ? 1 : 0;
@@ -1839,14 +1862,14 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
   // times (support update, nEstimate, six roughness terms), the second
   // derivatives once, the support plan's not at all
   auto plan = [&](int kind, int nc, int work_weight) -> cudaError_t {
-    key_assign_kernel<T><<<kb, kThreads, 0, s>>>(P, B, kind, kind == 1 ? key1 : key2, st.d_keys);
     if (kind == 1)
-      plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.wtab, st.wtab, st.wtab, 0, plan1, nc, st.t1_cap,
-                                             st.t2_cap, st.d_need, S, work_weight);
+      key_assign_kernel<T><<<kb, kThreads, 0, s>>>(P, B, kind, key1, st.d_keys, st.wtab, st.wtab, st.wtab, plan1, nc,
+                                                   st.t1_cap, st.t2_cap, st.d_need, S, work_weight);
     else
-      plan_kernel<<<1, kPlanThreads, 0, s>>>(P, st.d_keys, st.sdtab[0], st.sdtab[1], st.sdtab[2], 1, plan2, nc,
-                                             st.t1_cap, st.t2_cap, st.d_need, S, work_weight);
-    st.launches += 2;
+      key_assign_kernel<T><<<kb, kThreads, 0, s>>>(P, B, kind, key2, st.d_keys, st.sdtab[0], st.sdtab[1],
+                                                   st.sdtab[2], plan2, nc, st.t1_cap, st.t2_cap, st.d_need, S,
+                                                   work_weight);
+    st.launches += 1;
     return cudaGetLastError();
   };
   // FP64: the gathers compute only the pass elements that are read (the

@@ -55,6 +55,7 @@ struct KeyAcc {
   int box[KDE_KMAX][6];
   int lev[KDE_KMAX][3];
   int cnt[KDE_KMAX];
+  unsigned int done;  // blocks of the key assignment that have merged (the last one plans)
 };
 
 // The keys present, compacted: per key its half widths and the offsets of its
