@@ -88,9 +88,7 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t
 }
 
 // Exact Irwin-Hall(12) normal from three Philox blocks; advances ctr by 3.
-// The 36-bit word sum S is placed in the mantissa of 2^20 + S*2^-32 (exponent
-// field 0x413, mantissa LSB 2^-32), so the normal S*2^-32 - 6 costs one exact
-// FP64 subtraction instead of an int64 conversion.
+// The normal is S*2^-32 - 6 for the 36-bit sum S of the twelve words.
 __device__ __forceinline__ double normal_ih12(uint64_t seed, uint64_t id, uint64_t &ctr) {
   uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
   uint32_t i0 = (uint32_t)id, i1 = (uint32_t)(id >> 32);
@@ -102,8 +100,17 @@ __device__ __forceinline__ double normal_ih12(uint64_t seed, uint64_t id, uint64
     philox4x32_10((uint32_t)n, (uint32_t)(n >> 32), i0, i1, k0, k1, o);
     sum += (uint64_t)o[0] + o[1] + o[2] + o[3];
   }
-  double d = __longlong_as_double((long long)(0x4130000000000000ULL | sum));
-  return d - 1048582.0;  // 2^20 + 6
+  // (sum - 6*2^32) * 2^-32, exact (|sum - 6*2^32| < 2^36), assembled from
+  // its sign, exponent and mantissa on the integer pipe (GB300's FP64 pipe
+  // is the step kernel's limit); the same bits as (2^20 + sum*2^-32) - (2^20 + 6)
+  // in FP64, +0 for sum = 6*2^32
+  const long long k = (long long)sum - (6LL << 32);
+  const unsigned long long m = (unsigned long long)(k < 0 ? -k : k);
+  const int e = 63 - __clzll((long long)m);  // most significant bit, 0..35
+  const unsigned long long bits = ((unsigned long long)k & 0x8000000000000000ULL) |
+                                  ((unsigned long long)(e + 991) << 52) |  // 991 = 1023 - 32
+                                  ((m << (52 - e)) & 0x000FFFFFFFFFFFFFULL);
+  return __longlong_as_double((long long)(m ? bits : 0ULL));
 }
 
 // MIXED-precision normals: the same three Philox blocks (twelve 32-bit

@@ -35,6 +35,84 @@ struct Lane {
   __device__ __forceinline__ R operator()(int f) const { return p[f * stride]; }
 };
 
+// Tests against the constants 0, 1/2 and 1.  GB300 issues two FP64 lanes per
+// clock per SM, so an FP64 compare holds the FP64 pipe as long as a
+// multiply-add; the FP64 versions below take the same decision from the
+// IEEE-754 bit pattern in a few integer instructions, for every input
+// (signed zeros, subnormals and infinities as the compare orders them, NaN
+// false like the compare).  Each range test is one unsigned subtraction and
+// compare: b in [lo, hi] <=> b - lo < hi - lo + 1.
+__device__ __forceinline__ unsigned long long fbits(double v) { return (unsigned long long)__double_as_longlong(v); }
+template <typename R>
+__device__ __forceinline__ bool above1(R v) { return v > R(1); }
+template <>
+__device__ __forceinline__ bool above1<double>(double v) {  // (1, +inf]
+  return fbits(v) - 0x3FF0000000000001ULL < 0x4000000000000000ULL;
+}
+template <typename R>
+__device__ __forceinline__ bool below0(R v) { return v < R(0); }
+template <>
+__device__ __forceinline__ bool below0<double>(double v) {  // [-inf, 0), -0 excluded
+  return fbits(v) - 0x8000000000000001ULL < 0x7FF0000000000000ULL;
+}
+template <typename R>
+__device__ __forceinline__ bool above0(R v) { return v > R(0); }
+template <>
+__device__ __forceinline__ bool above0<double>(double v) {  // (0, +inf]
+  return fbits(v) - 1ULL < 0x7FF0000000000000ULL;
+}
+template <typename R>
+__device__ __forceinline__ bool is0(R v) { return v == R(0); }
+template <>
+__device__ __forceinline__ bool is0<double>(double v) {  // +0 or -0
+  return (fbits(v) << 1) == 0ULL;
+}
+template <typename R>
+__device__ __forceinline__ bool nonneg(R v) { return v >= R(0); }
+template <>
+__device__ __forceinline__ bool nonneg<double>(double v) {  // [+0, +inf] or -0
+  const unsigned long long b = fbits(v);
+  return (b <= 0x7FF0000000000000ULL) | (b == 0x8000000000000000ULL);
+}
+template <typename R>
+__device__ __forceinline__ bool abs_above_half(R v) { return fabs(v) > R(0.5); }
+template <>
+__device__ __forceinline__ bool abs_above_half<double>(double v) {  // |v| in (1/2, +inf]
+  return (fbits(v) & 0x7FFFFFFFFFFFFFFFULL) - 0x3FE0000000000001ULL < 0x4010000000000000ULL;
+}
+template <typename R>
+__device__ __forceinline__ bool out01(R v) { return v > R(1) || v < R(0); }
+template <>
+__device__ __forceinline__ bool out01<double>(double v) { return above1(v) | below0(v); }
+template <typename R>
+__device__ __forceinline__ bool is1(R v) { return v == R(1); }
+template <>
+__device__ __forceinline__ bool is1<double>(double v) { return fbits(v) == 0x3FF0000000000000ULL; }
+// a < b for a, b > 0 (positive finite or +inf, not NaN): the bit patterns of
+// positive doubles are ordered as their values
+template <typename R>
+__device__ __forceinline__ bool pos_lt(R a, R b) { return a < b; }
+template <>
+__device__ __forceinline__ bool pos_lt<double>(double a, double b) { return fbits(a) < fbits(b); }
+// a < b and a == b for any two doubles (the simulation times).  Mapped to
+// two's-complement keys (negative values: the magnitude bits flipped, so
+// larger magnitudes are smaller keys; -0 first taken as +0) the keys are
+// ordered as the values; NaN compares false.
+__device__ __forceinline__ bool isnan_bits(double v) {
+  return (fbits(v) & 0x7FFFFFFFFFFFFFFFULL) > 0x7FF0000000000000ULL;
+}
+__device__ __forceinline__ long long order_key(double v) {
+  long long b = __double_as_longlong(v);
+  b = (b == (long long)0x8000000000000000ULL) ? 0LL : b;
+  return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
+__device__ __forceinline__ bool lt_any(double a, double b) {
+  return !(isnan_bits(a) | isnan_bits(b)) & (order_key(a) < order_key(b));
+}
+__device__ __forceinline__ bool eq_any(double a, double b) {
+  return !(isnan_bits(a) | isnan_bits(b)) & (order_key(a) == order_key(b));
+}
+
 // The staged fields are the record's first NFIELDS values and records are
 // 16-byte aligned, so they are read with 16-byte loads (FP32: 16 float4 and
 // one float2; FP64: 33 double2) and scattered to the lane's SoA slots.
@@ -148,7 +226,7 @@ __device__ __forceinline__ void random_displacement(const Lane<R> &F, int ndim, 
     R nxy2 = fma(vx, vx, vy * vy);
     R n2 = fma(vz, vz, nxy2);
     R B11 = zero, B12 = zero, B13 = zero, B21 = zero, B22 = zero, B23 = zero, B31 = zero, B32 = zero;
-    if (n2 > zero) {
+    if (sizeof(R) == 8 ? above0(n2) : n2 > zero) {
       R inv = rsqrt(n2);
       R nrm = n2 * inv;
       R sL = sqrt(tr * fma(aL, nrm, dm));
@@ -158,7 +236,7 @@ __device__ __forceinline__ void random_displacement(const Lane<R> &F, int ndim, 
       B11 = vx * sLi;
       B21 = vy * sLi;
       B31 = vz * sLi;
-      if (nxy2 > zero) {
+      if (sizeof(R) == 8 ? above0(nxy2) : nxy2 > zero) {
         R invxy = rsqrt(nxy2);
         R nxy = nxy2 * invxy;
         R sTi = sT * inv;
@@ -272,6 +350,62 @@ __device__ __forceinline__ bool quad_axis(R npos, R pos, R d, R v, R divD, R dB,
     }
   }
   if ((T)dtaxis > dt) dtaxis = zero;
+  return false;
+}
+
+// quad_axis in FP64 with its tests against 0 and 1 and its step compare on
+// the integer pipe (the same decisions, see above).
+__device__ __forceinline__ bool quad_axis_f64(double npos, double pos, double d, double v, double divD, double dB,
+                                              int faceLo, int faceHi, double dt, double &dtaxis, int &exitAxis,
+                                              int &exitFace, double &dtout) {
+  using R = double;
+  const R zero = R(0), one = R(1);
+  R dI;
+  if (above1(npos)) {
+    dI = d * (one - pos);
+    exitAxis = faceHi;
+  } else {
+    dI = -d * pos;
+    exitAxis = faceLo;
+  }
+  if (is0(dI)) {
+    exitFace = exitAxis;
+    dtout = 0.0;
+    return true;
+  }
+  R A = v + divD, B = dB;
+  R arg = B * B + R(4) * dI * A;
+  if (nonneg(arg) && !is0(A)) {
+    R zs = sqrt(arg);
+    R z1, z2;
+    z1 = (-B + zs) / (R(2) * A);
+    z2 = (-B - zs) / (R(2) * A);
+    const bool p1 = above0(z1), p2 = above0(z2);
+    if (p1 || p2) {
+      R zm = (p1 && p2) ? (pos_lt(z1, z2) ? z1 : z2) : (p1 ? z1 : z2);
+      dtaxis = zm * zm;
+      if (is0(dtaxis)) {
+        exitFace = exitAxis;
+        dtout = 0.0;
+        return true;
+      }
+    } else if (is0(z1) || is0(z2)) {
+      exitFace = exitAxis;
+      dtout = 0.0;
+      return true;
+    }
+  } else if (is0(A)) {
+    if (!is0(B)) {
+      R q = dI / B;
+      dtaxis = q * q;
+      if (is0(dtaxis)) {
+        exitFace = exitAxis;
+        dtout = 0.0;
+        return true;
+      }
+    }
+  }
+  if (lt_any(dt, dtaxis)) dtaxis = zero;
   return false;
 }
 
@@ -490,13 +624,25 @@ __device__ __forceinline__ T pick3(int k, T a, T b, T c) {
 // bit k set when component k of the proposed position is outside [0, 1]
 template <typename R>
 __device__ __forceinline__ unsigned axes_outside(R nx, R ny, R nz) {
-  const R zero = R(0), one = R(1);
-  return ((nx > one || nx < zero) ? 1u : 0u) | ((ny > one || ny < zero) ? 2u : 0u) |
-         ((nz > one || nz < zero) ? 4u : 0u);
+  if constexpr (sizeof(R) == 8) {
+    return (out01(nx) ? 1u : 0u) | (out01(ny) ? 2u : 0u) | (out01(nz) ? 4u : 0u);
+  } else {
+    const R zero = R(0), one = R(1);
+    return ((nx > one || nx < zero) ? 1u : 0u) | ((ny > one || ny < zero) ? 2u : 0u) |
+           ((nz > one || nz < zero) ? 4u : 0u);
+  }
 }
 
-#define MPRW_OUTSIDE(a, b, c) \
-  (((a) > one) || ((a) < zero) || ((b) > one) || ((b) < zero) || ((c) > one) || ((c) < zero))
+template <typename R>
+__device__ __forceinline__ bool outside3(R a, R b, R c) {
+  if constexpr (sizeof(R) == 8) {
+    return out01(a) | out01(b) | out01(c);
+  } else {
+    const R zero = R(0), one = R(1);
+    return (a > one) || (a < zero) || (b > one) || (b < zero) || (c > one) || (c < zero);
+  }
+}
+#define MPRW_OUTSIDE(a, b, c) outside3(a, b, c)
 
 // The first interface iteration's exit-face solves of the leaving lanes of
 // `grp`, dealt out to every lane of `grp` (FP64).  Each (leaving lane,
@@ -558,7 +704,7 @@ __device__ __forceinline__ void warp_exit_solves(unsigned grp, unsigned need, do
     if (t < total) {
       int ef_unused = 0;
       double dt_unused = 0.0;
-      r = quad_axis<double>(pick3(a, onx, ony, onz), pick3(a, ox, oy, oz), pick3(a, odX, odY, odZ),
+      r = quad_axis_f64(pick3(a, onx, ony, onz), pick3(a, ox, oy, oz), pick3(a, odX, odY, odZ),
                             pick3(a, ovx, ovy, ovz), pick3(a, oddx, oddy, oddz), pick3(a, obx, oby, obz),
                             2 * a + 1, 2 * a + 2, odt, dta, efa, ef_unused, dt_unused);
     }
@@ -593,7 +739,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
   double dt = V.dtcell;
   R rdt = V.rdt_cell, sdt = V.sqrt_dtcell;  // FP32 copies: no conversion on the common pass
   V.t = V.t + dt;
-  if (maxTime < V.t) {
+  if (sizeof(R) == 8 ? lt_any(maxTime, V.t) : maxTime < V.t) {
     V.t = V.t - dt;
     dt = fmax(maxTime - V.t, 0.0);
     V.t = maxTime;
@@ -661,7 +807,8 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
       V.reachedMax = false;
     }
   } else
-  while ((fabs(dxrw * iX) > half) || (fabs(dyrw * iY) > half) || (fabs(dzrw * iZ) > half)) {
+  while (sizeof(R) == 8 ? abs_above_half(dxrw * iX) | abs_above_half(dyrw * iY) | abs_above_half(dzrw * iZ)
+                        : (fabs(dxrw * iX) > half) || (fabs(dyrw * iY) > half) || (fabs(dzrw * iZ) > half)) {
     V.t = V.t - dt;
     dt = dtRed * dt;
     rdt = (R)dt;
@@ -759,7 +906,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
           need &= need - 1;
           R dta = zero;
           int efa = 0;
-          ret = quad_axis(pick3(k, nx, ny, nz), pick3(k, x, y, z), pick3(k, dX, dY, dZ), pick3(k, vx, vy, vz),
+          ret = quad_axis_f64(pick3(k, nx, ny, nz), pick3(k, x, y, z), pick3(k, dX, dY, dZ), pick3(k, vx, vy, vz),
                           pick3(k, ddx, ddy, ddz), pick3(k, bx, by, bz), 2 * k + 1, 2 * k + 2, dt, dta, efa,
                           V.exitFace, dt);
           if (k == 0) { dtx = dta; efx = efa; }
@@ -775,14 +922,21 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
           ret = quad_axis(nz, z, dZ, vz, ddz, bz, 5, 6, rdt, dtz, efz, V.exitFace, dt);
       }
       if (!ret) {
-        if (dtx == zero && dty == zero && dtz == zero) {
+        if (sizeof(R) == 8 ? is0(dtx) && is0(dty) && is0(dtz) : dtx == zero && dty == zero && dtz == zero) {
           if constexpr (sizeof(R) == 8) V.t = V.t + dt;
         } else {
           int im = -1;
           R best = zero;
-          if (dtx > zero) { im = 0; best = dtx; }
-          if (dty > zero && (im < 0 || dty < best)) { im = 1; best = dty; }
-          if (dtz > zero && (im < 0 || dtz < best)) { im = 2; best = dtz; }
+          if constexpr (sizeof(R) == 8) {
+            // (best > 0 once im >= 0)
+            if (above0(dtx)) { im = 0; best = dtx; }
+            if (above0(dty) && (im < 0 || pos_lt(dty, best))) { im = 1; best = dty; }
+            if (above0(dtz) && (im < 0 || pos_lt(dtz, best))) { im = 2; best = dtz; }
+          } else {
+            if (dtx > zero) { im = 0; best = dtx; }
+            if (dty > zero && (im < 0 || dty < best)) { im = 1; best = dty; }
+            if (dtz > zero && (im < 0 || dtz < best)) { im = 2; best = dtz; }
+          }
           dt = (double)best;
           V.exitFace = (im == 0) ? efx : (im == 1 ? efy : efz);
           if constexpr (sizeof(R) == 8) {
@@ -862,7 +1016,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
         return PASS_UNDEFINED;
       }
       R xi = nx, yi = ny, zi = nz;
-      if (dt == 0.0) {
+      if (sizeof(R) == 8 ? is0(dt) : dt == 0.0) {
         nx = V.ix; ny = V.iy; nz = V.iz;
         V.t = V.t - dt;
         dt = V.dtcell;
@@ -871,7 +1025,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
         break;
       }
       V.t = V.t + dt;
-      if (maxTime < V.t) {
+      if (sizeof(R) == 8 ? lt_any(maxTime, V.t) : maxTime < V.t) {
         V.t = V.t - dt;
         dt = fmax(maxTime - V.t, 0.0);
         V.t = maxTime;
@@ -900,12 +1054,21 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
       } else {
         dt = V.dtcell;
         V.exitFace = 0;
-        if (nx == zero) V.exitFace = 1;
-        if (nx == one) V.exitFace = 2;
-        if (ny == zero) V.exitFace = 3;
-        if (ny == one) V.exitFace = 4;
-        if (nz == zero) V.exitFace = 5;
-        if (nz == one) V.exitFace = 6;
+        if constexpr (sizeof(R) == 8) {
+          if (is0(nx)) V.exitFace = 1;
+          if (is1(nx)) V.exitFace = 2;
+          if (is0(ny)) V.exitFace = 3;
+          if (is1(ny)) V.exitFace = 4;
+          if (is0(nz)) V.exitFace = 5;
+          if (is1(nz)) V.exitFace = 6;
+        } else {
+          if (nx == zero) V.exitFace = 1;
+          if (nx == one) V.exitFace = 2;
+          if (ny == zero) V.exitFace = 3;
+          if (ny == one) V.exitFace = 4;
+          if (nz == zero) V.exitFace = 5;
+          if (nz == one) V.exitFace = 6;
+        }
       }
     }
   }
@@ -1037,7 +1200,8 @@ __global__ void __launch_bounds__(step_threads(sizeof(R) == 8, EXP), (sizeof(R) 
       need_cell = false;
       int32_t fin = 0;  // 0 track, else final status
       bool use_last = false;
-      if (ex < zero || ex > one || ey < zero || ey > one || ez < zero || ez > one) {
+      if (sizeof(R) == 8 ? outside3(ex, ey, ez)
+                         : ex < zero || ex > one || ey < zero || ey > one || ez < zero || ez > one) {
         fin = ST_UNDEFINED;  // InvalidLocation (TrackCell.f90:410-413)
         use_last = true;
       } else {
@@ -1094,7 +1258,7 @@ __global__ void __launch_bounds__(step_threads(sizeof(R) == 8, EXP), (sizeof(R) 
         a.ctr[p] = ctr;
         p = -1;
       } else if (r == PASS_EXIT &&
-                 ((exits = ((exits & 0xFFFFFu) + 1u) | ((V.t == V.tinit) ? ((exits >> 20) + 1u) << 20 : 0u)) >> 20 >
+                 ((exits = ((exits & 0xFFFFFu) + 1u) | ((sizeof(R) == 8 ? eq_any(V.t, V.tinit) : V.t == V.tinit) ? ((exits >> 20) + 1u) << 20 : 0u)) >> 20 >
                       (uint32_t)kMaxZeroTimeExits ||
                   (exits & 0xFFFFFu) > (uint32_t)kMaxVisitsPerAdvance)) {
         a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
@@ -1109,8 +1273,11 @@ __global__ void __launch_bounds__(step_threads(sizeof(R) == 8, EXP), (sizeof(R) 
         // (not held in registers through the visit)
         const int32_t nc = __ldg(&a.recs[c].conn[face - 1]);
         // ConvertFromNeighbor: the exit coordinate must sit exactly on the face
-        const bool bad = (face == 2 && ox != one) || (face == 1 && ox != zero) || (face == 4 && oy != one) ||
-                         (face == 3 && oy != zero) || (face == 6 && oz != one) || (face == 5 && oz != zero);
+        const bool bad = sizeof(R) == 8
+                             ? (face == 2 && !is1(ox)) || (face == 1 && !is0(ox)) || (face == 4 && !is1(oy)) ||
+                                   (face == 3 && !is0(oy)) || (face == 6 && !is1(oz)) || (face == 5 && !is0(oz))
+                             : (face == 2 && ox != one) || (face == 1 && ox != zero) || (face == 4 && oy != one) ||
+                                   (face == 3 && oy != zero) || (face == 6 && oz != one) || (face == 5 && oz != zero);
         if (nc < 0 || bad) {
           a.cell[p] = lc; a.x[p] = lx; a.y[p] = ly; a.z[p] = lz; a.t[p] = lt;
           a.status[p] = (nc < 0) ? ST_BOUNDARY : ST_UNDEFINED;
