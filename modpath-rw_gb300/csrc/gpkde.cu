@@ -1625,6 +1625,7 @@ void KdeState::release() {
   if (h_scalars) cudaFreeHost(h_scalars);
   if (h_need) cudaFreeHost(h_need);
   if (h_out) cudaFreeHost(h_out);
+  if (body_exec) cudaGraphExecDestroy(body_exec);
   *this = KdeState();
 }
 
@@ -1804,6 +1805,30 @@ static cudaError_t read_work(KdeState &st, double *h, cudaStream_t s, bool copie
   for (int k = 0; k < 64; ++k) t += w[k];
   st.work_madds = (double)t;
   return cudaSuccess;
+}
+
+// The executable graph of the host-driven loop's body.  A batch's workers
+// run one reconstruction after another, each capturing the same kernels in
+// the same order (the same options) with new pointers, sizes and grids: the
+// executable graph kept from the previous one is updated in place, which
+// skips the instantiation, the costly step.  A capture of another topology
+// (another precision or dimension) is instantiated afresh.  No launch of the
+// kept graph is in flight here: every reconstruction ends with a stream
+// synchronisation.  (The device loop's graph is instantiated every time: its
+// loop-control kernel sets the conditional handle of its own capture.)
+static cudaGraphExec_t body_exec_for(KdeState &st, cudaGraph_t g) {
+  if (st.body_exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(st.body_exec, g, &info) == cudaSuccess) return st.body_exec;
+    (void)cudaGetLastError();
+    cudaGraphExecDestroy(st.body_exec);
+    st.body_exec = nullptr;
+  }
+  if (cudaGraphInstantiate(&st.body_exec, g, 0) != cudaSuccess) {
+    (void)cudaGetLastError();
+    st.body_exec = nullptr;
+  }
+  return st.body_exec;
 }
 
 // One reconstruction attempt in arithmetic type T; *overflow is set when a
@@ -2057,20 +2082,12 @@ static cudaError_t kde_attempt(KdeState &st, const KdeParams &P, double hs, doub
     const cudaError_t ee = cudaStreamEndCapture(s, &g);
     body_launches = st.launches - l0;
     st.launches = l0;
-    if (eb == cudaSuccess && ee == cudaSuccess && g) {
-      if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) exec = nullptr;
-    }
+    if (eb == cudaSuccess && ee == cudaSuccess && g) exec = body_exec_for(st, g);
     if (g) cudaGraphDestroy(g);
     (void)cudaGetLastError();  // a failed capture leaves no sticky error
   } else {
     (void)cudaGetLastError();  // the stream cannot be captured: run the body directly
   }
-  struct ExecGuard {
-    cudaGraphExec_t e;
-    ~ExecGuard() {
-      if (e) cudaGraphExecDestroy(e);
-    }
-  } guard{exec};
   int m = 0;
   for (m = 1; m <= n_opt_loops; ++m) {
     if (exec) {

@@ -109,6 +109,9 @@ struct KdeState {
   // reconstructions in flight: building each one's conditional graph cost
   // more than the host's per-loop reads)
   bool device_loop = true;
+  // the host-driven loop's body as an executable graph, kept across
+  // reconstructions and updated in place when a new capture has its topology
+  cudaGraphExec_t body_exec = nullptr;
   unsigned long long *d_wcnt = nullptr;  // the density scatters' part of it, spread over 64 counters
   long long *d_need = nullptr, *h_need = nullptr;  // pass-buffer sizes a plan needed, overflow flag
   KdeTable wtab{}, sdtab[3]{};

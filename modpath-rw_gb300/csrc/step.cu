@@ -112,6 +112,16 @@ __device__ __forceinline__ bool lt_any(double a, double b) {
 __device__ __forceinline__ bool eq_any(double a, double b) {
   return !(isnan_bits(a) | isnan_bits(b)) & (order_key(a) == order_key(b));
 }
+// maxTime < t (the end of the tracking interval passed), every pass of the
+// FP64 kernel: for maxTime in [+0, +inf] exactly one unsigned range test on t's
+// bits, t > maxTime <=> bits(t) in [bits(maxTime) + 1, bits(+inf)] (NaN and
+// negative t fall outside); any other maxTime takes the FP64 compare.  The
+// branch is uniform (maxTime is the launch's).
+__device__ __forceinline__ bool past_end(double maxTime, double t) {
+  const unsigned long long km = fbits(maxTime);
+  if (km <= 0x7FF0000000000000ULL) return fbits(t) - (km + 1ULL) < 0x7FF0000000000000ULL - km;
+  return maxTime < t;
+}
 
 // The staged fields are the record's first NFIELDS values and records are
 // 16-byte aligned, so they are read with 16-byte loads (FP32: 16 float4 and
@@ -739,7 +749,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
   double dt = V.dtcell;
   R rdt = V.rdt_cell, sdt = V.sqrt_dtcell;  // FP32 copies: no conversion on the common pass
   V.t = V.t + dt;
-  if (sizeof(R) == 8 ? lt_any(maxTime, V.t) : maxTime < V.t) {
+  if (sizeof(R) == 8 ? past_end(maxTime, V.t) : maxTime < V.t) {
     V.t = V.t - dt;
     dt = fmax(maxTime - V.t, 0.0);
     V.t = maxTime;
@@ -1025,7 +1035,7 @@ __device__ int rw_pass(Visit<R> &V, const Lane<R> &F, uint32_t massb, double max
         break;
       }
       V.t = V.t + dt;
-      if (sizeof(R) == 8 ? lt_any(maxTime, V.t) : maxTime < V.t) {
+      if (sizeof(R) == 8 ? past_end(maxTime, V.t) : maxTime < V.t) {
         V.t = V.t - dt;
         dt = fmax(maxTime - V.t, 0.0);
         V.t = maxTime;
