@@ -15,6 +15,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include "fpbits.cuh"
 
 namespace mprw {
 
@@ -100,17 +101,9 @@ __device__ __forceinline__ double normal_ih12(uint64_t seed, uint64_t id, uint64
     philox4x32_10((uint32_t)n, (uint32_t)(n >> 32), i0, i1, k0, k1, o);
     sum += (uint64_t)o[0] + o[1] + o[2] + o[3];
   }
-  // (sum - 6*2^32) * 2^-32, exact (|sum - 6*2^32| < 2^36), assembled from
-  // its sign, exponent and mantissa on the integer pipe (GB300's FP64 pipe
-  // is the step kernel's limit); the same bits as (2^20 + sum*2^-32) - (2^20 + 6)
-  // in FP64, +0 for sum = 6*2^32
-  const long long k = (long long)sum - (6LL << 32);
-  const unsigned long long m = (unsigned long long)(k < 0 ? -k : k);
-  const int e = 63 - __clzll((long long)m);  // most significant bit, 0..35
-  const unsigned long long bits = ((unsigned long long)k & 0x8000000000000000ULL) |
-                                  ((unsigned long long)(e + 991) << 52) |  // 991 = 1023 - 32
-                                  ((m << (52 - e)) & 0x000FFFFFFFFFFFFFULL);
-  return __longlong_as_double((long long)(m ? bits : 0ULL));
+  // assembled from its bits on the integer pipe (GB300's FP64 pipe is the
+  // step kernel's limit)
+  return fb::ih12_normal(sum);
 }
 
 // MIXED-precision normals: the same three Philox blocks (twelve 32-bit

@@ -35,93 +35,49 @@ struct Lane {
   __device__ __forceinline__ R operator()(int f) const { return p[f * stride]; }
 };
 
-// Tests against the constants 0, 1/2 and 1.  GB300 issues two FP64 lanes per
-// clock per SM, so an FP64 compare holds the FP64 pipe as long as a
-// multiply-add; the FP64 versions below take the same decision from the
-// IEEE-754 bit pattern in a few integer instructions, for every input
-// (signed zeros, subnormals and infinities as the compare orders them, NaN
-// false like the compare).  Each range test is one unsigned subtraction and
-// compare: b in [lo, hi] <=> b - lo < hi - lo + 1.
-__device__ __forceinline__ unsigned long long fbits(double v) { return (unsigned long long)__double_as_longlong(v); }
+// Tests against the constants 0, 1/2 and 1 and the time compares: native in
+// the FP32 kernel, from the IEEE-754 bit patterns in the FP64 kernel (the
+// same decisions for every input; fpbits.cuh).
 template <typename R>
 __device__ __forceinline__ bool above1(R v) { return v > R(1); }
 template <>
-__device__ __forceinline__ bool above1<double>(double v) {  // (1, +inf]
-  return fbits(v) - 0x3FF0000000000001ULL < 0x4000000000000000ULL;
-}
+__device__ __forceinline__ bool above1<double>(double v) { return fb::above1(v); }
 template <typename R>
 __device__ __forceinline__ bool below0(R v) { return v < R(0); }
 template <>
-__device__ __forceinline__ bool below0<double>(double v) {  // [-inf, 0), -0 excluded
-  return fbits(v) - 0x8000000000000001ULL < 0x7FF0000000000000ULL;
-}
+__device__ __forceinline__ bool below0<double>(double v) { return fb::below0(v); }
 template <typename R>
 __device__ __forceinline__ bool above0(R v) { return v > R(0); }
 template <>
-__device__ __forceinline__ bool above0<double>(double v) {  // (0, +inf]
-  return fbits(v) - 1ULL < 0x7FF0000000000000ULL;
-}
+__device__ __forceinline__ bool above0<double>(double v) { return fb::above0(v); }
 template <typename R>
 __device__ __forceinline__ bool is0(R v) { return v == R(0); }
 template <>
-__device__ __forceinline__ bool is0<double>(double v) {  // +0 or -0
-  return (fbits(v) << 1) == 0ULL;
-}
+__device__ __forceinline__ bool is0<double>(double v) { return fb::is0(v); }
 template <typename R>
 __device__ __forceinline__ bool nonneg(R v) { return v >= R(0); }
 template <>
-__device__ __forceinline__ bool nonneg<double>(double v) {  // [+0, +inf] or -0
-  const unsigned long long b = fbits(v);
-  return (b <= 0x7FF0000000000000ULL) | (b == 0x8000000000000000ULL);
-}
+__device__ __forceinline__ bool nonneg<double>(double v) { return fb::nonneg(v); }
 template <typename R>
 __device__ __forceinline__ bool abs_above_half(R v) { return fabs(v) > R(0.5); }
 template <>
-__device__ __forceinline__ bool abs_above_half<double>(double v) {  // |v| in (1/2, +inf]
-  return (fbits(v) & 0x7FFFFFFFFFFFFFFFULL) - 0x3FE0000000000001ULL < 0x4010000000000000ULL;
-}
+__device__ __forceinline__ bool abs_above_half<double>(double v) { return fb::abs_above_half(v); }
 template <typename R>
 __device__ __forceinline__ bool out01(R v) { return v > R(1) || v < R(0); }
 template <>
-__device__ __forceinline__ bool out01<double>(double v) { return above1(v) | below0(v); }
+__device__ __forceinline__ bool out01<double>(double v) { return fb::out01(v); }
 template <typename R>
 __device__ __forceinline__ bool is1(R v) { return v == R(1); }
 template <>
-__device__ __forceinline__ bool is1<double>(double v) { return fbits(v) == 0x3FF0000000000000ULL; }
-// a < b for a, b > 0 (positive finite or +inf, not NaN): the bit patterns of
-// positive doubles are ordered as their values
+__device__ __forceinline__ bool is1<double>(double v) { return fb::is1(v); }
+// a < b for a, b > 0 (not NaN)
 template <typename R>
 __device__ __forceinline__ bool pos_lt(R a, R b) { return a < b; }
 template <>
-__device__ __forceinline__ bool pos_lt<double>(double a, double b) { return fbits(a) < fbits(b); }
-// a < b and a == b for any two doubles (the simulation times).  Mapped to
-// two's-complement keys (negative values: the magnitude bits flipped, so
-// larger magnitudes are smaller keys; -0 first taken as +0) the keys are
-// ordered as the values; NaN compares false.
-__device__ __forceinline__ bool isnan_bits(double v) {
-  return (fbits(v) & 0x7FFFFFFFFFFFFFFFULL) > 0x7FF0000000000000ULL;
-}
-__device__ __forceinline__ long long order_key(double v) {
-  long long b = __double_as_longlong(v);
-  b = (b == (long long)0x8000000000000000ULL) ? 0LL : b;
-  return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
-}
-__device__ __forceinline__ bool lt_any(double a, double b) {
-  return !(isnan_bits(a) | isnan_bits(b)) & (order_key(a) < order_key(b));
-}
-__device__ __forceinline__ bool eq_any(double a, double b) {
-  return !(isnan_bits(a) | isnan_bits(b)) & (order_key(a) == order_key(b));
-}
-// maxTime < t (the end of the tracking interval passed), every pass of the
-// FP64 kernel: for maxTime in [+0, +inf] exactly one unsigned range test on t's
-// bits, t > maxTime <=> bits(t) in [bits(maxTime) + 1, bits(+inf)] (NaN and
-// negative t fall outside); any other maxTime takes the FP64 compare.  The
-// branch is uniform (maxTime is the launch's).
-__device__ __forceinline__ bool past_end(double maxTime, double t) {
-  const unsigned long long km = fbits(maxTime);
-  if (km <= 0x7FF0000000000000ULL) return fbits(t) - (km + 1ULL) < 0x7FF0000000000000ULL - km;
-  return maxTime < t;
-}
+__device__ __forceinline__ bool pos_lt<double>(double a, double b) { return fb::pos_lt(a, b); }
+using fb::eq_any;
+using fb::lt_any;
+using fb::past_end;
 
 // The staged fields are the record's first NFIELDS values and records are
 // 16-byte aligned, so they are read with 16-byte loads (FP32: 16 float4 and
