@@ -518,7 +518,7 @@ __global__ void __launch_bounds__(kThreads) key_assign_kernel(KdeParams P, KdeBi
 }
 
 // Compact the keys present and lay out the pass regions, one thread per
-// key (launched with kPlanThreads >= KDE_KMAX threads), offsets by a block
+// key (a block of kPlanThreads >= KDE_KMAX threads), offsets by a block
 // prefix sum in key order.  Gather: pass 1 (x) covers the bins' x range and
 // the y, z ranges widened by the half widths; pass 2 (y) the bins' x, y
 // ranges and the widened z range; the z pass runs per bin.  Scatter: pass 1
@@ -526,13 +526,14 @@ __global__ void __launch_bounds__(kThreads) key_assign_kernel(KdeParams P, KdeBi
 // region of each axis's keys.
 constexpr int kPlanThreads = 256;
 static_assert(kPlanThreads >= KDE_KMAX, "one plan thread per key");
+static_assert(kThreads == kPlanThreads, "the key assignment's last block runs the plan");
 
 // Pass-buffer capacity is checked here, on the device: a plan that needs
 // more than cap1 / cap2 elements (nc per region cell) records the sizes it
 // needs in need[0..1], sets need[2] and presents no key, so the passes do
 // nothing and the host reruns the reconstruction with larger buffers.
-// (run by the last block of the key assignment, kPlanThreads threads; the
-// accumulators other blocks merged are read through L2)
+// Run by the last block of the key assignment; the accumulators the other
+// blocks merged are read through L2.
 __device__ void plan_body(const KdeParams &P, KeyAcc *K, const KdeTable &t0, const KdeTable &t1,
                           const KdeTable &t2, int scatter, SepPlan *pl, int nc, long long cap1, long long cap2,
                           long long *need, double *S, int work_weight) {
