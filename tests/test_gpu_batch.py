@@ -52,6 +52,14 @@ def test_batch_members_equal_separate_runs(gpu_lib, precision):
     # every member at once, three reconstructions in flight
     dens_all, loops = b.gpkde(doms, (1.0, 1.0, 1.0), concurrency=3)
     assert (loops >= 1).all()
+    # one worker for every member, twice: the executable graph of its loop
+    # body, kept from one reconstruction to the next, is updated in place for
+    # each member's grid -- the same densities as three workers
+    for _ in range(2):
+        dens_one, loops_one = b.gpkde(doms, (1.0, 1.0, 1.0), concurrency=1)
+        np.testing.assert_array_equal(loops_one, loops)
+        for k in range(len(mem)):
+            assert np.linalg.norm(dens_one[k] - dens_all[k]) <= 1e-12 * np.linalg.norm(dens_all[k])
     total = 0
     for k, (g, f, p) in enumerate(mem):
         ref, s, hist, dens = _separate(g, f, p, opt, iv)
