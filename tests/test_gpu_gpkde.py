@@ -117,16 +117,21 @@ def test_gpkde_scaling_and_empty(gpu_lib):
     tr.close()
 
 
-@pytest.mark.parametrize("case", ["1d", "3d"])
+@pytest.mark.parametrize("case", ["1d", "2d", "3d", "3d_isotropic"])
 def test_gpkde_fp32_against_fp64(gpu_lib, case):
     """The mixed-precision reconstruction (FP32 passes and per-bin updates,
     FP64 convergence sums) against the FP64 one on the same particles: the
     same number of optimisation loops, the density within 1e-3 of its
-    maximum, the mass conserved to FP32 rounding."""
+    maximum, the mass conserved to FP32 rounding -- in 1-D, 2-D (the
+    reference example's 250 x 50 grid) and 3-D, anisotropic and isotropic."""
     from mprw.model import MIXED
+    iso = case == "3d_isotropic"
     if case == "1d":
         g, f, p, opt = W.uniform_pulse(n_particles=20000)
         t1, dom, lo = 50.0, (200.0, 1.0, 1.0), 10
+    elif case == "2d":
+        g, f, p, opt, info = W.lognormal_slab(n_particles=20000, nlay=1, nrow=50, ncol=250, seed=3, use_torch=False)
+        t1, dom, lo = 40.0, (250.0, 50.0, 1.0), 10
     else:
         g, f, p, opt, info = W.lognormal_slab(n_particles=20000, nlay=6, nrow=20, ncol=40, seed=1, use_torch=False)
         t1, dom, lo = 30.0, (40.0, 20.0, 6.0), 10
@@ -135,8 +140,8 @@ def test_gpkde_fp32_against_fp64(gpu_lib, case):
     tr.set_particles(p)
     tr.advance(0.0, t1)
     n = _positions(tr).shape[0]
-    d64, h64, l64 = tr.gpkde(dom, (1.0, 1.0, 1.0), n_opt_loops=lo)
-    d32, h32, l32 = tr.gpkde(dom, (1.0, 1.0, 1.0), n_opt_loops=lo, precision=MIXED)
+    d64, h64, l64 = tr.gpkde(dom, (1.0, 1.0, 1.0), n_opt_loops=lo, isotropic=iso)
+    d32, h32, l32 = tr.gpkde(dom, (1.0, 1.0, 1.0), n_opt_loops=lo, precision=MIXED, isotropic=iso)
     tr.close()
     np.testing.assert_array_equal(h32, h64)
     assert l32 == l64
