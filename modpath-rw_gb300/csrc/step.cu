@@ -37,7 +37,10 @@ struct Lane {
 
 // Tests against the constants 0, 1/2 and 1 and the time compares: native in
 // the FP32 kernel, from the IEEE-754 bit patterns in the FP64 kernel (the
-// same decisions for every input; fpbits.cuh).
+// same decisions for every input; fpbits.cuh).  Where a site reads
+// `sizeof(R) == 8 ? <bit-pattern form> : <compare>`, the FP32 kernel keeps
+// its compare written as before: it is latency-bound at 80 registers, and
+// every reshaping of its compares measured slower.
 template <typename R>
 __device__ __forceinline__ bool above1(R v) { return v > R(1); }
 template <>
